@@ -1,0 +1,171 @@
+/*
+ * ttg.h — C ABI of the GB300 task-graph executor (libttg.so).
+ *
+ * This is the boundary between the host-side drop-in of TaskTorrent's
+ * ttor::Taskflow<K> / ttor::Threadpool_shared (C++ headers under
+ * tasktorrent_gb300/tasktorrent/) and the CUDA runtime.  In the reference the
+ * same boundary is the call from Taskflow into the thread pool:
+ *
+ *   Taskflow::fulfill_promise -> Threadpool_shared::insert(Task*, where, binding)
+ *     (tasktorrent/src/taskflow.hpp:241-296, threadpool_shared.cpp:200-224)
+ *   Threadpool_shared::join()  (threadpool_shared.cpp:234-241)
+ *
+ * Here the host records the task graph once (task kind + operand tiles, the
+ * indegree, priority and binding of every task, and the successor lists that
+ * fulfill() produces), uploads it, and one persistent kernel runs it: its
+ * blocks pop ready tasks from device queues, run the tile kernel, and
+ * decrement successor counters with atomics.
+ *
+ * Conventions: every function returns a ttg_status (0 = success) and never
+ * aborts; pointers named d_* are device pointers, h_* host pointers; matrices
+ * and tiles are column-major.  A ttg_ctx is not thread-safe: use one per host
+ * thread.  Device buffers passed in are owned by the caller; the context owns
+ * the uploaded graph, the queues, the counters and the trace buffer.
+ */
+#ifndef TTG_H
+#define TTG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int ttg_status;
+enum {
+    TTG_OK = 0,
+    TTG_EINVAL = 1,     /* bad argument                                            */
+    TTG_ECUDA = 2,      /* a CUDA runtime call failed                              */
+    TTG_ETIMEOUT = 3,   /* the executor made no progress within the time limit     */
+    TTG_EOVERCOUNT = 4, /* a task received more promises than its indegree         */
+    TTG_ENOTPD = 5,     /* a diagonal tile is not positive definite                */
+    TTG_ENOMEM = 6,     /* device allocation failed                                */
+    TTG_ESTATE = 7,     /* call out of order (e.g. launch before upload)           */
+    TTG_EUNDERRUN = 8,  /* some tasks never became ready (indegree too large)      */
+    TTG_ENOCONV = 9     /* iterative refinement did not reach the requested error  */
+};
+
+const char* ttg_strerror(ttg_status s);
+
+/* ------------------------------------------------------------------ tasks */
+
+/* Tile operation of one task.  The reference task bodies call BLAS/LAPACK on
+ * tiles (miniapp/dense_cholesky/2d_cholesky.cpp:319,404-405,490-494;
+ * miniapp/gemm/2d_gemm.cpp:157); each kind below is one of those calls. */
+enum {
+    TTG_OP_NOP = 0,       /* no device work (pure dependency task)                  */
+    TTG_OP_POTRF_L = 1,   /* c[n×n] <- lower Cholesky factor, in place (LAPACKE_dpotrf 'L') */
+    TTG_OP_TRSM_RLTN = 2, /* c[m×n] <- alpha c · a⁻ᵀ, a[n×n] lower non-unit (cblas_dtrsm R,L,T,N) */
+    TTG_OP_SYRK_LN = 3,   /* lower(c[n×n]) <- alpha a·aᵀ + beta c, a[n×k] (cblas_dsyrk L,N) */
+    TTG_OP_GEMM_NT = 4,   /* c[m×n] <- alpha a·bᵀ + beta c, a[m×k], b[n×k] (cblas_dgemm N,T) */
+    TTG_OP_GEMM_NN = 5,   /* c[m×n] <- alpha a·b + beta c, a[m×k], b[k×n]  (cblas_dgemm N,N) */
+    TTG_OP_GEADD = 6      /* c[m×n] <- alpha a + beta c  (tile accumulation)          */
+};
+
+/* Arithmetic of one task. */
+enum {
+    TTG_PREC_F64 = 0,      /* a, b, c are double                                         */
+    TTG_PREC_MIXED = 1     /* mixed-precision tile path, see ttg_mixed_tile below        */
+};
+
+typedef struct ttg_op {
+    int32_t kind;      /* TTG_OP_*                           */
+    int32_t prec;      /* TTG_PREC_*                         */
+    int32_t m, n, k;   /* dimensions as in the BLAS call      */
+    int32_t lda, ldb, ldc;
+    double alpha, beta;
+    const void* a;     /* device pointers                     */
+    const void* b;
+    void* c;
+    void* aux;         /* per-kind extra data (mixed path)    */
+} ttg_op;
+
+/* A task graph in compressed form.  Task t is ready when its counter reaches
+ * zero; init_count[t] is its indegree minus the promises made before launch
+ * (the reference's seeding from the main thread, 2d_cholesky.cpp:613-615). */
+typedef struct ttg_graph_desc {
+    int32_t n_tasks;
+    const ttg_op* ops;          /* [n_tasks] host array                                    */
+    const int32_t* init_count;  /* [n_tasks]                                               */
+    const double* priority;     /* [n_tasks] or NULL; higher runs first (set_priority)     */
+    const int32_t* bind;        /* [n_tasks] or NULL; -1 = stealable, w >= 0 = run only on
+                                   worker w mod workers (set_mapping + set_binding)        */
+    const int64_t* succ_ptr;    /* [n_tasks+1] CSR offsets into succ_idx                   */
+    const int32_t* succ_idx;    /* successors; one entry per fulfill_promise call          */
+} ttg_graph_desc;
+
+/* ---------------------------------------------------------------- context */
+
+typedef struct ttg_opts {
+    int device;          /* CUDA device ordinal                                     */
+    int workers;         /* persistent blocks; 0 = one per SM                         */
+    double timeout_s;    /* no-progress limit of the executor; 0 = 10 s              */
+    int trace;           /* record per-task start/end times and worker               */
+} ttg_opts;
+
+typedef struct ttg_report {
+    int64_t tasks_total;    /* tasks in the graph                                    */
+    int64_t tasks_run;      /* tasks the device completed                            */
+    int64_t tasks_pending;  /* counters that did not reach zero                      */
+    int64_t bad_runs;       /* tasks that ran other than exactly once                */
+    int32_t status;         /* ttg_status of the run                                 */
+    int32_t error_task;     /* first task that reported an error, or -1              */
+    int32_t info;           /* POTRF: 1-based failing column inside error_task        */
+    int32_t workers;        /* blocks used                                           */
+    float elapsed_ms;       /* launch to completion (CUDA events on the stream)       */
+} ttg_report;
+
+typedef struct ttg_ctx ttg_ctx;
+
+ttg_status ttg_create(ttg_ctx** ctx, const ttg_opts* opts);
+ttg_status ttg_destroy(ttg_ctx* ctx);
+
+/* Upload a task graph (replaces any previous one).  Copies everything. */
+ttg_status ttg_graph_upload(ttg_ctx* ctx, const ttg_graph_desc* g);
+
+/* Reset the counters and queues and launch the persistent executor on
+ * `stream` (a cudaStream_t; NULL = legacy default stream).  Asynchronous. */
+ttg_status ttg_launch(ttg_ctx* ctx, void* stream);
+
+/* Wait for the launched run and fill `rep` (may be NULL). */
+ttg_status ttg_wait(ttg_ctx* ctx, ttg_report* rep);
+
+/* ttg_launch + ttg_wait. */
+ttg_status ttg_run(ttg_ctx* ctx, void* stream, ttg_report* rep);
+
+/* Per-task record of the last run: how often each task ran and its counter at
+ * the end (both int32[n_tasks], host). */
+ttg_status ttg_task_record(ttg_ctx* ctx, int32_t* h_runs, int32_t* h_final_count);
+
+/* Per-task trace of the last run (opts.trace): start/end in ns of the GPU
+ * global timer relative to the earliest start, and the worker (block) id. */
+ttg_status ttg_trace(ttg_ctx* ctx, int64_t* h_start_ns, int64_t* h_end_ns, int32_t* h_worker);
+
+/* Number of persistent workers the context launches. */
+int ttg_workers(const ttg_ctx* ctx);
+
+/* ------------------------------------------------------------ generators */
+/* Seeded inputs of the workloads (include/ttg_philox.h), built on the device. */
+
+/* Lower tiles of A = G·Gᵀ/N + alpha·I, G the quantised Gaussian of (seed).
+ * Tiles are stored back to back, tile (i,j), i >= j, at d_tiles + off[i,j],
+ * column-major with leading dimension bs[i]; off/bs as in ttg_tile_layout. */
+ttg_status ttg_gen_gram_tiles(ttg_ctx* ctx, int32_t n, const int32_t* h_block_sizes, int32_t num_blocks,
+                              double alpha, uint32_t seed, double* d_tiles, void* stream);
+
+/* Dense N×N column-major U[-1,1] matrix from (seed, stream id). */
+ttg_status ttg_gen_uniform(ttg_ctx* ctx, int64_t count, uint32_t seed, uint32_t stream_id, double* d_out, void* stream);
+
+/* Dense column-major N(0,1) matrix from (seed, stream id). */
+ttg_status ttg_gen_normal(ttg_ctx* ctx, int64_t count, uint32_t seed, uint32_t stream_id, double* d_out, void* stream);
+
+/* Offsets (in elements) of the packed lower-tile layout: off[i + j*nb] for
+ * i >= j, and the total element count. */
+int64_t ttg_tile_layout(const int32_t* h_block_sizes, int32_t num_blocks, int64_t* h_off);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TTG_H */

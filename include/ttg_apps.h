@@ -1,0 +1,111 @@
+/*
+ * ttg_apps.h — C ABI of the two workloads of the reference's miniapps, built
+ * on the Taskflow<K> drop-in and the persistent executor (libttg.so).
+ *
+ *   Cholesky plan: the task graph of miniapp/dense_cholesky/2d_cholesky.cpp at
+ *     one rank (potrf/trsm/gemm flows, optional accu flow, priorities, uneven
+ *     block sizes) on lower tiles resident in device memory.
+ *   GEMM plan: the task graph of miniapp/gemm/2d_gemm.cpp at one rank
+ *     (send_Aij, send_Bij, gemm_Cikj chained over k) on resident tiles.
+ *
+ * A plan is created once (tiles allocated, graph captured and uploaded) and
+ * then factorised / multiplied any number of times; each run restores the
+ * input tiles first.  All functions return a ttg_status and never abort.
+ */
+#ifndef TTG_APPS_H
+#define TTG_APPS_H
+
+#include "ttg.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Arguments of 2d_cholesky (2d_cholesky.cpp:705-719) at one rank, plus the
+ * GB300 additions (matrix, alpha, seed, precision, workers). */
+typedef struct ttg_chol_args {
+    int32_t n_threads;        /* --n_threads: mapping modulus of the task graph     */
+    int32_t verb;             /* --verb                                            */
+    int32_t block_size;       /* --block_size                                      */
+    int32_t num_blocks;       /* --num_blocks                                      */
+    int32_t kind;             /* --kind: 0 none, 1 row, 2 critical path, 3 cp+row   */
+    int32_t accumulate;       /* --accumulate                                      */
+    int32_t upper_block_size; /* --upper_block_size (-1 = block_size)              */
+    int32_t matrix;           /* 0: 1/((i-j)^2+1) (the miniapp's); 1: G·Gᵀ/N + αI    */
+    double alpha;
+    uint32_t seed;
+    int32_t precision;        /* TTG_PREC_F64 or TTG_PREC_MIXED                     */
+    int32_t mixed_kind;       /* mixed path: 0 = BF16 updates, 1 = FP32 updates       */
+} ttg_chol_args;
+
+typedef struct ttg_chol_plan ttg_chol_plan;
+
+ttg_status ttg_chol_plan_create(ttg_ctx* ctx, const ttg_chol_args* args, ttg_chol_plan** plan);
+ttg_status ttg_chol_plan_destroy(ttg_chol_plan* plan);
+
+/* Matrix order and block sizes (h_bs may be NULL). */
+int32_t ttg_chol_plan_n(const ttg_chol_plan* plan, int32_t* h_bs);
+/* Number of device tasks of the captured graph and the capture time (s). */
+int32_t ttg_chol_plan_tasks(const ttg_chol_plan* plan, double* capture_s);
+
+/* Input: regenerate it on the device from args (matrix/alpha/seed). */
+ttg_status ttg_chol_plan_generate(ttg_chol_plan* plan, void* stream);
+/* Input: dense N×N column-major symmetric matrix in host memory (lower part
+ * read).  Copies into the pristine tiles. */
+ttg_status ttg_chol_plan_set_matrix(ttg_chol_plan* plan, const double* h_A, void* stream);
+
+/* Restore the working tiles from the pristine input (device copy). */
+ttg_status ttg_chol_plan_restore(ttg_chol_plan* plan, void* stream);
+/* Run the captured task graph once on the working tiles (no restore). */
+ttg_status ttg_chol_plan_factor(ttg_chol_plan* plan, void* stream, ttg_report* rep);
+
+/* End-to-end: host matrix in (pinned or pageable), factor, host factor out.
+ * h_L receives the dense N×N lower factor (upper part zeroed). */
+ttg_status ttg_chol_factor_host(ttg_chol_plan* plan, const double* h_A, double* h_L, void* stream, ttg_report* rep);
+
+/* The factor as a dense N×N column-major lower-triangular host array. */
+ttg_status ttg_chol_plan_get_factor(ttg_chol_plan* plan, double* h_L);
+/* The input as a dense N×N column-major symmetric host array. */
+ttg_status ttg_chol_plan_get_input(ttg_chol_plan* plan, double* h_A);
+
+/* Device pointers of the working tiles (lower, packed) and their offsets. */
+double* ttg_chol_plan_tiles(ttg_chol_plan* plan, const int64_t** h_off);
+
+/* DAG record of the last run in the oracle's CSV format. */
+ttg_status ttg_chol_plan_dump_dag(ttg_chol_plan* plan, const char* prefix);
+/* Capture the Cholesky task graph on the host only (no device, no tiles)
+ * and write its DAG record — the graph a plan with these arguments runs. */
+ttg_status ttg_chol_dag_dump(const ttg_chol_args* args, const char* prefix);
+
+/* Per-kind device busy time (ms) of the last run (needs ctx trace). */
+ttg_status ttg_chol_plan_kind_times(ttg_chol_plan* plan, double* potrf_ms, double* trsm_ms, double* gemm_ms, double* accu_ms);
+
+/* Arguments of 2d_gemm (2d_gemm.cpp:243-253) at one rank. */
+typedef struct ttg_gemm_args {
+    int32_t n_threads;
+    int32_t verb;
+    int32_t block_size;
+    int32_t matrix_size;
+    int32_t inputs;           /* 0: val_global (gemm_shared.hpp:74-76); 1: U[-1,1] from seed */
+    uint32_t seed;
+} ttg_gemm_args;
+
+typedef struct ttg_gemm_plan ttg_gemm_plan;
+
+ttg_status ttg_gemm_plan_create(ttg_ctx* ctx, const ttg_gemm_args* args, ttg_gemm_plan** plan);
+ttg_status ttg_gemm_plan_destroy(ttg_gemm_plan* plan);
+int32_t ttg_gemm_plan_tasks(const ttg_gemm_plan* plan, double* capture_s);
+/* Zero C and run the task graph once. */
+ttg_status ttg_gemm_plan_run(ttg_gemm_plan* plan, void* stream, ttg_report* rep);
+/* End-to-end: host A and B in, C = A·B out (dense N×N column-major). */
+ttg_status ttg_gemm_host(ttg_gemm_plan* plan, const double* h_A, const double* h_B, double* h_C, void* stream, ttg_report* rep);
+ttg_status ttg_gemm_plan_get_C(ttg_gemm_plan* plan, double* h_C);
+ttg_status ttg_gemm_plan_dump_dag(ttg_gemm_plan* plan, const char* prefix);
+/* Capture the block GEMM task graph on the host only and write its DAG record. */
+ttg_status ttg_gemm_dag_dump(const ttg_gemm_args* args, const char* prefix);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

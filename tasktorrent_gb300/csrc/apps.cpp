@@ -1,0 +1,628 @@
+// apps.cpp — the two miniapp workloads written against the Taskflow<K>
+// drop-in (include/ttg_apps.h).
+//
+// The task graphs are the reference's, at one rank (nprows = npcols = 1):
+//   Cholesky: miniapp/dense_cholesky/2d_cholesky.cpp — block sizes (:63-104),
+//     thread map (:125-130), priorities (:158-204), names (:206-217), potrf
+//     (:316-361), trsm (:398-464), gemm/syrk (:469-551), accu (:556-608),
+//     seeding potrf(0) (:613-615).  With one rank every active-message send is
+//     skipped (dest == rank), so only the local fulfill loops remain.
+//   GEMM: miniapp/gemm/2d_gemm.cpp — send_Aij (:98-120), send_Bij (:122-144),
+//     gemm_Cikj (:151-168), seeding every (i,j) (:174-181).
+// The flows, indegrees, keys and names must equal the reference's for the
+// graph to be the same graph; the task bodies call the ttor::gpu spellings of
+// the same BLAS/LAPACK routines on device tiles.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "../../include/ttg.h"
+#include "../../include/ttg_apps.h"
+#include "../../include/ttg_philox.h"
+#include "../tasktorrent/tasktorrent.hpp"
+#include "ttg_internal.h"
+#include "ttg_mixed_api.h"
+
+using namespace ttor;
+typedef std::array<int, 2> Key2;  // the reference's int2 (CUDA headers own that name)
+typedef std::array<int, 3> Key3;  // the reference's int3
+
+namespace {
+
+// Block sizes of 2d_cholesky.cpp:63-104 (uniform unless upper > block).
+bool cholesky_block_sizes(int block_size, int num_blocks, int upper, std::vector<int>& bs) {
+    const int N = block_size * num_blocks;
+    if (upper < 0) upper = block_size;
+    if (upper < block_size || upper > 2 * block_size) return false;
+    const int lower = 2 * block_size - upper;
+    std::mt19937 gen(2020);
+    std::uniform_int_distribution<> distrib(lower, upper);
+    bs.assign(num_blocks, block_size);
+    int n = 0;
+    for (int i = 0; i < num_blocks - 1; ++i) {
+        const int b = std::min(N - n, distrib(gen));
+        n += b;
+        bs[i] = b;
+    }
+    bs[num_blocks - 1] = N - n;
+    return true;
+}
+
+}  // namespace
+
+struct ttg_chol_plan {
+    ttg_ctx* ctx = nullptr;
+    ttg_chol_args args{};
+    int N = 0, nb = 0;
+    std::vector<int> bs, displ;
+    std::vector<int64_t> off;
+    int64_t elems = 0;
+    double* tiles = nullptr;     // working tiles (factorised in place)
+    double* pristine = nullptr;  // input copy
+    std::unique_ptr<Threadpool_shared> tp;
+    std::vector<int> kind_of_dev;  // per device task: 0 potrf, 1 trsm, 2 gemm, 3 accu, -1 other
+    std::vector<double*> tmp;      // accumulate-flow temporaries (device)
+    ttg_mixed_state* mixed = nullptr;
+};
+
+static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry) {
+    const ttg_chol_args& a = P->args;
+    const int nb = P->nb, n_threads = a.n_threads;
+    const bool accumulate = a.accumulate != 0;
+    const int pk = a.kind;
+    const bool mixed = a.precision == TTG_PREC_MIXED;
+    auto block = [P](int i, int j) { return P->tiles + P->off[i + (size_t)j * P->nb]; };
+    auto lda = [P](int i) { return std::max(1, P->bs[i]); };
+    auto block_2_thread = [=](int i, int j) { return (i + j * nb) % n_threads; };
+
+    auto potf_block_2_prio = [=](int j) -> double {
+        if (pk == 3) return (double)(9 * (nb - j) - 1) + 18 * nb * nb;
+        if (pk == 2) return (double)(9 * (nb - j) - 1);
+        if (pk == 1) return 3.0 * (double)(nb - j);
+        return 3.0;
+    };
+    auto trsm_block_2_prio = [=](Key2 ij) -> double {
+        if (pk == 3) return (double)((nb - ij[0]) + nb * (9.0 * nb - 9.0 * ij[1] - 2.0) + 9 * nb * nb);
+        if (pk == 2) return (double)(9 * (nb - ij[1]) - 2);
+        if (pk == 1) return 2.0 * (double)(nb - ij[0]);
+        return 2.0;
+    };
+    auto gemm_block_2_prio = [=](Key3 kij) -> double {
+        if (pk == 3) {
+            if (accumulate) return (double)(nb - kij[1]) + nb * (9.0 * nb - 9.0 * kij[2] - 2.0);
+            return (double)(nb - kij[1]) + nb * (9.0 * nb - 3.0 * kij[2] - 6.0 * kij[0] - 2.0);
+        }
+        if (pk == 2) return (double)(9 * nb - 9 * kij[2] - 2);
+        if (pk == 1) return (double)(nb - kij[1]);
+        return 1.0;
+    };
+
+    // Accumulation temporaries: one per (k, i, j) gemm of the accumulate flow.
+    std::map<std::array<int, 3>, double*> tmp_of;
+    if (accumulate) {
+        for (int j = 0; j < nb; ++j)
+            for (int i = j; i < nb; ++i)
+                for (int k = 0; k < j; ++k) {
+                    double* t = nullptr;
+                    if (!dry) {
+                        if (cudaMalloc((void**)&t, sizeof(double) * std::max(1, P->bs[i] * P->bs[j])) != cudaSuccess)
+                            return TTG_ENOMEM;
+                        P->tmp.push_back(t);
+                    }
+                    tmp_of[{k, i, j}] = t;
+                }
+    }
+
+    P->tp.reset(new Threadpool_shared(n_threads, a.verb, "Wk_Chol_0_"));
+    Threadpool_shared& tp = *P->tp;
+    if (!dry) tp.set_context(P->ctx);
+    Taskflow<int> potrf(&tp, a.verb);
+    Taskflow<Key2> trsm(&tp, a.verb);
+    Taskflow<Key3> gemm(&tp, a.verb);
+    Taskflow<Key3> accu(&tp, a.verb);
+
+    potrf.set_task([&](int j) {
+             if (mixed) ttg_mixed_record_potrf(P->mixed, j);
+             else gpu::LAPACKE_dpotrf(gpu::LAPACK_COL_MAJOR, 'L', P->bs[j], block(j, j), lda(j));
+         })
+        .set_fulfill([&](int j) {
+            for (int i = j + 1; i < nb; i++) trsm.fulfill_promise({i, j});
+        })
+        .set_indegree([&](int j) { return accumulate ? (j == 0 ? 1 : j) : 1; })
+        .set_priority(potf_block_2_prio)
+        .set_mapping([&](int j) { return block_2_thread(j, j); })
+        .set_name([](int j) { return "POTRF_" + std::to_string(j); });
+
+    trsm.set_task([&](Key2 ij) {
+            const int i = ij[0], j = ij[1];
+            if (mixed) ttg_mixed_record_trsm(P->mixed, i, j);
+            else
+                gpu::cblas_dtrsm(gpu::CblasColMajor, gpu::CblasRight, gpu::CblasLower, gpu::CblasTrans, gpu::CblasNonUnit,
+                                 P->bs[i], P->bs[j], 1.0, block(j, j), lda(j), block(i, j), lda(i));
+        })
+        .set_fulfill([&](Key2 ij) {
+            const int i = ij[0], j = ij[1];
+            for (int k = j + 1; k < i; k++) gemm.fulfill_promise({j, i, k});
+            for (int k = i; k < nb; k++) gemm.fulfill_promise({j, k, i});
+        })
+        .set_indegree([&](Key2 ij) { return accumulate ? 1 + ij[1] : 1 + (ij[1] == 0 ? 0 : 1); })
+        .set_priority(trsm_block_2_prio)
+        .set_mapping([&](Key2 ij) { return block_2_thread(ij[0], ij[1]); })
+        .set_name([](Key2 ij) { return "TRSM_" + std::to_string(ij[0]) + "_" + std::to_string(ij[1]); });
+
+    gemm.set_task([&](Key3 kij) {
+            const int k = kij[0], i = kij[1], j = kij[2];
+            double* C = accumulate ? tmp_of[{k, i, j}] : block(i, j);
+            const double beta = accumulate ? 0.0 : 1.0;
+            if (mixed) {
+                ttg_mixed_record_update(P->mixed, k, i, j);
+            } else if (i == j) {
+                gpu::cblas_dsyrk(gpu::CblasColMajor, gpu::CblasLower, gpu::CblasNoTrans, P->bs[i], P->bs[k], -1.0, block(i, k),
+                                 lda(i), beta, C, lda(i));
+            } else {
+                gpu::cblas_dgemm(gpu::CblasColMajor, gpu::CblasNoTrans, gpu::CblasTrans, P->bs[i], P->bs[j], P->bs[k], -1.0,
+                                 block(i, k), lda(i), block(j, k), lda(j), beta, C, lda(i));
+            }
+        })
+        .set_fulfill([&](Key3 kij) {
+            const int k = kij[0], i = kij[1], j = kij[2];
+            if (accumulate) {
+                accu.fulfill_promise(kij);
+            } else if (k < j - 1) {
+                gemm.fulfill_promise({k + 1, i, j});
+            } else if (i == j) {
+                potrf.fulfill_promise(i);
+            } else {
+                trsm.fulfill_promise({i, j});
+            }
+        })
+        .set_indegree([&](Key3 kij) {
+            if (accumulate) return kij[1] == kij[2] ? 1 : 2;
+            return (kij[1] == kij[2] ? 1 : 2) + (kij[0] == 0 ? 0 : 1);
+        })
+        .set_priority(gemm_block_2_prio)
+        .set_mapping([&](Key3 kij) { return block_2_thread(kij[1], kij[2]); })
+        .set_binding([](Key3) { return false; })
+        .set_name([](Key3 kij) {
+            return "GEMM_" + std::to_string(kij[0]) + "_" + std::to_string(kij[1]) + "_" + std::to_string(kij[2]);
+        });
+
+    accu.set_task([&](Key3 kij) {
+            const int k = kij[0], i = kij[1], j = kij[2];
+            gpu::geadd(P->bs[i], P->bs[j], 1.0, tmp_of[{k, i, j}], lda(i), 1.0, block(i, j), lda(i));
+        })
+        .set_fulfill([&](Key3 kij) {
+            if (kij[1] == kij[2]) potrf.fulfill_promise(kij[1]);
+            else trsm.fulfill_promise({kij[1], kij[2]});
+        })
+        .set_indegree([](Key3) { return 1; })
+        .set_mapping([&](Key3 kij) { return block_2_thread(kij[1], kij[2]); })
+        .set_priority(gemm_block_2_prio)
+        .set_binding([](Key3) { return true; })
+        .set_name([](Key3 kij) {
+            return "ACCU_" + std::to_string(kij[0]) + "_" + std::to_string(kij[1]) + "_" + std::to_string(kij[2]);
+        });
+
+    // Capture: seed potrf(0) and run the closures on the host; join() would
+    // also execute on the device — here the graph is only built, the plan
+    // runs it later (ttg_chol_plan_factor).
+    potrf.fulfill_promise(0);
+    try {
+        if (dry) tp.capture_dry();
+        else tp.capture_only();
+    } catch (const std::exception& e) {
+        fprintf(stderr, "ttg_chol_plan: %s\n", e.what());
+        return TTG_EINVAL;
+    }
+    if (dry) return TTG_OK;
+    // Kind of each device task, from the captured names' prefixes.
+    const auto& nodes = tp.device_task_nodes();
+    P->kind_of_dev.resize(nodes.size());
+    for (size_t d = 0; d < nodes.size(); ++d) {
+        const std::string nm = tp.node_name(nodes[d]);
+        P->kind_of_dev[d] = nm[0] == 'P' ? 0 : nm[0] == 'T' ? 1 : nm[0] == 'G' ? 2 : nm[0] == 'A' ? 3 : -1;
+    }
+    return TTG_OK;
+}
+
+extern "C" ttg_status ttg_chol_plan_create(ttg_ctx* ctx, const ttg_chol_args* args, ttg_chol_plan** out) {
+    if (!ctx || !args || !out) return TTG_EINVAL;
+    *out = nullptr;
+    if (args->block_size <= 0 || args->num_blocks <= 0 || args->n_threads <= 0) return TTG_EINVAL;
+    if (args->precision != TTG_PREC_F64 && args->precision != TTG_PREC_MIXED) return TTG_EINVAL;
+    if (args->precision == TTG_PREC_MIXED && args->accumulate) return TTG_EINVAL;
+    std::unique_ptr<ttg_chol_plan> P(new ttg_chol_plan());
+    P->ctx = ctx;
+    P->args = *args;
+    if (!cholesky_block_sizes(args->block_size, args->num_blocks, args->upper_block_size, P->bs)) return TTG_EINVAL;
+    P->nb = args->num_blocks;
+    P->displ.assign(P->nb + 1, 0);
+    for (int i = 0; i < P->nb; ++i) P->displ[i + 1] = P->displ[i] + P->bs[i];
+    P->N = P->displ[P->nb];
+    P->off.assign((size_t)P->nb * P->nb, 0);
+    P->elems = ttg_tile_layout(P->bs.data(), P->nb, P->off.data());
+    TTG_CUDA_CHECK(cudaSetDevice(ctx->device));
+    TTG_CUDA_CHECK(cudaMalloc((void**)&P->tiles, sizeof(double) * std::max<int64_t>(1, P->elems)));
+    TTG_CUDA_CHECK(cudaMalloc((void**)&P->pristine, sizeof(double) * std::max<int64_t>(1, P->elems)));
+    if (args->precision == TTG_PREC_MIXED) {
+        ttg_status s = ttg_mixed_state_create(ctx, P->N, P->nb, P->bs.data(), P->off.data(), P->tiles, args->mixed_kind, &P->mixed);
+        if (s != TTG_OK) return s;
+    }
+    ttg_status s = chol_build_graph(P.get(), false);
+    if (s != TTG_OK) {
+        ttg_chol_plan_destroy(P.release());
+        return s;
+    }
+    s = ttg_chol_plan_generate(P.get(), nullptr);
+    if (s != TTG_OK) {
+        ttg_chol_plan_destroy(P.release());
+        return s;
+    }
+    *out = P.release();
+    return TTG_OK;
+}
+
+// Capture the Cholesky graph without a device and write its DAG record.
+extern "C" ttg_status ttg_chol_dag_dump(const ttg_chol_args* args, const char* prefix) {
+    if (!args || !prefix || args->block_size <= 0 || args->num_blocks <= 0 || args->n_threads <= 0) return TTG_EINVAL;
+    if (args->precision != TTG_PREC_F64) return TTG_EINVAL;
+    ttg_chol_plan P;
+    P.args = *args;
+    if (!cholesky_block_sizes(args->block_size, args->num_blocks, args->upper_block_size, P.bs)) return TTG_EINVAL;
+    P.nb = args->num_blocks;
+    P.off.assign((size_t)P.nb * P.nb, 0);
+    P.elems = ttg_tile_layout(P.bs.data(), P.nb, P.off.data());
+    ttg_status s = chol_build_graph(&P, true);
+    if (s != TTG_OK) return s;
+    P.tp->dump_dag(prefix);
+    return TTG_OK;
+}
+
+extern "C" ttg_status ttg_chol_plan_destroy(ttg_chol_plan* P) {
+    if (!P) return TTG_OK;
+    cudaSetDevice(P->ctx->device);
+    P->tp.reset();
+    for (double* t : P->tmp) cudaFree(t);
+    if (P->tiles) cudaFree(P->tiles);
+    if (P->pristine) cudaFree(P->pristine);
+    if (P->mixed) ttg_mixed_state_destroy(P->mixed);
+    delete P;
+    return TTG_OK;
+}
+
+extern "C" int32_t ttg_chol_plan_n(const ttg_chol_plan* P, int32_t* h_bs) {
+    if (!P) return 0;
+    if (h_bs)
+        for (int i = 0; i < P->nb; ++i) h_bs[i] = P->bs[i];
+    return P->N;
+}
+
+extern "C" int32_t ttg_chol_plan_tasks(const ttg_chol_plan* P, double* capture_s) {
+    if (!P) return 0;
+    if (capture_s) *capture_s = P->tp->capture_seconds();
+    return P->tp->n_device_tasks();
+}
+
+extern "C" double* ttg_chol_plan_tiles(ttg_chol_plan* P, const int64_t** h_off) {
+    if (!P) return nullptr;
+    if (h_off) *h_off = P->off.data();
+    return P->tiles;
+}
+
+extern "C" ttg_status ttg_chol_plan_generate(ttg_chol_plan* P, void* stream) {
+    if (!P) return TTG_EINVAL;
+    ttg_status s;
+    if (P->args.matrix == 1)
+        s = ttg_gen_gram_tiles(P->ctx, P->N, P->bs.data(), P->nb, P->args.alpha, P->args.seed, P->pristine, stream);
+    else
+        s = ttg_gen_miniapp_tiles(P->ctx, P->bs.data(), P->nb, P->pristine, stream);
+    if (s != TTG_OK) return s;
+    return ttg_chol_plan_restore(P, stream);
+}
+
+// Copy the lower tiles of a dense host matrix into device tiles.
+static ttg_status dense_to_tiles(const ttg_chol_plan* P, const double* h_A, double* d_tiles, cudaStream_t s) {
+    for (int j = 0; j < P->nb; ++j)
+        for (int i = j; i < P->nb; ++i) {
+            if (P->bs[i] == 0 || P->bs[j] == 0) continue;
+            TTG_CUDA_CHECK(cudaMemcpy2DAsync(d_tiles + P->off[i + (size_t)j * P->nb], sizeof(double) * P->bs[i],
+                                             h_A + P->displ[i] + (size_t)P->displ[j] * P->N, sizeof(double) * P->N,
+                                             sizeof(double) * P->bs[i], P->bs[j], cudaMemcpyHostToDevice, s));
+        }
+    return TTG_OK;
+}
+
+static ttg_status tiles_to_dense(const ttg_chol_plan* P, const double* d_tiles, double* h_A, cudaStream_t s) {
+    for (int j = 0; j < P->nb; ++j)
+        for (int i = j; i < P->nb; ++i) {
+            if (P->bs[i] == 0 || P->bs[j] == 0) continue;
+            TTG_CUDA_CHECK(cudaMemcpy2DAsync(h_A + P->displ[i] + (size_t)P->displ[j] * P->N, sizeof(double) * P->N,
+                                             d_tiles + P->off[i + (size_t)j * P->nb], sizeof(double) * P->bs[i],
+                                             sizeof(double) * P->bs[i], P->bs[j], cudaMemcpyDeviceToHost, s));
+        }
+    return TTG_OK;
+}
+
+extern "C" ttg_status ttg_chol_plan_set_matrix(ttg_chol_plan* P, const double* h_A, void* stream) {
+    if (!P || !h_A) return TTG_EINVAL;
+    TTG_CUDA_CHECK(cudaSetDevice(P->ctx->device));
+    cudaStream_t s = (cudaStream_t)stream;
+    ttg_status st = dense_to_tiles(P, h_A, P->pristine, s);
+    if (st != TTG_OK) return st;
+    TTG_CUDA_CHECK(cudaStreamSynchronize(s));
+    return ttg_chol_plan_restore(P, stream);
+}
+
+extern "C" ttg_status ttg_chol_plan_restore(ttg_chol_plan* P, void* stream) {
+    if (!P) return TTG_EINVAL;
+    TTG_CUDA_CHECK(cudaSetDevice(P->ctx->device));
+    TTG_CUDA_CHECK(cudaMemcpyAsync(P->tiles, P->pristine, sizeof(double) * P->elems, cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
+    return TTG_OK;
+}
+
+extern "C" ttg_status ttg_chol_plan_factor(ttg_chol_plan* P, void* stream, ttg_report* rep) {
+    if (!P) return TTG_EINVAL;
+    TTG_CUDA_CHECK(cudaSetDevice(P->ctx->device));
+    if (P->mixed) {
+        ttg_status s = ttg_mixed_prepare(P->mixed, stream);
+        if (s != TTG_OK) return s;
+    }
+    ttg_status s = P->tp->replay(stream);
+    if (rep) *rep = P->tp->report();
+    return s;
+}
+
+extern "C" ttg_status ttg_chol_factor_host(ttg_chol_plan* P, const double* h_A, double* h_L, void* stream, ttg_report* rep) {
+    if (!P || !h_A) return TTG_EINVAL;
+    TTG_CUDA_CHECK(cudaSetDevice(P->ctx->device));
+    cudaStream_t s = (cudaStream_t)stream;
+    ttg_status st = dense_to_tiles(P, h_A, P->tiles, s);
+    if (st != TTG_OK) return st;
+    st = ttg_chol_plan_factor(P, stream, rep);
+    if (st != TTG_OK) return st;
+    if (h_L) {
+        st = tiles_to_dense(P, P->tiles, h_L, s);
+        if (st != TTG_OK) return st;
+        TTG_CUDA_CHECK(cudaStreamSynchronize(s));
+        for (int j = 0; j < P->N; ++j) std::fill(h_L + (size_t)j * P->N, h_L + (size_t)j * P->N + j, 0.0);
+    }
+    return TTG_OK;
+}
+
+extern "C" ttg_status ttg_chol_plan_get_factor(ttg_chol_plan* P, double* h_L) {
+    if (!P || !h_L) return TTG_EINVAL;
+    TTG_CUDA_CHECK(cudaSetDevice(P->ctx->device));
+    const double* src = P->tiles;
+    if (P->mixed) src = ttg_mixed_factor_tiles(P->mixed);
+    ttg_status st = tiles_to_dense(P, src, h_L, nullptr);
+    if (st != TTG_OK) return st;
+    TTG_CUDA_CHECK(cudaStreamSynchronize(nullptr));
+    for (int j = 0; j < P->N; ++j) std::fill(h_L + (size_t)j * P->N, h_L + (size_t)j * P->N + j, 0.0);
+    return TTG_OK;
+}
+
+extern "C" ttg_status ttg_chol_plan_get_input(ttg_chol_plan* P, double* h_A) {
+    if (!P || !h_A) return TTG_EINVAL;
+    TTG_CUDA_CHECK(cudaSetDevice(P->ctx->device));
+    ttg_status st = tiles_to_dense(P, P->pristine, h_A, nullptr);
+    if (st != TTG_OK) return st;
+    TTG_CUDA_CHECK(cudaStreamSynchronize(nullptr));
+    for (int j = 0; j < P->N; ++j)
+        for (int i = 0; i < j; ++i) h_A[i + (size_t)j * P->N] = h_A[j + (size_t)i * P->N];
+    return TTG_OK;
+}
+
+extern "C" ttg_status ttg_chol_plan_dump_dag(ttg_chol_plan* P, const char* prefix) {
+    if (!P || !prefix) return TTG_EINVAL;
+    P->tp->dump_dag(prefix);
+    return TTG_OK;
+}
+
+extern "C" ttg_status ttg_chol_plan_kind_times(ttg_chol_plan* P, double* potrf_ms, double* trsm_ms, double* gemm_ms, double* accu_ms) {
+    if (!P) return TTG_EINVAL;
+    const int nd = (int)P->kind_of_dev.size();
+    std::vector<int64_t> s(nd), e(nd);
+    ttg_status st = ttg_trace(P->ctx, s.data(), e.data(), nullptr);
+    if (st != TTG_OK) return st;
+    double t[4] = {0, 0, 0, 0};
+    for (int d = 0; d < nd; ++d)
+        if (s[d] >= 0 && P->kind_of_dev[d] >= 0) t[P->kind_of_dev[d]] += (e[d] - s[d]) * 1e-6;
+    if (potrf_ms) *potrf_ms = t[0];
+    if (trsm_ms) *trsm_ms = t[1];
+    if (gemm_ms) *gemm_ms = t[2];
+    if (accu_ms) *accu_ms = t[3];
+    return TTG_OK;
+}
+
+// ------------------------------------------------------------------ GEMM
+
+struct ttg_gemm_plan {
+    ttg_ctx* ctx = nullptr;
+    ttg_gemm_args args{};
+    int N = 0, b = 0, nb = 0;
+    double *A = nullptr, *B = nullptr, *C = nullptr;  // tiles, b×b each, tile (i,j) at (i + j·nb)·b²
+    std::unique_ptr<Threadpool_shared> tp;
+};
+
+static ttg_status gemm_build_graph(ttg_gemm_plan* Pp, bool dry) {
+    const ttg_gemm_args* a = &Pp->args;
+    const int nb = Pp->nb, b = Pp->b, n_threads = a->n_threads;
+    auto tile = [Pp](double* M, int i, int j) { return M + ((size_t)i + (size_t)j * Pp->nb) * Pp->b * Pp->b; };
+    Pp->tp.reset(new Threadpool_shared(n_threads, a->verb, "Wk_Gemm_0_"));
+    Threadpool_shared& tp = *Pp->tp;
+    if (!dry) tp.set_context(Pp->ctx);
+    Taskflow<Key2> send_Aij(&tp, a->verb);
+    Taskflow<Key2> send_Bij(&tp, a->verb);
+    Taskflow<Key3> gemm_Cikj(&tp, a->verb);
+
+    send_Aij.set_task([&](Key2 ij) {
+                for (int k = 0; k < nb; k++) gemm_Cikj.fulfill_promise({ij[0], ij[1], k});
+            })
+        .set_indegree([](Key2) { return 1; })
+        .set_priority([&](Key2 ij) { return (double)(nb - ij[1]); })
+        .set_mapping([&](Key2 ij) { return (ij[0] + ij[1] * nb) % n_threads; })
+        .set_name([](Key2 ij) { return "send_A_" + std::to_string(ij[0]) + "_" + std::to_string(ij[1]); });
+
+    send_Bij.set_task([&](Key2 ij) {
+                for (int k = 0; k < nb; k++) gemm_Cikj.fulfill_promise({k, ij[0], ij[1]});
+            })
+        .set_indegree([](Key2) { return 1; })
+        .set_priority([&](Key2 ij) { return (double)(nb - ij[0]); })
+        .set_mapping([&](Key2 ij) { return (ij[0] + ij[1] * nb) % n_threads; })
+        .set_name([](Key2 ij) { return "send_B_" + std::to_string(ij[0]) + "_" + std::to_string(ij[1]); });
+
+    gemm_Cikj.set_task([&](Key3 ikj) {
+                 const int i = ikj[0], k = ikj[1], j = ikj[2];
+                 gpu::cblas_dgemm(gpu::CblasColMajor, gpu::CblasNoTrans, gpu::CblasNoTrans, b, b, b, 1.0, tile(Pp->A, i, k), b,
+                                  tile(Pp->B, k, j), b, 1.0, tile(Pp->C, i, j), b);
+                 if (k < nb - 1) gemm_Cikj.fulfill_promise({i, k + 1, j});
+             })
+        .set_indegree([](Key3 ikj) { return ikj[1] == 0 ? 2 : 3; })
+        .set_mapping([&](Key3 ikj) { return (ikj[0] + ikj[2] * nb) % n_threads; })
+        .set_name([](Key3 ikj) {
+            return "prod_C_" + std::to_string(ikj[0]) + "_" + std::to_string(ikj[1]) + "_" + std::to_string(ikj[2]);
+        });
+
+    for (int i = 0; i < nb; i++)
+        for (int j = 0; j < nb; j++) {
+            send_Aij.fulfill_promise({i, j});
+            send_Bij.fulfill_promise({i, j});
+        }
+    try {
+        if (dry) tp.capture_dry();
+        else tp.capture_only();
+    } catch (const std::exception& e) {
+        fprintf(stderr, "ttg_gemm_plan: %s\n", e.what());
+        return TTG_EINVAL;
+    }
+    return TTG_OK;
+}
+
+// Capture the block GEMM graph without a device and write its DAG record.
+extern "C" ttg_status ttg_gemm_dag_dump(const ttg_gemm_args* a, const char* prefix) {
+    if (!a || !prefix || a->block_size <= 0 || a->matrix_size <= 0 || a->matrix_size % a->block_size != 0 || a->n_threads <= 0)
+        return TTG_EINVAL;
+    ttg_gemm_plan P;
+    P.args = *a;
+    P.N = a->matrix_size;
+    P.b = a->block_size;
+    P.nb = P.N / P.b;
+    ttg_status s = gemm_build_graph(&P, true);
+    if (s != TTG_OK) return s;
+    P.tp->dump_dag(prefix);
+    return TTG_OK;
+}
+
+extern "C" ttg_status ttg_gemm_plan_create(ttg_ctx* ctx, const ttg_gemm_args* a, ttg_gemm_plan** out) {
+    if (!ctx || !a || !out) return TTG_EINVAL;
+    *out = nullptr;
+    if (a->block_size <= 0 || a->matrix_size <= 0 || a->matrix_size % a->block_size != 0 || a->n_threads <= 0)
+        return TTG_EINVAL;
+    std::unique_ptr<ttg_gemm_plan> P(new ttg_gemm_plan());
+    P->ctx = ctx;
+    P->args = *a;
+    P->N = a->matrix_size;
+    P->b = a->block_size;
+    P->nb = P->N / P->b;
+    const size_t elems = (size_t)P->N * P->N;
+    TTG_CUDA_CHECK(cudaSetDevice(ctx->device));
+    TTG_CUDA_CHECK(cudaMalloc((void**)&P->A, sizeof(double) * elems));
+    TTG_CUDA_CHECK(cudaMalloc((void**)&P->B, sizeof(double) * elems));
+    TTG_CUDA_CHECK(cudaMalloc((void**)&P->C, sizeof(double) * elems));
+    // Inputs in tile layout: val_global (gemm_shared.hpp:74-76, A = B) or
+    // iid U[-1,1] (A from stream 2, B from stream 3 of the seed).
+    {
+        ttg_status s = ttg_gen_gemm_tiles(ctx, P->N, P->b, a->inputs, a->seed, P->A, P->B, nullptr);
+        if (s != TTG_OK) return s;
+    }
+    ttg_status st = gemm_build_graph(P.get(), false);
+    if (st != TTG_OK) {
+        ttg_gemm_plan_destroy(P.release());
+        return st;
+    }
+    *out = P.release();
+    return TTG_OK;
+}
+
+extern "C" ttg_status ttg_gemm_plan_destroy(ttg_gemm_plan* P) {
+    if (!P) return TTG_OK;
+    cudaSetDevice(P->ctx->device);
+    P->tp.reset();
+    if (P->A) cudaFree(P->A);
+    if (P->B) cudaFree(P->B);
+    if (P->C) cudaFree(P->C);
+    delete P;
+    return TTG_OK;
+}
+
+extern "C" int32_t ttg_gemm_plan_tasks(const ttg_gemm_plan* P, double* capture_s) {
+    if (!P) return 0;
+    if (capture_s) *capture_s = P->tp->capture_seconds();
+    return P->tp->n_device_tasks();
+}
+
+extern "C" ttg_status ttg_gemm_plan_run(ttg_gemm_plan* P, void* stream, ttg_report* rep) {
+    if (!P) return TTG_EINVAL;
+    TTG_CUDA_CHECK(cudaSetDevice(P->ctx->device));
+    TTG_CUDA_CHECK(cudaMemsetAsync(P->C, 0, sizeof(double) * (size_t)P->N * P->N, (cudaStream_t)stream));
+    ttg_status s = P->tp->replay(stream);
+    if (rep) *rep = P->tp->report();
+    return s;
+}
+
+// Dense column-major N×N host matrix <-> tiles (b×b, tile (i,j) at (i + j·nb)·b²).
+static ttg_status gemm_dense_to_tiles(const ttg_gemm_plan* P, const double* h, double* d, cudaStream_t s) {
+    for (int j = 0; j < P->nb; ++j)
+        for (int i = 0; i < P->nb; ++i)
+            TTG_CUDA_CHECK(cudaMemcpy2DAsync(d + ((size_t)i + (size_t)j * P->nb) * P->b * P->b, sizeof(double) * P->b,
+                                             h + (size_t)i * P->b + (size_t)j * P->b * P->N, sizeof(double) * P->N,
+                                             sizeof(double) * P->b, P->b, cudaMemcpyHostToDevice, s));
+    return TTG_OK;
+}
+
+static ttg_status gemm_tiles_to_dense(const ttg_gemm_plan* P, const double* d, double* h, cudaStream_t s) {
+    for (int j = 0; j < P->nb; ++j)
+        for (int i = 0; i < P->nb; ++i)
+            TTG_CUDA_CHECK(cudaMemcpy2DAsync(h + (size_t)i * P->b + (size_t)j * P->b * P->N, sizeof(double) * P->N,
+                                             d + ((size_t)i + (size_t)j * P->nb) * P->b * P->b, sizeof(double) * P->b,
+                                             sizeof(double) * P->b, P->b, cudaMemcpyDeviceToHost, s));
+    return TTG_OK;
+}
+
+extern "C" ttg_status ttg_gemm_host(ttg_gemm_plan* P, const double* h_A, const double* h_B, double* h_C, void* stream,
+                                    ttg_report* rep) {
+    if (!P || !h_A || !h_B) return TTG_EINVAL;
+    TTG_CUDA_CHECK(cudaSetDevice(P->ctx->device));
+    cudaStream_t s = (cudaStream_t)stream;
+    ttg_status st = gemm_dense_to_tiles(P, h_A, P->A, s);
+    if (st == TTG_OK) st = gemm_dense_to_tiles(P, h_B, P->B, s);
+    if (st == TTG_OK) st = ttg_gemm_plan_run(P, stream, rep);
+    if (st == TTG_OK && h_C) {
+        st = gemm_tiles_to_dense(P, P->C, h_C, s);
+        if (st == TTG_OK) TTG_CUDA_CHECK(cudaStreamSynchronize(s));
+    }
+    return st;
+}
+
+extern "C" ttg_status ttg_gemm_plan_get_C(ttg_gemm_plan* P, double* h_C) {
+    if (!P || !h_C) return TTG_EINVAL;
+    TTG_CUDA_CHECK(cudaSetDevice(P->ctx->device));
+    ttg_status st = gemm_tiles_to_dense(P, P->C, h_C, nullptr);
+    if (st != TTG_OK) return st;
+    TTG_CUDA_CHECK(cudaStreamSynchronize(nullptr));
+    return TTG_OK;
+}
+
+extern "C" ttg_status ttg_gemm_plan_dump_dag(ttg_gemm_plan* P, const char* prefix) {
+    if (!P || !prefix) return TTG_EINVAL;
+    P->tp->dump_dag(prefix);
+    return TTG_OK;
+}

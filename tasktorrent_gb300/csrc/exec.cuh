@@ -1,0 +1,241 @@
+// exec.cuh — the persistent task-graph executor (replaces ttor::Threadpool_shared).
+//
+// Reference behaviour kept (tasktorrent/src/threadpool_shared.cpp):
+//   - a task runs once its dependency counter reaches zero, then its
+//     fulfill() decrements its successors (Taskflow::fulfill_promise,
+//     taskflow.hpp:241-296) — here the successor lists are the edges recorded
+//     on the host and the decrement is an atomicSub on a device counter;
+//   - higher priority runs first (less_pTask, tasks.cpp:13-16) — here 32
+//     priority levels, each a FIFO, scanned by the 32 lanes of warp 0;
+//   - bound tasks run only on their mapped worker (insert(.., binding=true),
+//     threadpool_shared.cpp:214-223) — here a per-worker queue;
+//   - completion when no task is left (test_completion, :73-79) — here when the
+//     completed count reaches the number of runnable tasks;
+//   - a negative count is an error (taskflow.hpp:278-282) — here an atomicSub
+//     that finds a counter already at zero sets TTG_EOVERCOUNT.
+// Every wait is bounded: a worker that sees no progress for timeout_ns sets
+// TTG_ETIMEOUT and returns; nothing traps.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/ttg.h"
+
+namespace ttg {
+
+constexpr int kMaxLevels = 32;
+
+struct ExecParams {
+    const ttg_op* ops;
+    int n_tasks;      // tasks in the graph
+    int n_runnable;   // tasks that will reach zero
+    int* count;       // dependency counters
+    int* runs;        // per-task run count
+    const int64_t* succ_ptr;
+    const int32_t* succ_idx;
+    const uint8_t* level;   // priority level, 0 = highest
+    const int32_t* bind;    // -1 or worker
+    int n_levels;
+    int n_workers;
+    int* qbuf;              // all level queues back to back
+    const int* q_off;       // [n_levels + 1]
+    int* q_head;            // [kMaxLevels * 32] (one 128-byte line per level)
+    int* q_tail;
+    int* bq_buf;            // per-worker bound queues back to back
+    const int* bq_off;      // [n_workers + 1]
+    int* bq_head;           // [n_workers]
+    int* bq_tail;
+    int has_bound;
+    int* done;              // completed tasks
+    int* err;               // first error status
+    int* err_task;
+    int* err_info;
+    long long* trace;       // [3 * n_tasks] start, end, worker; or null
+    long long timeout_ns;
+};
+
+__device__ __forceinline__ long long globaltimer() {
+    long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ int ld_volatile(const int* p) { return *(const volatile int*)p; }
+__device__ __forceinline__ void st_volatile(int* p, int v) { *(volatile int*)p = v; }
+
+__device__ __forceinline__ void set_error(const ExecParams& p, int status, int task, int info) {
+    if (atomicCAS(p.err, 0, status) == 0) {
+        *p.err_task = task;
+        *p.err_info = info;
+    }
+}
+
+// Wait for a reserved queue slot to be written by its producer.  Returns the
+// task id, or -1 after timeout (error already set).
+__device__ inline int wait_slot(const ExecParams& p, int* slot) {
+    long long t0 = 0;
+    for (int it = 0;; ++it) {
+        int v = ld_volatile(slot);
+        if (v >= 0) return v;
+        if ((it & 63) == 0) {
+            long long now = globaltimer();
+            if (it == 0) t0 = now;
+            else if (now - t0 > p.timeout_ns) {
+                set_error(p, TTG_ETIMEOUT, -1, 0);
+                return -1;
+            }
+        }
+    }
+}
+
+// Called by all lanes of warp 0.  Returns a claimed task id, or -1 to exit.
+__device__ inline int claim_task(const ExecParams& p) {
+    const int lane = threadIdx.x & 31;
+    const int w = blockIdx.x;
+    int last_done = -1;
+    long long idle_since = 0;
+    {
+        int e = 0;
+        if (lane == 0) e = ld_volatile(p.err);
+        if (__shfl_sync(0xffffffffu, e, 0) != 0) return -1;
+    }
+    for (unsigned spin = 0;; ++spin) {
+        if (p.has_bound) {
+            int task = -1;
+            if (lane == 0) {
+                const int h = p.bq_head[w];
+                if (h < ld_volatile(p.bq_tail + w)) {
+                    task = wait_slot(p, p.bq_buf + p.bq_off[w] + h);
+                    if (task >= 0) p.bq_head[w] = h + 1;
+                    else task = -2;
+                }
+            }
+            task = __shfl_sync(0xffffffffu, task, 0);
+            if (task == -2) return -1;
+            if (task >= 0) {
+                __threadfence();
+                return task;
+            }
+        }
+        int h = 0, t = 0;
+        if (lane < p.n_levels) {
+            h = ld_volatile(p.q_head + lane * 32);
+            t = ld_volatile(p.q_tail + lane * 32);
+        }
+        const unsigned mask = __ballot_sync(0xffffffffu, lane < p.n_levels && h < t);
+        if (mask) {
+            const int lvl = __ffs(mask) - 1;
+            int got = -1;
+            if (lane == lvl) {
+                if (atomicCAS(p.q_head + lvl * 32, h, h + 1) == h) {
+                    got = wait_slot(p, p.qbuf + p.q_off[lvl] + h);
+                    if (got < 0) got = -2;
+                }
+            }
+            got = __shfl_sync(0xffffffffu, got, lvl);
+            if (got == -2) return -1;
+            if (got >= 0) {
+                __threadfence();
+                return got;
+            }
+            continue;  // lost the race for this slot; rescan at once
+        }
+        int d = 0, e = 0;
+        if (lane == 0) {
+            d = ld_volatile(p.done);
+            e = ld_volatile(p.err);
+        }
+        d = __shfl_sync(0xffffffffu, d, 0);
+        e = __shfl_sync(0xffffffffu, e, 0);
+        if (d >= p.n_runnable || e != 0) return -1;
+        long long now = 0;
+        if (lane == 0) now = globaltimer();
+        now = __shfl_sync(0xffffffffu, now, 0);
+        if (d != last_done) {
+            last_done = d;
+            idle_since = now;
+        } else if (now - idle_since > p.timeout_ns) {
+            if (lane == 0) set_error(p, TTG_ETIMEOUT, -1, 0);
+            return -1;
+        }
+        __nanosleep(spin < 64 ? 32 : 256);
+    }
+}
+
+__device__ __forceinline__ void push_ready(const ExecParams& p, int s) {
+    const int b = p.bind[s];
+    // Every task is pushed at most once (only the decrement that finds the
+    // counter at one pushes), so a queue never outgrows the number of tasks
+    // assigned to it; the bound checks below only guard against a corrupted
+    // graph.
+    if (b >= 0) {
+        const int w = b % p.n_workers;
+        const int slot = atomicAdd(p.bq_tail + w, 1);
+        if (p.bq_off[w] + slot < p.bq_off[w + 1]) st_volatile(p.bq_buf + p.bq_off[w] + slot, s);
+        else set_error(p, TTG_EOVERCOUNT, s, 0);
+    } else {
+        const int lvl = p.level[s];
+        const int slot = atomicAdd(p.q_tail + lvl * 32, 1);
+        if (p.q_off[lvl] + slot < p.q_off[lvl + 1]) st_volatile(p.qbuf + p.q_off[lvl] + slot, s);
+        else set_error(p, TTG_EOVERCOUNT, s, 0);
+    }
+}
+
+// Called by all lanes of warp 0 after the block finished task t.
+__device__ inline void fulfil_successors(const ExecParams& p, int t) {
+    const int lane = threadIdx.x & 31;
+    __threadfence();  // release the tile writes of the whole block (after bar.sync)
+    const int64_t e0 = p.succ_ptr[t], e1 = p.succ_ptr[t + 1];
+    for (int64_t e = e0 + lane; e < e1; e += 32) {
+        const int s = p.succ_idx[e];
+        const int old = atomicSub(p.count + s, 1);
+        if (old == 1) {
+            __threadfence();
+            push_ready(p, s);
+        } else if (old < 1) {
+            set_error(p, TTG_EOVERCOUNT, s, 0);
+        }
+    }
+    __syncwarp();
+    if (lane == 0) {
+        atomicAdd(p.runs + t, 1);
+        __threadfence();
+        atomicAdd(p.done, 1);
+    }
+}
+
+// The persistent kernel body: `RunOp(op, smem)` runs one tile task on the
+// whole block and returns 0 or an error info (POTRF failing column).
+template <class RunOp>
+__device__ void executor_loop(const ExecParams& p, double* smem, RunOp run_op) {
+    __shared__ int s_task;
+    __shared__ int s_info;
+    for (;;) {
+        if (threadIdx.x < 32) {
+            const int t = claim_task(p);
+            if (threadIdx.x == 0) {
+                s_task = t;
+                if (t >= 0 && p.trace) p.trace[3 * (size_t)t] = globaltimer();
+            }
+        }
+        __syncthreads();
+        const int t = s_task;
+        if (t < 0) break;
+        const ttg_op op = p.ops[t];
+        const int info = run_op(op, smem);
+        if (threadIdx.x == 0) s_info = info;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            if (threadIdx.x == 0) {
+                if (s_info != 0) set_error(p, TTG_ENOTPD, t, s_info);
+                if (p.trace) {
+                    p.trace[3 * (size_t)t + 1] = globaltimer();
+                    p.trace[3 * (size_t)t + 2] = blockIdx.x;
+                }
+            }
+            fulfil_successors(p, t);
+        }
+    }
+}
+
+}  // namespace ttg

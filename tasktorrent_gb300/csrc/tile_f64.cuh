@@ -1,0 +1,231 @@
+// tile_f64.cuh — FP64 tile kernels run by one block of the persistent executor.
+//
+// Each function is executed by all kThreads threads of a block on one tile task
+// and replaces one BLAS/LAPACK call of the reference's task bodies:
+//   potrf_l_f64   LAPACKE_dpotrf(COL_MAJOR,'L')      2d_cholesky.cpp:319
+//   trsm_rltn_f64 cblas_dtrsm(Right,Lower,Trans,NonUnit) 2d_cholesky.cpp:404-405
+//   gemm_f64<..., LOWER=true>  cblas_dsyrk(Lower,NoTrans) 2d_cholesky.cpp:490-491
+//   gemm_f64<NT>  cblas_dgemm(NoTrans,Trans)         2d_cholesky.cpp:493-494
+//   gemm_f64<NN>  cblas_dgemm(NoTrans,NoTrans)       2d_gemm.cpp:157
+//
+// The FP64 rate of a GB300 SM is a few DFMA per clock, so these kernels are
+// built to keep the DFMA pipe busy (8×8 register blocking, 64 independent
+// accumulators per thread) rather than to save bandwidth.  Tiles written by
+// other blocks are read through L2 only (ld.global.cg): a persistent block can
+// hold stale L1 lines of a tile another block has since updated.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ttg {
+
+constexpr int kThreads = 256;
+constexpr int kBM = 128, kBN = 128, kBK = 16;
+constexpr int kBNP = kBN + 1;  // padded row of the B stage (conflict-free transposed store)
+constexpr int kPanel = 32;     // POTRF / TRSM panel width
+// Shared memory used by the FP64 kernels (doubles).
+constexpr int kF64SmemDoubles = kBK * kBM + kBK * kBNP + kPanel * (kPanel + 1);
+
+__device__ __forceinline__ double ldcg(const double* p) { return __ldcg(p); }
+
+// C[m×n] = alpha·A·op(B) + beta·C on the block.  A is m×k (lda).  op(B)(kk,j)
+// is B[j + kk·ldb] (B_NN = false: B is n×k, "NT") or B[kk + j·ldb] (B_NN =
+// true: B is k×n, "NN").  LOWER restricts the update to i >= j (SYRK, m == n).
+// beta == 0 never reads C, as in BLAS.
+template <bool B_NN, bool LOWER>
+__device__ void gemm_f64(int m, int n, int k, double alpha, const double* __restrict__ A, int lda,
+                         const double* __restrict__ B, int ldb, double beta, double* C, int ldc, double* smem) {
+    double(*As)[kBM] = reinterpret_cast<double(*)[kBM]>(smem);
+    double(*Bs)[kBNP] = reinterpret_cast<double(*)[kBNP]>(smem + kBK * kBM);
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    for (int m0 = 0; m0 < m; m0 += kBM) {
+        for (int n0 = 0; n0 < n; n0 += kBN) {
+            if (LOWER && n0 > m0 + kBM - 1) continue;  // block strictly above the diagonal
+            double acc[8][8];
+#pragma unroll
+            for (int r = 0; r < 8; ++r)
+#pragma unroll
+                for (int c = 0; c < 8; ++c) acc[r][c] = 0.0;
+            for (int k0 = 0; k0 < k; k0 += kBK) {
+#pragma unroll
+                for (int r = 0; r < (kBK * kBM) / kThreads; ++r) {
+                    const int idx = tid + kThreads * r;
+                    const int i = idx & (kBM - 1), kk = idx / kBM;
+                    const int gi = m0 + i, gk = k0 + kk;
+                    As[kk][i] = (gi < m && gk < k) ? ldcg(A + gi + (size_t)gk * lda) : 0.0;
+                }
+#pragma unroll
+                for (int r = 0; r < (kBK * kBN) / kThreads; ++r) {
+                    const int idx = tid + kThreads * r;
+                    int j, kk;
+                    if (B_NN) { kk = idx & (kBK - 1); j = idx / kBK; }
+                    else { j = idx & (kBN - 1); kk = idx / kBN; }
+                    const int gj = n0 + j, gk = k0 + kk;
+                    double v = 0.0;
+                    if (gj < n && gk < k) v = B_NN ? ldcg(B + gk + (size_t)gj * ldb) : ldcg(B + gj + (size_t)gk * ldb);
+                    Bs[kk][j] = v;
+                }
+                __syncthreads();
+#pragma unroll
+                for (int kk = 0; kk < kBK; ++kk) {
+                    double a[8], b[8];
+#pragma unroll
+                    for (int r = 0; r < 8; ++r) a[r] = As[kk][tx + 16 * r];
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) b[c] = Bs[kk][ty + 16 * c];
+#pragma unroll
+                    for (int r = 0; r < 8; ++r)
+#pragma unroll
+                        for (int c = 0; c < 8; ++c) acc[r][c] = fma(a[r], b[c], acc[r][c]);
+                }
+                __syncthreads();
+            }
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                const int gj = n0 + ty + 16 * c;
+#pragma unroll
+                for (int r = 0; r < 8; ++r) {
+                    const int gi = m0 + tx + 16 * r;
+                    if (gi < m && gj < n && (!LOWER || gi >= gj)) {
+                        double* p = C + gi + (size_t)gj * ldc;
+                        double v = alpha * acc[r][c];
+                        if (beta != 0.0) v = fma(beta, ldcg(p), v);
+                        *p = v;
+                    }
+                }
+            }
+        }
+    }
+}
+
+// Unblocked lower Cholesky of the nb×nb (nb <= 32) diagonal block at A (lda)
+// by one warp, lane = row.  Returns 0 or the 1-based failing column.
+__device__ inline int potrf_diag32_warp(double* A, int lda, int nb) {
+    const int lane = threadIdx.x & 31;
+    double r[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) r[j] = (lane < nb && j < nb && j <= lane) ? ldcg(A + lane + (size_t)j * lda) : 0.0;
+    int info = 0;
+#pragma unroll
+    for (int c = 0; c < 32; ++c) {
+        if (c < nb && info == 0) {
+            const double dcc = __shfl_sync(0xffffffffu, r[c], c);
+            if (!(dcc > 0.0)) {
+                info = c + 1;
+            } else {
+                const double d = sqrt(dcc);
+                if (lane == c) r[c] = d;
+                else if (lane > c) r[c] = r[c] / d;
+#pragma unroll
+                for (int j = c + 1; j < 32; ++j) {
+                    const double ljc = __shfl_sync(0xffffffffu, r[c], j);
+                    if (lane >= j) r[j] = fma(-r[c], ljc, r[j]);
+                }
+            }
+        }
+    }
+    if (info == 0) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+            if (lane < nb && j < nb && j <= lane) A[lane + (size_t)j * lda] = r[j];
+    }
+    return info;
+}
+
+// Rows [row0, m) of X[:, 0:nb] (ldx) <- X · Lᵀ⁻¹ with the nb×nb lower block
+// Ls (shared, ld kPanel+1); one thread per row.
+__device__ inline void trsm_rows_panel(double* X, int ldx, int row0, int m, int nb, const double* Ls, double alpha) {
+    for (int i = row0 + threadIdx.x; i < m; i += kThreads) {
+        double x[kPanel];
+#pragma unroll
+        for (int c = 0; c < kPanel; ++c) x[c] = (c < nb) ? alpha * ldcg(X + i + (size_t)c * ldx) : 0.0;
+#pragma unroll
+        for (int c = 0; c < kPanel; ++c) {
+            if (c < nb) {
+                double s = x[c];
+#pragma unroll
+                for (int l = 0; l < c; ++l) s = fma(-x[l], Ls[c * (kPanel + 1) + l], s);
+                x[c] = s / Ls[c * (kPanel + 1) + c];
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < kPanel; ++c)
+            if (c < nb) X[i + (size_t)c * ldx] = x[c];
+    }
+}
+
+// Load the nb×nb lower block at L (ldl) into Ls (ld kPanel+1), zero above.
+__device__ inline void load_panel_block(const double* L, int ldl, int nb, double* Ls) {
+    for (int e = threadIdx.x; e < kPanel * kPanel; e += kThreads) {
+        const int c = e / kPanel, l = e % kPanel;  // Ls[c][l] = L(c, l)
+        Ls[c * (kPanel + 1) + l] = (c < nb && l < nb && l <= c) ? ldcg(L + c + (size_t)l * ldl) : 0.0;
+    }
+}
+
+// In-place lower Cholesky of A[n×n] (right-looking, 32-column panels).
+// Returns 0 or the 1-based failing column (as LAPACK's info).
+__device__ inline int potrf_l_f64(int n, double* A, int lda, double* smem) {
+    __shared__ int s_info;
+    double* Ls = smem + kBK * kBM + kBK * kBNP;
+    for (int p = 0; p < n; p += kPanel) {
+        const int nb = min(kPanel, n - p);
+        double* Dpp = A + p + (size_t)p * lda;
+        if (threadIdx.x < 32) {
+            int info = potrf_diag32_warp(Dpp, lda, nb);
+            if (threadIdx.x == 0) s_info = info ? p + info : 0;
+        }
+        __syncthreads();
+        const int info = s_info;
+        if (info) return info;
+        load_panel_block(Dpp, lda, nb, Ls);
+        __syncthreads();
+        const int rest = n - p - nb;
+        if (rest > 0) {
+            trsm_rows_panel(A + (size_t)p * lda, lda, p + nb, n, nb, Ls, 1.0);
+            __syncthreads();
+            double* P = A + (p + nb) + (size_t)p * lda;
+            gemm_f64<false, true>(rest, rest, nb, -1.0, P, lda, P, lda, 1.0, A + (p + nb) + (size_t)(p + nb) * lda, lda, smem);
+        }
+        __syncthreads();
+    }
+    return 0;
+}
+
+// B[m×n] <- alpha·B·L⁻ᵀ, L n×n lower non-unit (right-looking, 32-column panels).
+__device__ inline void trsm_rltn_f64(int m, int n, double alpha, const double* L, int ldl, double* B, int ldb, double* smem) {
+    double* Ls = smem + kBK * kBM + kBK * kBNP;
+    for (int p = 0; p < n; p += kPanel) {
+        const int nb = min(kPanel, n - p);
+        load_panel_block(L + p + (size_t)p * ldl, ldl, nb, Ls);
+        __syncthreads();
+        // Columns right of p are scaled by alpha when their panel is solved;
+        // the update below subtracts solved (already scaled) columns, so scale
+        // the remaining columns once, before the first update touches them.
+        if (p == 0 && alpha != 1.0 && n > nb) {
+            for (int e = threadIdx.x; e < m * (n - nb); e += kThreads) {
+                const int i = e % m, j = nb + e / m;
+                B[i + (size_t)j * ldb] = alpha * ldcg(B + i + (size_t)j * ldb);
+            }
+        }
+        trsm_rows_panel(B + (size_t)p * ldb, ldb, 0, m, nb, Ls, p == 0 ? alpha : 1.0);
+        __syncthreads();
+        const int rest = n - p - nb;
+        if (rest > 0)
+            gemm_f64<false, false>(m, rest, nb, -1.0, B + (size_t)p * ldb, ldb, L + (p + nb) + (size_t)p * ldl, ldl, 1.0,
+                                   B + (size_t)(p + nb) * ldb, ldb, smem);
+        __syncthreads();
+    }
+}
+
+// C[m×n] <- alpha·A + beta·C.
+__device__ inline void geadd_f64(int m, int n, double alpha, const double* A, int lda, double beta, double* C, int ldc) {
+    for (long e = threadIdx.x; e < (long)m * n; e += kThreads) {
+        const int i = (int)(e % m), j = (int)(e / m);
+        double v = alpha * ldcg(A + i + (size_t)j * lda);
+        if (beta != 0.0) v = fma(beta, ldcg(C + i + (size_t)j * ldc), v);
+        C[i + (size_t)j * ldc] = v;
+    }
+    __syncthreads();
+}
+
+}  // namespace ttg

@@ -1,0 +1,539 @@
+// ttg_exec.cu — C ABI of the persistent executor (include/ttg.h).
+//
+// Host side: graph validation and upload, priority levels, queue layout,
+// launch/wait and the run report.  Device side: the persistent kernel that
+// runs the FP64 tile tasks (tile_f64.cuh) and the mixed-precision tile tasks
+// (tile_mixed.cuh) through the executor loop (exec.cuh).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <vector>
+
+#include "../../include/ttg.h"
+#include "exec.cuh"
+#include "tile_f64.cuh"
+#include "ttg_internal.h"
+
+namespace ttg {
+
+// One FP64 tile task on the whole block.  Returns POTRF's info (0 = ok).
+__device__ int run_op_f64(const ttg_op& op, double* smem) {
+    switch (op.kind) {
+        case TTG_OP_POTRF_L:
+            return potrf_l_f64(op.n, (double*)op.c, op.ldc, smem);
+        case TTG_OP_TRSM_RLTN:
+            trsm_rltn_f64(op.m, op.n, op.alpha, (const double*)op.a, op.lda, (double*)op.c, op.ldc, smem);
+            return 0;
+        case TTG_OP_SYRK_LN:
+            gemm_f64<false, true>(op.n, op.n, op.k, op.alpha, (const double*)op.a, op.lda, (const double*)op.a, op.lda,
+                                  op.beta, (double*)op.c, op.ldc, smem);
+            return 0;
+        case TTG_OP_GEMM_NT:
+            gemm_f64<false, false>(op.m, op.n, op.k, op.alpha, (const double*)op.a, op.lda, (const double*)op.b, op.ldb,
+                                   op.beta, (double*)op.c, op.ldc, smem);
+            return 0;
+        case TTG_OP_GEMM_NN:
+            gemm_f64<true, false>(op.m, op.n, op.k, op.alpha, (const double*)op.a, op.lda, (const double*)op.b, op.ldb,
+                                  op.beta, (double*)op.c, op.ldc, smem);
+            return 0;
+        case TTG_OP_GEADD:
+            geadd_f64(op.m, op.n, op.alpha, (const double*)op.a, op.lda, op.beta, (double*)op.c, op.ldc);
+            return 0;
+        default:
+            return 0;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads, 1) exec_kernel(ExecParams p) {
+    extern __shared__ __align__(128) double smem_f64[];
+    executor_loop(p, smem_f64, [](const ttg_op& op, double* smem) { return run_op_f64(op, smem); });
+}
+
+// Post-run summary: tasks that ran other than once, counters not at zero.
+__global__ void summarize_kernel(const int* runs, const int* count, const uint8_t* runnable, int n, int* out) {
+    int bad = 0, pending = 0, ran = 0;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int r = runs[t];
+        ran += r;
+        if (runnable[t] ? (r != 1) : (r != 0)) ++bad;
+        if (count[t] != 0) ++pending;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        bad += __shfl_down_sync(0xffffffffu, bad, o);
+        pending += __shfl_down_sync(0xffffffffu, pending, o);
+        ran += __shfl_down_sync(0xffffffffu, ran, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(out + 0, ran);
+        atomicAdd(out + 1, pending);
+        atomicAdd(out + 2, bad);
+    }
+}
+
+}  // namespace ttg
+
+using namespace ttg;
+
+#define TTG_CUDA_TRY(expr)                                                                          \
+    do {                                                                                            \
+        cudaError_t _e = (expr);                                                                    \
+        if (_e != cudaSuccess) {                                                                    \
+            ttg_set_last_cuda_error(_e, #expr, __FILE__, __LINE__);                                 \
+            return _e == cudaErrorMemoryAllocation ? TTG_ENOMEM : TTG_ECUDA;                        \
+        }                                                                                           \
+    } while (0)
+
+static char g_last_cuda[512];
+
+void ttg_set_last_cuda_error(cudaError_t e, const char* expr, const char* file, int line) {
+    snprintf(g_last_cuda, sizeof(g_last_cuda), "%s: %s (%s:%d)", cudaGetErrorString(e), expr, file, line);
+}
+
+extern "C" const char* ttg_last_cuda_error(void) { return g_last_cuda; }
+
+extern "C" const char* ttg_strerror(ttg_status s) {
+    switch (s) {
+        case TTG_OK: return "ok";
+        case TTG_EINVAL: return "invalid argument";
+        case TTG_ECUDA: return "CUDA runtime error";
+        case TTG_ETIMEOUT: return "executor made no progress within the time limit";
+        case TTG_EOVERCOUNT: return "a task received more promises than its indegree";
+        case TTG_ENOTPD: return "a diagonal tile is not positive definite";
+        case TTG_ENOMEM: return "device allocation failed";
+        case TTG_ESTATE: return "call out of order";
+        case TTG_EUNDERRUN: return "some tasks never became ready";
+        case TTG_ENOCONV: return "iterative refinement did not converge";
+        default: return "unknown status";
+    }
+}
+
+namespace {
+
+template <class T>
+ttg_status dev_alloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    TTG_CUDA_TRY(cudaMalloc((void**)p, count * sizeof(T)));
+    return TTG_OK;
+}
+
+template <class T>
+void dev_free(T*& p) {
+    if (p) cudaFree((void*)p);
+    p = nullptr;
+}
+
+}  // namespace
+
+void ttg_graph_free(ttg_ctx* c) {
+    DevGraph& g = c->g;
+    dev_free(g.ops);
+    dev_free(g.init);
+    dev_free(g.count);
+    dev_free(g.runs);
+    dev_free(g.succ_ptr);
+    dev_free(g.succ_idx);
+    dev_free(g.level);
+    dev_free(g.bind);
+    dev_free(g.runnable);
+    dev_free(g.qbuf);
+    dev_free(g.qinit);
+    dev_free(g.q_off);
+    dev_free(g.q_head);
+    dev_free(g.q_tail);
+    dev_free(g.q_tail_init);
+    dev_free(g.bq_buf);
+    dev_free(g.bq_off);
+    dev_free(g.bq_head);
+    dev_free(g.bq_tail);
+    dev_free(g.trace);
+    g = DevGraph();
+}
+
+extern "C" ttg_status ttg_create(ttg_ctx** out, const ttg_opts* opts) {
+    if (!out) return TTG_EINVAL;
+    *out = nullptr;
+    ttg_ctx* c = new ttg_ctx();
+    c->device = opts ? opts->device : 0;
+    c->timeout_s = (opts && opts->timeout_s > 0) ? opts->timeout_s : 10.0;
+    c->trace = opts ? opts->trace : 0;
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) {
+        ttg_set_last_cuda_error(e, "cudaSetDevice", __FILE__, __LINE__);
+        delete c;
+        return TTG_ECUDA;
+    }
+    cudaDeviceProp prop;
+    e = cudaGetDeviceProperties(&prop, c->device);
+    if (e != cudaSuccess) {
+        ttg_set_last_cuda_error(e, "cudaGetDeviceProperties", __FILE__, __LINE__);
+        delete c;
+        return TTG_ECUDA;
+    }
+    c->sms = prop.multiProcessorCount;
+    c->workers = (opts && opts->workers > 0) ? opts->workers : c->sms;
+    ttg_status st = ttg_ctx_init_device(c);
+    if (st != TTG_OK) {
+        delete c;
+        return st;
+    }
+    *out = c;
+    return TTG_OK;
+}
+
+ttg_status ttg_ctx_init_device(ttg_ctx* c) {
+    TTG_CUDA_TRY(cudaMalloc((void**)&c->status, sizeof(int) * 8));
+    TTG_CUDA_TRY(cudaMallocHost((void**)&c->h_status, sizeof(int) * 8));
+    TTG_CUDA_TRY(cudaEventCreate(&c->ev0));
+    TTG_CUDA_TRY(cudaEventCreate(&c->ev1));
+    const int smem = kF64SmemDoubles * (int)sizeof(double);
+    TTG_CUDA_TRY(cudaFuncSetAttribute(exec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    return ttg_mixed_init(c);
+}
+
+extern "C" ttg_status ttg_destroy(ttg_ctx* c) {
+    if (!c) return TTG_OK;
+    cudaSetDevice(c->device);
+    ttg_graph_free(c);
+    ttg_mixed_free(c);
+    if (c->status) cudaFree(c->status);
+    if (c->h_status) cudaFreeHost(c->h_status);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    delete c;
+    return TTG_OK;
+}
+
+extern "C" int ttg_workers(const ttg_ctx* c) { return c ? c->workers : 0; }
+
+// Priority levels: distinct priorities ranked from high to low; more than
+// kMaxLevels distinct values are split into kMaxLevels equal-count groups.
+static void assign_levels(int n, const double* prio, const std::vector<uint8_t>& runnable, std::vector<uint8_t>& level,
+                          int* n_levels) {
+    level.assign(n, 0);
+    if (!prio) {
+        *n_levels = 1;
+        return;
+    }
+    std::vector<double> vals;
+    vals.reserve(n);
+    for (int t = 0; t < n; ++t)
+        if (runnable[t]) vals.push_back(prio[t]);
+    std::sort(vals.begin(), vals.end(), std::greater<double>());
+    std::vector<double> distinct;
+    for (double v : vals)
+        if (distinct.empty() || distinct.back() != v) distinct.push_back(v);
+    if (distinct.empty()) {
+        *n_levels = 1;
+        return;
+    }
+    if ((int)distinct.size() <= kMaxLevels) {
+        std::map<double, int> rank;
+        for (size_t r = 0; r < distinct.size(); ++r) rank[distinct[r]] = (int)r;
+        for (int t = 0; t < n; ++t) level[t] = (uint8_t)(runnable[t] ? rank[prio[t]] : 0);
+        *n_levels = (int)distinct.size();
+        return;
+    }
+    // Equal-count split of the sorted (descending) runnable priorities.
+    std::vector<double> cut(kMaxLevels);
+    for (int l = 0; l < kMaxLevels; ++l) cut[l] = vals[std::min(vals.size() - 1, (size_t)((l + 1) * vals.size() / kMaxLevels) - 1)];
+    for (int t = 0; t < n; ++t) {
+        if (!runnable[t]) continue;
+        int l = 0;
+        while (l < kMaxLevels - 1 && prio[t] < cut[l]) ++l;
+        level[t] = (uint8_t)l;
+    }
+    *n_levels = kMaxLevels;
+}
+
+extern "C" ttg_status ttg_graph_upload(ttg_ctx* c, const ttg_graph_desc* gd) {
+    if (!c || !gd || gd->n_tasks < 0 || (gd->n_tasks > 0 && (!gd->ops || !gd->init_count || !gd->succ_ptr)))
+        return TTG_EINVAL;
+    TTG_CUDA_TRY(cudaSetDevice(c->device));
+    ttg_graph_free(c);
+    const int n = gd->n_tasks;
+    const int64_t n_edges = n > 0 ? gd->succ_ptr[n] : 0;
+    if (n_edges > 0 && !gd->succ_idx) return TTG_EINVAL;
+    for (int t = 0; t < n; ++t) {
+        if (gd->init_count[t] < 0 || gd->succ_ptr[t] > gd->succ_ptr[t + 1]) return TTG_EINVAL;
+        const int k = gd->ops[t].kind;
+        if (k < TTG_OP_NOP || k > TTG_OP_GEADD) return TTG_EINVAL;
+    }
+    if (n > 0 && gd->succ_ptr[0] != 0) return TTG_EINVAL;
+    for (int64_t e = 0; e < n_edges; ++e)
+        if (gd->succ_idx[e] < 0 || gd->succ_idx[e] >= n) return TTG_EINVAL;
+
+    // Host simulation of the counters: which tasks will reach zero, and
+    // whether any counter would be decremented below zero.
+    std::vector<int> cnt(gd->init_count, gd->init_count + n);
+    std::vector<uint8_t> runnable(n, 0);
+    std::vector<int> stack;
+    for (int t = 0; t < n; ++t)
+        if (cnt[t] == 0) {
+            runnable[t] = 1;
+            stack.push_back(t);
+        }
+    bool over = false;
+    while (!stack.empty()) {
+        const int t = stack.back();
+        stack.pop_back();
+        for (int64_t e = gd->succ_ptr[t]; e < gd->succ_ptr[t + 1]; ++e) {
+            const int s = gd->succ_idx[e];
+            if (--cnt[s] == 0) {
+                runnable[s] = 1;
+                stack.push_back(s);
+            } else if (cnt[s] < 0) {
+                over = true;
+            }
+        }
+    }
+    int n_runnable = 0;
+    for (int t = 0; t < n; ++t) n_runnable += runnable[t];
+    c->pending_host = n - n_runnable;
+    c->overcount_host = over;
+
+    std::vector<uint8_t> level;
+    int n_levels = 1;
+    assign_levels(n, gd->priority, runnable, level, &n_levels);
+
+    // Queue layout: level queues sized by runnable unbound tasks per level,
+    // bound queues by runnable tasks bound to each worker.
+    const int W = c->workers;
+    std::vector<int> bind(n, -1);
+    if (gd->bind)
+        for (int t = 0; t < n; ++t) bind[t] = gd->bind[t] < 0 ? -1 : gd->bind[t];
+    std::vector<int> qcount(kMaxLevels, 0), bqcount(W, 0);
+    for (int t = 0; t < n; ++t) {
+        if (!runnable[t]) continue;
+        if (bind[t] >= 0) bqcount[bind[t] % W]++;
+        else qcount[level[t]]++;
+    }
+    std::vector<int> q_off(kMaxLevels + 1, 0), bq_off(W + 1, 0);
+    for (int l = 0; l < kMaxLevels; ++l) q_off[l + 1] = q_off[l] + qcount[l];
+    for (int w = 0; w < W; ++w) bq_off[w + 1] = bq_off[w] + bqcount[w];
+    bool has_bound = bq_off[W] > 0;
+    // Initial queue images: initially-ready tasks in index order.
+    std::vector<int> qinit(std::max(1, q_off[kMaxLevels]), -1), bqinit(std::max(1, bq_off[W]), -1);
+    std::vector<int> tail0(kMaxLevels * 32, 0), btail0(W, 0);
+    for (int t = 0; t < n; ++t) {
+        if (gd->init_count[t] != 0) continue;
+        if (bind[t] >= 0) {
+            const int w = bind[t] % W;
+            bqinit[bq_off[w] + btail0[w]++] = t;
+        } else {
+            const int l = level[t];
+            qinit[q_off[l] + tail0[l * 32]++] = t;
+        }
+    }
+
+    DevGraph& g = c->g;
+    g.n_tasks = n;
+    g.n_runnable = n_runnable;
+    g.n_levels = n_levels;
+    g.has_bound = has_bound;
+    g.q_total = q_off[kMaxLevels];
+    g.bq_total = bq_off[W];
+    ttg_status st;
+#define ALLOC(ptr, cnt)                                 \
+    if ((st = dev_alloc(&g.ptr, (cnt))) != TTG_OK) {    \
+        ttg_graph_free(c);                              \
+        return st;                                      \
+    }
+    ALLOC(ops, n);
+    ALLOC(init, n);
+    ALLOC(count, n);
+    ALLOC(runs, n);
+    ALLOC(succ_ptr, n + 1);
+    ALLOC(succ_idx, n_edges);
+    ALLOC(level, n);
+    ALLOC(bind, n);
+    ALLOC(runnable, n);
+    ALLOC(qbuf, qinit.size());
+    ALLOC(qinit, qinit.size());
+    ALLOC(q_off, kMaxLevels + 1);
+    ALLOC(q_head, kMaxLevels * 32);
+    ALLOC(q_tail, kMaxLevels * 32);
+    ALLOC(q_tail_init, kMaxLevels * 32);
+    ALLOC(bq_buf, bqinit.size() * 2);  // second half: initial image
+    ALLOC(bq_off, W + 1);
+    ALLOC(bq_head, W * 2);             // head + initial tail
+    ALLOC(bq_tail, W);
+    if (c->trace) ALLOC(trace, 3 * (size_t)std::max(1, n));
+#undef ALLOC
+    TTG_CUDA_TRY(cudaMemcpy(g.ops, gd->ops, sizeof(ttg_op) * n, cudaMemcpyHostToDevice));
+    TTG_CUDA_TRY(cudaMemcpy(g.init, gd->init_count, sizeof(int) * n, cudaMemcpyHostToDevice));
+    TTG_CUDA_TRY(cudaMemcpy(g.succ_ptr, gd->succ_ptr, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice));
+    if (n_edges) TTG_CUDA_TRY(cudaMemcpy(g.succ_idx, gd->succ_idx, sizeof(int32_t) * n_edges, cudaMemcpyHostToDevice));
+    TTG_CUDA_TRY(cudaMemcpy(g.level, level.data(), n, cudaMemcpyHostToDevice));
+    TTG_CUDA_TRY(cudaMemcpy(g.bind, bind.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    TTG_CUDA_TRY(cudaMemcpy(g.runnable, runnable.data(), n, cudaMemcpyHostToDevice));
+    TTG_CUDA_TRY(cudaMemcpy(g.qinit, qinit.data(), sizeof(int) * qinit.size(), cudaMemcpyHostToDevice));
+    TTG_CUDA_TRY(cudaMemcpy(g.q_off, q_off.data(), sizeof(int) * (kMaxLevels + 1), cudaMemcpyHostToDevice));
+    TTG_CUDA_TRY(cudaMemcpy(g.q_tail_init, tail0.data(), sizeof(int) * kMaxLevels * 32, cudaMemcpyHostToDevice));
+    TTG_CUDA_TRY(cudaMemcpy(g.bq_buf + bqinit.size(), bqinit.data(), sizeof(int) * bqinit.size(), cudaMemcpyHostToDevice));
+    TTG_CUDA_TRY(cudaMemcpy(g.bq_off, bq_off.data(), sizeof(int) * (W + 1), cudaMemcpyHostToDevice));
+    TTG_CUDA_TRY(cudaMemcpy(g.bq_head + W, btail0.data(), sizeof(int) * W, cudaMemcpyHostToDevice));
+    g.bq_image = (int)bqinit.size();
+    c->uploaded = true;
+    c->launched = false;
+    return TTG_OK;
+}
+
+ttg_status ttg_reset_state(ttg_ctx* c, cudaStream_t s) {
+    DevGraph& g = c->g;
+    const int n = g.n_tasks, W = c->workers;
+    TTG_CUDA_TRY(cudaMemcpyAsync(g.count, g.init, sizeof(int) * std::max(1, n), cudaMemcpyDeviceToDevice, s));
+    TTG_CUDA_TRY(cudaMemsetAsync(g.runs, 0, sizeof(int) * std::max(1, n), s));
+    TTG_CUDA_TRY(cudaMemcpyAsync(g.qbuf, g.qinit, sizeof(int) * std::max(1, g.q_total), cudaMemcpyDeviceToDevice, s));
+    TTG_CUDA_TRY(cudaMemsetAsync(g.q_head, 0, sizeof(int) * kMaxLevels * 32, s));
+    TTG_CUDA_TRY(cudaMemcpyAsync(g.q_tail, g.q_tail_init, sizeof(int) * kMaxLevels * 32, cudaMemcpyDeviceToDevice, s));
+    TTG_CUDA_TRY(cudaMemcpyAsync(g.bq_buf, g.bq_buf + g.bq_image, sizeof(int) * g.bq_image, cudaMemcpyDeviceToDevice, s));
+    TTG_CUDA_TRY(cudaMemsetAsync(g.bq_head, 0, sizeof(int) * W, s));
+    TTG_CUDA_TRY(cudaMemcpyAsync(g.bq_tail, g.bq_head + W, sizeof(int) * W, cudaMemcpyDeviceToDevice, s));
+    TTG_CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int) * 8, s));
+    if (g.trace) TTG_CUDA_TRY(cudaMemsetAsync(g.trace, 0, sizeof(long long) * 3 * std::max(1, n), s));
+    return TTG_OK;
+}
+
+static ExecParams ttg_make_params(ttg_ctx* c) {
+    DevGraph& g = c->g;
+    ExecParams p;
+    p.ops = g.ops;
+    p.n_tasks = g.n_tasks;
+    p.n_runnable = g.n_runnable;
+    p.count = g.count;
+    p.runs = g.runs;
+    p.succ_ptr = g.succ_ptr;
+    p.succ_idx = g.succ_idx;
+    p.level = g.level;
+    p.bind = g.bind;
+    p.n_levels = g.n_levels;
+    p.n_workers = c->workers;
+    p.qbuf = g.qbuf;
+    p.q_off = g.q_off;
+    p.q_head = g.q_head;
+    p.q_tail = g.q_tail;
+    p.bq_buf = g.bq_buf;
+    p.bq_off = g.bq_off;
+    p.bq_head = g.bq_head;
+    p.bq_tail = g.bq_tail;
+    p.has_bound = g.has_bound;
+    p.done = c->status + 0;
+    p.err = c->status + 1;
+    p.err_task = c->status + 2;
+    p.err_info = c->status + 3;
+    p.trace = (long long*)g.trace;
+    p.timeout_ns = (long long)(c->timeout_s * 1e9);
+    return p;
+}
+
+extern "C" ttg_status ttg_launch(ttg_ctx* c, void* stream) {
+    if (!c) return TTG_EINVAL;
+    if (!c->uploaded) return TTG_ESTATE;
+    TTG_CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t s = (cudaStream_t)stream;
+    c->stream = s;
+    ttg_status st = ttg_reset_state(c, s);
+    if (st != TTG_OK) return st;
+    TTG_CUDA_TRY(cudaEventRecord(c->ev0, s));
+    if (c->g.n_runnable > 0) {
+        ExecParams p = ttg_make_params(c);
+        st = ttg_launch_executor(c, p, s);
+        if (st != TTG_OK) return st;
+    }
+    TTG_CUDA_TRY(cudaEventRecord(c->ev1, s));
+    c->launched = true;
+    return TTG_OK;
+}
+
+ttg_status ttg_launch_executor(ttg_ctx* c, const ExecParams& p, cudaStream_t s) {
+    if (c->g_mixed) return ttg_launch_mixed(c, p, s);
+    const int smem = kF64SmemDoubles * (int)sizeof(double);
+    exec_kernel<<<c->workers, kThreads, smem, s>>>(p);
+    TTG_CUDA_TRY(cudaGetLastError());
+    return TTG_OK;
+}
+
+extern "C" ttg_status ttg_wait(ttg_ctx* c, ttg_report* rep) {
+    if (!c) return TTG_EINVAL;
+    if (!c->launched) return TTG_ESTATE;
+    TTG_CUDA_TRY(cudaSetDevice(c->device));
+    DevGraph& g = c->g;
+    // status[4..6] <- ran, pending, bad
+    summarize_kernel<<<std::max(1, std::min(256, (g.n_tasks + 255) / 256)), 256, 0, c->stream>>>(
+        g.runs, g.count, g.runnable, g.n_tasks, c->status + 4);
+    TTG_CUDA_TRY(cudaGetLastError());
+    TTG_CUDA_TRY(cudaMemcpyAsync(c->h_status, c->status, sizeof(int) * 8, cudaMemcpyDeviceToHost, c->stream));
+    TTG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->launched = false;
+    const int* h = c->h_status;
+    ttg_status st = h[1];
+    if (st == TTG_OK && c->overcount_host) st = TTG_EOVERCOUNT;
+    if (st == TTG_OK && c->pending_host > 0) st = TTG_EUNDERRUN;
+    if (rep) {
+        rep->tasks_total = g.n_tasks;
+        rep->tasks_run = h[4];
+        rep->tasks_pending = h[5];
+        rep->bad_runs = h[6];
+        rep->status = st;
+        rep->error_task = h[1] ? h[2] : -1;
+        rep->info = h[3];
+        rep->workers = c->workers;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        rep->elapsed_ms = ms;
+    }
+    c->last_status = st;
+    return st;
+}
+
+extern "C" ttg_status ttg_run(ttg_ctx* c, void* stream, ttg_report* rep) {
+    ttg_status st = ttg_launch(c, stream);
+    if (st != TTG_OK) return st;
+    return ttg_wait(c, rep);
+}
+
+extern "C" ttg_status ttg_task_record(ttg_ctx* c, int32_t* h_runs, int32_t* h_final_count) {
+    if (!c || !c->uploaded) return TTG_ESTATE;
+    TTG_CUDA_TRY(cudaSetDevice(c->device));
+    const int n = c->g.n_tasks;
+    if (h_runs) TTG_CUDA_TRY(cudaMemcpy(h_runs, c->g.runs, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    if (h_final_count) TTG_CUDA_TRY(cudaMemcpy(h_final_count, c->g.count, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    return TTG_OK;
+}
+
+extern "C" ttg_status ttg_trace(ttg_ctx* c, int64_t* h_start, int64_t* h_end, int32_t* h_worker) {
+    if (!c || !c->uploaded || !c->g.trace) return TTG_ESTATE;
+    TTG_CUDA_TRY(cudaSetDevice(c->device));
+    const int n = c->g.n_tasks;
+    std::vector<long long> tr(3 * (size_t)n);
+    TTG_CUDA_TRY(cudaMemcpy(tr.data(), c->g.trace, sizeof(long long) * 3 * n, cudaMemcpyDeviceToHost));
+    long long t0 = 0;
+    bool any = false;
+    for (int t = 0; t < n; ++t)
+        if (tr[3 * t] > 0 && (!any || tr[3 * t] < t0)) {
+            t0 = tr[3 * t];
+            any = true;
+        }
+    for (int t = 0; t < n; ++t) {
+        const bool ran = tr[3 * t] > 0;
+        if (h_start) h_start[t] = ran ? tr[3 * t] - t0 : -1;
+        if (h_end) h_end[t] = ran ? tr[3 * t + 1] - t0 : -1;
+        if (h_worker) h_worker[t] = ran ? (int32_t)tr[3 * t + 2] : -1;
+    }
+    return TTG_OK;
+}
+
+extern "C" int64_t ttg_tile_layout(const int32_t* bs, int32_t nb, int64_t* off) {
+    int64_t o = 0;
+    for (int j = 0; j < nb; ++j)
+        for (int i = j; i < nb; ++i) {
+            if (off) off[i + (int64_t)j * nb] = o;
+            o += (int64_t)bs[i] * bs[j];
+        }
+    return o;
+}

@@ -1,0 +1,88 @@
+// ttg_internal.h — context and device-graph state shared by the .cu files of
+// libttg.so.  Not part of the public ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/ttg.h"
+
+namespace ttg {
+struct ExecParams;
+}
+
+struct DevGraph {
+    int n_tasks = 0;
+    int n_runnable = 0;
+    int n_levels = 1;
+    int has_bound = 0;
+    int q_total = 0;
+    int bq_total = 0;
+    int bq_image = 0;
+    ttg_op* ops = nullptr;
+    int* init = nullptr;
+    int* count = nullptr;
+    int* runs = nullptr;
+    int64_t* succ_ptr = nullptr;
+    int32_t* succ_idx = nullptr;
+    uint8_t* level = nullptr;
+    int* bind = nullptr;
+    uint8_t* runnable = nullptr;
+    int* qbuf = nullptr;
+    int* qinit = nullptr;
+    int* q_off = nullptr;
+    int* q_head = nullptr;
+    int* q_tail = nullptr;
+    int* q_tail_init = nullptr;
+    int* bq_buf = nullptr;
+    int* bq_off = nullptr;
+    int* bq_head = nullptr;
+    int* bq_tail = nullptr;
+    long long* trace = nullptr;
+};
+
+struct ttg_ctx {
+    int device = 0;
+    int sms = 0;
+    int workers = 0;
+    double timeout_s = 10.0;
+    int trace = 0;
+    bool uploaded = false;
+    bool launched = false;
+    bool g_mixed = false;     // the uploaded graph has mixed-precision tasks
+    int pending_host = 0;     // tasks that will never become ready
+    bool overcount_host = false;
+    ttg_status last_status = TTG_OK;
+    DevGraph g;
+    int* status = nullptr;    // device: done, err, err_task, err_info, ran, pending, bad, spare
+    int* h_status = nullptr;  // pinned host copy
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaStream_t stream = nullptr;
+    void* mixed = nullptr;    // mixed-path resources (ttg_mixed.cu)
+};
+
+void ttg_set_last_cuda_error(cudaError_t e, const char* expr, const char* file, int line);
+ttg_status ttg_ctx_init_device(ttg_ctx* c);
+ttg_status ttg_reset_state(ttg_ctx* c, cudaStream_t s);
+ttg_status ttg_launch_executor(ttg_ctx* c, const ttg::ExecParams& p, cudaStream_t s);
+void ttg_graph_free(ttg_ctx* c);
+
+// Lower tiles of the miniapp matrix 1/((i-j)^2+1) (ttg_gen.cu).
+ttg_status ttg_gen_miniapp_tiles(ttg_ctx* c, const int32_t* h_bs, int32_t nb, double* d_tiles, void* stream);
+
+// Block-GEMM inputs in tile layout (ttg_gen.cu).
+ttg_status ttg_gen_gemm_tiles(ttg_ctx* c, int32_t N, int32_t b, int32_t inputs, uint32_t seed, double* d_A, double* d_B,
+                              void* stream);
+
+// Mixed-precision path (ttg_mixed.cu).
+ttg_status ttg_mixed_init(ttg_ctx* c);
+void ttg_mixed_free(ttg_ctx* c);
+ttg_status ttg_launch_mixed(ttg_ctx* c, const ttg::ExecParams& p, cudaStream_t s);
+
+#define TTG_CUDA_CHECK(expr)                                                            \
+    do {                                                                                \
+        cudaError_t _e = (expr);                                                        \
+        if (_e != cudaSuccess) {                                                        \
+            ttg_set_last_cuda_error(_e, #expr, __FILE__, __LINE__);                     \
+            return _e == cudaErrorMemoryAllocation ? TTG_ENOMEM : TTG_ECUDA;            \
+        }                                                                               \
+    } while (0)
