@@ -1,0 +1,284 @@
+#!/usr/bin/env python
+"""Benchmark of the tiled dense Cholesky task graph on the GB300 executor.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (one step): the FP64 tiled Cholesky factorisation of
+A = G·Gᵀ/N + αI (N = 32768, tile 512, 45,760 tasks, α = 1, seed 2), run as one
+persistent-kernel launch of the task graph captured from the Taskflow<K>
+drop-in.  Inputs (4.3 GB of packed lower tiles) are resident in HBM and
+larger than L2; each step first restores the tiles (outside the timed
+interval).  `value` is N³/3 / step time.  `e2e` runs the same step through the
+C ABI with pinned host buffers (tiles in, factor out) and counts the copies.
+
+With torchrun (N > 1 GPUs) every rank factorises its own matrix ("replicas
+only": the path has no exchange step) and `value` sums the ranks' work over
+the slowest rank's time.  `--impl reference` times the reference's algorithm
+on the host cores instead (the oracle port: restated Taskflow/Threadpool with
+OpenBLAS, one BLAS thread per task) on a bounded sample of the workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Cholesky TFLOP/s & solves/s, p50/p99: mixed+IR vs FP64 on GB300 at bwd err≤1e-14"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sms, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sms.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sms) if sms else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sms)}
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl" if os.environ.get("TTG_BENCH_GLOO") is None else "gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(world, v):
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample(steps, warmup, N=16384, b=512):
+    """The reference's algorithm on the host cores: the oracle port (restated
+    Taskflow/Threadpool_shared + OpenBLAS, one BLAS thread per task) on all
+    cores, FP64 Cholesky of N×N with tile b.  Returns (TFLOP/s, cores, blas)."""
+    from oracle import oracle as orc
+    orc.lib(use_blas=True)
+    cores = os.cpu_count() or 1
+    times = []
+    for i in range(warmup + steps):
+        r = orc.cholesky(block_size=b, num_blocks=N // b, n_threads=cores, kind=2, matrix=0, want_L=False)
+        if r["info"] != 0:
+            raise RuntimeError("oracle factorisation failed")
+        if i >= warmup:
+            times.append(r["time_s"])
+    t = statistics.median(times)
+    return N ** 3 / 3.0 / t / 1e12, cores, r["blas"], t
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    v, cores, blas, t = cpu_sample(args.steps, args.warmup, args.cpu_n, args.cpu_b)
+    sample = "FP64 tiled Cholesky N=%d tile %d (%d tasks), oracle port of 2d_cholesky at one rank, %d threads, %s" % (
+        args.cpu_n, args.cpu_b, _tasks(args.cpu_n // args.cpu_b), cores, os.path.basename(blas))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "tiled Cholesky FP64 (bounded CPU sample)", "matrix_size": args.cpu_n,
+                       "block_size": args.cpu_b},
+            "cpu_baseline": {"value": v, "unit": "TFLOP/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def _tasks(nb):
+    return nb + nb * (nb - 1) // 2 + (nb - 1) * nb * (nb + 1) // 6
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    import tasktorrent_gb300 as t
+    torch.cuda.set_device(local)
+    ctx = t.Context(device=local, timeout_s=60.0)
+    nb = args.n // args.block
+    N = nb * args.block
+    plan = t.CholPlan(ctx, args.block, nb, n_threads=16, kind=args.kind, matrix=1, alpha=args.alpha, seed=args.seed + rank)
+    n_tasks, capture_s = plan.tasks()
+    flops = N ** 3 / 3.0
+    stream = None  # the legacy default stream: torch's current stream here
+
+    def step():
+        t.check(t.lib().ttg_chol_plan_restore(plan.h, stream), "restore")
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        st, rep = plan.factor(restore=False, stream=stream)
+        e1.record()
+        if st != t.TTG_OK:
+            raise RuntimeError("factor failed: %s" % t.strerror(st))
+        return e0, e1, rep
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier(world)
+    evs, kernel_ms = [], []
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        for _ in range(args.steps):
+            e0, e1, rep = step()
+            evs.append((e0, e1))
+            kernel_ms.append(rep.elapsed_ms)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - w0
+    barrier(world)
+    step_ms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
+    step_ms = allmax(world, step_ms)
+    value = world * flops / (step_ms * 1e-3) / 1e12
+
+    # Roofline of the executor kernel (the only compute kernel of a step).
+    peak = ctx.fp64_peak(200.0)
+    kms = statistics.mean(kernel_ms)
+    achieved = flops / (kms * 1e-3) / 1e12
+
+    # Correctness of the measured factor.
+    err = None
+    if args.check:
+        import numpy as np
+        from oracle import oracle as orc  # noqa: F401  (checker only)
+        if N <= 8192:
+            L = plan.factor_L()
+            A = plan.input_A()
+            err = float(np.linalg.norm(L @ L.T - A) / np.linalg.norm(A))
+
+    # End to end through the C ABI with pinned host buffers.
+    elems = plan.tile_elems()
+    e2e = None
+    if not args.no_e2e:
+        hin = torch.empty(elems, dtype=torch.float64, pin_memory=True)
+        hout = torch.empty(elems, dtype=torch.float64, pin_memory=True)
+        plan.copy_tiles(1, hin.data_ptr())
+        plan.factor_host_tiles(hin.data_ptr(), hout.data_ptr())  # warm the copy path
+        barrier(world)
+        ts = []
+        for _ in range(args.steps):
+            s0 = time.perf_counter()
+            st, rep = plan.factor_host_tiles(hin.data_ptr(), hout.data_ptr())
+            ts.append(time.perf_counter() - s0)
+            if st != t.TTG_OK:
+                raise RuntimeError("e2e failed: %s" % t.strerror(st))
+        e2e_s = allmax(world, statistics.mean(ts))
+        e2e = {"value": world * flops / e2e_s / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": elems * 8,
+               "d2h_bytes_per_step": elems * 8}
+        del hin, hout
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        v, cores, blas, tcpu = cpu_sample(2, 1, args.cpu_n, args.cpu_b)
+        cpu = {"value": v, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+               "sample": "FP64 tiled Cholesky N=%d tile %d, oracle port of 2d_cholesky at one rank, %d threads, %s, "
+                         "median of 2 after 1 warm-up" % (args.cpu_n, args.cpu_b, cores, os.path.basename(blas))}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic: A = G*G^T/N + alpha*I, G quantised N(0,1) (Philox-4x32-10, seed %d)" % args.seed,
+                "config": {"workload": "tiled Cholesky factorisation, FP64 path", "matrix_size": N, "block_size": args.block,
+                           "tasks": n_tasks, "alpha": args.alpha, "priority_kind": args.kind,
+                           "l2": "inputs larger than L2 (%.1f GB of tiles)" % (elems * 8 / 1e9),
+                           "capture_s": capture_s, "wall_s_timed": wall},
+                "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                             "frac": achieved / peak, "traffic": None,
+                             "peak_source": "measured: ttg_measure_fp64_peak (DFMA chains on every SM)"},
+                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 2 * args.steps, "clocks": clk.summary(),
+                "factor_error": err}
+        print(json.dumps(line))
+    plan.close()
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=32768)
+    ap.add_argument("--block", type=int, default=512)
+    ap.add_argument("--alpha", type=float, default=1.0)
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--kind", type=int, default=2)
+    ap.add_argument("--cpu-n", dest="cpu_n", type=int, default=16384)
+    ap.add_argument("--cpu-b", dest="cpu_b", type=int, default=512)
+    ap.add_argument("--no-e2e", dest="no_e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", dest="no_cpu_baseline", action="store_true")
+    ap.add_argument("--check", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be at least 3")
+    world, rank, local = dist_init()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

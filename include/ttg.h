@@ -74,6 +74,10 @@ typedef struct ttg_op {
     int32_t prec;      /* TTG_PREC_*                         */
     int32_t m, n, k;   /* dimensions as in the BLAS call      */
     int32_t lda, ldb, ldc;
+    int32_t parts;     /* blocks that share the task: 0 = chosen by the executor
+                          (one per 128×128 output block, up to 16; TRSM by
+                          128-row slices; POTRF always 1), else that many      */
+    int32_t flags;     /* reserved, 0                         */
     double alpha, beta;
     const void* a;     /* device pointers                     */
     const void* b;
@@ -144,6 +148,11 @@ ttg_status ttg_trace(ttg_ctx* ctx, int64_t* h_start_ns, int64_t* h_end_ns, int32
 
 /* Number of persistent workers the context launches. */
 int ttg_workers(const ttg_ctx* ctx);
+
+/* Measured FP64 FMA throughput of the device (TFLOP/s): every block of the
+ * device runs independent DFMA chains for about `ms` milliseconds.  The
+ * roofline denominator of the FP64 tile kernels. */
+ttg_status ttg_measure_fp64_peak(ttg_ctx* ctx, double ms, double* tflops);
 
 /* ------------------------------------------------------------ generators */
 /* Seeded inputs of the workloads (include/ttg_philox.h), built on the device. */

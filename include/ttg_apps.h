@@ -63,6 +63,17 @@ ttg_status ttg_chol_plan_factor(ttg_chol_plan* plan, void* stream, ttg_report* r
  * h_L receives the dense N×N lower factor (upper part zeroed). */
 ttg_status ttg_chol_factor_host(ttg_chol_plan* plan, const double* h_A, double* h_L, void* stream, ttg_report* rep);
 
+/* End-to-end with host buffers in the plan's packed lower-tile layout
+ * (ttg_tile_layout order; host memory, pinned for full bandwidth): h_tiles_in
+ * -> factor -> h_tiles_out (may alias).  One copy each way. */
+ttg_status ttg_chol_factor_host_tiles(ttg_chol_plan* plan, const double* h_tiles_in, double* h_tiles_out, void* stream,
+                                      ttg_report* rep);
+/* Copy the packed tiles to host: which = 0 working tiles (the factor after a
+ * run), 1 the pristine input. */
+ttg_status ttg_chol_plan_copy_tiles(ttg_chol_plan* plan, int32_t which, double* h_dst);
+/* Number of doubles of the packed lower-tile layout. */
+int64_t ttg_chol_plan_tile_elems(const ttg_chol_plan* plan);
+
 /* The factor as a dense N×N column-major lower-triangular host array. */
 ttg_status ttg_chol_plan_get_factor(ttg_chol_plan* plan, double* h_L);
 /* The input as a dense N×N column-major symmetric host array. */

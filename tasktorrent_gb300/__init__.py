@@ -30,7 +30,7 @@ class TTGError(RuntimeError):
 class Op(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int32), ("prec", ctypes.c_int32), ("m", ctypes.c_int32), ("n", ctypes.c_int32),
                 ("k", ctypes.c_int32), ("lda", ctypes.c_int32), ("ldb", ctypes.c_int32), ("ldc", ctypes.c_int32),
-                ("alpha", ctypes.c_double), ("beta", ctypes.c_double), ("a", ctypes.c_void_p), ("b", ctypes.c_void_p),
+                ("parts", ctypes.c_int32), ("flags", ctypes.c_int32), ("alpha", ctypes.c_double), ("beta", ctypes.c_double), ("a", ctypes.c_void_p), ("b", ctypes.c_void_p),
                 ("c", ctypes.c_void_p), ("aux", ctypes.c_void_p)]
 
 
@@ -85,6 +85,7 @@ SIGNATURES = {
     "ttg_gen_uniform": (_STATUS, [_P, ctypes.c_int64, ctypes.c_uint32, ctypes.c_uint32, _P, _P]),
     "ttg_gen_normal": (_STATUS, [_P, ctypes.c_int64, ctypes.c_uint32, ctypes.c_uint32, _P, _P]),
     "ttg_tile_layout": (ctypes.c_int64, [_P, _I32, _P]),
+    "ttg_measure_fp64_peak": (_STATUS, [_P, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
     # include/ttg_apps.h
     "ttg_chol_plan_create": (_STATUS, [_P, ctypes.POINTER(CholArgs), ctypes.POINTER(_P)]),
     "ttg_chol_plan_destroy": (_STATUS, [_P]),
@@ -96,6 +97,9 @@ SIGNATURES = {
     "ttg_chol_plan_factor": (_STATUS, [_P, _P, ctypes.POINTER(Report)]),
     "ttg_chol_factor_host": (_STATUS, [_P, _P, _P, _P, ctypes.POINTER(Report)]),
     "ttg_chol_plan_get_factor": (_STATUS, [_P, _P]),
+    "ttg_chol_factor_host_tiles": (_STATUS, [_P, _P, _P, _P, ctypes.POINTER(Report)]),
+    "ttg_chol_plan_tile_elems": (ctypes.c_int64, [_P]),
+    "ttg_chol_plan_copy_tiles": (_STATUS, [_P, _I32, _P]),
     "ttg_chol_plan_get_input": (_STATUS, [_P, _P]),
     "ttg_chol_plan_tiles": (_P, [_P, _P]),
     "ttg_chol_plan_dump_dag": (_STATUS, [_P, ctypes.c_char_p]),
@@ -147,6 +151,12 @@ def _ptr(a):
 
 class Context:
     """A device context (ttg_create)."""
+
+    def fp64_peak(self, ms=200.0):
+        """Measured FP64 FMA throughput (TFLOP/s) of the device."""
+        v = ctypes.c_double()
+        check(lib().ttg_measure_fp64_peak(self.h, ms, ctypes.byref(v)), "ttg_measure_fp64_peak")
+        return v.value
 
     def __init__(self, device=0, workers=0, timeout_s=10.0, trace=False):
         self.h = ctypes.c_void_p()
@@ -258,6 +268,23 @@ class CholPlan:
         rep = Report()
         st = lib().ttg_chol_factor_host(self.h, _ptr(A), _ptr(L), None, ctypes.byref(rep))
         return st, rep, L
+
+    def tile_elems(self):
+        return lib().ttg_chol_plan_tile_elems(self.h)
+
+    def factor_host_tiles(self, h_in, h_out=None, stream=None):
+        """End-to-end through host buffers in the packed lower-tile layout
+        (numpy arrays, ideally pinned)."""
+        rep = Report()
+        def addr(x):
+            return ctypes.c_void_p(x.ctypes.data if hasattr(x, "ctypes") else x) if x is not None else None
+        st = lib().ttg_chol_factor_host_tiles(self.h, addr(h_in), addr(h_out), stream, ctypes.byref(rep))
+        return st, rep
+
+    def copy_tiles(self, which, h_dst):
+        """Packed tiles to a host buffer (numpy array or raw address)."""
+        addr = h_dst.ctypes.data if hasattr(h_dst, "ctypes") else h_dst
+        check(lib().ttg_chol_plan_copy_tiles(self.h, which, ctypes.c_void_p(addr)), "copy_tiles")
 
     def factor_L(self):
         L = np.zeros((self.N, self.N), dtype=np.float64, order="F")

@@ -397,6 +397,32 @@ extern "C" ttg_status ttg_chol_factor_host(ttg_chol_plan* P, const double* h_A, 
     return TTG_OK;
 }
 
+extern "C" int64_t ttg_chol_plan_tile_elems(const ttg_chol_plan* P) { return P ? P->elems : 0; }
+
+extern "C" ttg_status ttg_chol_plan_copy_tiles(ttg_chol_plan* P, int32_t which, double* h_dst) {
+    if (!P || !h_dst || (which != 0 && which != 1)) return TTG_EINVAL;
+    TTG_CUDA_CHECK(cudaSetDevice(P->ctx->device));
+    const double* src = which == 1 ? P->pristine : (P->mixed ? ttg_mixed_factor_tiles(P->mixed) : P->tiles);
+    TTG_CUDA_CHECK(cudaMemcpy(h_dst, src, sizeof(double) * P->elems, cudaMemcpyDeviceToHost));
+    return TTG_OK;
+}
+
+extern "C" ttg_status ttg_chol_factor_host_tiles(ttg_chol_plan* P, const double* h_in, double* h_out, void* stream,
+                                                 ttg_report* rep) {
+    if (!P || !h_in) return TTG_EINVAL;
+    TTG_CUDA_CHECK(cudaSetDevice(P->ctx->device));
+    cudaStream_t s = (cudaStream_t)stream;
+    TTG_CUDA_CHECK(cudaMemcpyAsync(P->tiles, h_in, sizeof(double) * P->elems, cudaMemcpyHostToDevice, s));
+    ttg_status st = ttg_chol_plan_factor(P, stream, rep);
+    if (st != TTG_OK) return st;
+    if (h_out) {
+        const double* src = P->mixed ? ttg_mixed_factor_tiles(P->mixed) : P->tiles;
+        TTG_CUDA_CHECK(cudaMemcpyAsync(h_out, src, sizeof(double) * P->elems, cudaMemcpyDeviceToHost, s));
+    }
+    TTG_CUDA_CHECK(cudaStreamSynchronize(s));
+    return TTG_OK;
+}
+
 extern "C" ttg_status ttg_chol_plan_get_factor(ttg_chol_plan* P, double* h_L) {
     if (!P || !h_L) return TTG_EINVAL;
     TTG_CUDA_CHECK(cudaSetDevice(P->ctx->device));

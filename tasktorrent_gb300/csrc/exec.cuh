@@ -31,6 +31,9 @@ struct ExecParams {
     int n_runnable;   // tasks that will reach zero
     int* count;       // dependency counters
     int* runs;        // per-task run count
+    const int* parts; // blocks sharing each task (>= 1)
+    int* part_next;   // next part index to hand out
+    int* part_done;   // parts finished
     const int64_t* succ_ptr;
     const int32_t* succ_idx;
     const uint8_t* level;   // priority level, 0 = highest
@@ -164,20 +167,28 @@ __device__ inline int claim_task(const ExecParams& p) {
 
 __device__ __forceinline__ void push_ready(const ExecParams& p, int s) {
     const int b = p.bind[s];
+    const int P = p.parts[s];
     // Every task is pushed at most once (only the decrement that finds the
     // counter at one pushes), so a queue never outgrows the number of tasks
     // assigned to it; the bound checks below only guard against a corrupted
     // graph.
+    // A task of P parts takes P consecutive slots, one per part.
     if (b >= 0) {
         const int w = b % p.n_workers;
-        const int slot = atomicAdd(p.bq_tail + w, 1);
-        if (p.bq_off[w] + slot < p.bq_off[w + 1]) st_volatile(p.bq_buf + p.bq_off[w] + slot, s);
-        else set_error(p, TTG_EOVERCOUNT, s, 0);
+        const int slot = atomicAdd(p.bq_tail + w, P);
+        if (p.bq_off[w] + slot + P <= p.bq_off[w + 1]) {
+            for (int q = 0; q < P; ++q) st_volatile(p.bq_buf + p.bq_off[w] + slot + q, s);
+        } else {
+            set_error(p, TTG_EOVERCOUNT, s, 0);
+        }
     } else {
         const int lvl = p.level[s];
-        const int slot = atomicAdd(p.q_tail + lvl * 32, 1);
-        if (p.q_off[lvl] + slot < p.q_off[lvl + 1]) st_volatile(p.qbuf + p.q_off[lvl] + slot, s);
-        else set_error(p, TTG_EOVERCOUNT, s, 0);
+        const int slot = atomicAdd(p.q_tail + lvl * 32, P);
+        if (p.q_off[lvl] + slot + P <= p.q_off[lvl + 1]) {
+            for (int q = 0; q < P; ++q) st_volatile(p.qbuf + p.q_off[lvl] + slot + q, s);
+        } else {
+            set_error(p, TTG_EOVERCOUNT, s, 0);
+        }
     }
 }
 
@@ -204,37 +215,51 @@ __device__ inline void fulfil_successors(const ExecParams& p, int t) {
     }
 }
 
-// The persistent kernel body: `RunOp(op, smem)` runs one tile task on the
-// whole block and returns 0 or an error info (POTRF failing column).
+// The persistent kernel body: `RunOp(op, part, parts, smem)` runs one part
+// of a tile task on the whole block and returns 0 or an error info (POTRF
+// failing column).  The block that finishes the last part of a task fulfils
+// its successors.
 template <class RunOp>
 __device__ void executor_loop(const ExecParams& p, double* smem, RunOp run_op) {
-    __shared__ int s_task;
-    __shared__ int s_info;
+    __shared__ int s_task, s_part, s_info, s_last;
     for (;;) {
         if (threadIdx.x < 32) {
             const int t = claim_task(p);
             if (threadIdx.x == 0) {
                 s_task = t;
-                if (t >= 0 && p.trace) p.trace[3 * (size_t)t] = globaltimer();
+                if (t >= 0) {
+                    const int part = atomicAdd(p.part_next + t, 1);
+                    s_part = part;
+                    if (part == 0 && p.trace) p.trace[3 * (size_t)t] = globaltimer();
+                }
             }
         }
         __syncthreads();
         const int t = s_task;
         if (t < 0) break;
         const ttg_op op = p.ops[t];
-        const int info = run_op(op, smem);
-        if (threadIdx.x == 0) s_info = info;
+        const int nparts = p.parts[t];
+        const int info = run_op(op, s_part, nparts, smem);
         __syncthreads();
+        if (threadIdx.x == 0) {
+            s_info = info;
+            __threadfence();  // release this part's writes (after bar.sync)
+            const int finished = atomicAdd(p.part_done + t, 1);
+            s_last = finished == nparts - 1;
+            if (s_last) __threadfence();  // acquire the other parts' writes
+        }
+        __syncwarp();
         if (threadIdx.x < 32) {
-            if (threadIdx.x == 0) {
-                if (s_info != 0) set_error(p, TTG_ENOTPD, t, s_info);
-                if (p.trace) {
+            if (threadIdx.x == 0 && s_info != 0) set_error(p, TTG_ENOTPD, t, s_info);
+            if (s_last) {
+                if (threadIdx.x == 0 && p.trace) {
                     p.trace[3 * (size_t)t + 1] = globaltimer();
                     p.trace[3 * (size_t)t + 2] = blockIdx.x;
                 }
+                fulfil_successors(p, t);
             }
-            fulfil_successors(p, t);
         }
+        __syncthreads();  // s_task/s_part are rewritten by the next claim
     }
 }
 

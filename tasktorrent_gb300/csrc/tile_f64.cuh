@@ -31,16 +31,34 @@ __device__ __forceinline__ double ldcg(const double* p) { return __ldcg(p); }
 // C[m×n] = alpha·A·op(B) + beta·C on the block.  A is m×k (lda).  op(B)(kk,j)
 // is B[j + kk·ldb] (B_NN = false: B is n×k, "NT") or B[kk + j·ldb] (B_NN =
 // true: B is k×n, "NN").  LOWER restricts the update to i >= j (SYRK, m == n).
-// beta == 0 never reads C, as in BLAS.
+// beta == 0 never reads C, as in BLAS.  The 128×128 output blocks (the lower
+// ones only for LOWER) are numbered column by column; part `part` of `parts`
+// computes blocks part, part + parts, ...
 template <bool B_NN, bool LOWER>
 __device__ void gemm_f64(int m, int n, int k, double alpha, const double* __restrict__ A, int lda,
-                         const double* __restrict__ B, int ldb, double beta, double* C, int ldc, double* smem) {
+                         const double* __restrict__ B, int ldb, double beta, double* C, int ldc, double* smem,
+                         int part = 0, int parts = 1) {
     double(*As)[kBM] = reinterpret_cast<double(*)[kBM]>(smem);
     double(*Bs)[kBNP] = reinterpret_cast<double(*)[kBNP]>(smem + kBK * kBM);
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-    for (int m0 = 0; m0 < m; m0 += kBM) {
-        for (int n0 = 0; n0 < n; n0 += kBN) {
-            if (LOWER && n0 > m0 + kBM - 1) continue;  // block strictly above the diagonal
+    const int nbm = (m + kBM - 1) / kBM, nbn = (n + kBN - 1) / kBN;
+    const int nblk = LOWER ? nbm * (nbm + 1) / 2 : nbm * nbn;
+    for (int bidx = part; bidx < nblk; bidx += parts) {
+        int bi, bj;
+        if (LOWER) {
+            int r = bidx;
+            bj = 0;
+            while (r >= nbm - bj) {
+                r -= nbm - bj;
+                ++bj;
+            }
+            bi = bj + r;
+        } else {
+            bi = bidx % nbm;
+            bj = bidx / nbm;
+        }
+        const int m0 = bi * kBM, n0 = bj * kBN;
+        {
             double acc[8][8];
 #pragma unroll
             for (int r = 0; r < 8; ++r)
@@ -192,8 +210,16 @@ __device__ inline int potrf_l_f64(int n, double* A, int lda, double* smem) {
 }
 
 // B[m×n] <- alpha·B·L⁻ᵀ, L n×n lower non-unit (right-looking, 32-column panels).
-__device__ inline void trsm_rltn_f64(int m, int n, double alpha, const double* L, int ldl, double* B, int ldb, double* smem) {
+// Rows are independent: part `part` of `parts` solves one slice of rows.
+__device__ inline void trsm_rltn_f64(int m, int n, double alpha, const double* L, int ldl, double* B, int ldb, double* smem,
+                                     int part = 0, int parts = 1) {
     double* Ls = smem + kBK * kBM + kBK * kBNP;
+    {
+        const int per = ((m + parts - 1) / parts + 15) / 16 * 16;
+        const int r0 = min(m, part * per), r1 = min(m, r0 + per);
+        B += r0;
+        m = r1 - r0;
+    }
     for (int p = 0; p < n; p += kPanel) {
         const int nb = min(kPanel, n - p);
         load_panel_block(L + p + (size_t)p * ldl, ldl, nb, Ls);
@@ -217,9 +243,10 @@ __device__ inline void trsm_rltn_f64(int m, int n, double alpha, const double* L
     }
 }
 
-// C[m×n] <- alpha·A + beta·C.
-__device__ inline void geadd_f64(int m, int n, double alpha, const double* A, int lda, double beta, double* C, int ldc) {
-    for (long e = threadIdx.x; e < (long)m * n; e += kThreads) {
+// C[m×n] <- alpha·A + beta·C; part `part` of `parts` takes every parts-th element chunk.
+__device__ inline void geadd_f64(int m, int n, double alpha, const double* A, int lda, double beta, double* C, int ldc,
+                                 int part = 0, int parts = 1) {
+    for (long e = threadIdx.x + (long)part * kThreads; e < (long)m * n; e += (long)kThreads * parts) {
         const int i = (int)(e % m), j = (int)(e / m);
         double v = alpha * ldcg(A + i + (size_t)j * lda);
         if (beta != 0.0) v = fma(beta, ldcg(C + i + (size_t)j * ldc), v);

@@ -20,28 +20,28 @@
 
 namespace ttg {
 
-// One FP64 tile task on the whole block.  Returns POTRF's info (0 = ok).
-__device__ int run_op_f64(const ttg_op& op, double* smem) {
+// One part of an FP64 tile task on the whole block.  Returns POTRF's info (0 = ok).
+__device__ int run_op_f64(const ttg_op& op, int part, int parts, double* smem) {
     switch (op.kind) {
         case TTG_OP_POTRF_L:
             return potrf_l_f64(op.n, (double*)op.c, op.ldc, smem);
         case TTG_OP_TRSM_RLTN:
-            trsm_rltn_f64(op.m, op.n, op.alpha, (const double*)op.a, op.lda, (double*)op.c, op.ldc, smem);
+            trsm_rltn_f64(op.m, op.n, op.alpha, (const double*)op.a, op.lda, (double*)op.c, op.ldc, smem, part, parts);
             return 0;
         case TTG_OP_SYRK_LN:
             gemm_f64<false, true>(op.n, op.n, op.k, op.alpha, (const double*)op.a, op.lda, (const double*)op.a, op.lda,
-                                  op.beta, (double*)op.c, op.ldc, smem);
+                                  op.beta, (double*)op.c, op.ldc, smem, part, parts);
             return 0;
         case TTG_OP_GEMM_NT:
             gemm_f64<false, false>(op.m, op.n, op.k, op.alpha, (const double*)op.a, op.lda, (const double*)op.b, op.ldb,
-                                   op.beta, (double*)op.c, op.ldc, smem);
+                                   op.beta, (double*)op.c, op.ldc, smem, part, parts);
             return 0;
         case TTG_OP_GEMM_NN:
             gemm_f64<true, false>(op.m, op.n, op.k, op.alpha, (const double*)op.a, op.lda, (const double*)op.b, op.ldb,
-                                  op.beta, (double*)op.c, op.ldc, smem);
+                                  op.beta, (double*)op.c, op.ldc, smem, part, parts);
             return 0;
         case TTG_OP_GEADD:
-            geadd_f64(op.m, op.n, op.alpha, (const double*)op.a, op.lda, op.beta, (double*)op.c, op.ldc);
+            geadd_f64(op.m, op.n, op.alpha, (const double*)op.a, op.lda, op.beta, (double*)op.c, op.ldc, part, parts);
             return 0;
         default:
             return 0;
@@ -50,7 +50,9 @@ __device__ int run_op_f64(const ttg_op& op, double* smem) {
 
 __global__ void __launch_bounds__(kThreads, 1) exec_kernel(ExecParams p) {
     extern __shared__ __align__(128) double smem_f64[];
-    executor_loop(p, smem_f64, [](const ttg_op& op, double* smem) { return run_op_f64(op, smem); });
+    executor_loop(p, smem_f64, [](const ttg_op& op, int part, int parts, double* smem) {
+        return run_op_f64(op, part, parts, smem);
+    });
 }
 
 // Post-run summary: tasks that ran other than once, counters not at zero.
@@ -72,6 +74,16 @@ __global__ void summarize_kernel(const int* runs, const int* count, const uint8_
         atomicAdd(out + 1, pending);
         atomicAdd(out + 2, bad);
     }
+}
+
+// Independent DFMA chains (8 per thread) for the FP64 peak measurement.
+__global__ void fp64_peak_kernel(double* out, int iters, double a, double b) {
+    double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    for (int i = 0; i < iters; ++i) {
+        x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+        x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
 
 }  // namespace ttg
@@ -135,6 +147,9 @@ void ttg_graph_free(ttg_ctx* c) {
     dev_free(g.init);
     dev_free(g.count);
     dev_free(g.runs);
+    dev_free(g.parts);
+    dev_free(g.part_next);
+    dev_free(g.part_done);
     dev_free(g.succ_ptr);
     dev_free(g.succ_idx);
     dev_free(g.level);
@@ -192,6 +207,13 @@ ttg_status ttg_ctx_init_device(ttg_ctx* c) {
     TTG_CUDA_TRY(cudaEventCreate(&c->ev1));
     const int smem = kF64SmemDoubles * (int)sizeof(double);
     TTG_CUDA_TRY(cudaFuncSetAttribute(exec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    // Workers of a bound queue wait for their own block, so every block must
+    // be resident: the executor is a cooperative launch and its size is
+    // clamped to what the device can hold at once.
+    int per_sm = 0;
+    TTG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, exec_kernel, kThreads, smem));
+    c->max_workers_f64 = std::max(1, per_sm) * c->sms;
+    if (c->workers > c->max_workers_f64) c->workers = c->max_workers_f64;
     return ttg_mixed_init(c);
 }
 
@@ -209,6 +231,39 @@ extern "C" ttg_status ttg_destroy(ttg_ctx* c) {
 }
 
 extern "C" int ttg_workers(const ttg_ctx* c) { return c ? c->workers : 0; }
+
+// Blocks that share one task: explicit op.parts, else one per 128×128 output
+// block (lower blocks for SYRK) up to 16, TRSM by 128-row slices up to 8;
+// POTRF and no-op tasks are never split.
+int ttg_task_parts(const ttg_op& op) {
+    auto cdiv = [](long a, long b) { return (int)((a + b - 1) / b); };
+    int auto_parts = 1, max_parts = 1;
+    switch (op.kind) {
+        case TTG_OP_GEMM_NT:
+        case TTG_OP_GEMM_NN:
+            max_parts = std::max(1, cdiv(op.m, 128) * cdiv(op.n, 128));
+            auto_parts = std::min(16, max_parts);
+            break;
+        case TTG_OP_SYRK_LN: {
+            const int b = cdiv(op.n, 128);
+            max_parts = std::max(1, b * (b + 1) / 2);
+            auto_parts = std::min(16, max_parts);
+            break;
+        }
+        case TTG_OP_TRSM_RLTN:
+            max_parts = std::max(1, cdiv(op.m, 16));
+            auto_parts = std::min(8, std::max(1, cdiv(op.m, 128)));
+            break;
+        case TTG_OP_GEADD:
+            max_parts = std::max(1, cdiv((long)op.m * op.n, 256));
+            auto_parts = std::min(8, std::max(1, cdiv((long)op.m * op.n, 65536)));
+            break;
+        default:
+            return 1;
+    }
+    if (op.parts > 0) return std::max(1, std::min(op.parts, std::min(64, max_parts)));
+    return std::max(1, auto_parts);
+}
 
 // Priority levels: distinct priorities ranked from high to low; more than
 // kMaxLevels distinct values are split into kMaxLevels equal-count groups.
@@ -299,6 +354,8 @@ extern "C" ttg_status ttg_graph_upload(ttg_ctx* c, const ttg_graph_desc* gd) {
     std::vector<uint8_t> level;
     int n_levels = 1;
     assign_levels(n, gd->priority, runnable, level, &n_levels);
+    std::vector<int> parts(n, 1);
+    for (int t = 0; t < n; ++t) parts[t] = ttg_task_parts(gd->ops[t]);
 
     // Queue layout: level queues sized by runnable unbound tasks per level,
     // bound queues by runnable tasks bound to each worker.
@@ -309,8 +366,8 @@ extern "C" ttg_status ttg_graph_upload(ttg_ctx* c, const ttg_graph_desc* gd) {
     std::vector<int> qcount(kMaxLevels, 0), bqcount(W, 0);
     for (int t = 0; t < n; ++t) {
         if (!runnable[t]) continue;
-        if (bind[t] >= 0) bqcount[bind[t] % W]++;
-        else qcount[level[t]]++;
+        if (bind[t] >= 0) bqcount[bind[t] % W] += parts[t];
+        else qcount[level[t]] += parts[t];
     }
     std::vector<int> q_off(kMaxLevels + 1, 0), bq_off(W + 1, 0);
     for (int l = 0; l < kMaxLevels; ++l) q_off[l + 1] = q_off[l] + qcount[l];
@@ -321,12 +378,14 @@ extern "C" ttg_status ttg_graph_upload(ttg_ctx* c, const ttg_graph_desc* gd) {
     std::vector<int> tail0(kMaxLevels * 32, 0), btail0(W, 0);
     for (int t = 0; t < n; ++t) {
         if (gd->init_count[t] != 0) continue;
-        if (bind[t] >= 0) {
-            const int w = bind[t] % W;
-            bqinit[bq_off[w] + btail0[w]++] = t;
-        } else {
-            const int l = level[t];
-            qinit[q_off[l] + tail0[l * 32]++] = t;
+        for (int q = 0; q < parts[t]; ++q) {
+            if (bind[t] >= 0) {
+                const int w = bind[t] % W;
+                bqinit[bq_off[w] + btail0[w]++] = t;
+            } else {
+                const int l = level[t];
+                qinit[q_off[l] + tail0[l * 32]++] = t;
+            }
         }
     }
 
@@ -347,6 +406,9 @@ extern "C" ttg_status ttg_graph_upload(ttg_ctx* c, const ttg_graph_desc* gd) {
     ALLOC(init, n);
     ALLOC(count, n);
     ALLOC(runs, n);
+    ALLOC(parts, n);
+    ALLOC(part_next, n);
+    ALLOC(part_done, n);
     ALLOC(succ_ptr, n + 1);
     ALLOC(succ_idx, n_edges);
     ALLOC(level, n);
@@ -369,6 +431,7 @@ extern "C" ttg_status ttg_graph_upload(ttg_ctx* c, const ttg_graph_desc* gd) {
     TTG_CUDA_TRY(cudaMemcpy(g.succ_ptr, gd->succ_ptr, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice));
     if (n_edges) TTG_CUDA_TRY(cudaMemcpy(g.succ_idx, gd->succ_idx, sizeof(int32_t) * n_edges, cudaMemcpyHostToDevice));
     TTG_CUDA_TRY(cudaMemcpy(g.level, level.data(), n, cudaMemcpyHostToDevice));
+    TTG_CUDA_TRY(cudaMemcpy(g.parts, parts.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
     TTG_CUDA_TRY(cudaMemcpy(g.bind, bind.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
     TTG_CUDA_TRY(cudaMemcpy(g.runnable, runnable.data(), n, cudaMemcpyHostToDevice));
     TTG_CUDA_TRY(cudaMemcpy(g.qinit, qinit.data(), sizeof(int) * qinit.size(), cudaMemcpyHostToDevice));
@@ -388,6 +451,8 @@ ttg_status ttg_reset_state(ttg_ctx* c, cudaStream_t s) {
     const int n = g.n_tasks, W = c->workers;
     TTG_CUDA_TRY(cudaMemcpyAsync(g.count, g.init, sizeof(int) * std::max(1, n), cudaMemcpyDeviceToDevice, s));
     TTG_CUDA_TRY(cudaMemsetAsync(g.runs, 0, sizeof(int) * std::max(1, n), s));
+    TTG_CUDA_TRY(cudaMemsetAsync(g.part_next, 0, sizeof(int) * std::max(1, n), s));
+    TTG_CUDA_TRY(cudaMemsetAsync(g.part_done, 0, sizeof(int) * std::max(1, n), s));
     TTG_CUDA_TRY(cudaMemcpyAsync(g.qbuf, g.qinit, sizeof(int) * std::max(1, g.q_total), cudaMemcpyDeviceToDevice, s));
     TTG_CUDA_TRY(cudaMemsetAsync(g.q_head, 0, sizeof(int) * kMaxLevels * 32, s));
     TTG_CUDA_TRY(cudaMemcpyAsync(g.q_tail, g.q_tail_init, sizeof(int) * kMaxLevels * 32, cudaMemcpyDeviceToDevice, s));
@@ -407,6 +472,9 @@ static ExecParams ttg_make_params(ttg_ctx* c) {
     p.n_runnable = g.n_runnable;
     p.count = g.count;
     p.runs = g.runs;
+    p.parts = g.parts;
+    p.part_next = g.part_next;
+    p.part_done = g.part_done;
     p.succ_ptr = g.succ_ptr;
     p.succ_idx = g.succ_idx;
     p.level = g.level;
@@ -453,8 +521,8 @@ extern "C" ttg_status ttg_launch(ttg_ctx* c, void* stream) {
 ttg_status ttg_launch_executor(ttg_ctx* c, const ExecParams& p, cudaStream_t s) {
     if (c->g_mixed) return ttg_launch_mixed(c, p, s);
     const int smem = kF64SmemDoubles * (int)sizeof(double);
-    exec_kernel<<<c->workers, kThreads, smem, s>>>(p);
-    TTG_CUDA_TRY(cudaGetLastError());
+    void* args[] = {(void*)&p};
+    TTG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)exec_kernel, dim3(c->workers), dim3(kThreads), args, smem, s));
     return TTG_OK;
 }
 
@@ -525,6 +593,39 @@ extern "C" ttg_status ttg_trace(ttg_ctx* c, int64_t* h_start, int64_t* h_end, in
         if (h_end) h_end[t] = ran ? tr[3 * t + 1] - t0 : -1;
         if (h_worker) h_worker[t] = ran ? (int32_t)tr[3 * t + 2] : -1;
     }
+    return TTG_OK;
+}
+
+extern "C" ttg_status ttg_measure_fp64_peak(ttg_ctx* c, double ms, double* tflops) {
+    if (!c || !tflops || ms <= 0) return TTG_EINVAL;
+    TTG_CUDA_TRY(cudaSetDevice(c->device));
+    const int blocks = c->sms * 2, threads = 256;
+    double* out = nullptr;
+    TTG_CUDA_TRY(cudaMalloc((void**)&out, sizeof(double) * blocks * threads));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    // Calibrate the iteration count on a short run, then time the long one.
+    int iters = 2000;
+    float t = 0.f;
+    for (int pass = 0; pass < 2; ++pass) {
+        fp64_peak_kernel<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+        cudaEventRecord(e0);
+        fp64_peak_kernel<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        cudaEventElapsedTime(&t, e0, e1);
+        if (pass == 0) iters = (int)std::max(1000.0, std::min(2e8, iters * ms / std::max(1e-3, (double)t)));
+    }
+    cudaError_t err = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (err != cudaSuccess) {
+        ttg_set_last_cuda_error(err, "fp64_peak_kernel", __FILE__, __LINE__);
+        return TTG_ECUDA;
+    }
+    *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (t * 1e-3) / 1e12;
     return TTG_OK;
 }
 

@@ -22,6 +22,9 @@ struct DevGraph {
     int* init = nullptr;
     int* count = nullptr;
     int* runs = nullptr;
+    int* parts = nullptr;
+    int* part_next = nullptr;
+    int* part_done = nullptr;
     int64_t* succ_ptr = nullptr;
     int32_t* succ_idx = nullptr;
     uint8_t* level = nullptr;
@@ -44,6 +47,7 @@ struct ttg_ctx {
     int device = 0;
     int sms = 0;
     int workers = 0;
+    int max_workers_f64 = 0;  // co-resident blocks of the FP64 executor
     double timeout_s = 10.0;
     int trace = 0;
     bool uploaded = false;
@@ -65,6 +69,7 @@ ttg_status ttg_ctx_init_device(ttg_ctx* c);
 ttg_status ttg_reset_state(ttg_ctx* c, cudaStream_t s);
 ttg_status ttg_launch_executor(ttg_ctx* c, const ttg::ExecParams& p, cudaStream_t s);
 void ttg_graph_free(ttg_ctx* c);
+int ttg_task_parts(const ttg_op& op);
 
 // Lower tiles of the miniapp matrix 1/((i-j)^2+1) (ttg_gen.cu).
 ttg_status ttg_gen_miniapp_tiles(ttg_ctx* c, const int32_t* h_bs, int32_t nb, double* d_tiles, void* stream);

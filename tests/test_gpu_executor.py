@@ -150,8 +150,9 @@ def run_single(ctx, op):
     return st, rep
 
 
+@pytest.mark.parametrize("parts", [0, 1, 3])
 @pytest.mark.parametrize("m,n,k", [(1, 1, 1), (17, 33, 5), (128, 128, 128), (200, 131, 257), (512, 512, 512)])
-def test_gemm_kernels(ctx, m, n, k):
+def test_gemm_kernels(ctx, m, n, k, parts):
     import torch
     rng = np.random.default_rng(m + n + k)
     A = rng.standard_normal((m, k))
@@ -163,7 +164,7 @@ def test_gemm_kernels(ctx, m, n, k):
         dB, pB = _colmajor(B)
         dC, pC = _colmajor(C0)
         torch.cuda.synchronize()
-        op = t.Op(kind=kind, m=m, n=n, k=k, lda=m, ldb=B.shape[0], ldc=m, alpha=-1.0, beta=1.0, a=pA, b=pB, c=pC)
+        op = t.Op(kind=kind, m=m, n=n, k=k, lda=m, ldb=B.shape[0], ldc=m, parts=parts, alpha=-1.0, beta=1.0, a=pA, b=pB, c=pC)
         st, _ = run_single(ctx, op)
         assert st == t.TTG_OK
         got = _back(dC, (m, n))
@@ -171,8 +172,9 @@ def test_gemm_kernels(ctx, m, n, k):
         assert np.abs(got - want).max() <= 1e-13 * max(1.0, np.abs(want).max()) * k
 
 
-@pytest.mark.parametrize("n,k", [(1, 3), (40, 17), (128, 64), (300, 301)])
-def test_syrk_kernel_lower_only(ctx, n, k):
+@pytest.mark.parametrize("parts", [0, 2])
+@pytest.mark.parametrize("n,k", [(1, 3), (40, 17), (128, 64), (300, 301), (512, 512)])
+def test_syrk_kernel_lower_only(ctx, n, k, parts):
     import torch
     rng = np.random.default_rng(n * 7 + k)
     A = rng.standard_normal((n, k))
@@ -180,7 +182,7 @@ def test_syrk_kernel_lower_only(ctx, n, k):
     dA, pA = _colmajor(A)
     dC, pC = _colmajor(C0)
     torch.cuda.synchronize()
-    op = t.Op(kind=t.OP_SYRK_LN, m=n, n=n, k=k, lda=n, ldc=n, alpha=-1.0, beta=1.0, a=pA, c=pC)
+    op = t.Op(kind=t.OP_SYRK_LN, m=n, n=n, k=k, lda=n, ldc=n, parts=parts, alpha=-1.0, beta=1.0, a=pA, c=pC)
     assert run_single(ctx, op)[0] == t.TTG_OK
     got = _back(dC, (n, n))
     want = C0 - A @ A.T
@@ -217,8 +219,9 @@ def test_potrf_not_positive_definite(ctx):
     assert st == t.TTG_ENOTPD and rep.info == 46 and rep.error_task == 0
 
 
+@pytest.mark.parametrize("parts", [0, 1, 5])
 @pytest.mark.parametrize("m,n,alpha", [(1, 1, 1.0), (50, 33, 1.0), (300, 128, 2.0), (512, 512, 1.0)])
-def test_trsm_kernel(ctx, m, n, alpha):
+def test_trsm_kernel(ctx, m, n, alpha, parts):
     import torch
     rng = np.random.default_rng(m + 3 * n)
     G = rng.standard_normal((n, n))
@@ -227,7 +230,7 @@ def test_trsm_kernel(ctx, m, n, alpha):
     dL, pL = _colmajor(L)
     dB, pB = _colmajor(B)
     torch.cuda.synchronize()
-    op = t.Op(kind=t.OP_TRSM_RLTN, m=m, n=n, lda=n, ldc=m, alpha=alpha, a=pL, c=pB)
+    op = t.Op(kind=t.OP_TRSM_RLTN, m=m, n=n, lda=n, ldc=m, parts=parts, alpha=alpha, a=pL, c=pB)
     assert run_single(ctx, op)[0] == t.TTG_OK
     got = _back(dB, (m, n))
     want = np.linalg.solve(L, (alpha * B).T).T
@@ -243,6 +246,6 @@ def test_geadd_kernel(ctx):
     dA, pA = _colmajor(A)
     dC, pC = _colmajor(C)
     torch.cuda.synchronize()
-    op = t.Op(kind=t.OP_GEADD, m=77, n=45, lda=77, ldc=77, alpha=2.0, beta=1.0, a=pA, c=pC)
+    op = t.Op(kind=t.OP_GEADD, m=77, n=45, lda=77, ldc=77, parts=3, alpha=2.0, beta=1.0, a=pA, c=pC)
     assert run_single(ctx, op)[0] == t.TTG_OK
     assert np.allclose(_back(dC, (77, 45)), 2 * A + C, rtol=0, atol=1e-15)
