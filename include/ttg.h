@@ -154,6 +154,39 @@ int ttg_workers(const ttg_ctx* ctx);
  * roofline denominator of the FP64 tile kernels. */
 ttg_status ttg_measure_fp64_peak(ttg_ctx* ctx, double ms, double* tflops);
 
+/* ---------------------------------------------------- run without allocation */
+
+/* No counterpart in the reference: an addition for callers that cannot call
+ * cudaMalloc — a service whose memory pool already owns the free device
+ * memory, an operator hosted by another framework that may only allocate
+ * through that framework, or a caller that cannot afford the device-wide
+ * synchronisation an allocation can cause.  ttg_run_graph_noalloc uploads the
+ * graph and runs the FP64 executor with all of its scratch (the graph copy,
+ * counters, queues, status words) in one fixed device array of
+ * TTG_NOALLOC_SCRATCH_BYTES that every GPU loading libttg.so reserves until
+ * the process exits; it calls no device allocation routine.
+ *
+ * Limits: n_tasks <= TTG_NOALLOC_MAX_TASKS, successor entries <=
+ * TTG_NOALLOC_MAX_EDGES, queue entries (parts of the runnable tasks, see
+ * ttg_op.parts) <= TTG_NOALLOC_MAX_QUEUE, workers <= TTG_NOALLOC_MAX_WORKERS;
+ * larger graphs are rejected with TTG_EINVAL before anything is written.
+ * Only TTG_PREC_F64 tasks.  The tiles in the ops are the caller's (inputs and
+ * outputs); `workers` 0 = one per SM; `timeout_s` 0 = 10 s.
+ *
+ * Every call shares the array and finds the previous call's contents in it:
+ * each call rewrites all of it that the kernel reads.  Calls that overlapped
+ * on the GPU would race on it, so calls are serialised by a process-wide lock
+ * and each call waits for `stream` before returning.  The first call on a
+ * device also looks up the array's device address (with that device
+ * current); make that first call before any stream capture begins. */
+#define TTG_NOALLOC_MAX_TASKS 16384
+#define TTG_NOALLOC_MAX_EDGES 131072
+#define TTG_NOALLOC_MAX_QUEUE 262144
+#define TTG_NOALLOC_MAX_WORKERS 1024
+#define TTG_NOALLOC_SCRATCH_BYTES (4u << 20)
+ttg_status ttg_run_graph_noalloc(int device, const ttg_graph_desc* g, int workers, double timeout_s, void* stream,
+                                 ttg_report* rep);
+
 /* ------------------------------------------------------------ generators */
 /* Seeded inputs of the workloads (include/ttg_philox.h), built on the device. */
 

@@ -86,6 +86,8 @@ SIGNATURES = {
     "ttg_gen_normal": (_STATUS, [_P, ctypes.c_int64, ctypes.c_uint32, ctypes.c_uint32, _P, _P]),
     "ttg_tile_layout": (ctypes.c_int64, [_P, _I32, _P]),
     "ttg_measure_fp64_peak": (_STATUS, [_P, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
+    "ttg_run_graph_noalloc": (_STATUS, [ctypes.c_int, ctypes.POINTER(GraphDesc), ctypes.c_int, ctypes.c_double, _P,
+                                        ctypes.POINTER(Report)]),
     # include/ttg_apps.h
     "ttg_chol_plan_create": (_STATUS, [_P, ctypes.POINTER(CholArgs), ctypes.POINTER(_P)]),
     "ttg_chol_plan_destroy": (_STATUS, [_P]),
