@@ -91,6 +91,44 @@ ttg_status ttg_chol_dag_dump(const ttg_chol_args* args, const char* prefix);
 /* Per-kind device busy time (ms) of the last run (needs ctx trace). */
 ttg_status ttg_chol_plan_kind_times(ttg_chol_plan* plan, double* potrf_ms, double* trsm_ms, double* gemm_ms, double* accu_ms);
 
+/* ------------------------------------------------------------------ solve */
+
+/* Solve A X = B with the plan's factor.  FP64 plan: X = L⁻ᵀL⁻¹B (block
+ * sweeps with inverted diagonal tiles).  Mixed plan: GMRES-based iterative
+ * refinement preconditioned by the low-precision factor, with the residual
+ * r = B − A X and the update X += D in FP64, until the backward error
+ * ‖b − A x‖∞ / (‖A‖∞ ‖x‖∞) of every column is ≤ tol. */
+typedef struct ttg_solve_opts {
+    int32_t nrhs;       /* right-hand sides, 1..16                                     */
+    double tol;         /* target backward error (0 = 1e-14)                           */
+    int32_t max_outer;  /* refinement steps (0 = 10)                                   */
+    int32_t restart;    /* GMRES iterations per step (0 = 20, at most 60)              */
+    int32_t gmres_prec; /* 0 auto (FP32 Krylov work, FP64 once FP32 stalls), 32, 64    */
+    double inner_tol;   /* relative GMRES tolerance per step (0 = 1e-6)                */
+} ttg_solve_opts;
+
+typedef struct ttg_solve_report {
+    int32_t status;     /* TTG_OK or TTG_ENOCONV                                       */
+    int32_t outer;      /* refinement steps taken                                      */
+    int32_t inner;      /* GMRES iterations, all steps                                 */
+    int32_t gmres_prec; /* precision of the last GMRES cycle (32 or 64)                */
+    double bwd_err;     /* max over columns of ‖b − A x‖∞ / (‖A‖∞ ‖x‖∞), FP64          */
+    double anorm_inf;   /* ‖A‖∞                                                        */
+    double factor_ms;   /* factorisation (device events; 0 for ttg_chol_plan_solve)     */
+    double solve_ms;    /* solve and refinement (host clock)                           */
+} ttg_solve_report;
+
+/* d_B, d_X: device N×nrhs column-major (ld N). */
+ttg_status ttg_chol_plan_solve(ttg_chol_plan* plan, const double* d_B, double* d_X, const ttg_solve_opts* opts,
+                               ttg_solve_report* rep, void* stream);
+/* Time to solution on the resident input: restore, factor, solve. */
+ttg_status ttg_chol_posv(ttg_chol_plan* plan, const double* d_B, double* d_X, const ttg_solve_opts* opts,
+                         ttg_solve_report* rep, void* stream);
+/* End to end with host buffers: h_tiles (packed lower tiles of A, or NULL to
+ * keep the resident input), h_B in, h_X out (N×nrhs column-major). */
+ttg_status ttg_chol_posv_host(ttg_chol_plan* plan, const double* h_tiles, const double* h_B, double* h_X,
+                              const ttg_solve_opts* opts, ttg_solve_report* rep, void* stream);
+
 /* Arguments of 2d_gemm (2d_gemm.cpp:243-253) at one rank. */
 typedef struct ttg_gemm_args {
     int32_t n_threads;

@@ -65,6 +65,20 @@ class GemmArgs(ctypes.Structure):
                 ("matrix_size", ctypes.c_int32), ("inputs", ctypes.c_int32), ("seed", ctypes.c_uint32)]
 
 
+class SolveOpts(ctypes.Structure):
+    _fields_ = [("nrhs", ctypes.c_int32), ("tol", ctypes.c_double), ("max_outer", ctypes.c_int32),
+                ("restart", ctypes.c_int32), ("gmres_prec", ctypes.c_int32), ("inner_tol", ctypes.c_double)]
+
+
+class SolveReport(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("outer", ctypes.c_int32), ("inner", ctypes.c_int32),
+                ("gmres_prec", ctypes.c_int32), ("bwd_err", ctypes.c_double), ("anorm_inf", ctypes.c_double),
+                ("factor_ms", ctypes.c_double), ("solve_ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 # Every symbol the public headers declare, with its ctypes signature.
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32
@@ -108,6 +122,9 @@ SIGNATURES = {
     "ttg_chol_plan_kind_times": (_STATUS, [_P, _P, _P, _P, _P]),
     "ttg_chol_dag_dump": (_STATUS, [ctypes.POINTER(CholArgs), ctypes.c_char_p]),
     "ttg_gemm_dag_dump": (_STATUS, [ctypes.POINTER(GemmArgs), ctypes.c_char_p]),
+    "ttg_chol_plan_solve": (_STATUS, [_P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveReport), _P]),
+    "ttg_chol_posv": (_STATUS, [_P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveReport), _P]),
+    "ttg_chol_posv_host": (_STATUS, [_P, _P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveReport), _P]),
     "ttg_gemm_plan_create": (_STATUS, [_P, ctypes.POINTER(GemmArgs), ctypes.POINTER(_P)]),
     "ttg_gemm_plan_destroy": (_STATUS, [_P]),
     "ttg_gemm_plan_tasks": (_I32, [_P, ctypes.POINTER(ctypes.c_double)]),
@@ -300,6 +317,28 @@ class CholPlan:
 
     def dump_dag(self, prefix):
         check(lib().ttg_chol_plan_dump_dag(self.h, prefix.encode()), "dump_dag")
+
+    def solve_host(self, B, tiles=None, tol=1e-14, max_outer=10, restart=20, gmres_prec=0, inner_tol=0.0, factor=True):
+        """Factor (unless factor=False) and solve A X = B with host arrays
+        (B: N×nrhs).  Returns (status, SolveReport, X)."""
+        B = np.asfortranarray(B, dtype=np.float64)
+        if B.ndim == 1:
+            B = B.reshape(-1, 1, order="F")
+        X = np.zeros_like(B, order="F")
+        o = SolveOpts(B.shape[1], tol, max_outer, restart, gmres_prec, inner_tol)
+        rep = SolveReport()
+        if factor:
+            st = lib().ttg_chol_posv_host(self.h, _ptr(tiles) if tiles is not None else None, _ptr(B), _ptr(X),
+                                          ctypes.byref(o), ctypes.byref(rep), None)
+        else:
+            import torch
+            dB = torch.from_numpy(np.ascontiguousarray(B.T)).cuda()
+            dX = torch.zeros_like(dB)
+            torch.cuda.synchronize()
+            st = lib().ttg_chol_plan_solve(self.h, ctypes.c_void_p(dB.data_ptr()), ctypes.c_void_p(dX.data_ptr()),
+                                           ctypes.byref(o), ctypes.byref(rep), None)
+            X = np.asfortranarray(dX.cpu().numpy().T)
+        return st, rep, X
 
     def kind_times(self):
         v = [ctypes.c_double() for _ in range(4)]

@@ -16,6 +16,7 @@
 
 #include <algorithm>
 #include <array>
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -30,6 +31,7 @@
 #include "../tasktorrent/tasktorrent.hpp"
 #include "ttg_internal.h"
 #include "ttg_mixed_api.h"
+#include "ttg_solve_api.h"
 
 using namespace ttor;
 typedef std::array<int, 2> Key2;  // the reference's int2 (CUDA headers own that name)
@@ -71,6 +73,11 @@ struct ttg_chol_plan {
     std::vector<int> kind_of_dev;  // per device task: 0 potrf, 1 trsm, 2 gemm, 3 accu, -1 other
     std::vector<double*> tmp;      // accumulate-flow temporaries (device)
     ttg_mixed_state* mixed = nullptr;
+    ttg_solver* solver = nullptr;
+    double* d_b = nullptr;         // device B and X of ttg_chol_posv_host
+    size_t host_b_elems = 0;
+    long factor_gen = 0;   // incremented by every successful factorisation
+    long solver_gen = -1;  // factorisation the solver's inverted tiles belong to
 };
 
 static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry) {
@@ -130,7 +137,7 @@ static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry) {
     Taskflow<Key3> accu(&tp, a.verb);
 
     potrf.set_task([&](int j) {
-             if (mixed) ttg_mixed_record_potrf(P->mixed, j);
+             if (mixed) gpu::record_op(ttg_mixed_potrf_op(P->mixed, j));
              else gpu::LAPACKE_dpotrf(gpu::LAPACK_COL_MAJOR, 'L', P->bs[j], block(j, j), lda(j));
          })
         .set_fulfill([&](int j) {
@@ -143,7 +150,7 @@ static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry) {
 
     trsm.set_task([&](Key2 ij) {
             const int i = ij[0], j = ij[1];
-            if (mixed) ttg_mixed_record_trsm(P->mixed, i, j);
+            if (mixed) gpu::record_op(ttg_mixed_trsm_op(P->mixed, i, j));
             else
                 gpu::cblas_dtrsm(gpu::CblasColMajor, gpu::CblasRight, gpu::CblasLower, gpu::CblasTrans, gpu::CblasNonUnit,
                                  P->bs[i], P->bs[j], 1.0, block(j, j), lda(j), block(i, j), lda(i));
@@ -163,7 +170,7 @@ static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry) {
             double* C = accumulate ? tmp_of[{k, i, j}] : block(i, j);
             const double beta = accumulate ? 0.0 : 1.0;
             if (mixed) {
-                ttg_mixed_record_update(P->mixed, k, i, j);
+                gpu::record_op(ttg_mixed_update_op(P->mixed, k, i, j));
             } else if (i == j) {
                 gpu::cblas_dsyrk(gpu::CblasColMajor, gpu::CblasLower, gpu::CblasNoTrans, P->bs[i], P->bs[k], -1.0, block(i, k),
                                  lda(i), beta, C, lda(i));
@@ -294,6 +301,8 @@ extern "C" ttg_status ttg_chol_plan_destroy(ttg_chol_plan* P) {
     if (P->tiles) cudaFree(P->tiles);
     if (P->pristine) cudaFree(P->pristine);
     if (P->mixed) ttg_mixed_state_destroy(P->mixed);
+    if (P->solver) ttg_solver_destroy(P->solver);
+    if (P->d_b) cudaFree(P->d_b);
     delete P;
     return TTG_OK;
 }
@@ -325,6 +334,7 @@ extern "C" ttg_status ttg_chol_plan_generate(ttg_chol_plan* P, void* stream) {
     else
         s = ttg_gen_miniapp_tiles(P->ctx, P->bs.data(), P->nb, P->pristine, stream);
     if (s != TTG_OK) return s;
+    if (P->solver) ttg_solver_input_changed(P->solver);
     return ttg_chol_plan_restore(P, stream);
 }
 
@@ -358,6 +368,7 @@ extern "C" ttg_status ttg_chol_plan_set_matrix(ttg_chol_plan* P, const double* h
     ttg_status st = dense_to_tiles(P, h_A, P->pristine, s);
     if (st != TTG_OK) return st;
     TTG_CUDA_CHECK(cudaStreamSynchronize(s));
+    if (P->solver) ttg_solver_input_changed(P->solver);
     return ttg_chol_plan_restore(P, stream);
 }
 
@@ -377,6 +388,7 @@ extern "C" ttg_status ttg_chol_plan_factor(ttg_chol_plan* P, void* stream, ttg_r
     }
     ttg_status s = P->tp->replay(stream);
     if (rep) *rep = P->tp->report();
+    if (s == TTG_OK) ++P->factor_gen;
     return s;
 }
 
@@ -444,6 +456,69 @@ extern "C" ttg_status ttg_chol_plan_get_input(ttg_chol_plan* P, double* h_A) {
     for (int j = 0; j < P->N; ++j)
         for (int i = 0; i < j; ++i) h_A[i + (size_t)j * P->N] = h_A[j + (size_t)i * P->N];
     return TTG_OK;
+}
+
+extern "C" ttg_status ttg_chol_plan_solve(ttg_chol_plan* P, const double* d_B, double* d_X, const ttg_solve_opts* o,
+                                          ttg_solve_report* rep, void* stream) {
+    if (!P || !o || !d_B || !d_X) return TTG_EINVAL;
+    if (P->factor_gen == 0) return TTG_ESTATE;
+    TTG_CUDA_CHECK(cudaSetDevice(P->ctx->device));
+    cudaStream_t s = (cudaStream_t)stream;
+    const bool mixed = P->mixed != nullptr;
+    if (!P->solver) {
+        ttg_status st = ttg_solver_create(P->ctx, P->N, P->nb, P->bs.data(), P->off.data(), mixed, &P->solver);
+        if (st != TTG_OK) return st;
+    }
+    auto t0 = std::chrono::steady_clock::now();
+    const float* L32 = mixed ? ttg_mixed_factor32(P->mixed) : nullptr;
+    if (P->solver_gen != P->factor_gen) {
+        ttg_status st = ttg_solver_factor_done(P->solver, P->tiles, L32, s);
+        if (st != TTG_OK) return st;
+        P->solver_gen = P->factor_gen;
+    }
+    ttg_solve_report r{};
+    ttg_status st = ttg_solver_solve(P->solver, P->pristine, P->tiles, L32, d_B, d_X, o, &r, s);
+    r.solve_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (rep) *rep = r;
+    return st;
+}
+
+extern "C" ttg_status ttg_chol_posv(ttg_chol_plan* P, const double* d_B, double* d_X, const ttg_solve_opts* o,
+                                   ttg_solve_report* rep, void* stream) {
+    if (!P) return TTG_EINVAL;
+    ttg_status st = ttg_chol_plan_restore(P, stream);
+    if (st != TTG_OK) return st;
+    ttg_report fr{};
+    st = ttg_chol_plan_factor(P, stream, &fr);
+    if (st != TTG_OK) return st;
+    st = ttg_chol_plan_solve(P, d_B, d_X, o, rep, stream);
+    if (rep) rep->factor_ms = fr.elapsed_ms;
+    return st;
+}
+
+extern "C" ttg_status ttg_chol_posv_host(ttg_chol_plan* P, const double* h_tiles, const double* h_B, double* h_X,
+                                        const ttg_solve_opts* o, ttg_solve_report* rep, void* stream) {
+    if (!P || !o || !h_B || !h_X || o->nrhs < 1 || o->nrhs > 16) return TTG_EINVAL;
+    TTG_CUDA_CHECK(cudaSetDevice(P->ctx->device));
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t blk = (size_t)P->N * o->nrhs;
+    if (P->host_b_elems < blk) {
+        if (P->d_b) cudaFree(P->d_b);
+        P->d_b = nullptr;
+        P->host_b_elems = 0;
+        TTG_CUDA_CHECK(cudaMalloc((void**)&P->d_b, sizeof(double) * 2 * blk));
+        P->host_b_elems = blk;
+    }
+    if (h_tiles) {
+        TTG_CUDA_CHECK(cudaMemcpyAsync(P->pristine, h_tiles, sizeof(double) * P->elems, cudaMemcpyHostToDevice, s));
+        if (P->solver) ttg_solver_input_changed(P->solver);
+    }
+    TTG_CUDA_CHECK(cudaMemcpyAsync(P->d_b, h_B, sizeof(double) * blk, cudaMemcpyHostToDevice, s));
+    ttg_status st = ttg_chol_posv(P, P->d_b, P->d_b + blk, o, rep, stream);
+    if (st != TTG_OK && st != TTG_ENOCONV) return st;
+    TTG_CUDA_CHECK(cudaMemcpyAsync(h_X, P->d_b + blk, sizeof(double) * blk, cudaMemcpyDeviceToHost, s));
+    TTG_CUDA_CHECK(cudaStreamSynchronize(s));
+    return st;
 }
 
 extern "C" ttg_status ttg_chol_plan_dump_dag(ttg_chol_plan* P, const char* prefix) {

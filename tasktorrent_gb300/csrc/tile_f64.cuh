@@ -27,6 +27,7 @@ constexpr int kPanel = 32;     // POTRF / TRSM panel width
 constexpr int kF64SmemDoubles = kBK * kBM + kBK * kBNP + kPanel * (kPanel + 1);
 
 __device__ __forceinline__ double ldcg(const double* p) { return __ldcg(p); }
+__device__ __forceinline__ float ldcg(const float* p) { return __ldcg(p); }
 
 // C[m×n] = alpha·A·op(B) + beta·C on the block.  A is m×k (lda).  op(B)(kk,j)
 // is B[j + kk·ldb] (B_NN = false: B is n×k, "NT") or B[kk + j·ldb] (B_NN =
@@ -34,12 +35,12 @@ __device__ __forceinline__ double ldcg(const double* p) { return __ldcg(p); }
 // beta == 0 never reads C, as in BLAS.  The 128×128 output blocks (the lower
 // ones only for LOWER) are numbered column by column; part `part` of `parts`
 // computes blocks part, part + parts, ...
-template <bool B_NN, bool LOWER>
-__device__ void gemm_f64(int m, int n, int k, double alpha, const double* __restrict__ A, int lda,
-                         const double* __restrict__ B, int ldb, double beta, double* C, int ldc, double* smem,
-                         int part = 0, int parts = 1) {
-    double(*As)[kBM] = reinterpret_cast<double(*)[kBM]>(smem);
-    double(*Bs)[kBNP] = reinterpret_cast<double(*)[kBNP]>(smem + kBK * kBM);
+// T is double (the FP64 path) or float (the FP32 updates of the mixed path).
+template <class T, bool B_NN, bool LOWER>
+__device__ void gemm_tile(int m, int n, int k, T alpha, const T* __restrict__ A, int lda, const T* __restrict__ B, int ldb,
+                          T beta, T* C, int ldc, T* smem, int part = 0, int parts = 1) {
+    T(*As)[kBM] = reinterpret_cast<T(*)[kBM]>(smem);
+    T(*Bs)[kBNP] = reinterpret_cast<T(*)[kBNP]>(smem + kBK * kBM);
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     const int nbm = (m + kBM - 1) / kBM, nbn = (n + kBN - 1) / kBN;
     const int nblk = LOWER ? nbm * (nbm + 1) / 2 : nbm * nbn;
@@ -59,18 +60,18 @@ __device__ void gemm_f64(int m, int n, int k, double alpha, const double* __rest
         }
         const int m0 = bi * kBM, n0 = bj * kBN;
         {
-            double acc[8][8];
+            T acc[8][8];
 #pragma unroll
             for (int r = 0; r < 8; ++r)
 #pragma unroll
-                for (int c = 0; c < 8; ++c) acc[r][c] = 0.0;
+                for (int c = 0; c < 8; ++c) acc[r][c] = T(0);
             for (int k0 = 0; k0 < k; k0 += kBK) {
 #pragma unroll
                 for (int r = 0; r < (kBK * kBM) / kThreads; ++r) {
                     const int idx = tid + kThreads * r;
                     const int i = idx & (kBM - 1), kk = idx / kBM;
                     const int gi = m0 + i, gk = k0 + kk;
-                    As[kk][i] = (gi < m && gk < k) ? ldcg(A + gi + (size_t)gk * lda) : 0.0;
+                    As[kk][i] = (gi < m && gk < k) ? ldcg(A + gi + (size_t)gk * lda) : T(0);
                 }
 #pragma unroll
                 for (int r = 0; r < (kBK * kBN) / kThreads; ++r) {
@@ -79,14 +80,14 @@ __device__ void gemm_f64(int m, int n, int k, double alpha, const double* __rest
                     if (B_NN) { kk = idx & (kBK - 1); j = idx / kBK; }
                     else { j = idx & (kBN - 1); kk = idx / kBN; }
                     const int gj = n0 + j, gk = k0 + kk;
-                    double v = 0.0;
+                    T v = T(0);
                     if (gj < n && gk < k) v = B_NN ? ldcg(B + gk + (size_t)gj * ldb) : ldcg(B + gj + (size_t)gk * ldb);
                     Bs[kk][j] = v;
                 }
                 __syncthreads();
 #pragma unroll
                 for (int kk = 0; kk < kBK; ++kk) {
-                    double a[8], b[8];
+                    T a[8], b[8];
 #pragma unroll
                     for (int r = 0; r < 8; ++r) a[r] = As[kk][tx + 16 * r];
 #pragma unroll
@@ -105,15 +106,21 @@ __device__ void gemm_f64(int m, int n, int k, double alpha, const double* __rest
                 for (int r = 0; r < 8; ++r) {
                     const int gi = m0 + tx + 16 * r;
                     if (gi < m && gj < n && (!LOWER || gi >= gj)) {
-                        double* p = C + gi + (size_t)gj * ldc;
-                        double v = alpha * acc[r][c];
-                        if (beta != 0.0) v = fma(beta, ldcg(p), v);
+                        T* p = C + gi + (size_t)gj * ldc;
+                        T v = alpha * acc[r][c];
+                        if (beta != T(0)) v = fma(beta, ldcg(p), v);
                         *p = v;
                     }
                 }
             }
         }
     }
+}
+
+template <bool B_NN, bool LOWER>
+__device__ __forceinline__ void gemm_f64(int m, int n, int k, double alpha, const double* A, int lda, const double* B, int ldb,
+                                         double beta, double* C, int ldc, double* smem, int part = 0, int parts = 1) {
+    gemm_tile<double, B_NN, LOWER>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, smem, part, parts);
 }
 
 // Unblocked lower Cholesky of the nb×nb (nb <= 32) diagonal block at A (lda)
@@ -152,15 +159,16 @@ __device__ inline int potrf_diag32_warp(double* A, int lda, int nb) {
 
 // Rows [row0, m) of X[:, 0:nb] (ldx) <- X · Lᵀ⁻¹ with the nb×nb lower block
 // Ls (shared, ld kPanel+1); one thread per row.
-__device__ inline void trsm_rows_panel(double* X, int ldx, int row0, int m, int nb, const double* Ls, double alpha) {
+template <class T>
+__device__ inline void trsm_rows_panel(T* X, int ldx, int row0, int m, int nb, const T* Ls, T alpha) {
     for (int i = row0 + threadIdx.x; i < m; i += kThreads) {
-        double x[kPanel];
+        T x[kPanel];
 #pragma unroll
-        for (int c = 0; c < kPanel; ++c) x[c] = (c < nb) ? alpha * ldcg(X + i + (size_t)c * ldx) : 0.0;
+        for (int c = 0; c < kPanel; ++c) x[c] = (c < nb) ? alpha * ldcg(X + i + (size_t)c * ldx) : T(0);
 #pragma unroll
         for (int c = 0; c < kPanel; ++c) {
             if (c < nb) {
-                double s = x[c];
+                T s = x[c];
 #pragma unroll
                 for (int l = 0; l < c; ++l) s = fma(-x[l], Ls[c * (kPanel + 1) + l], s);
                 x[c] = s / Ls[c * (kPanel + 1) + c];
@@ -173,10 +181,11 @@ __device__ inline void trsm_rows_panel(double* X, int ldx, int row0, int m, int 
 }
 
 // Load the nb×nb lower block at L (ldl) into Ls (ld kPanel+1), zero above.
-__device__ inline void load_panel_block(const double* L, int ldl, int nb, double* Ls) {
+template <class T>
+__device__ inline void load_panel_block(const T* L, int ldl, int nb, T* Ls) {
     for (int e = threadIdx.x; e < kPanel * kPanel; e += kThreads) {
         const int c = e / kPanel, l = e % kPanel;  // Ls[c][l] = L(c, l)
-        Ls[c * (kPanel + 1) + l] = (c < nb && l < nb && l <= c) ? ldcg(L + c + (size_t)l * ldl) : 0.0;
+        Ls[c * (kPanel + 1) + l] = (c < nb && l < nb && l <= c) ? ldcg(L + c + (size_t)l * ldl) : T(0);
     }
 }
 
@@ -195,11 +204,11 @@ __device__ inline int potrf_l_f64(int n, double* A, int lda, double* smem) {
         __syncthreads();
         const int info = s_info;
         if (info) return info;
-        load_panel_block(Dpp, lda, nb, Ls);
+        load_panel_block<double>(Dpp, lda, nb, Ls);
         __syncthreads();
         const int rest = n - p - nb;
         if (rest > 0) {
-            trsm_rows_panel(A + (size_t)p * lda, lda, p + nb, n, nb, Ls, 1.0);
+            trsm_rows_panel<double>(A + (size_t)p * lda, lda, p + nb, n, nb, Ls, 1.0);
             __syncthreads();
             double* P = A + (p + nb) + (size_t)p * lda;
             gemm_f64<false, true>(rest, rest, nb, -1.0, P, lda, P, lda, 1.0, A + (p + nb) + (size_t)(p + nb) * lda, lda, smem);
@@ -211,9 +220,10 @@ __device__ inline int potrf_l_f64(int n, double* A, int lda, double* smem) {
 
 // B[m×n] <- alpha·B·L⁻ᵀ, L n×n lower non-unit (right-looking, 32-column panels).
 // Rows are independent: part `part` of `parts` solves one slice of rows.
-__device__ inline void trsm_rltn_f64(int m, int n, double alpha, const double* L, int ldl, double* B, int ldb, double* smem,
-                                     int part = 0, int parts = 1) {
-    double* Ls = smem + kBK * kBM + kBK * kBNP;
+template <class T>
+__device__ inline void trsm_rltn_tile(int m, int n, T alpha, const T* L, int ldl, T* B, int ldb, T* smem, int part = 0,
+                                      int parts = 1) {
+    T* Ls = smem + kBK * kBM + kBK * kBNP;
     {
         const int per = ((m + parts - 1) / parts + 15) / 16 * 16;
         const int r0 = min(m, part * per), r1 = min(m, r0 + per);
@@ -222,37 +232,48 @@ __device__ inline void trsm_rltn_f64(int m, int n, double alpha, const double* L
     }
     for (int p = 0; p < n; p += kPanel) {
         const int nb = min(kPanel, n - p);
-        load_panel_block(L + p + (size_t)p * ldl, ldl, nb, Ls);
+        load_panel_block<T>(L + p + (size_t)p * ldl, ldl, nb, Ls);
         __syncthreads();
         // Columns right of p are scaled by alpha when their panel is solved;
         // the update below subtracts solved (already scaled) columns, so scale
         // the remaining columns once, before the first update touches them.
-        if (p == 0 && alpha != 1.0 && n > nb) {
+        if (p == 0 && alpha != T(1) && n > nb) {
             for (int e = threadIdx.x; e < m * (n - nb); e += kThreads) {
                 const int i = e % m, j = nb + e / m;
                 B[i + (size_t)j * ldb] = alpha * ldcg(B + i + (size_t)j * ldb);
             }
         }
-        trsm_rows_panel(B + (size_t)p * ldb, ldb, 0, m, nb, Ls, p == 0 ? alpha : 1.0);
+        trsm_rows_panel<T>(B + (size_t)p * ldb, ldb, 0, m, nb, Ls, p == 0 ? alpha : T(1));
         __syncthreads();
         const int rest = n - p - nb;
         if (rest > 0)
-            gemm_f64<false, false>(m, rest, nb, -1.0, B + (size_t)p * ldb, ldb, L + (p + nb) + (size_t)p * ldl, ldl, 1.0,
-                                   B + (size_t)(p + nb) * ldb, ldb, smem);
+            gemm_tile<T, false, false>(m, rest, nb, T(-1), B + (size_t)p * ldb, ldb, L + (p + nb) + (size_t)p * ldl, ldl, T(1),
+                                       B + (size_t)(p + nb) * ldb, ldb, smem);
         __syncthreads();
     }
 }
 
+__device__ __forceinline__ void trsm_rltn_f64(int m, int n, double alpha, const double* L, int ldl, double* B, int ldb,
+                                              double* smem, int part = 0, int parts = 1) {
+    trsm_rltn_tile<double>(m, n, alpha, L, ldl, B, ldb, smem, part, parts);
+}
+
 // C[m×n] <- alpha·A + beta·C; part `part` of `parts` takes every parts-th element chunk.
-__device__ inline void geadd_f64(int m, int n, double alpha, const double* A, int lda, double beta, double* C, int ldc,
-                                 int part = 0, int parts = 1) {
+template <class T>
+__device__ inline void geadd_tile(int m, int n, T alpha, const T* A, int lda, T beta, T* C, int ldc, int part = 0,
+                                  int parts = 1) {
     for (long e = threadIdx.x + (long)part * kThreads; e < (long)m * n; e += (long)kThreads * parts) {
         const int i = (int)(e % m), j = (int)(e / m);
-        double v = alpha * ldcg(A + i + (size_t)j * lda);
-        if (beta != 0.0) v = fma(beta, ldcg(C + i + (size_t)j * ldc), v);
+        T v = alpha * ldcg(A + i + (size_t)j * lda);
+        if (beta != T(0)) v = fma(beta, ldcg(C + i + (size_t)j * ldc), v);
         C[i + (size_t)j * ldc] = v;
     }
     __syncthreads();
+}
+
+__device__ __forceinline__ void geadd_f64(int m, int n, double alpha, const double* A, int lda, double beta, double* C,
+                                          int ldc, int part = 0, int parts = 1) {
+    geadd_tile<double>(m, n, alpha, A, lda, beta, C, ldc, part, parts);
 }
 
 }  // namespace ttg

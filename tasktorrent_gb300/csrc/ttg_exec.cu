@@ -317,6 +317,7 @@ extern "C" ttg_status ttg_graph_upload(ttg_ctx* c, const ttg_graph_desc* gd) {
         if (gd->init_count[t] < 0 || gd->succ_ptr[t] > gd->succ_ptr[t + 1]) return TTG_EINVAL;
         const int k = gd->ops[t].kind;
         if (k < TTG_OP_NOP || k > TTG_OP_GEADD) return TTG_EINVAL;
+        if (gd->ops[t].prec != TTG_PREC_F64 && gd->ops[t].prec != TTG_PREC_MIXED) return TTG_EINVAL;
     }
     if (n > 0 && gd->succ_ptr[0] != 0) return TTG_EINVAL;
     for (int64_t e = 0; e < n_edges; ++e)
@@ -349,6 +350,9 @@ extern "C" ttg_status ttg_graph_upload(ttg_ctx* c, const ttg_graph_desc* gd) {
     int n_runnable = 0;
     for (int t = 0; t < n; ++t) n_runnable += runnable[t];
     c->pending_host = n - n_runnable;
+    c->g_mixed = false;
+    for (int t = 0; t < n; ++t)
+        if (gd->ops[t].prec == TTG_PREC_MIXED) c->g_mixed = true;
     c->overcount_host = over;
 
     std::vector<uint8_t> level;

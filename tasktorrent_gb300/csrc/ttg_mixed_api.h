@@ -1,5 +1,11 @@
 // ttg_mixed_api.h — host interface of the mixed-precision Cholesky path,
 // used by the Cholesky plan (apps.cpp).  Not part of the public ABI.
+//
+// Working data of one mixed factorisation: an FP32 copy of the packed lower
+// tiles (the trailing updates accumulate there in FP32), BF16 copies of the
+// factored panel tiles with one power-of-two scale per tile (operands of the
+// tensor-core updates), and the FP64 tiles of the plan used as scratch for the
+// FP64 diagonal POTRF.
 #pragma once
 #include <stdint.h>
 
@@ -7,14 +13,17 @@
 
 struct ttg_mixed_state;
 
-ttg_status ttg_mixed_state_create(ttg_ctx* ctx, int N, int nb, const int* bs, const int64_t* off, double* tiles, int kind,
+// kind: 0 = BF16 updates on tensor cores, 1 = FP32 updates.
+ttg_status ttg_mixed_state_create(ttg_ctx* ctx, int N, int nb, const int* bs, const int64_t* off, double* tiles64, int kind,
                                   ttg_mixed_state** out);
 void ttg_mixed_state_destroy(ttg_mixed_state* m);
-// Record the mixed-precision tile operation of a task into the running task.
-void ttg_mixed_record_potrf(ttg_mixed_state* m, int j);
-void ttg_mixed_record_trsm(ttg_mixed_state* m, int i, int j);
-void ttg_mixed_record_update(ttg_mixed_state* m, int k, int i, int j);
-// Convert the FP64 input tiles to the working precision before a run.
+// Tile operations of the three task kinds.
+ttg_op ttg_mixed_potrf_op(ttg_mixed_state* m, int j);
+ttg_op ttg_mixed_trsm_op(ttg_mixed_state* m, int i, int j);
+ttg_op ttg_mixed_update_op(ttg_mixed_state* m, int k, int i, int j);
+// Convert the FP64 input tiles (tiles64) to the FP32 working tiles.
 ttg_status ttg_mixed_prepare(ttg_mixed_state* m, void* stream);
-// FP64 tiles holding the low-precision factor after a run.
+// The low-precision factor as FP64 tiles (converted into tiles64).
 const double* ttg_mixed_factor_tiles(ttg_mixed_state* m);
+// The FP32 factor tiles (same layout as tiles64).
+const float* ttg_mixed_factor32(ttg_mixed_state* m);

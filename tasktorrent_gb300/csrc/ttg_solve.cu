@@ -1,0 +1,452 @@
+// ttg_solve.cu — triangular solves with a Cholesky plan's factor, the FP64
+// residual and GMRES-based iterative refinement (include/ttg_apps.h,
+// ttg_chol_plan_solve / ttg_chol_posv).
+//
+// FP64 plan: X = L⁻ᵀ L⁻¹ B with the FP64 factor (two block sweeps with the
+//   inverted diagonal tiles), then one FP64 residual for the backward error.
+// Mixed plan (low-precision factor L̃, FP32): GMRES-IR —
+//   x0 = M⁻¹ b with M = L̃L̃ᵀ (FP32 sweeps);
+//   repeat: r = b − A x in FP64 (dense FP64 copy of A);
+//           stop when ‖r‖∞ / (‖A‖∞ ‖x‖∞) ≤ tol for every column;
+//           solve A d = r by GMRES left-preconditioned with M (the Krylov
+//           basis, the matrix-vector products and M⁻¹ in FP32, or in FP64
+//           when FP32 stops making progress; orthogonalisation sums in FP64);
+//           x += d in FP64.
+// All RHS columns run in lockstep; each column has its own Krylov space and
+// Hessenberg matrix (solved on the host; they are tiny).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "../../include/ttg.h"
+#include "../../include/ttg_apps.h"
+#include "solve_kernels.cuh"
+#include "ttg_internal.h"
+#include "ttg_solve_api.h"
+
+using namespace ttg;
+using namespace ttg::solve;
+
+namespace {
+
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    ttg_status ensure(size_t count) {
+        if (count <= n) return TTG_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        cudaError_t e = cudaMalloc((void**)&p, sizeof(T) * std::max<size_t>(1, count));
+        if (e != cudaSuccess) {
+            ttg_set_last_cuda_error(e, "cudaMalloc (solve)", __FILE__, __LINE__);
+            return TTG_ENOMEM;
+        }
+        n = count;
+        return TTG_OK;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+}  // namespace
+
+struct ttg_solver {
+    ttg_ctx* ctx = nullptr;
+    int N = 0, nb = 0;
+    bool mixed = false;
+    int64_t elems = 0;
+    TileLayout lay{};
+    DevBuf<int64_t> d_off;
+    DevBuf<int> d_bs, d_displ, d_rowblk;
+    // Dense copies of the input (rebuilt when the input changes).
+    DevBuf<double> A64;
+    DevBuf<float> A32;
+    bool dense_valid = false;
+    double anorm_inf = 0.0;
+    // Inverted diagonal tiles of the current factor.
+    DevBuf<double> inv64;
+    DevBuf<float> inv32;
+    // Work vectors (N × 16).
+    DevBuf<double> B, X, R, D, W, T1, T2, P;
+    DevBuf<float> f1, f2, f3;
+    DevBuf<double> Vd;  // Krylov basis, FP64 variant
+    DevBuf<float> Vf;   // Krylov basis, FP32 variant
+    DevBuf<double> part, colv, coefA, coefB;
+    int sweep_grid64 = 0, sweep_grid32 = 0, sweep_grid_mix = 0;
+};
+
+static ttg_status solver_init(ttg_solver* S) {
+    TTG_CUDA_CHECK(cudaSetDevice(S->ctx->device));
+    int per = 0;
+    TTG_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep_forward<double, double>, 256, 0));
+    S->sweep_grid64 = std::max(1, per) * S->ctx->sms;
+    TTG_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep_forward<float, float>, 256, 0));
+    S->sweep_grid32 = std::max(1, per) * S->ctx->sms;
+    TTG_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep_forward<double, float>, 256, 0));
+    S->sweep_grid_mix = std::max(1, per) * S->ctx->sms;
+    int per_b = 0;
+    TTG_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_b, sweep_backward<double, double>, 256, 0));
+    S->sweep_grid64 = std::min(S->sweep_grid64, std::max(1, per_b) * S->ctx->sms);
+    TTG_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_b, sweep_backward<float, float>, 256, 0));
+    S->sweep_grid32 = std::min(S->sweep_grid32, std::max(1, per_b) * S->ctx->sms);
+    TTG_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_b, sweep_backward<double, float>, 256, 0));
+    S->sweep_grid_mix = std::min(S->sweep_grid_mix, std::max(1, per_b) * S->ctx->sms);
+    const int smem = kF64SmemDoubles * (int)sizeof(double);
+    TTG_CUDA_CHECK(cudaFuncSetAttribute(invert_diag_tiles<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    TTG_CUDA_CHECK(cudaFuncSetAttribute(invert_diag_tiles<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    return TTG_OK;
+}
+
+ttg_status ttg_solver_create(ttg_ctx* ctx, int N, int nb, const int* bs, const int64_t* off, bool mixed, ttg_solver** out) {
+    *out = nullptr;
+    ttg_solver* S = new ttg_solver();
+    S->ctx = ctx;
+    S->N = N;
+    S->nb = nb;
+    S->mixed = mixed;
+    std::vector<int> displ(nb + 1, 0);
+    for (int i = 0; i < nb; ++i) displ[i + 1] = displ[i] + bs[i];
+    S->elems = 0;
+    for (int j = 0; j < nb; ++j)
+        for (int i = j; i < nb; ++i) S->elems += (int64_t)bs[i] * bs[j];
+    ttg_status st;
+    if ((st = S->d_off.ensure((size_t)nb * nb)) != TTG_OK || (st = S->d_bs.ensure(nb)) != TTG_OK ||
+        (st = S->d_displ.ensure(nb + 1)) != TTG_OK) {
+        ttg_solver_destroy(S);
+        return st;
+    }
+    cudaMemcpy(S->d_off.p, off, sizeof(int64_t) * nb * nb, cudaMemcpyHostToDevice);
+    cudaMemcpy(S->d_bs.p, bs, sizeof(int) * nb, cudaMemcpyHostToDevice);
+    cudaMemcpy(S->d_displ.p, displ.data(), sizeof(int) * (nb + 1), cudaMemcpyHostToDevice);
+    {
+        std::vector<int> rowblk(N);
+        for (int i = 0; i < nb; ++i)
+            for (int r = displ[i]; r < displ[i + 1]; ++r) rowblk[r] = i;
+        if ((st = S->d_rowblk.ensure(std::max(1, N))) != TTG_OK) {
+            ttg_solver_destroy(S);
+            return st;
+        }
+        cudaMemcpy(S->d_rowblk.p, rowblk.data(), sizeof(int) * N, cudaMemcpyHostToDevice);
+    }
+    S->lay.off = S->d_off.p;
+    S->lay.bs = S->d_bs.p;
+    S->lay.displ = S->d_displ.p;
+    S->lay.nb = nb;
+    S->lay.N = N;
+    if ((st = solver_init(S)) != TTG_OK) {
+        ttg_solver_destroy(S);
+        return st;
+    }
+    *out = S;
+    return TTG_OK;
+}
+
+void ttg_solver_destroy(ttg_solver* S) {
+    if (!S) return;
+    cudaSetDevice(S->ctx->device);
+    for (auto* b : {&S->A64, &S->inv64, &S->B, &S->X, &S->R, &S->D, &S->W, &S->T1, &S->T2, &S->P, &S->Vd, &S->part, &S->colv,
+                    &S->coefA, &S->coefB})
+        b->release();
+    for (auto* b : {&S->A32, &S->inv32, &S->f1, &S->f2, &S->f3, &S->Vf}) b->release();
+    S->d_off.release();
+    S->d_bs.release();
+    S->d_displ.release();
+    S->d_rowblk.release();
+    delete S;
+}
+
+void ttg_solver_input_changed(ttg_solver* S) {
+    if (S) S->dense_valid = false;
+}
+
+// Dense copies of A (FP64, and FP32 for the mixed path) and ‖A‖∞.
+static ttg_status ensure_dense(ttg_solver* S, const double* pristine, cudaStream_t s) {
+    if (S->dense_valid) return TTG_OK;
+    const size_t NN = (size_t)S->N * S->N;
+    ttg_status st = S->A64.ensure(NN);
+    if (st != TTG_OK) return st;
+    dense_from_tiles<double, double><<<S->ctx->sms * 8, 256, 0, s>>>(S->lay, S->d_rowblk.p, pristine, S->A64.p);
+    if (S->mixed) {
+        if ((st = S->A32.ensure(NN)) != TTG_OK) return st;
+        dense_from_tiles<double, float><<<S->ctx->sms * 8, 256, 0, s>>>(S->lay, S->d_rowblk.p, pristine, S->A32.p);
+    }
+    if ((st = S->T1.ensure(S->N)) != TTG_OK) return st;
+    row_abs_sums<double><<<(S->N + 255) / 256, 256, 0, s>>>(S->N, S->A64.p, S->T1.p);
+    TTG_CUDA_CHECK(cudaGetLastError());
+    std::vector<double> rs(S->N);
+    TTG_CUDA_CHECK(cudaMemcpyAsync(rs.data(), S->T1.p, sizeof(double) * S->N, cudaMemcpyDeviceToHost, s));
+    TTG_CUDA_CHECK(cudaStreamSynchronize(s));
+    S->anorm_inf = 0.0;
+    for (double v : rs) S->anorm_inf = std::max(S->anorm_inf, v);
+    S->dense_valid = true;
+    return TTG_OK;
+}
+
+ttg_status ttg_solver_factor_done(ttg_solver* S, const double* L64, const float* L32, cudaStream_t s) {
+    const int parts = 8;
+    const int smem = kF64SmemDoubles * (int)sizeof(double);
+    dim3 grid(S->nb, parts);
+    ttg_status st;
+    if (S->mixed) {
+        if ((st = S->inv32.ensure(S->elems)) != TTG_OK) return st;
+        invert_diag_tiles<float><<<grid, kThreads, smem, s>>>(S->lay, L32, S->inv32.p, parts);
+    } else {
+        if ((st = S->inv64.ensure(S->elems)) != TTG_OK) return st;
+        invert_diag_tiles<double><<<grid, kThreads, smem, s>>>(S->lay, L64, S->inv64.p, parts);
+    }
+    TTG_CUDA_CHECK(cudaGetLastError());
+    return TTG_OK;
+}
+
+namespace {
+
+template <class T, class TM>
+ttg_status sweeps(ttg_solver* S, const TM* L, const TM* inv, T* R, T* Y, T* X, int nrhs, int grid, cudaStream_t s) {
+    // R (scratch, overwritten) -> Y = L⁻¹ R -> X = L⁻ᵀ Y (Y overwritten).
+    TileLayout lay = S->lay;
+    void* fa[] = {(void*)&lay, (void*)&L, (void*)&inv, (void*)&R, (void*)&Y, (void*)&nrhs};
+    TTG_CUDA_CHECK(cudaLaunchCooperativeKernel((const void*)sweep_forward<T, TM>, dim3(grid), dim3(256), fa, 0, s));
+    void* ba[] = {(void*)&lay, (void*)&L, (void*)&inv, (void*)&Y, (void*)&X, (void*)&nrhs};
+    TTG_CUDA_CHECK(cudaLaunchCooperativeKernel((const void*)sweep_backward<T, TM>, dim3(grid), dim3(256), ba, 0, s));
+    return TTG_OK;
+}
+
+// Y = A X (mode 0) or Y = B − A X (mode 2) with the dense copy.
+template <class T>
+ttg_status matmul(ttg_solver* S, const T* A, const T* X, const T* B, T* Y, T* P, int nrhs, int mode, cudaStream_t s) {
+    const int splits = 4;
+    dim3 grid((S->N + 127) / 128, splits);
+    dense_matmul_partial<T><<<grid, 256, 0, s>>>(S->N, A, X, nrhs, P, splits);
+    reduce_partials<T><<<S->ctx->sms * 4, 256, 0, s>>>(S->N, nrhs, P, splits, B, Y, mode);
+    TTG_CUDA_CHECK(cudaGetLastError());
+    return TTG_OK;
+}
+
+// Per-column reduction to host: kind 0 dot(X, Y), kind 1 max|X|.
+template <class T>
+ttg_status colreduce(ttg_solver* S, const T* X, const T* Y, int nrhs, int kind, double* host, cudaStream_t s) {
+    const int blocks = 128;
+    column_reduce_partial<T><<<blocks, 256, 0, s>>>(S->N, nrhs, X, Y, kind, S->part.p);
+    column_reduce_final<<<1, 32, 0, s>>>(nrhs, blocks, S->part.p, kind, S->colv.p);
+    TTG_CUDA_CHECK(cudaGetLastError());
+    TTG_CUDA_CHECK(cudaMemcpyAsync(host, S->colv.p, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s));
+    TTG_CUDA_CHECK(cudaStreamSynchronize(s));
+    return TTG_OK;
+}
+
+// Y[:,q] = a[q] X[:,q] + b[q] Y[:,q] (b = nullptr: Y = a X).
+template <class TX, class TY>
+ttg_status axpby(ttg_solver* S, const std::vector<double>& a, const TX* X, const std::vector<double>* b, TY* Y, int nrhs,
+                 cudaStream_t s) {
+    TTG_CUDA_CHECK(cudaMemcpyAsync(S->coefA.p, a.data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, s));
+    if (b) TTG_CUDA_CHECK(cudaMemcpyAsync(S->coefB.p, b->data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, s));
+    column_axpby<TX, TY><<<S->ctx->sms * 4, 256, 0, s>>>(S->N, nrhs, S->coefA.p, X, b ? S->coefB.p : nullptr, Y);
+    TTG_CUDA_CHECK(cudaGetLastError());
+    return TTG_OK;
+}
+
+// Backward errors ‖R_q‖∞ / (‖A‖∞ ‖X_q‖∞) of the current X (R = B − A X).
+ttg_status backward_errors(ttg_solver* S, int nrhs, cudaStream_t s, std::vector<double>& be, std::vector<double>& rnorm) {
+    ttg_status st = matmul<double>(S, S->A64.p, S->X.p, S->B.p, S->R.p, S->P.p, nrhs, 2, s);
+    if (st != TTG_OK) return st;
+    std::vector<double> xn(nrhs);
+    rnorm.assign(nrhs, 0.0);
+    if ((st = colreduce<double>(S, S->R.p, nullptr, nrhs, 1, rnorm.data(), s)) != TTG_OK) return st;
+    if ((st = colreduce<double>(S, S->X.p, nullptr, nrhs, 1, xn.data(), s)) != TTG_OK) return st;
+    be.assign(nrhs, 0.0);
+    for (int q = 0; q < nrhs; ++q) be[q] = xn[q] > 0 ? rnorm[q] / (S->anorm_inf * xn[q]) : (rnorm[q] > 0 ? INFINITY : 0.0);
+    return TTG_OK;
+}
+
+// One GMRES(m) cycle on A d = r, preconditioned on the left by M = L̃L̃ᵀ,
+// in precision TG (float or double).  r is in S->R (FP64), d goes to S->D.
+// Returns the number of iterations.
+template <class TG>
+ttg_status gmres_cycle(ttg_solver* S, const float* L32, int nrhs, int m, double inner_tol, cudaStream_t s, int* iters) {
+    const int N = S->N;
+    const size_t blk = (size_t)N * nrhs;
+    TG* V;
+    TG *t1, *t2, *t3;
+    ttg_status st;
+    if (sizeof(TG) == 4) {
+        if ((st = S->Vf.ensure(blk * (m + 1))) != TTG_OK) return st;
+        V = (TG*)S->Vf.p;
+        t1 = (TG*)S->f1.p;
+        t2 = (TG*)S->f2.p;
+        t3 = (TG*)S->f3.p;
+    } else {
+        if ((st = S->Vd.ensure(blk * (m + 1))) != TTG_OK) return st;
+        V = (TG*)S->Vd.p;
+        t1 = (TG*)S->T1.p;
+        t2 = (TG*)S->T2.p;
+        t3 = (TG*)S->P.p;  // matmul partials (4 × N × nrhs)
+    }
+    const TG* A = sizeof(TG) == 4 ? (const TG*)S->A32.p : (const TG*)S->A64.p;
+    const int grid = sizeof(TG) == 4 ? S->sweep_grid32 : S->sweep_grid_mix;
+    // Scale r per column by 1/‖r‖∞ (keeps FP32 in range), z0 = M⁻¹ r̂.
+    std::vector<double> rn(nrhs), inv(nrhs), one(nrhs, 1.0);
+    if ((st = colreduce<double>(S, S->R.p, nullptr, nrhs, 1, rn.data(), s)) != TTG_OK) return st;
+    for (int q = 0; q < nrhs; ++q) inv[q] = rn[q] > 0 ? 1.0 / rn[q] : 0.0;
+    if ((st = axpby<double, TG>(S, inv, S->R.p, nullptr, t1, nrhs, s)) != TTG_OK) return st;
+    if ((st = sweeps<TG, float>(S, L32, S->inv32.p, t1, t2, V, nrhs, grid, s)) != TTG_OK) return st;
+    std::vector<double> beta(nrhs);
+    if ((st = colreduce<TG>(S, V, V, nrhs, 0, beta.data(), s)) != TTG_OK) return st;
+    std::vector<double> scale(nrhs);
+    for (int q = 0; q < nrhs; ++q) {
+        beta[q] = std::sqrt(beta[q]);
+        scale[q] = beta[q] > 0 ? 1.0 / beta[q] : 0.0;
+    }
+    if ((st = axpby<TG, TG>(S, scale, V, nullptr, V, nrhs, s)) != TTG_OK) return st;
+    // Hessenberg H (m+1)×m per column, Givens (c, s), g.
+    std::vector<double> H((size_t)nrhs * (m + 1) * m, 0.0), cs((size_t)nrhs * m), sn((size_t)nrhs * m),
+        g((size_t)nrhs * (m + 1), 0.0);
+    for (int q = 0; q < nrhs; ++q) g[(size_t)q * (m + 1)] = beta[q];
+    auto h = [&](int q, int i, int j) -> double& { return H[((size_t)q * (m + 1) + i) * m + j]; };
+    int k = 0;
+    for (; k < m; ++k) {
+        TG* vk = V + blk * k;
+        TG* w = V + blk * (k + 1);
+        // w = M⁻¹ (A v_k)
+        if ((st = matmul<TG>(S, A, vk, nullptr, t1, t3, nrhs, 0, s)) != TTG_OK) return st;
+        if ((st = sweeps<TG, float>(S, L32, S->inv32.p, t1, t2, w, nrhs, grid, s)) != TTG_OK) return st;
+        // Modified Gram-Schmidt.
+        for (int j = 0; j <= k; ++j) {
+            std::vector<double> d(nrhs), neg(nrhs);
+            if ((st = colreduce<TG>(S, w, V + blk * j, nrhs, 0, d.data(), s)) != TTG_OK) return st;
+            for (int q = 0; q < nrhs; ++q) {
+                h(q, j, k) = d[q];
+                neg[q] = -d[q];
+            }
+            if ((st = axpby<TG, TG>(S, neg, V + blk * j, &one, w, nrhs, s)) != TTG_OK) return st;
+        }
+        std::vector<double> nw(nrhs), sc(nrhs);
+        if ((st = colreduce<TG>(S, w, w, nrhs, 0, nw.data(), s)) != TTG_OK) return st;
+        bool done = true;
+        for (int q = 0; q < nrhs; ++q) {
+            const double hn = std::sqrt(nw[q]);
+            h(q, k + 1, k) = hn;
+            sc[q] = hn > 0 ? 1.0 / hn : 0.0;
+            // Apply previous rotations to column k, then a new one.
+            for (int i = 0; i < k; ++i) {
+                const double a = h(q, i, k), b = h(q, i + 1, k);
+                h(q, i, k) = cs[(size_t)q * m + i] * a + sn[(size_t)q * m + i] * b;
+                h(q, i + 1, k) = -sn[(size_t)q * m + i] * a + cs[(size_t)q * m + i] * b;
+            }
+            const double a = h(q, k, k), b = h(q, k + 1, k);
+            const double r = std::hypot(a, b);
+            const double c = r > 0 ? a / r : 1.0, sv = r > 0 ? b / r : 0.0;
+            cs[(size_t)q * m + k] = c;
+            sn[(size_t)q * m + k] = sv;
+            h(q, k, k) = r;
+            h(q, k + 1, k) = 0.0;
+            const double gk = g[(size_t)q * (m + 1) + k];
+            g[(size_t)q * (m + 1) + k] = c * gk;
+            g[(size_t)q * (m + 1) + k + 1] = -sv * gk;
+            if (beta[q] > 0 && std::fabs(g[(size_t)q * (m + 1) + k + 1]) > inner_tol * beta[q]) done = false;
+        }
+        if ((st = axpby<TG, TG>(S, sc, w, nullptr, w, nrhs, s)) != TTG_OK) return st;
+        if (done) {
+            ++k;
+            break;
+        }
+    }
+    // y = H⁻¹ g per column; d = V y (times ‖r‖∞ undoes the scaling).
+    std::vector<double> y((size_t)nrhs * k, 0.0);
+    for (int q = 0; q < nrhs; ++q)
+        for (int i = k - 1; i >= 0; --i) {
+            double v = g[(size_t)q * (m + 1) + i];
+            for (int j = i + 1; j < k; ++j) v -= h(q, i, j) * y[(size_t)q * k + j];
+            y[(size_t)q * k + i] = h(q, i, i) != 0 ? v / h(q, i, i) : 0.0;
+        }
+    std::vector<double> zero(nrhs, 0.0);
+    if ((st = axpby<double, double>(S, zero, S->D.p, nullptr, S->D.p, nrhs, s)) != TTG_OK) return st;
+    for (int j = 0; j < k; ++j) {
+        std::vector<double> c(nrhs);
+        for (int q = 0; q < nrhs; ++q) c[q] = y[(size_t)q * k + j] * rn[q];
+        if ((st = axpby<TG, double>(S, c, V + blk * j, &one, S->D.p, nrhs, s)) != TTG_OK) return st;
+    }
+    *iters = k;
+    return TTG_OK;
+}
+
+}  // namespace
+
+ttg_status ttg_solver_solve(ttg_solver* S, const double* pristine, const double* L64, const float* L32, const double* d_B,
+                            double* d_X, const ttg_solve_opts* o, ttg_solve_report* rep, cudaStream_t s) {
+    const int nrhs = o->nrhs;
+    if (nrhs < 1 || nrhs > kMaxRhs || !d_B || !d_X) return TTG_EINVAL;
+    TTG_CUDA_CHECK(cudaSetDevice(S->ctx->device));
+    const size_t blk = (size_t)S->N * nrhs;
+    ttg_status st;
+    for (auto* b : {&S->B, &S->X, &S->R, &S->D, &S->W, &S->T1, &S->T2})
+        if ((st = b->ensure(blk)) != TTG_OK) return st;
+    if ((st = S->P.ensure(blk * 4)) != TTG_OK) return st;
+    for (auto* b : {&S->f1, &S->f2, &S->f3})
+        if ((st = b->ensure(blk * 4)) != TTG_OK) return st;  // also the FP32 matmul partials
+    if ((st = S->part.ensure(128 * kMaxRhs)) != TTG_OK || (st = S->colv.ensure(kMaxRhs)) != TTG_OK ||
+        (st = S->coefA.ensure(kMaxRhs)) != TTG_OK || (st = S->coefB.ensure(kMaxRhs)) != TTG_OK)
+        return st;
+    if ((st = ensure_dense(S, pristine, s)) != TTG_OK) return st;
+    TTG_CUDA_CHECK(cudaMemcpyAsync(S->B.p, d_B, sizeof(double) * blk, cudaMemcpyDeviceToDevice, s));
+    const double tol = o->tol > 0 ? o->tol : 1e-14;
+    const int max_outer = o->max_outer > 0 ? o->max_outer : 10;
+    const int m = o->restart > 0 ? std::min(o->restart, 60) : 20;
+    ttg_solve_report r{};
+    r.status = TTG_OK;
+    std::vector<double> be, rn;
+    if (!S->mixed) {
+        // FP64 direct: X = L⁻ᵀ L⁻¹ B.
+        TTG_CUDA_CHECK(cudaMemcpyAsync(S->R.p, S->B.p, sizeof(double) * blk, cudaMemcpyDeviceToDevice, s));
+        if ((st = sweeps<double, double>(S, L64, S->inv64.p, S->R.p, S->T1.p, S->X.p, nrhs, S->sweep_grid64, s)) != TTG_OK)
+            return st;
+        if ((st = backward_errors(S, nrhs, s, be, rn)) != TTG_OK) return st;
+        r.gmres_prec = 64;
+    } else {
+        // x0 = M⁻¹ b (FP32 sweeps).
+        std::vector<double> one(nrhs, 1.0);
+        if ((st = axpby<double, float>(S, one, S->B.p, nullptr, S->f1.p, nrhs, s)) != TTG_OK) return st;
+        if ((st = sweeps<float, float>(S, L32, S->inv32.p, S->f1.p, S->f2.p, S->f3.p, nrhs, S->sweep_grid32, s)) != TTG_OK)
+            return st;
+        if ((st = axpby<float, double>(S, one, S->f3.p, nullptr, S->X.p, nrhs, s)) != TTG_OK) return st;
+        int prec = o->gmres_prec == 64 ? 64 : 32;
+        double prev = INFINITY;
+        const double inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-6;
+        for (int outer = 0;; ++outer) {
+            if ((st = backward_errors(S, nrhs, s, be, rn)) != TTG_OK) return st;
+            const double worst = *std::max_element(be.begin(), be.end());
+            if (worst <= tol) break;
+            if (outer >= max_outer) {
+                r.status = TTG_ENOCONV;
+                break;
+            }
+            // Switch to FP64 Krylov work when FP32 stops gaining (auto mode).
+            if (o->gmres_prec == 0 && prec == 32 && outer > 0 && worst > 0.1 * prev) prec = 64;
+            prev = worst;
+            int it = 0;
+            st = prec == 32 ? gmres_cycle<float>(S, L32, nrhs, m, prec == 32 ? std::max(inner_tol, 1e-6) : inner_tol, s, &it)
+                            : gmres_cycle<double>(S, L32, nrhs, m, inner_tol, s, &it);
+            if (st != TTG_OK) return st;
+            r.inner += it;
+            r.outer = outer + 1;
+            std::vector<double> ones(nrhs, 1.0);
+            if ((st = axpby<double, double>(S, ones, S->D.p, &ones, S->X.p, nrhs, s)) != TTG_OK) return st;
+        }
+        r.gmres_prec = prec;
+    }
+    r.bwd_err = be.empty() ? 0.0 : *std::max_element(be.begin(), be.end());
+    r.anorm_inf = S->anorm_inf;
+    TTG_CUDA_CHECK(cudaMemcpyAsync(d_X, S->X.p, sizeof(double) * blk, cudaMemcpyDeviceToDevice, s));
+    TTG_CUDA_CHECK(cudaStreamSynchronize(s));
+    if (rep) *rep = r;
+    return r.status;
+}

@@ -1,0 +1,74 @@
+"""Solves with a Cholesky plan's factor: FP64 direct, and the mixed path
+(low-precision factor + GMRES-IR with FP64 residuals) to backward error
+≤ 1e-14; forward errors against the FP64 oracle solution."""
+import numpy as np
+import pytest
+
+import tasktorrent_gb300 as t
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+BWD = 1e-14  # ‖b − A x‖∞ / (‖A‖∞ ‖x‖∞), per column
+
+
+def bwd_err(A, X, B):
+    R = B - A @ X
+    return np.max(np.abs(R).max(axis=0) / (np.abs(A).sum(axis=1).max() * np.abs(X).max(axis=0)))
+
+
+def rhs(N, nrhs, seed=9):
+    return orc.normals(0, N * nrhs, seed, 1).reshape(N, nrhs, order="F")
+
+
+@pytest.mark.parametrize("b,nb,alpha,nrhs", [(64, 8, 1.0, 1), (128, 8, 1e-4, 16), (96, 10, 1e-8, 4)])
+def test_fp64_direct_solve(ctx, b, nb, alpha, nrhs):
+    p = t.CholPlan(ctx, b, nb, kind=2, matrix=1, alpha=alpha, seed=2)
+    A = p.input_A()
+    B = rhs(p.N, nrhs)
+    st, rep, X = p.solve_host(B)
+    assert st == t.TTG_OK, t.strerror(st)
+    assert rep.bwd_err <= 1e-15 * 10 and bwd_err(A, X, B) <= 1e-15 * 10
+    Xref = np.linalg.solve(A, B)
+    kappa = np.linalg.cond(A)
+    assert np.linalg.norm(X - Xref) / np.linalg.norm(Xref) <= 1e-15 * kappa * 100
+    p.close()
+
+
+def test_mixed_factor_is_fp32_accurate(ctx):
+    p = t.CholPlan(ctx, 64, 8, kind=2, matrix=1, alpha=1.0, seed=0, precision=t.PREC_MIXED, mixed_kind=1)
+    st, rep = p.factor()
+    assert st == t.TTG_OK
+    A = p.input_A()
+    L = p.factor_L()
+    e = np.linalg.norm(L @ L.T - A) / np.linalg.norm(A)
+    assert 1e-9 < e < 1e-5  # FP32 trailing updates: FP32-level, not FP64-level
+    p.close()
+
+
+@pytest.mark.parametrize("alpha", [1.0, 1e-4, 1e-8])
+@pytest.mark.parametrize("gprec", [0, 64])
+def test_mixed_gmres_ir_reaches_fp64_backward_error(ctx, alpha, gprec):
+    p = t.CholPlan(ctx, 128, 8, kind=2, matrix=1, alpha=alpha, seed=2, precision=t.PREC_MIXED, mixed_kind=1)
+    A = p.input_A()
+    B = rhs(p.N, 16)
+    st, rep, X = p.solve_host(B, tol=BWD, gmres_prec=gprec, max_outer=12)
+    assert st == t.TTG_OK, (t.strerror(st), rep.as_dict())
+    assert rep.bwd_err <= BWD
+    assert bwd_err(A, X, B) <= 2 * BWD
+    Xref = np.linalg.solve(A, B)
+    kappa = np.linalg.cond(A)
+    assert np.linalg.norm(X - Xref) / np.linalg.norm(Xref) <= max(1e-12, 1e-15 * kappa * 100)
+    p.close()
+
+
+def test_follow_up_rhs_reuse_factor(ctx):
+    p = t.CholPlan(ctx, 64, 6, matrix=1, alpha=1e-4, seed=3, precision=t.PREC_MIXED, mixed_kind=1)
+    A = p.input_A()
+    B1 = rhs(p.N, 2, seed=1)
+    st, rep1, X1 = p.solve_host(B1)
+    assert st == t.TTG_OK
+    B2 = rhs(p.N, 3, seed=2)
+    st, rep2, X2 = p.solve_host(B2, factor=False)  # resident factor
+    assert st == t.TTG_OK and rep2.factor_ms == 0.0
+    assert bwd_err(A, X2, B2) <= 2 * BWD
+    p.close()
