@@ -149,6 +149,11 @@ ttg_status ttg_trace(ttg_ctx* ctx, int64_t* h_start_ns, int64_t* h_end_ns, int32
 /* Number of persistent workers the context launches. */
 int ttg_workers(const ttg_ctx* ctx);
 
+/* Identifier of the graph currently uploaded to the context (changes with
+ * every successful ttg_graph_upload): a host-side owner of a graph compares
+ * it to decide whether to upload again before relaunching. */
+uint64_t ttg_graph_generation(const ttg_ctx* ctx);
+
 /* Measured FP64 FMA throughput of the device (TFLOP/s): every block of the
  * device runs independent DFMA chains for about `ms` milliseconds.  The
  * roofline denominator of the FP64 tile kernels. */

@@ -124,6 +124,9 @@ ttg_status ttg_chol_plan_solve(ttg_chol_plan* plan, const double* d_B, double* d
 /* Time to solution on the resident input: restore, factor, solve. */
 ttg_status ttg_chol_posv(ttg_chol_plan* plan, const double* d_B, double* d_X, const ttg_solve_opts* opts,
                          ttg_solve_report* rep, void* stream);
+/* Solve with the resident factor (no factorisation), host B in, host X out. */
+ttg_status ttg_chol_solve_host(ttg_chol_plan* plan, const double* h_B, double* h_X, const ttg_solve_opts* opts,
+                               ttg_solve_report* rep, void* stream);
 /* End to end with host buffers: h_tiles (packed lower tiles of A, or NULL to
  * keep the resident input), h_B in, h_X out (N×nrhs column-major). */
 ttg_status ttg_chol_posv_host(ttg_chol_plan* plan, const double* h_tiles, const double* h_B, double* h_X,

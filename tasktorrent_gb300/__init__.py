@@ -95,6 +95,7 @@ SIGNATURES = {
     "ttg_task_record": (_STATUS, [_P, _P, _P]),
     "ttg_trace": (_STATUS, [_P, _P, _P, _P]),
     "ttg_workers": (ctypes.c_int, [_P]),
+    "ttg_graph_generation": (ctypes.c_uint64, [_P]),
     "ttg_gen_gram_tiles": (_STATUS, [_P, _I32, _P, _I32, ctypes.c_double, ctypes.c_uint32, _P, _P]),
     "ttg_gen_uniform": (_STATUS, [_P, ctypes.c_int64, ctypes.c_uint32, ctypes.c_uint32, _P, _P]),
     "ttg_gen_normal": (_STATUS, [_P, ctypes.c_int64, ctypes.c_uint32, ctypes.c_uint32, _P, _P]),
@@ -125,6 +126,7 @@ SIGNATURES = {
     "ttg_chol_plan_solve": (_STATUS, [_P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveReport), _P]),
     "ttg_chol_posv": (_STATUS, [_P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveReport), _P]),
     "ttg_chol_posv_host": (_STATUS, [_P, _P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveReport), _P]),
+    "ttg_chol_solve_host": (_STATUS, [_P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveReport), _P]),
     "ttg_gemm_plan_create": (_STATUS, [_P, ctypes.POINTER(GemmArgs), ctypes.POINTER(_P)]),
     "ttg_gemm_plan_destroy": (_STATUS, [_P]),
     "ttg_gemm_plan_tasks": (_I32, [_P, ctypes.POINTER(ctypes.c_double)]),
@@ -331,13 +333,7 @@ class CholPlan:
             st = lib().ttg_chol_posv_host(self.h, _ptr(tiles) if tiles is not None else None, _ptr(B), _ptr(X),
                                           ctypes.byref(o), ctypes.byref(rep), None)
         else:
-            import torch
-            dB = torch.from_numpy(np.ascontiguousarray(B.T)).cuda()
-            dX = torch.zeros_like(dB)
-            torch.cuda.synchronize()
-            st = lib().ttg_chol_plan_solve(self.h, ctypes.c_void_p(dB.data_ptr()), ctypes.c_void_p(dX.data_ptr()),
-                                           ctypes.byref(o), ctypes.byref(rep), None)
-            X = np.asfortranarray(dX.cpu().numpy().T)
+            st = lib().ttg_chol_solve_host(self.h, _ptr(B), _ptr(X), ctypes.byref(o), ctypes.byref(rep), None)
         return st, rep, X
 
     def kind_times(self):

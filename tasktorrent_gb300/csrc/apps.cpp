@@ -496,19 +496,40 @@ extern "C" ttg_status ttg_chol_posv(ttg_chol_plan* P, const double* d_B, double*
     return st;
 }
 
+static ttg_status ensure_host_b(ttg_chol_plan* P, size_t blk) {
+    if (P->host_b_elems >= blk) return TTG_OK;
+    if (P->d_b) cudaFree(P->d_b);
+    P->d_b = nullptr;
+    P->host_b_elems = 0;
+    TTG_CUDA_CHECK(cudaMalloc((void**)&P->d_b, sizeof(double) * 2 * blk));
+    P->host_b_elems = blk;
+    return TTG_OK;
+}
+
+extern "C" ttg_status ttg_chol_solve_host(ttg_chol_plan* P, const double* h_B, double* h_X, const ttg_solve_opts* o,
+                                         ttg_solve_report* rep, void* stream) {
+    if (!P || !o || !h_B || !h_X || o->nrhs < 1 || o->nrhs > 16) return TTG_EINVAL;
+    TTG_CUDA_CHECK(cudaSetDevice(P->ctx->device));
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t blk = (size_t)P->N * o->nrhs;
+    ttg_status st = ensure_host_b(P, blk);
+    if (st != TTG_OK) return st;
+    TTG_CUDA_CHECK(cudaMemcpyAsync(P->d_b, h_B, sizeof(double) * blk, cudaMemcpyHostToDevice, s));
+    st = ttg_chol_plan_solve(P, P->d_b, P->d_b + blk, o, rep, stream);
+    if (st != TTG_OK && st != TTG_ENOCONV) return st;
+    TTG_CUDA_CHECK(cudaMemcpyAsync(h_X, P->d_b + blk, sizeof(double) * blk, cudaMemcpyDeviceToHost, s));
+    TTG_CUDA_CHECK(cudaStreamSynchronize(s));
+    return st;
+}
+
 extern "C" ttg_status ttg_chol_posv_host(ttg_chol_plan* P, const double* h_tiles, const double* h_B, double* h_X,
                                         const ttg_solve_opts* o, ttg_solve_report* rep, void* stream) {
     if (!P || !o || !h_B || !h_X || o->nrhs < 1 || o->nrhs > 16) return TTG_EINVAL;
     TTG_CUDA_CHECK(cudaSetDevice(P->ctx->device));
     cudaStream_t s = (cudaStream_t)stream;
     const size_t blk = (size_t)P->N * o->nrhs;
-    if (P->host_b_elems < blk) {
-        if (P->d_b) cudaFree(P->d_b);
-        P->d_b = nullptr;
-        P->host_b_elems = 0;
-        TTG_CUDA_CHECK(cudaMalloc((void**)&P->d_b, sizeof(double) * 2 * blk));
-        P->host_b_elems = blk;
-    }
+    ttg_status sb = ensure_host_b(P, blk);
+    if (sb != TTG_OK) return sb;
     if (h_tiles) {
         TTG_CUDA_CHECK(cudaMemcpyAsync(P->pristine, h_tiles, sizeof(double) * P->elems, cudaMemcpyHostToDevice, s));
         if (P->solver) ttg_solver_input_changed(P->solver);

@@ -1,0 +1,314 @@
+// tile_bf16_tc.cuh — BF16 trailing update of the mixed Cholesky on the
+// 5th-generation tensor cores (tcgen05), run by one block of the persistent
+// executor.
+//
+//   C[m0:m0+128, n0:n0+256] += f · Â[m0:m0+128, :] · B̂[n0:n0+256, :]ᵀ
+//
+// C is an FP32 working tile (column-major, in HBM).  Â and B̂ are BF16 copies
+// of factored panel tiles (L_ik, L_jk), stored K-major (row-major) one slot
+// per tile and scaled by a power of two per tile; f = -s_A·s_B undoes the
+// scales.  This is the cblas_dgemm(NoTrans, Trans) / cblas_dsyrk trailing
+// update of 2d_cholesky.cpp:490-494 in the mixed-precision path.
+//
+// Data movement and compute:
+//   - one thread issues TMA loads (cp.async.bulk.tensor.3d, 128B swizzle) of
+//     64-wide K slabs into a 4-stage shared-memory ring guarded by mbarriers;
+//   - one thread issues tcgen05.mma.cta_group::1.kind::f16 (M=128, N=256,
+//     K=16; BF16 inputs, FP32 accumulator in 256 TMEM columns) and commits
+//     each stage back to the producer with tcgen05.commit;
+//   - all 8 warps read the accumulator with tcgen05.ld.32x32b.x32 (warp w
+//     reads TMEM lanes 32·(w%4)…, columns 128·(w/4)…) and update C.
+// Every wait is bounded: on timeout the block records an error and drains.
+#pragma once
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ttg {
+namespace tc {
+
+constexpr int kBM = 128;           // accumulator rows (TMEM lanes)
+constexpr int kBN = 256;           // accumulator columns
+constexpr int kBK = 64;            // K per stage (one 128-byte swizzle row of BF16)
+constexpr int kStages = 4;
+constexpr int kStageBytesA = kBM * kBK * 2;       // 16 KB
+constexpr int kStageBytesB = kBN * kBK * 2;       // 32 KB
+constexpr int kStageBytes = kStageBytesA + kStageBytesB;
+constexpr int kSmemBytes = kStages * kStageBytes + 1024;  // + alignment slack
+constexpr uint32_t kTmemCols = 256;
+
+// Per-block state kept in shared memory across tasks.
+struct TcShared {
+    uint64_t full[kStages];
+    uint64_t empty[kStages];
+    uint64_t accf;
+    uint32_t tmem_base;
+    uint32_t produced;   // stages produced (producer thread)
+    uint32_t consumed;   // stages consumed (MMA thread)
+    uint32_t acc_done;   // accumulations completed (all threads read)
+    int failed;          // a bounded wait gave up in this block
+    int acc_ok;          // the current accumulator is complete (block-uniform)
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ long long tc_globaltimer() {
+    long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Wait for `parity` with a time limit; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit_ns) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = tc_globaltimer();
+    for (uint32_t it = 0;; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 255) == 255 && tc_globaltimer() - t0 > limit_ns) return false;
+    }
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(
+            smem_u32(dst)),
+        "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(x), "r"(y), "r"(z)
+        : "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Whole warp: allocate kTmemCols TMEM columns, address written to *dst.
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)), "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(kTmemCols) : "memory");
+}
+
+// Instruction descriptor, kind::f16: FP32 accumulator (bits 4-5 = 1), A and B
+// BF16 (bits 7-9 = 1, 10-12 = 1), both K-major (bits 15, 16 = 0), N>>3 at
+// bits 17-22, M>>4 at bits 24-28.
+__host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// Shared-memory descriptor of a K-major, 128B-swizzled operand whose rows are
+// 128 bytes and whose 8-row groups are 1024 bytes apart: start address >> 4
+// (bits 0-13), leading offset (unused for this layout, 1), stride offset
+// 1024 >> 4 (bits 32-45), version 1 (bits 46-47), layout SWIZZLE_128B = 2
+// (bits 61-63).
+__device__ __forceinline__ uint64_t smem_desc_kmajor_sw128(uint32_t saddr) {
+    return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) | ((uint64_t)1 << 46) |
+           ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, "
+        "%17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr)
+        : "memory");
+}
+
+// Block setup (all threads): barriers and TMEM.  Call once per kernel.
+__device__ inline void tc_setup(TcShared* sh) {
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(&sh->full[s], 1);
+            mbar_init(&sh->empty[s], 1);
+        }
+        mbar_init(&sh->accf, 1);
+        sh->produced = 0;
+        sh->consumed = 0;
+        sh->acc_done = 0;
+        sh->failed = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        fence_proxy_async_smem();
+    }
+    __syncwarp();
+    if (threadIdx.x < 32) tmem_alloc(&sh->tmem_base);  // warp 0, converged
+    __syncthreads();
+    tc_fence_after();
+}
+
+// Block teardown (all threads, after the last task).  After a timeout, the
+// loads that were issued but never consumed are waited for (bounded) so no
+// copy lands in shared memory after the block exits; TMEM is always freed.
+__device__ inline void tc_teardown(TcShared* sh, long long limit_ns) {
+    if (threadIdx.x == 0 && sh->failed) {
+        for (uint32_t p = sh->consumed; p < sh->produced; ++p)
+            if (!mbar_wait(&sh->full[p % kStages], (p / kStages) & 1, limit_ns)) break;
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (threadIdx.x < 32) tmem_dealloc(sh->tmem_base);
+}
+
+// One 128×256 block of C += f·Â·B̂ᵀ over K = k (multiple of 64).  All
+// threads of the block call it; returns false if a wait timed out.
+// lower: only elements with (row0 + r) >= (col0 + c) are updated.
+__device__ inline bool tc_gemm_block(TcShared* sh, uint8_t* ring, const CUtensorMap* map, int slotA, int slotB, int row0,
+                                     int col0, int k, float f, float* C, int ldc, int m, int n, bool lower, long long limit_ns) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ksteps = k / kBK;
+    bool ok = !sh->failed;
+    if (threadIdx.x == 0 && ok) {
+        // Producer: K slabs of A (128 rows) and B (two boxes of 128 rows).
+        fence_proxy_async_global();  // panel tiles were written by other blocks' generic stores
+        uint32_t p = sh->produced;
+        for (int ks = 0; ks < ksteps; ++ks, ++p) {
+            const int s = p % kStages;
+            if (!mbar_wait(&sh->empty[s], ((p / kStages) & 1) ^ 1, limit_ns)) {
+                sh->failed = 1;
+                break;
+            }
+            uint8_t* st = ring + (size_t)s * kStageBytes;
+            mbar_expect_tx(&sh->full[s], kStageBytes);
+            tma_load_3d(st, map, &sh->full[s], ks * kBK, row0, slotA);
+            tma_load_3d(st + kStageBytesA, map, &sh->full[s], ks * kBK, col0, slotB);
+            tma_load_3d(st + kStageBytesA + kStageBytesB / 2, map, &sh->full[s], ks * kBK, col0 + 128, slotB);
+        }
+        sh->produced = p;
+    } else if (threadIdx.x == 32 && ok) {
+        // MMA issuer.
+        const uint32_t idesc = idesc_bf16_f32(kBM, kBN);
+        uint32_t c = sh->consumed;
+        bool good = true;
+        for (int ks = 0; ks < ksteps; ++ks, ++c) {
+            const int s = c % kStages;
+            if (!mbar_wait(&sh->full[s], (c / kStages) & 1, limit_ns)) {
+                sh->failed = 1;
+                good = false;
+                break;
+            }
+            tc_fence_after();
+            const uint32_t a0 = smem_u32(ring + (size_t)s * kStageBytes);
+            const uint32_t b0 = a0 + kStageBytesA;
+#pragma unroll
+            for (int kk = 0; kk < kBK / 16; ++kk) {
+                const uint64_t ad = smem_desc_kmajor_sw128(a0 + kk * 32);
+                const uint64_t bd = smem_desc_kmajor_sw128(b0 + kk * 32);
+                umma_bf16(sh->tmem_base, ad, bd, idesc, (ks > 0 || kk > 0) ? 1u : 0u);
+            }
+            umma_commit(&sh->empty[s]);
+        }
+        sh->consumed = c;
+        if (good) umma_commit(&sh->accf);
+    }
+    __syncthreads();
+    // Epilogue: one thread waits for the accumulator; the outcome is
+    // broadcast so that every warp takes the same path (tcgen05.ld is
+    // warp-collective).
+    if (threadIdx.x == 0) {
+        bool have = false;
+        if (!sh->failed) {
+            have = mbar_wait(&sh->accf, sh->acc_done & 1, limit_ns);
+            if (!have) sh->failed = 1;
+        }
+        sh->acc_ok = have ? 1 : 0;
+    }
+    __syncthreads();
+    const bool have = sh->acc_ok != 0;
+    if (have) {
+        tc_fence_after();
+        const int q = warp & 3, h = warp >> 2;
+        const int r = 32 * q + lane;  // accumulator row of this thread
+        const int gr = row0 + r;
+#pragma unroll 1
+        for (int ch = 0; ch < 4; ++ch) {
+            const int c0 = 128 * h + 32 * ch;
+            uint32_t v[32];
+            tmem_ld32(sh->tmem_base + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, v);
+            if (gr < m) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const int gc = col0 + c0 + j;
+                    if (gc < n && (!lower || gr >= gc)) {
+                        float* p = C + gr + (size_t)gc * ldc;
+                        *p = fmaf(f, __uint_as_float(v[j]), __ldcg(p));
+                    }
+                }
+            }
+        }
+        tc_fence_before();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && have) sh->acc_done += 1;
+    __syncthreads();
+    return !sh->failed;
+}
+
+// Number of 128×256 output blocks of an m×n tile (lower: blocks that meet
+// the lower triangle of a square tile), and the coordinates of block b.
+__device__ __forceinline__ int tc_num_blocks(int m, int n, bool lower) {
+    const int bm = (m + kBM - 1) / kBM, bn = (n + kBN - 1) / kBN;
+    if (!lower) return bm * bn;
+    int cnt = 0;
+    for (int j = 0; j < bn; ++j)
+        for (int i = 0; i < bm; ++i)
+            if (i * kBM + kBM - 1 >= j * kBN) ++cnt;
+    return cnt;
+}
+
+__device__ __forceinline__ void tc_block_coords(int b, int m, int n, bool lower, int* row0, int* col0) {
+    const int bm = (m + kBM - 1) / kBM, bn = (n + kBN - 1) / kBN;
+    int cnt = 0;
+    for (int j = 0; j < bn; ++j)
+        for (int i = 0; i < bm; ++i) {
+            if (lower && i * kBM + kBM - 1 < j * kBN) continue;
+            if (cnt == b) {
+                *row0 = i * kBM;
+                *col0 = j * kBN;
+                return;
+            }
+            ++cnt;
+        }
+    *row0 = 0;
+    *col0 = 0;
+}
+
+}  // namespace tc
+}  // namespace ttg

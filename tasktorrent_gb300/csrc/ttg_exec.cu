@@ -232,11 +232,24 @@ extern "C" ttg_status ttg_destroy(ttg_ctx* c) {
 
 extern "C" int ttg_workers(const ttg_ctx* c) { return c ? c->workers : 0; }
 
+extern "C" uint64_t ttg_graph_generation(const ttg_ctx* c) { return c ? c->graph_gen : 0; }
+
 // Blocks that share one task: explicit op.parts, else one per 128×128 output
 // block (lower blocks for SYRK) up to 16, TRSM by 128-row slices up to 8;
 // POTRF and no-op tasks are never split.
 int ttg_task_parts(const ttg_op& op) {
     auto cdiv = [](long a, long b) { return (int)((a + b - 1) / b); };
+    // Tensor-core updates of the mixed path: exactly one 128×256 output block
+    // per part (lower-triangle blocks only for SYRK).
+    if (op.prec == TTG_PREC_MIXED && op.flags == 2 && (op.kind == TTG_OP_GEMM_NT || op.kind == TTG_OP_SYRK_LN)) {
+        const int bm = cdiv(op.m, 128), bn = cdiv(op.n, 256);
+        if (op.kind == TTG_OP_GEMM_NT) return std::max(1, bm * bn);
+        int cnt = 0;
+        for (int j = 0; j < bn; ++j)
+            for (int i = 0; i < bm; ++i)
+                if (i * 128 + 127 >= j * 256) ++cnt;
+        return std::max(1, cnt);
+    }
     int auto_parts = 1, max_parts = 1;
     switch (op.kind) {
         case TTG_OP_GEMM_NT:
@@ -446,6 +459,7 @@ extern "C" ttg_status ttg_graph_upload(ttg_ctx* c, const ttg_graph_desc* gd) {
     TTG_CUDA_TRY(cudaMemcpy(g.bq_head + W, btail0.data(), sizeof(int) * W, cudaMemcpyHostToDevice));
     g.bq_image = (int)bqinit.size();
     c->uploaded = true;
+    c->graph_gen += 1;
     c->launched = false;
     return TTG_OK;
 }

@@ -53,6 +53,7 @@ struct ttg_ctx {
     bool uploaded = false;
     bool launched = false;
     bool g_mixed = false;     // the uploaded graph has mixed-precision tasks
+    uint64_t graph_gen = 0;   // incremented by every successful upload
     int pending_host = 0;     // tasks that will never become ready
     bool overcount_host = false;
     ttg_status last_status = TTG_OK;

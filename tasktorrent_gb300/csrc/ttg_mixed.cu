@@ -9,6 +9,8 @@
 // The same persistent executor loop runs these tasks (exec_kernel_mixed); a
 // graph that contains any TTG_PREC_MIXED task is launched on it, FP64 tasks
 // of such a graph run as in the FP64 executor.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -16,6 +18,7 @@
 
 #include "../../include/ttg.h"
 #include "exec.cuh"
+#include "tile_bf16_tc.cuh"
 #include "tile_f64.cuh"
 #include "ttg_internal.h"
 #include "ttg_mixed_api.h"
@@ -23,9 +26,36 @@
 namespace ttg {
 
 // Mixed-op variants carried in ttg_op::flags.
-enum { kMixedF32 = 1 };
+enum { kMixedF32 = 1, kMixedBF16 = 2 };
 
-__device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem) {
+// Device tables of the BF16 path: panel copies (one b×b K-major slot per lower
+// tile), the scale of each slot, and the power-of-two scale of each block row.
+struct MixedTables {
+    __nv_bfloat16* b16;
+    float* slot_scale;
+    const float* rowscale;
+    int b;
+};
+
+// Kernel parameters of the mixed executor (the tensor map must live in the
+// parameter space: __grid_constant__).
+struct __align__(64) MixedGlobals {
+    CUtensorMap tmap;  // 3D map over the BF16 slots: (K = b, rows = b, slot)
+    int has_tc;        // the graph has tensor-core updates
+};
+
+// Rows [r0, r1) of the FP32 tile W (column-major, ldw, n columns) to the
+// K-major BF16 slot dst (row r at dst + r·b), multiplied by inv.
+__device__ inline void rows_to_bf16(const float* W, int ldw, int r0, int r1, int n, __nv_bfloat16* dst, int b, float inv) {
+    const long total = (long)(r1 - r0) * n;
+    for (long e = threadIdx.x; e < total; e += kThreads) {
+        const int r = r0 + (int)(e / n), c = (int)(e % n);
+        dst[(size_t)r * b + c] = __float2bfloat16_rn(__ldcg(W + r + (size_t)c * ldw) * inv);
+    }
+}
+
+__device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem, tc::TcShared* tsh, uint8_t* ring,
+                             const CUtensorMap* tmap, int* err, long long limit_ns) {
     if (op.prec == TTG_PREC_F64) {
         switch (op.kind) {
             case TTG_OP_POTRF_L:
@@ -78,25 +108,79 @@ __device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem)
         case TTG_OP_TRSM_RLTN:
             trsm_rltn_tile<float>(op.m, op.n, (float)op.alpha, (const float*)op.a, op.lda, (float*)op.c, op.ldc, fsm, part,
                                   parts);
+            if (op.flags == kMixedBF16) {
+                // Publish this row slice as the tile's BF16 panel copy.
+                const MixedTables* tb = (const MixedTables*)op.aux;
+                const int per = ((op.m + parts - 1) / parts + 15) / 16 * 16;
+                const int r0 = min(op.m, part * per), r1 = min(op.m, r0 + per);
+                const float s = tb->rowscale[op.k];
+                __syncthreads();
+                rows_to_bf16((const float*)op.c, op.ldc, r0, r1, op.n, tb->b16 + (size_t)op.ldb * tb->b * tb->b, tb->b, 1.0f / s);
+                if (threadIdx.x == 0 && part == 0) tb->slot_scale[op.ldb] = s;
+                tc::fence_proxy_async_global();
+                __syncthreads();
+            }
             return 0;
         case TTG_OP_SYRK_LN:
+        case TTG_OP_GEMM_NT:
+            if (op.flags == kMixedBF16) {
+                const MixedTables* tb = (const MixedTables*)op.aux;
+                const bool lower = op.kind == TTG_OP_SYRK_LN;
+                int row0, col0;
+                tc::tc_block_coords(part, op.m, op.n, lower, &row0, &col0);
+                const float f = (float)op.alpha * __ldcg(tb->slot_scale + op.lda) * __ldcg(tb->slot_scale + op.ldb);
+                const bool ok = tc::tc_gemm_block(tsh, ring, tmap, op.lda, op.ldb, row0, col0, op.k, f, (float*)op.c, op.ldc,
+                                                  op.m, op.n, lower, limit_ns);
+                if (!ok && threadIdx.x == 0) atomicCAS(err, 0, TTG_ETIMEOUT);
+                return 0;
+            }
+            if (op.kind == TTG_OP_GEMM_NT) {
+                gemm_tile<float, false, false>(op.m, op.n, op.k, (float)op.alpha, (const float*)op.a, op.lda, (const float*)op.b,
+                                               op.ldb, (float)op.beta, (float*)op.c, op.ldc, fsm, part, parts);
+                return 0;
+            }
             gemm_tile<float, false, true>(op.n, op.n, op.k, (float)op.alpha, (const float*)op.a, op.lda, (const float*)op.a,
                                           op.lda, (float)op.beta, (float*)op.c, op.ldc, fsm, part, parts);
-            return 0;
-        case TTG_OP_GEMM_NT:
-            gemm_tile<float, false, false>(op.m, op.n, op.k, (float)op.alpha, (const float*)op.a, op.lda, (const float*)op.b,
-                                           op.ldb, (float)op.beta, (float*)op.c, op.ldc, fsm, part, parts);
             return 0;
         default:
             return 0;
     }
 }
 
-__global__ void __launch_bounds__(kThreads, 1) exec_kernel_mixed(ExecParams p) {
-    extern __shared__ __align__(128) double smem_mx[];
-    executor_loop(p, smem_mx, [](const ttg_op& op, int part, int parts, double* smem) {
-        return run_op_mixed(op, part, parts, smem);
+// Dynamic shared memory: the FP64/FP32 tile kernels use the front, the
+// tensor-core ring (1024-aligned) the rest; both are never live together.
+constexpr int kMixedSmemBytes = tc::kSmemBytes > kF64SmemDoubles * 8 ? tc::kSmemBytes : kF64SmemDoubles * 8;
+
+__global__ void __launch_bounds__(kThreads, 1) exec_kernel_mixed(ExecParams p, const __grid_constant__ MixedGlobals g) {
+    extern __shared__ __align__(1024) double smem_mx[];
+    __shared__ tc::TcShared tsh;
+    uint8_t* ring = reinterpret_cast<uint8_t*>(((uintptr_t)smem_mx + 1023) & ~(uintptr_t)1023);
+    if (g.has_tc) tc::tc_setup(&tsh);
+    const CUtensorMap* tmap = &g.tmap;
+    executor_loop(p, smem_mx, [&](const ttg_op& op, int part, int parts, double* smem) {
+        return run_op_mixed(op, part, parts, smem, &tsh, ring, tmap, p.err, p.timeout_ns);
     });
+    if (g.has_tc) tc::tc_teardown(&tsh, p.timeout_ns);
+}
+
+// Power-of-two scale of each block row: the smallest 2^e >= sqrt(max diag)
+// (a bound on the entries of the Cholesky factor's block row).
+__global__ void block_row_scales(const double* tiles, const int64_t* diag_off, int b, int nb, float* rowscale) {
+    const int i = blockIdx.x;
+    __shared__ double red[256];
+    double mx = 0.0;
+    for (int r = threadIdx.x; r < b; r += blockDim.x) mx = fmax(mx, fabs(tiles[diag_off[i] + r + (size_t)r * b]));
+    red[threadIdx.x] = mx;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        int e = 0;
+        frexp(sqrt(fmax(red[0], 1e-300)), &e);
+        rowscale[i] = ldexpf(1.0f, e);
+    }
 }
 
 __global__ void convert_f64_to_f32(const double* __restrict__ src, float* __restrict__ dst, int64_t n) {
@@ -115,11 +199,12 @@ using namespace ttg;
 
 struct MixedCtx {
     int max_workers = 0;
+    MixedGlobals globals{};  // tensor map of the plan whose graph is uploaded
 };
 
 ttg_status ttg_mixed_init(ttg_ctx* c) {
     MixedCtx* m = new MixedCtx();
-    const int smem = kF64SmemDoubles * (int)sizeof(double);
+    const int smem = kMixedSmemBytes;
     cudaError_t e = cudaFuncSetAttribute(exec_kernel_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     int per_sm = 0;
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, exec_kernel_mixed, kThreads, smem);
@@ -141,8 +226,8 @@ void ttg_mixed_free(ttg_ctx* c) {
 ttg_status ttg_launch_mixed(ttg_ctx* c, const ExecParams& p, cudaStream_t s) {
     MixedCtx* m = (MixedCtx*)c->mixed;
     if (!m || c->workers > m->max_workers) return TTG_EINVAL;
-    const int smem = kF64SmemDoubles * (int)sizeof(double);
-    void* args[] = {(void*)&p};
+    const int smem = kMixedSmemBytes;
+    void* args[] = {(void*)&p, (void*)&m->globals};
     TTG_CUDA_CHECK(cudaLaunchCooperativeKernel((const void*)exec_kernel_mixed, dim3(c->workers), dim3(kThreads), args, smem, s));
     return TTG_OK;
 }
@@ -151,34 +236,95 @@ ttg_status ttg_launch_mixed(ttg_ctx* c, const ExecParams& p, cudaStream_t s) {
 
 struct ttg_mixed_state {
     ttg_ctx* ctx = nullptr;
-    int N = 0, nb = 0, kind = 1;
+    int N = 0, nb = 0, kind = 1, b = 0;
     std::vector<int> bs;
     std::vector<int64_t> off;
     int64_t elems = 0;
     double* tiles64 = nullptr;  // the plan's FP64 tiles (input, then scratch)
     float* w32 = nullptr;       // FP32 working tiles -> low-precision factor
+    // BF16 tensor-core path (kind 0)
+    __nv_bfloat16* b16 = nullptr;  // one K-major b×b slot per lower tile
+    float* slot_scale = nullptr;
+    float* rowscale = nullptr;
+    int64_t* diag_off = nullptr;
+    MixedTables* tables = nullptr;  // device copy
+    MixedGlobals globals{};
 };
+
+static int slot_of(const ttg_mixed_state* m, int i, int j) { return (int)(m->off[i + (size_t)j * m->nb] / ((int64_t)m->b * m->b)); }
+
+static ttg_status encode_tmap(ttg_mixed_state* m, int n_slots) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || !fn || q != cudaDriverEntryPointSuccess) {
+        ttg_set_last_cuda_error(e, "cudaGetDriverEntryPointByVersion(cuTensorMapEncodeTiled)", __FILE__, __LINE__);
+        return TTG_ECUDA;
+    }
+    auto encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    const int b = m->b;
+    cuuint64_t dims[3] = {(cuuint64_t)b, (cuuint64_t)b, (cuuint64_t)n_slots};
+    cuuint64_t strides[2] = {(cuuint64_t)b * 2, (cuuint64_t)b * b * 2};
+    cuuint32_t box[3] = {(cuuint32_t)tc::kBK, 128u, 1u};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = encode(&m->globals.tmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, (void*)m->b16, dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        ttg_set_last_cuda_error(cudaErrorInvalidValue, "cuTensorMapEncodeTiled", __FILE__, __LINE__);
+        return TTG_EINVAL;
+    }
+    m->globals.has_tc = 1;
+    return TTG_OK;
+}
 
 ttg_status ttg_mixed_state_create(ttg_ctx* ctx, int N, int nb, const int* bs, const int64_t* off, double* tiles64, int kind,
                                   ttg_mixed_state** out) {
     *out = nullptr;
-    if (kind != 1) return TTG_EINVAL;  // only FP32 updates so far
+    if (kind != 0 && kind != 1) return TTG_EINVAL;
+    if (kind == 0) {
+        // Tensor-core updates: uniform tiles, a multiple of 128.
+        for (int i = 0; i < nb; ++i)
+            if (bs[i] != bs[0]) return TTG_EINVAL;
+        if (bs[0] <= 0 || bs[0] % 128 != 0) return TTG_EINVAL;
+    }
     ttg_mixed_state* m = new ttg_mixed_state();
     m->ctx = ctx;
     m->N = N;
     m->nb = nb;
     m->kind = kind;
+    m->b = bs[0];
     m->bs.assign(bs, bs + nb);
     m->off.assign(off, off + (size_t)nb * nb);
     m->elems = 0;
     for (int i = 0; i < nb; ++i)
         for (int j = 0; j <= i; ++j) m->elems += (int64_t)bs[i] * bs[j];
     m->tiles64 = tiles64;
+    auto fail = [&](cudaError_t e, const char* what) {
+        ttg_set_last_cuda_error(e, what, __FILE__, __LINE__);
+        ttg_mixed_state_destroy(m);
+        return e == cudaErrorMemoryAllocation ? TTG_ENOMEM : TTG_ECUDA;
+    };
     cudaError_t e = cudaMalloc((void**)&m->w32, sizeof(float) * std::max<int64_t>(1, m->elems));
-    if (e != cudaSuccess) {
-        delete m;
-        ttg_set_last_cuda_error(e, "cudaMalloc w32", __FILE__, __LINE__);
-        return TTG_ENOMEM;
+    if (e != cudaSuccess) return fail(e, "cudaMalloc w32");
+    if (kind == 0) {
+        const int n_slots = nb * (nb + 1) / 2;
+        if ((e = cudaMalloc((void**)&m->b16, sizeof(__nv_bfloat16) * m->elems)) != cudaSuccess) return fail(e, "cudaMalloc b16");
+        if ((e = cudaMemset(m->b16, 0, sizeof(__nv_bfloat16) * m->elems)) != cudaSuccess) return fail(e, "memset b16");
+        if ((e = cudaMalloc((void**)&m->slot_scale, sizeof(float) * n_slots)) != cudaSuccess) return fail(e, "cudaMalloc");
+        if ((e = cudaMalloc((void**)&m->rowscale, sizeof(float) * nb)) != cudaSuccess) return fail(e, "cudaMalloc");
+        if ((e = cudaMalloc((void**)&m->diag_off, sizeof(int64_t) * nb)) != cudaSuccess) return fail(e, "cudaMalloc");
+        if ((e = cudaMalloc((void**)&m->tables, sizeof(MixedTables))) != cudaSuccess) return fail(e, "cudaMalloc");
+        std::vector<int64_t> doff(nb);
+        for (int i = 0; i < nb; ++i) doff[i] = off[i + (size_t)i * nb];
+        cudaMemcpy(m->diag_off, doff.data(), sizeof(int64_t) * nb, cudaMemcpyHostToDevice);
+        MixedTables t{m->b16, m->slot_scale, m->rowscale, m->b};
+        cudaMemcpy(m->tables, &t, sizeof(t), cudaMemcpyHostToDevice);
+        ttg_status st = encode_tmap(m, n_slots);
+        if (st != TTG_OK) {
+            ttg_mixed_state_destroy(m);
+            return st;
+        }
     }
     *out = m;
     return TTG_OK;
@@ -187,20 +333,25 @@ ttg_status ttg_mixed_state_create(ttg_ctx* ctx, int N, int nb, const int* bs, co
 void ttg_mixed_state_destroy(ttg_mixed_state* m) {
     if (!m) return;
     if (m->w32) cudaFree(m->w32);
+    if (m->b16) cudaFree(m->b16);
+    if (m->slot_scale) cudaFree(m->slot_scale);
+    if (m->rowscale) cudaFree(m->rowscale);
+    if (m->diag_off) cudaFree(m->diag_off);
+    if (m->tables) cudaFree(m->tables);
     delete m;
 }
 
-static ttg_op mixed_op(int kind) {
+static ttg_op mixed_op(const ttg_mixed_state* m, int kind) {
     ttg_op op{};
     op.kind = kind;
     op.prec = TTG_PREC_MIXED;
-    op.flags = kMixedF32;
+    op.flags = m->kind == 0 ? kMixedBF16 : kMixedF32;
     op.alpha = 1.0;
     return op;
 }
 
 ttg_op ttg_mixed_potrf_op(ttg_mixed_state* m, int j) {
-    ttg_op op = mixed_op(TTG_OP_POTRF_L);
+    ttg_op op = mixed_op(m, TTG_OP_POTRF_L);
     const int64_t o = m->off[j + (size_t)j * m->nb];
     op.m = op.n = m->bs[j];
     op.c = m->w32 + o;
@@ -210,35 +361,55 @@ ttg_op ttg_mixed_potrf_op(ttg_mixed_state* m, int j) {
 }
 
 ttg_op ttg_mixed_trsm_op(ttg_mixed_state* m, int i, int j) {
-    ttg_op op = mixed_op(TTG_OP_TRSM_RLTN);
+    ttg_op op = mixed_op(m, TTG_OP_TRSM_RLTN);
     op.m = m->bs[i];
     op.n = m->bs[j];
     op.a = m->w32 + m->off[j + (size_t)j * m->nb];
     op.lda = std::max(1, m->bs[j]);
     op.c = m->w32 + m->off[i + (size_t)j * m->nb];
     op.ldc = std::max(1, m->bs[i]);
+    if (m->kind == 0) {
+        op.aux = m->tables;
+        op.ldb = slot_of(m, i, j);  // BF16 slot written by this task
+        op.k = i;                   // block row: its power-of-two scale
+    }
     return op;
 }
 
 ttg_op ttg_mixed_update_op(ttg_mixed_state* m, int k, int i, int j) {
-    ttg_op op = mixed_op(i == j ? TTG_OP_SYRK_LN : TTG_OP_GEMM_NT);
+    ttg_op op = mixed_op(m, i == j ? TTG_OP_SYRK_LN : TTG_OP_GEMM_NT);
     op.m = m->bs[i];
     op.n = m->bs[j];
     op.k = m->bs[k];
     op.alpha = -1.0;
     op.beta = 1.0;
+    op.c = m->w32 + m->off[i + (size_t)j * m->nb];
+    op.ldc = std::max(1, m->bs[i]);
+    if (m->kind == 0) {
+        op.aux = m->tables;
+        op.lda = slot_of(m, i, k);
+        op.ldb = slot_of(m, j, k);
+        return op;
+    }
     op.a = m->w32 + m->off[i + (size_t)k * m->nb];
     op.lda = std::max(1, m->bs[i]);
     op.b = m->w32 + m->off[j + (size_t)k * m->nb];
     op.ldb = std::max(1, m->bs[j]);
-    op.c = m->w32 + m->off[i + (size_t)j * m->nb];
-    op.ldc = std::max(1, m->bs[i]);
     return op;
 }
 
 ttg_status ttg_mixed_prepare(ttg_mixed_state* m, void* stream) {
-    convert_f64_to_f32<<<m->ctx->sms * 8, 256, 0, (cudaStream_t)stream>>>(m->tiles64, m->w32, m->elems);
+    cudaStream_t s = (cudaStream_t)stream;
+    convert_f64_to_f32<<<m->ctx->sms * 8, 256, 0, s>>>(m->tiles64, m->w32, m->elems);
     TTG_CUDA_CHECK(cudaGetLastError());
+    MixedCtx* mc = (MixedCtx*)m->ctx->mixed;
+    if (m->kind == 0) {
+        block_row_scales<<<m->nb, 256, 0, s>>>(m->tiles64, m->diag_off, m->b, m->nb, m->rowscale);
+        TTG_CUDA_CHECK(cudaGetLastError());
+        mc->globals = m->globals;
+    } else {
+        mc->globals.has_tc = 0;
+    }
     return TTG_OK;
 }
 

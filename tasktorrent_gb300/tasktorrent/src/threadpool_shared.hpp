@@ -393,20 +393,40 @@ class Threadpool_shared {
         // Device counters only count promises from tasks that ran; a node
         // that ran has all its promises (it became ready), so in_edges is
         // exact for it.
-        ttg_graph_desc g{};
-        g.n_tasks = nd;
-        g.ops = ops.data();
-        g.init_count = init.data();
-        g.priority = prio.data();
-        g.bind = bind.data();
-        g.succ_ptr = ptr.data();
-        g.succ_idx = idx.data();
-        ttg_status s = ttg_graph_upload(context(), &g);
-        if (s != TTG_OK) throw std::runtime_error(std::string("Threadpool_shared: graph upload failed: ") + ttg_strerror(s));
+        g_ops_ = std::move(ops);
+        g_init_ = std::move(init);
+        g_prio_ = std::move(prio);
+        g_bind_ = std::move(bind);
+        g_ptr_ = std::move(ptr);
+        g_idx_ = std::move(idx);
+        upload();
         uploaded_ = true;
     }
 
+    // Upload the recorded graph (again, if another graph replaced it in the
+    // context since).
+    void upload() {
+        ttg_graph_desc g{};
+        g.n_tasks = (int32_t)g_ops_.size();
+        g.ops = g_ops_.data();
+        g.init_count = g_init_.data();
+        g.priority = g_prio_.data();
+        g.bind = g_bind_.data();
+        g.succ_ptr = g_ptr_.data();
+        g.succ_idx = g_idx_.data();
+        ttg_status s = ttg_graph_upload(context(), &g);
+        if (s != TTG_OK) throw std::runtime_error(std::string("Threadpool_shared: graph upload failed: ") + ttg_strerror(s));
+        graph_gen_ = ttg_graph_generation(context());
+    }
+
     ttg_status run_device(void* stream = nullptr) {
+        if (ttg_graph_generation(context()) != graph_gen_) {
+            try {
+                upload();
+            } catch (const std::exception&) {
+                return TTG_ECUDA;
+            }
+        }
         timer t0 = wctime();
         ttg_status s = ttg_run(context(), stream, &report_);
         timer t1 = wctime();
@@ -452,6 +472,12 @@ class Threadpool_shared {
     std::priority_queue<std::pair<double, long>> ready_;
     std::vector<int> dev_node_;
     std::vector<char> dev_last_;
+    // The recorded graph, kept for re-uploads.
+    std::vector<ttg_op> g_ops_;
+    std::vector<int32_t> g_init_, g_bind_, g_idx_;
+    std::vector<double> g_prio_;
+    std::vector<int64_t> g_ptr_;
+    uint64_t graph_gen_ = 0;
 };
 
 #ifdef TTOR_SHARED

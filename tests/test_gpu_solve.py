@@ -45,6 +45,18 @@ def test_mixed_factor_is_fp32_accurate(ctx):
     p.close()
 
 
+@pytest.mark.parametrize("nrhs", [1, 2, 3, 16])
+def test_mixed_small_nrhs(ctx, nrhs):
+    p = t.CholPlan(ctx, 64, 6, matrix=1, alpha=1e-4, seed=3, precision=t.PREC_MIXED, mixed_kind=1)
+    A = p.input_A()
+    B = rhs(p.N, nrhs, seed=nrhs)
+    st, rep, X = p.solve_host(B)
+    assert st == t.TTG_OK, rep.as_dict()
+    assert np.isfinite(X).all()
+    assert bwd_err(A, X, B) <= 2 * BWD, rep.as_dict()
+    p.close()
+
+
 @pytest.mark.parametrize("alpha", [1.0, 1e-4, 1e-8])
 @pytest.mark.parametrize("gprec", [0, 64])
 def test_mixed_gmres_ir_reaches_fp64_backward_error(ctx, alpha, gprec):
@@ -67,6 +79,7 @@ def test_follow_up_rhs_reuse_factor(ctx):
     B1 = rhs(p.N, 2, seed=1)
     st, rep1, X1 = p.solve_host(B1)
     assert st == t.TTG_OK
+    assert bwd_err(A, X1, B1) <= 2 * BWD
     B2 = rhs(p.N, 3, seed=2)
     st, rep2, X2 = p.solve_host(B2, factor=False)  # resident factor
     assert st == t.TTG_OK and rep2.factor_ms == 0.0

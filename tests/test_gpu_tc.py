@@ -1,0 +1,67 @@
+"""Mixed Cholesky with BF16 trailing updates on tcgen05 tensor cores (TMA
+operands, TMEM accumulators): factor accuracy at BF16 level, identical task
+graph, and GMRES-IR to FP64 backward error."""
+import os
+
+import numpy as np
+import pytest
+
+import tasktorrent_gb300 as t
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+BWD = 1e-14
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def bwd_err(A, X, B):
+    R = B - A @ X
+    return np.max(np.abs(R).max(axis=0) / (np.abs(A).sum(axis=1).max() * np.abs(X).max(axis=0)))
+
+
+@pytest.mark.parametrize("b,nb", [(128, 2), (256, 2), (128, 5), (512, 4)])
+def test_bf16_factor_accuracy(ctx, b, nb):
+    p = t.CholPlan(ctx, b, nb, kind=2, matrix=1, alpha=1.0, seed=0, precision=t.PREC_MIXED, mixed_kind=0)
+    st, rep = p.factor()
+    assert st == t.TTG_OK, t.strerror(st)
+    assert rep.tasks_run == rep.tasks_total and rep.bad_runs == 0
+    A = p.input_A()
+    L = p.factor_L()
+    e = rel(L @ L.T, A)
+    # BF16 operands (8-bit mantissa), FP32 accumulation: ~1e-3 relative.
+    assert 1e-6 < e < 2e-2, e
+    # Compare with the FP32-update factor: same graph, lower-precision products.
+    q = t.CholPlan(ctx, b, nb, kind=2, matrix=1, alpha=1.0, seed=0, precision=t.PREC_MIXED, mixed_kind=1)
+    st, _ = q.factor()
+    assert st == t.TTG_OK
+    assert rel(L, q.factor_L()) < 2e-2
+    p.close()
+    q.close()
+
+
+def test_bf16_repeatable(ctx):
+    p = t.CholPlan(ctx, 256, 4, kind=2, matrix=1, alpha=1.0, seed=1, precision=t.PREC_MIXED, mixed_kind=0)
+    Ls = []
+    for _ in range(2):
+        st, _ = p.factor()
+        assert st == t.TTG_OK
+        Ls.append(p.factor_L())
+    assert np.array_equal(Ls[0], Ls[1])  # fixed k order per tile: same bits
+    p.close()
+
+
+@pytest.mark.parametrize("alpha,max_outer", [(1.0, 10), (1e-4, 15), (1e-8, 30)])
+def test_bf16_gmres_ir_to_fp64_backward_error(ctx, alpha, max_outer):
+    p = t.CholPlan(ctx, 128, 8, kind=2, matrix=1, alpha=alpha, seed=2, precision=t.PREC_MIXED, mixed_kind=0)
+    A = p.input_A()
+    B = orc.normals(0, p.N * 16, 9, 1).reshape(p.N, 16, order="F")
+    st, rep, X = p.solve_host(B, tol=BWD, max_outer=max_outer, restart=30)
+    assert st == t.TTG_OK, rep.as_dict()
+    assert rep.bwd_err <= BWD and bwd_err(A, X, B) <= 2 * BWD
+    Xref = np.linalg.solve(A, B)
+    assert rel(X, Xref) <= max(1e-12, 1e-15 * np.linalg.cond(A) * 100)
+    p.close()
