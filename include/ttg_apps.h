@@ -88,6 +88,10 @@ ttg_status ttg_chol_plan_dump_dag(ttg_chol_plan* plan, const char* prefix);
  * and write its DAG record — the graph a plan with these arguments runs. */
 ttg_status ttg_chol_dag_dump(const ttg_chol_args* args, const char* prefix);
 
+/* Mixed plans: how the last factorisation was obtained (see
+ * ttg_solve_report.remedy); -1 for a NULL plan. */
+int32_t ttg_chol_plan_remedy(const ttg_chol_plan* plan);
+
 /* Per-kind device busy time (ms) of the last run (needs ctx trace). */
 ttg_status ttg_chol_plan_kind_times(ttg_chol_plan* plan, double* potrf_ms, double* trsm_ms, double* gemm_ms, double* accu_ms);
 
@@ -116,6 +120,8 @@ typedef struct ttg_solve_report {
     double anorm_inf;   /* ‖A‖∞                                                        */
     double factor_ms;   /* factorisation (device events; 0 for ttg_chol_plan_solve)     */
     double solve_ms;    /* solve and refinement (host clock)                           */
+    int32_t remedy;     /* mixed factor: 0 BF16 updates, 1 BF16 with a diagonal shift,
+                           2 FP32 updates (after the BF16 factor lost definiteness)    */
 } ttg_solve_report;
 
 /* d_B, d_X: device N×nrhs column-major (ld N). */

@@ -73,7 +73,7 @@ class SolveOpts(ctypes.Structure):
 class SolveReport(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int32), ("outer", ctypes.c_int32), ("inner", ctypes.c_int32),
                 ("gmres_prec", ctypes.c_int32), ("bwd_err", ctypes.c_double), ("anorm_inf", ctypes.c_double),
-                ("factor_ms", ctypes.c_double), ("solve_ms", ctypes.c_double)]
+                ("factor_ms", ctypes.c_double), ("solve_ms", ctypes.c_double), ("remedy", ctypes.c_int32)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -121,6 +121,7 @@ SIGNATURES = {
     "ttg_chol_plan_tiles": (_P, [_P, _P]),
     "ttg_chol_plan_dump_dag": (_STATUS, [_P, ctypes.c_char_p]),
     "ttg_chol_plan_kind_times": (_STATUS, [_P, _P, _P, _P, _P]),
+    "ttg_chol_plan_remedy": (ctypes.c_int32, [_P]),
     "ttg_chol_dag_dump": (_STATUS, [ctypes.POINTER(CholArgs), ctypes.c_char_p]),
     "ttg_gemm_dag_dump": (_STATUS, [ctypes.POINTER(GemmArgs), ctypes.c_char_p]),
     "ttg_chol_plan_solve": (_STATUS, [_P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveReport), _P]),

@@ -69,7 +69,9 @@ struct ttg_chol_plan {
     int64_t elems = 0;
     double* tiles = nullptr;     // working tiles (factorised in place)
     double* pristine = nullptr;  // input copy
-    std::unique_ptr<Threadpool_shared> tp;
+    std::unique_ptr<Threadpool_shared> tp;    // the plan's graph (FP64, or mixed with BF16 updates when available)
+    std::unique_ptr<Threadpool_shared> tp32;  // mixed plans with tensor cores: the same graph with FP32 updates
+    int remedy = 0;                           // last mixed factorisation: 0 none, 1 diagonal shift, 2 FP32 updates
     std::vector<int> kind_of_dev;  // per device task: 0 potrf, 1 trsm, 2 gemm, 3 accu, -1 other
     std::vector<double*> tmp;      // accumulate-flow temporaries (device)
     ttg_mixed_state* mixed = nullptr;
@@ -80,7 +82,7 @@ struct ttg_chol_plan {
     long solver_gen = -1;  // factorisation the solver's inverted tiles belong to
 };
 
-static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry) {
+static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry, bool tc, std::unique_ptr<Threadpool_shared>& tp_out) {
     const ttg_chol_args& a = P->args;
     const int nb = P->nb, n_threads = a.n_threads;
     const bool accumulate = a.accumulate != 0;
@@ -128,8 +130,8 @@ static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry) {
                 }
     }
 
-    P->tp.reset(new Threadpool_shared(n_threads, a.verb, "Wk_Chol_0_"));
-    Threadpool_shared& tp = *P->tp;
+    tp_out.reset(new Threadpool_shared(n_threads, a.verb, "Wk_Chol_0_"));
+    Threadpool_shared& tp = *tp_out;
     if (!dry) tp.set_context(P->ctx);
     Taskflow<int> potrf(&tp, a.verb);
     Taskflow<Key2> trsm(&tp, a.verb);
@@ -137,7 +139,7 @@ static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry) {
     Taskflow<Key3> accu(&tp, a.verb);
 
     potrf.set_task([&](int j) {
-             if (mixed) gpu::record_op(ttg_mixed_potrf_op(P->mixed, j));
+             if (mixed) gpu::record_op(ttg_mixed_potrf_op(P->mixed, j, tc));
              else gpu::LAPACKE_dpotrf(gpu::LAPACK_COL_MAJOR, 'L', P->bs[j], block(j, j), lda(j));
          })
         .set_fulfill([&](int j) {
@@ -150,7 +152,7 @@ static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry) {
 
     trsm.set_task([&](Key2 ij) {
             const int i = ij[0], j = ij[1];
-            if (mixed) gpu::record_op(ttg_mixed_trsm_op(P->mixed, i, j));
+            if (mixed) gpu::record_op(ttg_mixed_trsm_op(P->mixed, i, j, tc));
             else
                 gpu::cblas_dtrsm(gpu::CblasColMajor, gpu::CblasRight, gpu::CblasLower, gpu::CblasTrans, gpu::CblasNonUnit,
                                  P->bs[i], P->bs[j], 1.0, block(j, j), lda(j), block(i, j), lda(i));
@@ -170,7 +172,7 @@ static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry) {
             double* C = accumulate ? tmp_of[{k, i, j}] : block(i, j);
             const double beta = accumulate ? 0.0 : 1.0;
             if (mixed) {
-                gpu::record_op(ttg_mixed_update_op(P->mixed, k, i, j));
+                gpu::record_op(ttg_mixed_update_op(P->mixed, k, i, j, tc));
             } else if (i == j) {
                 gpu::cblas_dsyrk(gpu::CblasColMajor, gpu::CblasLower, gpu::CblasNoTrans, P->bs[i], P->bs[k], -1.0, block(i, k),
                                  lda(i), beta, C, lda(i));
@@ -263,7 +265,9 @@ extern "C" ttg_status ttg_chol_plan_create(ttg_ctx* ctx, const ttg_chol_args* ar
         ttg_status s = ttg_mixed_state_create(ctx, P->N, P->nb, P->bs.data(), P->off.data(), P->tiles, args->mixed_kind, &P->mixed);
         if (s != TTG_OK) return s;
     }
-    ttg_status s = chol_build_graph(P.get(), false);
+    const bool tc = P->mixed && ttg_mixed_has_tc(P->mixed);
+    ttg_status s = chol_build_graph(P.get(), false, tc, P->tp);
+    if (s == TTG_OK && tc) s = chol_build_graph(P.get(), false, false, P->tp32);
     if (s != TTG_OK) {
         ttg_chol_plan_destroy(P.release());
         return s;
@@ -287,7 +291,7 @@ extern "C" ttg_status ttg_chol_dag_dump(const ttg_chol_args* args, const char* p
     P.nb = args->num_blocks;
     P.off.assign((size_t)P.nb * P.nb, 0);
     P.elems = ttg_tile_layout(P.bs.data(), P.nb, P.off.data());
-    ttg_status s = chol_build_graph(&P, true);
+    ttg_status s = chol_build_graph(&P, true, false, P.tp);
     if (s != TTG_OK) return s;
     P.tp->dump_dag(prefix);
     return TTG_OK;
@@ -297,6 +301,7 @@ extern "C" ttg_status ttg_chol_plan_destroy(ttg_chol_plan* P) {
     if (!P) return TTG_OK;
     cudaSetDevice(P->ctx->device);
     P->tp.reset();
+    P->tp32.reset();
     for (double* t : P->tmp) cudaFree(t);
     if (P->tiles) cudaFree(P->tiles);
     if (P->pristine) cudaFree(P->pristine);
@@ -382,15 +387,56 @@ extern "C" ttg_status ttg_chol_plan_restore(ttg_chol_plan* P, void* stream) {
 extern "C" ttg_status ttg_chol_plan_factor(ttg_chol_plan* P, void* stream, ttg_report* rep) {
     if (!P) return TTG_EINVAL;
     TTG_CUDA_CHECK(cudaSetDevice(P->ctx->device));
-    if (P->mixed) {
-        ttg_status s = ttg_mixed_prepare(P->mixed, stream);
-        if (s != TTG_OK) return s;
+    if (!P->mixed) {
+        ttg_status s = P->tp->replay(stream);
+        if (rep) *rep = P->tp->report();
+        if (s == TTG_OK) ++P->factor_gen;
+        return s;
     }
-    ttg_status s = P->tp->replay(stream);
-    if (rep) *rep = P->tp->report();
+    // Mixed: BF16 tensor-core updates when available.  A trailing diagonal
+    // block that loses positive definiteness (TTG_ENOTPD) is handled by a
+    // retry with a relative diagonal shift of a few BF16 units, then by FP32
+    // updates; iterative refinement always solves the unshifted system.
+    // Retries start from the restored input (a failed run overwrote it).
+    const bool tc = ttg_mixed_has_tc(P->mixed);
+    struct Attempt {
+        Threadpool_shared* tp;
+        double shift;
+        bool tc;
+        int remedy;
+    };
+    std::vector<Attempt> plan;
+    if (tc) {
+        plan.push_back({P->tp.get(), 0.0, true, 0});
+        plan.push_back({P->tp.get(), 8.0 * 0.00390625, true, 1});
+        plan.push_back({P->tp32.get(), 0.0, false, 2});
+    } else {
+        plan.push_back({P->tp.get(), 0.0, false, 0});
+    }
+    ttg_status s = TTG_OK;
+    float total_ms = 0.f;
+    for (size_t a = 0; a < plan.size(); ++a) {
+        if (a > 0) {
+            s = ttg_chol_plan_restore(P, stream);
+            if (s != TTG_OK) return s;
+        }
+        s = ttg_mixed_prepare(P->mixed, stream, plan[a].shift, plan[a].tc);
+        if (s != TTG_OK) return s;
+        s = plan[a].tp->replay(stream);
+        const ttg_report r = plan[a].tp->report();
+        total_ms += r.elapsed_ms;
+        if (rep) {
+            *rep = r;
+            rep->elapsed_ms = total_ms;
+        }
+        P->remedy = plan[a].remedy;
+        if (s != TTG_ENOTPD) break;
+    }
     if (s == TTG_OK) ++P->factor_gen;
     return s;
 }
+
+extern "C" int32_t ttg_chol_plan_remedy(const ttg_chol_plan* P) { return P ? P->remedy : -1; }
 
 extern "C" ttg_status ttg_chol_factor_host(ttg_chol_plan* P, const double* h_A, double* h_L, void* stream, ttg_report* rep) {
     if (!P || !h_A) return TTG_EINVAL;
@@ -424,8 +470,13 @@ extern "C" ttg_status ttg_chol_factor_host_tiles(ttg_chol_plan* P, const double*
     if (!P || !h_in) return TTG_EINVAL;
     TTG_CUDA_CHECK(cudaSetDevice(P->ctx->device));
     cudaStream_t s = (cudaStream_t)stream;
-    TTG_CUDA_CHECK(cudaMemcpyAsync(P->tiles, h_in, sizeof(double) * P->elems, cudaMemcpyHostToDevice, s));
-    ttg_status st = ttg_chol_plan_factor(P, stream, rep);
+    // The input becomes the plan's input (a mixed factorisation may restart
+    // from it), then the working tiles are restored from it and factored.
+    TTG_CUDA_CHECK(cudaMemcpyAsync(P->pristine, h_in, sizeof(double) * P->elems, cudaMemcpyHostToDevice, s));
+    if (P->solver) ttg_solver_input_changed(P->solver);
+    ttg_status st = ttg_chol_plan_restore(P, stream);
+    if (st != TTG_OK) return st;
+    st = ttg_chol_plan_factor(P, stream, rep);
     if (st != TTG_OK) return st;
     if (h_out) {
         const double* src = P->mixed ? ttg_mixed_factor_tiles(P->mixed) : P->tiles;
@@ -478,6 +529,7 @@ extern "C" ttg_status ttg_chol_plan_solve(ttg_chol_plan* P, const double* d_B, d
     }
     ttg_solve_report r{};
     ttg_status st = ttg_solver_solve(P->solver, P->pristine, P->tiles, L32, d_B, d_X, o, &r, s);
+    r.remedy = mixed ? P->remedy : 0;
     r.solve_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     if (rep) *rep = r;
     return st;

@@ -188,6 +188,15 @@ __global__ void convert_f64_to_f32(const double* __restrict__ src, float* __rest
         dst[e] = (float)src[e];
 }
 
+// W(i,i) += shift·|W(i,i)| on one diagonal tile (ld = b).
+__global__ void shift_diagonal(float* W, int b, double shift) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < b) {
+        float* p = W + i + (size_t)i * b;
+        *p = (float)((double)*p + shift * fabs((double)*p));
+    }
+}
+
 __global__ void convert_f32_to_f64(const float* __restrict__ src, double* __restrict__ dst, int64_t n) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
         dst[e] = (double)src[e];
@@ -341,17 +350,19 @@ void ttg_mixed_state_destroy(ttg_mixed_state* m) {
     delete m;
 }
 
-static ttg_op mixed_op(const ttg_mixed_state* m, int kind) {
+bool ttg_mixed_has_tc(const ttg_mixed_state* m) { return m && m->kind == 0; }
+
+static ttg_op mixed_op(const ttg_mixed_state* m, int kind, bool tc) {
     ttg_op op{};
     op.kind = kind;
     op.prec = TTG_PREC_MIXED;
-    op.flags = m->kind == 0 ? kMixedBF16 : kMixedF32;
+    op.flags = (tc && m->kind == 0) ? kMixedBF16 : kMixedF32;
     op.alpha = 1.0;
     return op;
 }
 
-ttg_op ttg_mixed_potrf_op(ttg_mixed_state* m, int j) {
-    ttg_op op = mixed_op(m, TTG_OP_POTRF_L);
+ttg_op ttg_mixed_potrf_op(ttg_mixed_state* m, int j, bool tc) {
+    ttg_op op = mixed_op(m, TTG_OP_POTRF_L, tc);
     const int64_t o = m->off[j + (size_t)j * m->nb];
     op.m = op.n = m->bs[j];
     op.c = m->w32 + o;
@@ -360,15 +371,15 @@ ttg_op ttg_mixed_potrf_op(ttg_mixed_state* m, int j) {
     return op;
 }
 
-ttg_op ttg_mixed_trsm_op(ttg_mixed_state* m, int i, int j) {
-    ttg_op op = mixed_op(m, TTG_OP_TRSM_RLTN);
+ttg_op ttg_mixed_trsm_op(ttg_mixed_state* m, int i, int j, bool tc) {
+    ttg_op op = mixed_op(m, TTG_OP_TRSM_RLTN, tc);
     op.m = m->bs[i];
     op.n = m->bs[j];
     op.a = m->w32 + m->off[j + (size_t)j * m->nb];
     op.lda = std::max(1, m->bs[j]);
     op.c = m->w32 + m->off[i + (size_t)j * m->nb];
     op.ldc = std::max(1, m->bs[i]);
-    if (m->kind == 0) {
+    if (op.flags == kMixedBF16) {
         op.aux = m->tables;
         op.ldb = slot_of(m, i, j);  // BF16 slot written by this task
         op.k = i;                   // block row: its power-of-two scale
@@ -376,8 +387,8 @@ ttg_op ttg_mixed_trsm_op(ttg_mixed_state* m, int i, int j) {
     return op;
 }
 
-ttg_op ttg_mixed_update_op(ttg_mixed_state* m, int k, int i, int j) {
-    ttg_op op = mixed_op(m, i == j ? TTG_OP_SYRK_LN : TTG_OP_GEMM_NT);
+ttg_op ttg_mixed_update_op(ttg_mixed_state* m, int k, int i, int j, bool tc) {
+    ttg_op op = mixed_op(m, i == j ? TTG_OP_SYRK_LN : TTG_OP_GEMM_NT, tc);
     op.m = m->bs[i];
     op.n = m->bs[j];
     op.k = m->bs[k];
@@ -385,7 +396,7 @@ ttg_op ttg_mixed_update_op(ttg_mixed_state* m, int k, int i, int j) {
     op.beta = 1.0;
     op.c = m->w32 + m->off[i + (size_t)j * m->nb];
     op.ldc = std::max(1, m->bs[i]);
-    if (m->kind == 0) {
+    if (op.flags == kMixedBF16) {
         op.aux = m->tables;
         op.lda = slot_of(m, i, k);
         op.ldb = slot_of(m, j, k);
@@ -398,12 +409,19 @@ ttg_op ttg_mixed_update_op(ttg_mixed_state* m, int k, int i, int j) {
     return op;
 }
 
-ttg_status ttg_mixed_prepare(ttg_mixed_state* m, void* stream) {
+ttg_status ttg_mixed_prepare(ttg_mixed_state* m, void* stream, double shift, bool tc) {
     cudaStream_t s = (cudaStream_t)stream;
     convert_f64_to_f32<<<m->ctx->sms * 8, 256, 0, s>>>(m->tiles64, m->w32, m->elems);
     TTG_CUDA_CHECK(cudaGetLastError());
+    if (shift > 0) {
+        for (int j = 0; j < m->nb; ++j) {
+            const int64_t o = m->off[j + (size_t)j * m->nb];
+            shift_diagonal<<<(m->bs[j] + 255) / 256, 256, 0, s>>>(m->w32 + o, m->bs[j], shift);
+        }
+        TTG_CUDA_CHECK(cudaGetLastError());
+    }
     MixedCtx* mc = (MixedCtx*)m->ctx->mixed;
-    if (m->kind == 0) {
+    if (m->kind == 0 && tc) {
         block_row_scales<<<m->nb, 256, 0, s>>>(m->tiles64, m->diag_off, m->b, m->nb, m->rowscale);
         TTG_CUDA_CHECK(cudaGetLastError());
         mc->globals = m->globals;

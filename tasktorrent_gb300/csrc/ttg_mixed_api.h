@@ -17,12 +17,17 @@ struct ttg_mixed_state;
 ttg_status ttg_mixed_state_create(ttg_ctx* ctx, int N, int nb, const int* bs, const int64_t* off, double* tiles64, int kind,
                                   ttg_mixed_state** out);
 void ttg_mixed_state_destroy(ttg_mixed_state* m);
-// Tile operations of the three task kinds.
-ttg_op ttg_mixed_potrf_op(ttg_mixed_state* m, int j);
-ttg_op ttg_mixed_trsm_op(ttg_mixed_state* m, int i, int j);
-ttg_op ttg_mixed_update_op(ttg_mixed_state* m, int k, int i, int j);
-// Convert the FP64 input tiles (tiles64) to the FP32 working tiles.
-ttg_status ttg_mixed_prepare(ttg_mixed_state* m, void* stream);
+// Whether the state has the BF16 tensor-core variant (kind 0).
+bool ttg_mixed_has_tc(const ttg_mixed_state* m);
+// Tile operations of the three task kinds; tc selects the BF16 tensor-core
+// variant (kind 0 states only), otherwise FP32 updates.
+ttg_op ttg_mixed_potrf_op(ttg_mixed_state* m, int j, bool tc);
+ttg_op ttg_mixed_trsm_op(ttg_mixed_state* m, int i, int j, bool tc);
+ttg_op ttg_mixed_update_op(ttg_mixed_state* m, int k, int i, int j, bool tc);
+// Convert the FP64 input tiles (tiles64) to the FP32 working tiles, adding
+// shift·|a_ii| to every diagonal entry (shift 0: none), and select the
+// tensor-core variant (tc) for the next run.
+ttg_status ttg_mixed_prepare(ttg_mixed_state* m, void* stream, double shift, bool tc);
 // The low-precision factor as FP64 tiles (converted into tiles64).
 const double* ttg_mixed_factor_tiles(ttg_mixed_state* m);
 // The FP32 factor tiles (same layout as tiles64).
