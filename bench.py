@@ -151,106 +151,167 @@ def _tasks(nb):
 
 
 def run_ours(args, world, rank, local):
+    import ctypes
+    import numpy as np
     import torch
     import tasktorrent_gb300 as t
     torch.cuda.set_device(local)
-    ctx = t.Context(device=local, timeout_s=60.0)
+    ctx = t.Context(device=local, timeout_s=120.0)
     nb = args.n // args.block
     N = nb * args.block
-    plan = t.CholPlan(ctx, args.block, nb, n_threads=16, kind=args.kind, matrix=1, alpha=args.alpha, seed=args.seed + rank)
-    n_tasks, capture_s = plan.tasks()
+    nrhs = args.nrhs
     flops = N ** 3 / 3.0
-    stream = None  # the legacy default stream: torch's current stream here
+    lib = t.lib()
 
-    def step():
-        t.check(t.lib().ttg_chol_plan_restore(plan.h, stream), "restore")
+    # Right-hand sides: iid N(0,1) from seed, on the device.
+    B = torch.empty(nrhs, N, dtype=torch.float64, device="cuda")  # column-major N×nrhs
+    X = torch.empty_like(B)
+    t.check(lib.ttg_gen_normal(ctx.h, N * nrhs, args.seed + 100 + rank, 1, ctypes.c_void_p(B.data_ptr()), None), "rhs")
+    torch.cuda.synchronize()
+
+    def opts():
+        return t.SolveOpts(nrhs, args.tol, 30, 30, 0, 0.0)
+
+    def posv(plan, restore=True):
+        """One time-to-solution step on the resident input: factor + solve.
+        The restore of the in-place factorisation's input is outside the timed
+        interval; returns (ms, report)."""
+        if restore:
+            t.check(lib.ttg_chol_plan_restore(plan.h, None), "restore")
+        rep = t.SolveReport()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record()
-        st, rep = plan.factor(restore=False, stream=stream)
-        e1.record()
+        fr = t.Report()
+        st = lib.ttg_chol_plan_factor(plan.h, None, ctypes.byref(fr))
         if st != t.TTG_OK:
             raise RuntimeError("factor failed: %s" % t.strerror(st))
-        return e0, e1, rep
+        st = lib.ttg_chol_plan_solve(plan.h, ctypes.c_void_p(B.data_ptr()), ctypes.c_void_p(X.data_ptr()),
+                                     ctypes.byref(opts()), ctypes.byref(rep), None)
+        e1.record()
+        torch.cuda.synchronize()
+        if st != t.TTG_OK:
+            raise RuntimeError("solve failed: %s (%s)" % (t.strerror(st), rep.as_dict()))
+        rep.factor_ms = fr.elapsed_ms
+        return e0.elapsed_time(e1), rep
 
+    # Headline: mixed precision (BF16 tensor-core updates) + GMRES-IR at alpha.
+    plan = t.CholPlan(ctx, args.block, nb, n_threads=16, kind=args.kind, matrix=1, alpha=args.alpha,
+                      seed=args.seed + rank, precision=t.PREC_MIXED, mixed_kind=0)
+    n_tasks, capture_s = plan.tasks()
     for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
+        posv(plan)
     barrier(world)
-    evs, kernel_ms = [], []
+    times, reps, kernel_ms = [], [], []
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
         w0 = time.perf_counter()
         for _ in range(args.steps):
-            e0, e1, rep = step()
-            evs.append((e0, e1))
-            kernel_ms.append(rep.elapsed_ms)
+            ms, rep = posv(plan)
+            times.append(ms)
+            reps.append(rep)
+            kernel_ms.append(rep.factor_ms)
         torch.cuda.synchronize()
         wall = time.perf_counter() - w0
     barrier(world)
-    step_ms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
-    step_ms = allmax(world, step_ms)
+    step_ms = allmax(world, statistics.mean(times))
     value = world * flops / (step_ms * 1e-3) / 1e12
+    X_mixed = X.clone()
 
-    # Roofline of the executor kernel (the only compute kernel of a step).
-    peak = ctx.fp64_peak(200.0)
-    kms = statistics.mean(kernel_ms)
-    achieved = flops / (kms * 1e-3) / 1e12
-
-    # Correctness of the measured factor.
-    err = None
-    if args.check:
-        import numpy as np
-        from oracle import oracle as orc  # noqa: F401  (checker only)
-        if N <= 8192:
-            L = plan.factor_L()
-            A = plan.input_A()
-            err = float(np.linalg.norm(L @ L.T - A) / np.linalg.norm(A))
-
-    # End to end through the C ABI with pinned host buffers.
+    # e2e through the C ABI: pinned host tiles of A and host B in, host X out.
     elems = plan.tile_elems()
     e2e = None
     if not args.no_e2e:
         hin = torch.empty(elems, dtype=torch.float64, pin_memory=True)
-        hout = torch.empty(elems, dtype=torch.float64, pin_memory=True)
+        hB = torch.empty(nrhs * N, dtype=torch.float64, pin_memory=True)
+        hX = torch.empty(nrhs * N, dtype=torch.float64, pin_memory=True)
         plan.copy_tiles(1, hin.data_ptr())
-        plan.factor_host_tiles(hin.data_ptr(), hout.data_ptr())  # warm the copy path
+        hB.copy_(B.reshape(-1).cpu())
+        o = opts()
+        rep = t.SolveReport()
+        t.check(lib.ttg_chol_posv_host(plan.h, ctypes.c_void_p(hin.data_ptr()), ctypes.c_void_p(hB.data_ptr()),
+                                       ctypes.c_void_p(hX.data_ptr()), ctypes.byref(o), ctypes.byref(rep), None), "e2e warm")
         barrier(world)
         ts = []
         for _ in range(args.steps):
             s0 = time.perf_counter()
-            st, rep = plan.factor_host_tiles(hin.data_ptr(), hout.data_ptr())
+            st = lib.ttg_chol_posv_host(plan.h, ctypes.c_void_p(hin.data_ptr()), ctypes.c_void_p(hB.data_ptr()),
+                                        ctypes.c_void_p(hX.data_ptr()), ctypes.byref(o), ctypes.byref(rep), None)
             ts.append(time.perf_counter() - s0)
             if st != t.TTG_OK:
                 raise RuntimeError("e2e failed: %s" % t.strerror(st))
         e2e_s = allmax(world, statistics.mean(ts))
-        e2e = {"value": world * flops / e2e_s / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": elems * 8,
-               "d2h_bytes_per_step": elems * 8}
-        del hin, hout
+        e2e = {"value": world * flops / e2e_s / 1e12, "unit": "TFLOP/s", "solves_per_s": world * nrhs / e2e_s,
+               "h2d_bytes_per_step": elems * 8 + N * nrhs * 8, "d2h_bytes_per_step": N * nrhs * 8}
+        del hin, hB, hX
+    plan.close()
+
+    # Roofline of the dominant kernel (the mixed executor: BF16 tensor-core
+    # updates, FP32 TRSM, FP64 diagonal POTRF) against the measured dense BF16
+    # tensor peak.
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except Exception:
+        pass
+    bf16_peak = peaks.get("bf16_tflops", 1900.0)
+    kms = statistics.mean(kernel_ms)
+    achieved = flops / (kms * 1e-3) / 1e12
+
+    extra = {}
+    if not args.quick:
+        # The plain FP64 device path on the same input (time to solution).
+        p64 = t.CholPlan(ctx, args.block, nb, n_threads=16, kind=args.kind, matrix=1, alpha=args.alpha, seed=args.seed + rank)
+        posv(p64)
+        ms64, rep64 = posv(p64)
+        X64 = X.clone()
+        fwd = float(torch.linalg.norm(X_mixed - X64) / torch.linalg.norm(X64))
+        extra["fp64"] = {"ms_per_solve": ms64, "tflops": flops / (ms64 * 1e-3) / 1e12, "factor_ms": rep64.factor_ms,
+                         "bwd_err": rep64.bwd_err, "fp64_peak_tflops": ctx.fp64_peak(200.0)}
+        extra["speedup_mixed_vs_fp64"] = ms64 / step_ms
+        extra["fwd_err_vs_fp64"] = fwd
+        p64.close()
+        # The three conditionings of the workload (one step each).
+        per_alpha = []
+        for a in (1.0, 1e-4, 1e-8):
+            pa = t.CholPlan(ctx, args.block, nb, n_threads=16, kind=args.kind, matrix=1, alpha=a, seed=args.seed + rank,
+                            precision=t.PREC_MIXED, mixed_kind=0)
+            posv(pa)
+            msa, ra = posv(pa)
+            per_alpha.append({"alpha": a, "ms": msa, "factor_ms": ra.factor_ms, "outer": ra.outer, "inner": ra.inner,
+                              "gmres_prec": ra.gmres_prec, "remedy": ra.remedy, "bwd_err": ra.bwd_err})
+            pa.close()
+        extra["mixed_per_alpha"] = per_alpha
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         v, cores, blas, tcpu = cpu_sample(2, 1, args.cpu_n, args.cpu_b)
         cpu = {"value": v, "unit": "TFLOP/s", "cores": cores, "kind": "port",
-               "sample": "FP64 tiled Cholesky N=%d tile %d, oracle port of 2d_cholesky at one rank, %d threads, %s, "
-                         "median of 2 after 1 warm-up" % (args.cpu_n, args.cpu_b, cores, os.path.basename(blas))}
+               "sample": "FP64 tiled Cholesky factorisation N=%d tile %d, oracle port of 2d_cholesky at one rank, %d threads, "
+                         "%s, median of 2 after 1 warm-up" % (args.cpu_n, args.cpu_b, cores, os.path.basename(blas))}
 
     if rank == 0:
+        last = reps[-1]
         line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic: A = G*G^T/N + alpha*I, G quantised N(0,1) (Philox-4x32-10, seed %d)" % args.seed,
-                "config": {"workload": "tiled Cholesky factorisation, FP64 path", "matrix_size": N, "block_size": args.block,
-                           "tasks": n_tasks, "alpha": args.alpha, "priority_kind": args.kind,
-                           "l2": "inputs larger than L2 (%.1f GB of tiles)" % (elems * 8 / 1e9),
-                           "capture_s": capture_s, "wall_s_timed": wall},
-                "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                             "frac": achieved / peak, "traffic": None,
-                             "peak_source": "measured: ttg_measure_fp64_peak (DFMA chains on every SM)"},
-                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 2 * args.steps, "clocks": clk.summary(),
-                "factor_error": err}
+                "vs_baseline": None, "dtype": "bf16",
+                "data": "synthetic: A = G*G^T/N + alpha*I, G quantised N(0,1) (Philox-4x32-10, seed %d); B iid N(0,1)" % args.seed,
+                "config": {"workload": "tiled Cholesky + solve, mixed precision (BF16 tensor-core updates, FP32 TRSM, FP64 "
+                                       "diagonal POTRF) + GMRES-IR to backward error <= %g" % args.tol,
+                           "matrix_size": N, "block_size": args.block, "nrhs": nrhs, "alpha": args.alpha, "tasks": n_tasks,
+                           "l2": "inputs larger than L2 (%.1f GB of FP64 tiles)" % (elems * 8 / 1e9), "capture_s": capture_s,
+                           "wall_s_timed": wall},
+                "solves_per_s": world * nrhs / (step_ms * 1e-3),
+                "bwd_err": last.bwd_err, "refinement": {"outer": last.outer, "inner": last.inner, "gmres_prec": last.gmres_prec,
+                                                          "remedy": last.remedy, "factor_ms": last.factor_ms},
+                "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
+                             "frac": achieved / bf16_peak, "traffic": None,
+                             "kernel": "exec_kernel_mixed (one launch per factorisation); achieved = N^3/3 / its duration",
+                             "peak_source": "measured: MEASURED_PEAKS.json bf16_tflops (burst)"},
+                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": None, "clocks": clk.summary()}
+        line.update(extra)
         print(json.dumps(line))
-    plan.close()
     ctx.close()
 
 
@@ -262,14 +323,16 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=32768)
     ap.add_argument("--block", type=int, default=512)
-    ap.add_argument("--alpha", type=float, default=1.0)
+    ap.add_argument("--alpha", type=float, default=1e-4)
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--kind", type=int, default=2)
     ap.add_argument("--cpu-n", dest="cpu_n", type=int, default=16384)
     ap.add_argument("--cpu-b", dest="cpu_b", type=int, default=512)
     ap.add_argument("--no-e2e", dest="no_e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", dest="no_cpu_baseline", action="store_true")
-    ap.add_argument("--check", action="store_true")
+    ap.add_argument("--nrhs", type=int, default=16)
+    ap.add_argument("--tol", type=float, default=1e-14)
+    ap.add_argument("--quick", action="store_true", help="skip the FP64 and per-alpha comparison runs")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

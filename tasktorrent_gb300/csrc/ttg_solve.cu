@@ -264,7 +264,10 @@ ttg_status backward_errors(ttg_solver* S, int nrhs, cudaStream_t s, std::vector<
     if ((st = colreduce<double>(S, S->R.p, nullptr, nrhs, 1, rnorm.data(), s)) != TTG_OK) return st;
     if ((st = colreduce<double>(S, S->X.p, nullptr, nrhs, 1, xn.data(), s)) != TTG_OK) return st;
     be.assign(nrhs, 0.0);
-    for (int q = 0; q < nrhs; ++q) be[q] = xn[q] > 0 ? rnorm[q] / (S->anorm_inf * xn[q]) : (rnorm[q] > 0 ? INFINITY : 0.0);
+    for (int q = 0; q < nrhs; ++q) {
+        be[q] = xn[q] > 0 ? rnorm[q] / (S->anorm_inf * xn[q]) : (rnorm[q] > 0 ? INFINITY : 0.0);
+        if (!(be[q] == be[q])) be[q] = INFINITY;  // NaN never counts as converged
+    }
     return TTG_OK;
 }
 

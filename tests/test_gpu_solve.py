@@ -85,3 +85,30 @@ def test_follow_up_rhs_reuse_factor(ctx):
     assert st == t.TTG_OK and rep2.factor_ms == 0.0
     assert bwd_err(A, X2, B2) <= 2 * BWD
     p.close()
+
+
+@pytest.mark.parametrize("nrhs", [3, 16])
+def test_device_pointer_solve_matches_host_path(ctx, nrhs):
+    """ttg_chol_plan_solve on device buffers owned by the caller (here torch
+    tensors) gives the host path's solution."""
+    import ctypes
+    import torch
+    p = t.CholPlan(ctx, 64, 6, matrix=1, alpha=1e-4, seed=3, precision=t.PREC_MIXED, mixed_kind=1)
+    A = p.input_A()
+    B = rhs(p.N, nrhs, seed=5)
+    st, rep, Xh = p.solve_host(B)
+    assert st == t.TTG_OK
+    dB = torch.from_numpy(np.ascontiguousarray(B.T)).cuda()
+    dX = torch.zeros_like(dB)
+    torch.cuda.synchronize()
+    o = t.SolveOpts(nrhs, BWD, 10, 20, 0, 0.0)
+    r = t.SolveReport()
+    st = t.lib().ttg_chol_plan_solve(p.h, ctypes.c_void_p(dB.data_ptr()), ctypes.c_void_p(dX.data_ptr()), ctypes.byref(o),
+                                     ctypes.byref(r), None)
+    torch.cuda.synchronize()
+    assert st == t.TTG_OK, r.as_dict()
+    Xd = np.asfortranarray(dX.cpu().numpy().T)
+    assert np.isfinite(Xd).all()
+    assert bwd_err(A, Xd, B) <= 2 * BWD
+    assert np.linalg.norm(Xd - Xh) <= 1e-10 * np.linalg.norm(Xh)
+    p.close()
