@@ -3,13 +3,18 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Workload (one step): the FP64 tiled Cholesky factorisation of
-A = G·Gᵀ/N + αI (N = 32768, tile 512, 45,760 tasks, α = 1, seed 2), run as one
-persistent-kernel launch of the task graph captured from the Taskflow<K>
-drop-in.  Inputs (4.3 GB of packed lower tiles) are resident in HBM and
-larger than L2; each step first restores the tiles (outside the timed
-interval).  `value` is N³/3 / step time.  `e2e` runs the same step through the
-C ABI with pinned host buffers (tiles in, factor out) and counts the copies.
+Workload (one step): solve A X = B to backward error ≤ 1e-14 per column with
+A = G·Gᵀ/N + αI (N = 32768, tile 512, 45,760 tasks, α = 1e-4, seed 2) and 16
+right-hand sides, through ttg_chol_posv: the mixed-precision tiled Cholesky
+(BF16 trailing updates on the tensor cores, FP32 TRSM, FP64 diagonal POTRF;
+one persistent-kernel launch of the task graph captured from the Taskflow<K>
+drop-in) followed by GMRES-based iterative refinement with FP64 residuals.
+Inputs (4.4 GB of FP64 lower tiles) are resident in HBM and larger than L2.
+`value` is N³/3 / time to solution (effective Cholesky TFLOP/s); solves/s is
+reported beside it.  `e2e` runs the same step through the C ABI with pinned
+host buffers (tiles and B in, X out).  The plain FP64 device path on the same
+input, the three conditionings α ∈ {1, 1e-4, 1e-8}, and the forward error of
+the mixed solution against the FP64 one are reported in the same line.
 
 With torchrun (N > 1 GPUs) every rank factorises its own matrix ("replicas
 only": the path has no exchange step) and `value` sums the ranks' work over
@@ -170,29 +175,22 @@ def run_ours(args, world, rank, local):
     torch.cuda.synchronize()
 
     def opts():
-        return t.SolveOpts(nrhs, args.tol, 30, 30, 0, 0.0)
+        return t.SolveOpts(nrhs, args.tol, 12, 30, 0, 0.0)
 
-    def posv(plan, restore=True):
-        """One time-to-solution step on the resident input: factor + solve.
-        The restore of the in-place factorisation's input is outside the timed
-        interval; returns (ms, report)."""
-        if restore:
-            t.check(lib.ttg_chol_plan_restore(plan.h, None), "restore")
+    def posv(plan):
+        """One time-to-solution step through ttg_chol_posv on the resident
+        input: restore the in-place input tiles (one device copy), factor,
+        solve and refine.  Returns (ms, report)."""
         rep = t.SolveReport()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record()
-        fr = t.Report()
-        st = lib.ttg_chol_plan_factor(plan.h, None, ctypes.byref(fr))
-        if st != t.TTG_OK:
-            raise RuntimeError("factor failed: %s" % t.strerror(st))
-        st = lib.ttg_chol_plan_solve(plan.h, ctypes.c_void_p(B.data_ptr()), ctypes.c_void_p(X.data_ptr()),
-                                     ctypes.byref(opts()), ctypes.byref(rep), None)
+        st = lib.ttg_chol_posv(plan.h, ctypes.c_void_p(B.data_ptr()), ctypes.c_void_p(X.data_ptr()), ctypes.byref(opts()),
+                               ctypes.byref(rep), None)
         e1.record()
         torch.cuda.synchronize()
         if st != t.TTG_OK:
-            raise RuntimeError("solve failed: %s (%s)" % (t.strerror(st), rep.as_dict()))
-        rep.factor_ms = fr.elapsed_ms
+            raise RuntimeError("posv failed: %s (%s)" % (t.strerror(st), rep.as_dict()))
         return e0.elapsed_time(e1), rep
 
     # Headline: mixed precision (BF16 tensor-core updates) + GMRES-IR at alpha.

@@ -384,7 +384,15 @@ extern "C" ttg_status ttg_chol_plan_restore(ttg_chol_plan* P, void* stream) {
     return TTG_OK;
 }
 
+static ttg_status chol_factor_from(ttg_chol_plan* P, void* stream, ttg_report* rep, size_t first_attempt);
+
 extern "C" ttg_status ttg_chol_plan_factor(ttg_chol_plan* P, void* stream, ttg_report* rep) {
+    return chol_factor_from(P, stream, rep, 0);
+}
+
+// Factorisation starting at attempt `first_attempt` of the mixed chain
+// (0 BF16, 1 BF16 + shift, 2 FP32 updates).
+static ttg_status chol_factor_from(ttg_chol_plan* P, void* stream, ttg_report* rep, size_t first_attempt) {
     if (!P) return TTG_EINVAL;
     TTG_CUDA_CHECK(cudaSetDevice(P->ctx->device));
     if (!P->mixed) {
@@ -415,8 +423,8 @@ extern "C" ttg_status ttg_chol_plan_factor(ttg_chol_plan* P, void* stream, ttg_r
     }
     ttg_status s = TTG_OK;
     float total_ms = 0.f;
-    for (size_t a = 0; a < plan.size(); ++a) {
-        if (a > 0) {
+    for (size_t a = std::min(first_attempt, plan.size() - 1); a < plan.size(); ++a) {
+        if (a > first_attempt) {
             s = ttg_chol_plan_restore(P, stream);
             if (s != TTG_OK) return s;
         }
@@ -537,14 +545,38 @@ extern "C" ttg_status ttg_chol_plan_solve(ttg_chol_plan* P, const double* d_B, d
 
 extern "C" ttg_status ttg_chol_posv(ttg_chol_plan* P, const double* d_B, double* d_X, const ttg_solve_opts* o,
                                    ttg_solve_report* rep, void* stream) {
-    if (!P) return TTG_EINVAL;
+    if (!P || !o) return TTG_EINVAL;
     ttg_status st = ttg_chol_plan_restore(P, stream);
     if (st != TTG_OK) return st;
     ttg_report fr{};
     st = ttg_chol_plan_factor(P, stream, &fr);
     if (st != TTG_OK) return st;
-    st = ttg_chol_plan_solve(P, d_B, d_X, o, rep, stream);
-    if (rep) rep->factor_ms = fr.elapsed_ms;
+    float factor_ms = fr.elapsed_ms;
+    double solve_ms = 0.0;
+    if (P->mixed && P->remedy == 1) {
+        // A shifted factor is a weaker preconditioner: give refinement a few
+        // steps, and if it stalls refactor with FP32 updates and start over.
+        ttg_solve_opts quick = *o;
+        quick.max_outer = std::min(o->max_outer > 0 ? o->max_outer : 10, 3);
+        ttg_solve_report r1{};
+        st = ttg_chol_plan_solve(P, d_B, d_X, &quick, &r1, stream);
+        solve_ms += r1.solve_ms;
+        if (st != TTG_ENOCONV) {
+            r1.factor_ms = factor_ms;
+            if (rep) *rep = r1;
+            return st;
+        }
+        st = ttg_chol_plan_restore(P, stream);
+        if (st != TTG_OK) return st;
+        st = chol_factor_from(P, stream, &fr, 2);
+        if (st != TTG_OK) return st;
+        factor_ms += fr.elapsed_ms;
+    }
+    ttg_solve_report r{};
+    st = ttg_chol_plan_solve(P, d_B, d_X, o, &r, stream);
+    r.factor_ms = factor_ms;
+    r.solve_ms += solve_ms;
+    if (rep) *rep = r;
     return st;
 }
 

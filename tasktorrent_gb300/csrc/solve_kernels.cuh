@@ -255,6 +255,9 @@ __global__ void reduce_partials(int N, int nrhs, const T* P, int splits, const T
     }
 }
 
+// max that propagates NaN (fmax would drop it and hide a broken column).
+__device__ __forceinline__ double nanmax(double a, double b) { return (a != a || b != b) ? __longlong_as_double(0x7ff8000000000000LL) : fmax(a, b); }
+
 // Per-column reductions over N × nrhs blocks.  kind 0: dot(X, Y); 1: max|X|.
 // Partials per block, then a fixed-order final pass (deterministic).
 template <class T>
@@ -265,12 +268,12 @@ __global__ void column_reduce_partial(int N, int nrhs, const T* X, const T* Y, i
         for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < N; r += (int64_t)gridDim.x * blockDim.x) {
             const double x = (double)X[r + (size_t)q * N];
             if (kind == 0) acc += x * (double)Y[r + (size_t)q * N];
-            else acc = fmax(acc, fabs(x));
+            else acc = nanmax(acc, fabs(x));
         }
         red[threadIdx.x] = acc;
         __syncthreads();
         for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-            if (threadIdx.x < s) red[threadIdx.x] = kind == 0 ? red[threadIdx.x] + red[threadIdx.x + s] : fmax(red[threadIdx.x], red[threadIdx.x + s]);
+            if (threadIdx.x < s) red[threadIdx.x] = kind == 0 ? red[threadIdx.x] + red[threadIdx.x + s] : nanmax(red[threadIdx.x], red[threadIdx.x + s]);
             __syncthreads();
         }
         if (threadIdx.x == 0) part[(size_t)q * gridDim.x + blockIdx.x] = red[0];
@@ -282,7 +285,7 @@ __global__ void column_reduce_final(int nrhs, int nparts, const double* part, in
     const int q = threadIdx.x;
     if (q >= nrhs) return;
     double acc = 0.0;
-    for (int p = 0; p < nparts; ++p) acc = kind == 0 ? acc + part[(size_t)q * nparts + p] : fmax(acc, part[(size_t)q * nparts + p]);
+    for (int p = 0; p < nparts; ++p) acc = kind == 0 ? acc + part[(size_t)q * nparts + p] : nanmax(acc, part[(size_t)q * nparts + p]);
     out[q] = acc;
 }
 

@@ -48,6 +48,7 @@ struct DevBuf {
             ttg_set_last_cuda_error(e, "cudaMalloc (solve)", __FILE__, __LINE__);
             return TTG_ENOMEM;
         }
+        cudaMemset(p, 0, sizeof(T) * std::max<size_t>(1, count));  // no stale NaN patterns
         n = count;
         return TTG_OK;
     }
@@ -371,8 +372,7 @@ ttg_status gmres_cycle(ttg_solver* S, const float* L32, int nrhs, int m, double 
             for (int j = i + 1; j < k; ++j) v -= h(q, i, j) * y[(size_t)q * k + j];
             y[(size_t)q * k + i] = h(q, i, i) != 0 ? v / h(q, i, i) : 0.0;
         }
-    std::vector<double> zero(nrhs, 0.0);
-    if ((st = axpby<double, double>(S, zero, S->D.p, nullptr, S->D.p, nrhs, s)) != TTG_OK) return st;
+    TTG_CUDA_CHECK(cudaMemsetAsync(S->D.p, 0, sizeof(double) * blk, s));
     for (int j = 0; j < k; ++j) {
         std::vector<double> c(nrhs);
         for (int q = 0; q < nrhs; ++q) c[q] = y[(size_t)q * k + j] * rn[q];
