@@ -534,6 +534,11 @@ extern "C" ttg_status ttg_chol_plan_solve(ttg_chol_plan* P, const double* d_B, d
         ttg_status st = ttg_solver_factor_done(P->solver, P->tiles, L32, s);
         if (st != TTG_OK) return st;
         P->solver_gen = P->factor_gen;
+        if (getenv("TTG_SOLVE_VERBOSE")) {
+            cudaStreamSynchronize(s);
+            fprintf(stderr, "[ttg solve] %-28s %9.3f ms\n", "invert diagonal tiles",
+                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
+        }
     }
     ttg_solve_report r{};
     ttg_status st = ttg_solver_solve(P->solver, P->pristine, P->tiles, L32, d_B, d_X, o, &r, s);

@@ -20,6 +20,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -384,8 +385,32 @@ ttg_status gmres_cycle(ttg_solver* S, const float* L32, int nrhs, int m, double 
 
 }  // namespace
 
+// TTG_SOLVE_VERBOSE=1 prints the time of each phase (host clock, after a
+// stream synchronisation).
+static bool solve_verbose() {
+    static const bool v = getenv("TTG_SOLVE_VERBOSE") && atoi(getenv("TTG_SOLVE_VERBOSE")) > 0;
+    return v;
+}
+
+namespace {
+struct PhaseClock {
+    cudaStream_t s;
+    bool on;
+    std::chrono::steady_clock::time_point t;
+    PhaseClock(cudaStream_t s_, bool on_) : s(s_), on(on_), t(std::chrono::steady_clock::now()) {}
+    void mark(const char* what) {
+        if (!on) return;
+        cudaStreamSynchronize(s);
+        const auto n = std::chrono::steady_clock::now();
+        fprintf(stderr, "[ttg solve] %-28s %9.3f ms\n", what, std::chrono::duration<double, std::milli>(n - t).count());
+        t = n;
+    }
+};
+}  // namespace
+
 ttg_status ttg_solver_solve(ttg_solver* S, const double* pristine, const double* L64, const float* L32, const double* d_B,
                             double* d_X, const ttg_solve_opts* o, ttg_solve_report* rep, cudaStream_t s) {
+    PhaseClock clk(s, solve_verbose());
     const int nrhs = o->nrhs;
     if (nrhs < 1 || nrhs > kMaxRhs || !d_B || !d_X) return TTG_EINVAL;
     TTG_CUDA_CHECK(cudaSetDevice(S->ctx->device));
@@ -399,7 +424,9 @@ ttg_status ttg_solver_solve(ttg_solver* S, const double* pristine, const double*
     if ((st = S->part.ensure(128 * kMaxRhs)) != TTG_OK || (st = S->colv.ensure(kMaxRhs)) != TTG_OK ||
         (st = S->coefA.ensure(kMaxRhs)) != TTG_OK || (st = S->coefB.ensure(kMaxRhs)) != TTG_OK)
         return st;
+    clk.mark("buffers");
     if ((st = ensure_dense(S, pristine, s)) != TTG_OK) return st;
+    clk.mark("dense copies of A");
     TTG_CUDA_CHECK(cudaMemcpyAsync(S->B.p, d_B, sizeof(double) * blk, cudaMemcpyDeviceToDevice, s));
     const double tol = o->tol > 0 ? o->tol : 1e-14;
     const int max_outer = o->max_outer > 0 ? o->max_outer : 10;
@@ -412,7 +439,9 @@ ttg_status ttg_solver_solve(ttg_solver* S, const double* pristine, const double*
         TTG_CUDA_CHECK(cudaMemcpyAsync(S->R.p, S->B.p, sizeof(double) * blk, cudaMemcpyDeviceToDevice, s));
         if ((st = sweeps<double, double>(S, L64, S->inv64.p, S->R.p, S->T1.p, S->X.p, nrhs, S->sweep_grid64, s)) != TTG_OK)
             return st;
+        clk.mark("FP64 sweeps");
         if ((st = backward_errors(S, nrhs, s, be, rn)) != TTG_OK) return st;
+        clk.mark("FP64 residual");
         r.gmres_prec = 64;
     } else {
         // x0 = M⁻¹ b (FP32 sweeps).
@@ -421,12 +450,15 @@ ttg_status ttg_solver_solve(ttg_solver* S, const double* pristine, const double*
         if ((st = sweeps<float, float>(S, L32, S->inv32.p, S->f1.p, S->f2.p, S->f3.p, nrhs, S->sweep_grid32, s)) != TTG_OK)
             return st;
         if ((st = axpby<float, double>(S, one, S->f3.p, nullptr, S->X.p, nrhs, s)) != TTG_OK) return st;
+        clk.mark("x0 = M^-1 b (FP32 sweeps)");
         int prec = o->gmres_prec == 64 ? 64 : 32;
         double prev = INFINITY;
         const double inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-6;
         for (int outer = 0;; ++outer) {
             if ((st = backward_errors(S, nrhs, s, be, rn)) != TTG_OK) return st;
             const double worst = *std::max_element(be.begin(), be.end());
+            clk.mark("FP64 residual");
+            if (solve_verbose()) fprintf(stderr, "[ttg solve] outer %d backward error %.3e\n", outer, worst);
             if (worst <= tol) break;
             if (outer >= max_outer) {
                 r.status = TTG_ENOCONV;
@@ -439,6 +471,8 @@ ttg_status ttg_solver_solve(ttg_solver* S, const double* pristine, const double*
             st = prec == 32 ? gmres_cycle<float>(S, L32, nrhs, m, prec == 32 ? std::max(inner_tol, 1e-6) : inner_tol, s, &it)
                             : gmres_cycle<double>(S, L32, nrhs, m, inner_tol, s, &it);
             if (st != TTG_OK) return st;
+            if (solve_verbose()) fprintf(stderr, "[ttg solve] GMRES(FP%d) %d iterations\n", prec, it);
+            clk.mark("GMRES cycle");
             r.inner += it;
             r.outer = outer + 1;
             std::vector<double> ones(nrhs, 1.0);
