@@ -24,6 +24,8 @@
 namespace ttg {
 
 constexpr int kMaxLevels = 32;
+// Counter words per team task (the POTRF tasks shared by several blocks).
+constexpr int kTeamStride = 256;
 
 struct ExecParams {
     const ttg_op* ops;
@@ -55,6 +57,8 @@ struct ExecParams {
     int* err_info;
     long long* trace;       // [3 * n_tasks] start, end, worker; or null
     long long timeout_ns;
+    int* team_ctr;          // kTeamStride words per team task, zero at launch; or null
+    const int* team_slot;   // per task: its team counter block, -1 if none; or null
 };
 
 __device__ __forceinline__ long long globaltimer() {
@@ -215,9 +219,9 @@ __device__ inline void fulfil_successors(const ExecParams& p, int t) {
     }
 }
 
-// The persistent kernel body: `RunOp(op, part, parts, smem)` runs one part
-// of a tile task on the whole block and returns 0 or an error info (POTRF
-// failing column).  The block that finishes the last part of a task fulfils
+// The persistent kernel body: `RunOp(op, part, parts, smem, team)` runs one
+// part of a tile task on the whole block and returns 0 or an error info (POTRF
+// failing column); team is the task's team counter block or null.  The block that finishes the last part of a task fulfils
 // its successors.
 template <class RunOp>
 __device__ void executor_loop(const ExecParams& p, double* smem, RunOp run_op) {
@@ -239,7 +243,12 @@ __device__ void executor_loop(const ExecParams& p, double* smem, RunOp run_op) {
         if (t < 0) break;
         const ttg_op op = p.ops[t];
         const int nparts = p.parts[t];
-        const int info = run_op(op, s_part, nparts, smem);
+        int* team = nullptr;
+        if (p.team_slot) {
+            const int slot = p.team_slot[t];
+            if (slot >= 0) team = p.team_ctr + (size_t)slot * kTeamStride;
+        }
+        const int info = run_op(op, s_part, nparts, smem, team);
         __syncthreads();
         if (threadIdx.x == 0) {
             s_info = info;

@@ -5,7 +5,6 @@
 // (i,j) at off[i + j*nb], column-major, ld = bs[i]); block vectors X are
 // N × nrhs column-major (ld = N); the dense copy of A is N × N column-major.
 #pragma once
-#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -13,8 +12,6 @@
 
 namespace ttg {
 namespace solve {
-
-namespace cg = cooperative_groups;
 
 constexpr int kMaxRhs = 16;
 constexpr int kRows = 32;  // output rows per work item of the sweeps
@@ -27,159 +24,263 @@ struct TileLayout {
     int N;
 };
 
-// Y[rows] = M · V, M row-major access through column-major storage: thread per
-// output row, loop over columns (coalesced for column-major M).  M is m×k
-// with leading dimension ldm; V is k×nrhs (ldv); Y is m×nrhs (ldy).
-// Mode: 0 store, 1 subtract (Y -= M V).
+// ------------------------------------------------------------------------
+// Block triangular sweeps as a dataflow over row strips.
+//
+// Forward (L Y = R): for block rows i = 0..nb-1 in turn, Y_i = L_ii⁻¹ R_i
+// (the "diagonal" items, one per 64-row strip of block row i), then
+// R_k -= L_ki Y_i for every k > i (the "update" items, one per strip of each
+// block row k).  Backward (Lᵀ X = Y) runs i = nb-1..0 with X_i = L_ii⁻ᵀ Y_i
+// and Y_j -= L_ijᵀ X_i for j < i.  Every item is the same operation
+//     out[strip] (=, or -=) M[strip rows, 0:kc] · V[0:kc, 0:nrhs]
+// on a column-major operand: L_ii⁻¹ (forward diagonal), L_ki (forward
+// update), L_ii⁻ᵀ (backward diagonal) and the transposed off-diagonal tiles
+// L_ijᵀ (backward update), so every operand is read with coalesced column
+// segments.
+//
+// Items are claimed in processing order (step by step, diagonal items first)
+// from one counter, and each waits for exactly what it reads: a diagonal item
+// of step s for every strip of its block row to have received s updates, an
+// update item for the step's diagonal items and for its own strip to have
+// received the s earlier updates.  Everything an item waits for was claimed
+// before it by a block that is running, so the sweep cannot deadlock, needs no
+// grid-wide barrier and no co-residency guarantee, and applies the updates of
+// every strip in step order (the result is deterministic).  Waits are bounded.
+constexpr int kStrip = 64;    // output rows per item
+constexpr int kChunk = 512;   // operand columns staged per pass
+
+struct SweepArgs {
+    const int64_t* off;        // packed tile offsets [nb*nb]
+    const int64_t* doff;       // compact diagonal tile offsets [nb]
+    const int* bs;             // [nb]
+    const int* displ;          // [nb+1]
+    const int* strip_pre;      // [nb+1] strips before each block row
+    const int* step_start;     // [nb+1] items before each step
+    int nb, N, nrhs, backward;
+    int* applied;              // per strip: updates applied
+    int* ready;                // per block row: diagonal strips done
+    int* claim;                // item counter
+    int* err;                  // nonzero after a timeout
+    long long timeout_ns;
+};
+
+__device__ __forceinline__ long long sweep_clock() {
+    long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// out[0:rows, q] (mode 0: =, 1: -=) Σ_c M[r + c·ldm] · V[c + q·ldv], rows <=
+// kStrip, on the whole block (256 threads).  Warp w takes columns w, w+8, ...
+// of each staged chunk, lane l rows 2l and 2l+1; the eight warp partials are
+// added in warp order.  smem: kChunk·kMaxRhs T.
 template <class T, class TM>
-__device__ void gemv_n_rows(int r0, int r1, int k, const TM* M, int ldm, const T* V, int ldv, T* Y, int ldy, int nrhs,
-                            int mode, T* sV) {
-    // Stage V (k × nrhs) through shared memory in chunks of 256 rows.
-    for (int c0 = 0; c0 < k; c0 += 256) {
-        const int kc = min(256, k - c0);
+__device__ void strip_gemv(int rows, int kc, const TM* __restrict__ M, int ldm, const T* V, int ldv, int nrhs, T* out,
+                           int ldo, int mode, T* smem) {
+    constexpr int U = 8;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int ra = 2 * lane, rb = 2 * lane + 1;
+    const bool oka = ra < rows, okb = rb < rows;
+    T acc0[kMaxRhs], acc1[kMaxRhs];
+#pragma unroll
+    for (int q = 0; q < kMaxRhs; ++q) acc0[q] = acc1[q] = T(0);
+    for (int c0 = 0; c0 < kc; c0 += kChunk) {
+        const int kcc = min(kChunk, kc - c0);
         __syncthreads();
-        for (int e = threadIdx.x; e < kc * nrhs; e += blockDim.x) {
-            const int c = e % kc, q = e / kc;
-            sV[c + q * 256] = ldcg(V + (c0 + c) + (size_t)q * ldv);
+        for (int e = threadIdx.x; e < kcc * kMaxRhs; e += blockDim.x) {
+            const int c = e % kcc, q = e / kcc;
+            smem[c * kMaxRhs + q] = q < nrhs ? ldcg(V + (c0 + c) + (size_t)q * ldv) : T(0);
         }
         __syncthreads();
-        for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-            T acc[kMaxRhs];
+        const TM* Mc = M + (size_t)c0 * ldm;
+        for (int cb = warp; cb < kcc; cb += 8 * U) {
+            TM ma[U], mb[U];
 #pragma unroll
-            for (int q = 0; q < kMaxRhs; ++q) acc[q] = T(0);
-            for (int c = 0; c < kc; ++c) {
-                const T m = (T)ldcg(M + r + (size_t)(c0 + c) * ldm);
-#pragma unroll
-                for (int q = 0; q < kMaxRhs; ++q)
-                    if (q < nrhs) acc[q] = fma(m, sV[c + q * 256], acc[q]);
+            for (int u = 0; u < U; ++u) {
+                const int c = cb + 8 * u;
+                ma[u] = (c < kcc && oka) ? Mc[ra + (size_t)c * ldm] : TM(0);
+                mb[u] = (c < kcc && okb) ? Mc[rb + (size_t)c * ldm] : TM(0);
             }
 #pragma unroll
-            for (int q = 0; q < kMaxRhs; ++q) {
-                if (q >= nrhs) break;
-                T* y = Y + r + (size_t)q * ldy;
-                if (mode == 0) *y = (c0 == 0) ? acc[q] : ldcg(y) + acc[q];
-                else *y = ldcg(y) - acc[q];
+            for (int u = 0; u < U; ++u) {
+                const int c = cb + 8 * u;
+                if (c < kcc) {
+                    const T* v = smem + c * kMaxRhs;
+                    const T a = (T)ma[u], b = (T)mb[u];
+#pragma unroll
+                    for (int q = 0; q < kMaxRhs; ++q) {
+                        const T vq = v[q];
+                        acc0[q] = fma(a, vq, acc0[q]);
+                        acc1[q] = fma(b, vq, acc1[q]);
+                    }
+                }
             }
+        }
+    }
+    // Warp partials: smem[(w·kMaxRhs + q)·kStrip + r].
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < kMaxRhs; ++q) {
+        smem[(warp * kMaxRhs + q) * kStrip + ra] = acc0[q];
+        smem[(warp * kMaxRhs + q) * kStrip + rb] = acc1[q];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < kStrip * nrhs; e += blockDim.x) {
+        const int r = e % kStrip, q = e / kStrip;
+        if (r >= rows) continue;
+        T sum = T(0);
+#pragma unroll
+        for (int w = 0; w < 8; ++w) sum += smem[(w * kMaxRhs + q) * kStrip + r];
+        T* o = out + r + (size_t)q * ldo;
+        *o = mode == 0 ? sum : ldcg(o) - sum;
+    }
+}
+
+// Largest idx with tab[idx] <= v (tab ascending, tab[0] = 0 <= v).
+__device__ __forceinline__ int upper_index(const int* tab, int n, int v) {
+    int lo = 0, hi = n;  // tab[lo] <= v < tab[hi] (tab[n] > v)
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (tab[mid] <= v) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// One sweep.  Forward: Vin = R (updated in place), Vout = Y, Mu = the factor
+// tiles, Md = L_ii⁻¹ (compact diagonal).  Backward: Vin = Y (updated in
+// place), Vout = X, Mu = the transposed tiles (L_ijᵀ at off[i + j·nb], ld
+// bs[j]), Md = L_ii⁻ᵀ.
+template <class T, class TM>
+__global__ void __launch_bounds__(256) sweep_kernel(SweepArgs a, const TM* __restrict__ Mu, const TM* __restrict__ Md, T* Vin,
+                                                    T* Vout) {
+    extern __shared__ __align__(16) unsigned char sweep_smem[];
+    T* smem = reinterpret_cast<T*>(sweep_smem);
+    __shared__ int s_item, s_abort;
+    const int nb = a.nb, N = a.N;
+    const int total = a.step_start[nb];
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_item = atomicAdd(a.claim, 1);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= total) break;
+        const int s = upper_index(a.step_start, nb, it);
+        const int i = a.backward ? nb - 1 - s : s;
+        int u = it - a.step_start[s];
+        const int Si = a.strip_pre[i + 1] - a.strip_pre[i];
+        const bool diag = u < Si;
+        int k, g;  // target block row and its global strip
+        if (diag) {
+            k = i;
+            g = a.strip_pre[i] + u;
+        } else {
+            u -= Si;
+            g = a.backward ? u : a.strip_pre[i + 1] + u;
+            k = upper_index(a.strip_pre, nb, g);
+        }
+        // Wait for the inputs of this item.
+        if (threadIdx.x == 0) {
+            int abort = 0;
+            const long long t0 = sweep_clock();
+            unsigned spin = 0;
+            for (;;) {
+                bool ok;
+                if (diag) {
+                    ok = true;
+                    for (int h = a.strip_pre[i]; h < a.strip_pre[i + 1] && ok; ++h)
+                        ok = *(const volatile int*)(a.applied + h) >= s;
+                } else {
+                    ok = *(const volatile int*)(a.ready + i) >= Si && *(const volatile int*)(a.applied + g) >= s;
+                }
+                if (ok) break;
+                if ((++spin & 63) == 0) {
+                    if (*(const volatile int*)a.err) {
+                        abort = 1;
+                        break;
+                    }
+                    if (sweep_clock() - t0 > a.timeout_ns) {
+                        atomicCAS(a.err, 0, 1);
+                        abort = 1;
+                        break;
+                    }
+                }
+                __nanosleep(32);
+            }
+            __threadfence();
+            s_abort = abort;
+        }
+        __syncthreads();
+        if (s_abort) break;
+        const int bk = a.bs[k], bi = a.bs[i];
+        const int r0 = (g - a.strip_pre[k]) * kStrip;
+        const int rows = min(kStrip, bk - r0);
+        if (diag) {
+            strip_gemv<T, TM>(rows, bi, Md + a.doff[i] + r0, bi, Vin + a.displ[i], N, a.nrhs, Vout + a.displ[i] + r0, N, 0,
+                              smem);
+        } else {
+            const int64_t o = a.backward ? a.off[i + (size_t)k * nb] : a.off[k + (size_t)i * nb];
+            strip_gemv<T, TM>(rows, bi, Mu + o + r0, bk, Vout + a.displ[i], N, a.nrhs, Vin + a.displ[k] + r0, N, 1, smem);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            if (diag) atomicAdd(a.ready + i, 1);
+            else atomicExch(a.applied + g, s + 1);
         }
     }
 }
 
-// Y[rows] (op) Mᵀ · V: output row r is column r of M (contiguous): warp per
-// output row, lanes over the column, shuffle reduction.  M is k×m (ldm).
-template <class T, class TM>
-__device__ void gemv_t_rows(int r0, int r1, int k, const TM* M, int ldm, const T* V, int ldv, T* Y, int ldy, int nrhs, int mode) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int r = r0 + warp; r < r1; r += nw) {
-        T acc[kMaxRhs];
-#pragma unroll
-        for (int q = 0; q < kMaxRhs; ++q) acc[q] = T(0);
-        const TM* col = M + (size_t)r * ldm;
-        for (int c = lane; c < k; c += 32) {
-            const T m = (T)ldcg(col + c);
-#pragma unroll
-            for (int q = 0; q < kMaxRhs; ++q)
-                if (q < nrhs) acc[q] = fma(m, ldcg(V + c + (size_t)q * ldv), acc[q]);
-        }
-#pragma unroll
-        for (int q = 0; q < kMaxRhs; ++q) {
-            T v = acc[q];
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            acc[q] = v;
-        }
-        if (lane < nrhs) {
-            T v = acc[0];
-#pragma unroll
-            for (int q = 1; q < kMaxRhs; ++q)
-                if (q == lane) v = acc[q];
-            T* y = Y + r + (size_t)lane * ldy;
-            *y = mode == 0 ? v : ldcg(y) - v;
-        }
-    }
-}
+// Transposes of tiles: dst[doff_t + c + r·rows_t] = src[soff_t + r + c·rows_t]
+// for the tiles of a descriptor list (rows × cols each, column-major source
+// with ld rows, column-major destination with ld cols).  Block = 32×8
+// threads over 32×32 sub-tiles; sub_pre[t] = sub-tiles before tile t.
+struct TransposeDesc {
+    int64_t src, dst;
+    int rows, cols;
+};
 
-// Forward sweep L Y = R (R is overwritten as scratch), with the transposed
-// inverses of the diagonal tiles (invT: tile j at off[j + j*nb], ld = bs[j],
-// holding L_jj^-T column-major).  One cooperative launch; grid syncs between
-// the diagonal apply and the updates of each block row.
-template <class T, class TM>
-__global__ void sweep_forward(TileLayout lay, const TM* L, const TM* invT, T* R, T* Y, int nrhs) {
-    cg::grid_group grid = cg::this_grid();
-    __shared__ T sV[256 * kMaxRhs];
-    const int N = lay.N;
-    for (int i = 0; i < lay.nb; ++i) {
-        const int bi = lay.bs[i], di = lay.displ[i];
-        // Y_i = L_ii^-1 R_i = (invT)^T R_i: output row r is column r of invT.
-        const TM* Ti = invT + lay.off[i + (size_t)i * lay.nb];
-        const int items = (bi + kRows - 1) / kRows;
-        for (int it = blockIdx.x; it < items; it += gridDim.x) {
-            const int r0 = it * kRows, r1 = min(bi, r0 + kRows);
-            gemv_t_rows<T, TM>(r0, r1, bi, Ti, bi, R + di, N, Y + di, N, nrhs, 0);
+template <class TM>
+__global__ void transpose_tiles(const TransposeDesc* __restrict__ d, const int64_t* __restrict__ sub_pre, int n_desc,
+                                const TM* __restrict__ src, TM* __restrict__ dst) {
+    __shared__ TM t[32][33];
+    const int64_t total = sub_pre[n_desc];
+    for (int64_t b = blockIdx.x; b < total; b += gridDim.x) {
+        int lo = 0, hi = n_desc;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (sub_pre[mid] <= b) lo = mid;
+            else hi = mid;
         }
-        grid.sync();
-        // R_k -= L_ki Y_i for k > i.
-        long total = 0;
-        for (int k = i + 1; k < lay.nb; ++k) total += (lay.bs[k] + kRows - 1) / kRows;
-        for (long it = blockIdx.x; it < total; it += gridDim.x) {
-            long rem = it;
-            int k = i + 1;
-            while (rem >= (lay.bs[k] + kRows - 1) / kRows) {
-                rem -= (lay.bs[k] + kRows - 1) / kRows;
-                ++k;
-            }
-            const int bk = lay.bs[k];
-            const int r0 = (int)rem * kRows, r1 = min(bk, r0 + kRows);
-            const TM* Lki = L + lay.off[k + (size_t)i * lay.nb];
-            gemv_n_rows<T, TM>(r0, r1, bi, Lki, bk, Y + di, N, R + lay.displ[k], N, nrhs, 1, sV);
+        const TransposeDesc td = d[lo];
+        const int64_t sb = b - sub_pre[lo];
+        const int nbr = (td.rows + 31) / 32;
+        const int br = (int)(sb % nbr), bc = (int)(sb / nbr);
+        const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+        __syncthreads();
+        for (int yy = ty; yy < 32; yy += 8) {
+            const int r = br * 32 + tx, c = bc * 32 + yy;
+            if (r < td.rows && c < td.cols) t[yy][tx] = src[td.src + r + (int64_t)c * td.rows];
         }
-        grid.sync();
-    }
-}
-
-// Backward sweep Lᵀ X = Y (Y is overwritten as scratch).
-template <class T, class TM>
-__global__ void sweep_backward(TileLayout lay, const TM* L, const TM* invT, T* Yv, T* X, int nrhs) {
-    cg::grid_group grid = cg::this_grid();
-    __shared__ T sV[256 * kMaxRhs];
-    const int N = lay.N;
-    for (int i = lay.nb - 1; i >= 0; --i) {
-        const int bi = lay.bs[i], di = lay.displ[i];
-        // X_i = L_ii^-T Y_i = invT Y_i (thread per row).
-        const TM* Ti = invT + lay.off[i + (size_t)i * lay.nb];
-        const int items = (bi + kRows - 1) / kRows;
-        for (int it = blockIdx.x; it < items; it += gridDim.x) {
-            const int r0 = it * kRows, r1 = min(bi, r0 + kRows);
-            gemv_n_rows<T, TM>(r0, r1, bi, Ti, bi, Yv + di, N, X + di, N, nrhs, 0, sV);
+        __syncthreads();
+        for (int yy = ty; yy < 32; yy += 8) {
+            const int c = bc * 32 + tx, r = br * 32 + yy;  // destination (c, r) in a cols × rows tile
+            if (r < td.rows && c < td.cols) dst[td.dst + c + (int64_t)r * td.cols] = t[tx][yy];
         }
-        grid.sync();
-        // Y_j -= L_ijᵀ X_i for j < i (output rows of block j are columns of L_ij).
-        long total = 0;
-        for (int j = 0; j < i; ++j) total += (lay.bs[j] + kRows - 1) / kRows;
-        for (long it = blockIdx.x; it < total; it += gridDim.x) {
-            long rem = it;
-            int j = 0;
-            while (rem >= (lay.bs[j] + kRows - 1) / kRows) {
-                rem -= (lay.bs[j] + kRows - 1) / kRows;
-                ++j;
-            }
-            const int bj = lay.bs[j];
-            const int r0 = (int)rem * kRows, r1 = min(bj, r0 + kRows);
-            const TM* Lij = L + lay.off[i + (size_t)j * lay.nb];
-            gemv_t_rows<T, TM>(r0, r1, bi, Lij, bi, X + di, N, Yv + lay.displ[j], N, nrhs, 1);
-        }
-        grid.sync();
     }
 }
 
 // invT of every diagonal tile: the right-side TRSM of the identity gives
-// I·L^-T = L^-T.  Grid (nb, parts): block (j, p) handles a row slice.
+// I·L^-T = L^-T, stored at doff[j] (ld bs[j]).  Grid (nb, parts): block (j, p)
+// handles a row slice.
 template <class TM>
-__global__ void invert_diag_tiles(TileLayout lay, const TM* L, TM* invT, int parts) {
+__global__ void invert_diag_tiles(TileLayout lay, const int64_t* doff, const TM* L, TM* invT, int parts) {
     extern __shared__ __align__(128) double smem_inv[];
     const int j = blockIdx.x, p = blockIdx.y;
     const int b = lay.bs[j];
     if (b == 0) return;
     const TM* Ljj = L + lay.off[j + (size_t)j * lay.nb];
-    TM* T = invT + lay.off[j + (size_t)j * lay.nb];
+    TM* T = invT + doff[j];
     const int per = ((b + parts - 1) / parts + 15) / 16 * 16;
     const int r0 = min(b, p * per), r1 = min(b, r0 + per);
     for (long e = threadIdx.x; e < (long)(r1 - r0) * b; e += blockDim.x) {

@@ -276,4 +276,218 @@ __device__ __forceinline__ void geadd_f64(int m, int n, double alpha, const doub
     geadd_tile<double>(m, n, alpha, A, lda, beta, C, ldc, part, parts);
 }
 
+
+// ------------------------------------------------------------------------
+// Team POTRF: one diagonal tile factored by several blocks of the executor.
+//
+// The factorisation runs as a sequence of phases; for every 32-column panel:
+// the 32×32 diagonal block (one warp), the panel rows below it (32-row
+// items), and the lower 64×64 blocks of the trailing update.  Every block
+// that holds a part of the task claims items of the current phase from a
+// per-task counter and then waits until all items of the phase are done.  A
+// block never waits for a part that has not started — whoever is present does
+// the work — so the team cannot deadlock, and a single block alone factors
+// the whole tile.  Waits are bounded by limit_ns.
+//
+// ctr: kTeamCounters ints per task, zero at launch: (claimed, done) per
+// phase; ctr[kTeamCounters - 2] = phases completed; ctr[kTeamCounters - 1] =
+// the first failing column.
+constexpr int kTeamCounters = 256;
+constexpr int kTeamPanelRows = 32;  // rows per panel item
+constexpr int kTeamCopyRows = 128;  // rows per widen / narrow item
+constexpr int kTeamBlock = 64;      // trailing-update block
+
+// Phases of potrf_l_f64_team on an n×n tile; the team form needs
+// 2·phases + 2 <= kTeamCounters.
+__host__ __device__ inline int team_phases(int n, bool widen) { return 3 * ((n + kPanel - 1) / kPanel) + (widen ? 2 : 0); }
+__host__ __device__ inline bool team_fits(int n, bool widen) { return 2 * team_phases(n, widen) + 2 <= kTeamCounters; }
+
+struct TeamCtx {
+    int* ctr;
+    long long limit_ns;
+    int* err;  // executor status word (set to TTG_ETIMEOUT on a timeout)
+};
+
+__device__ __forceinline__ long long team_clock() {
+    long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Claim the next item of phase ph (the same value on all threads).
+__device__ __forceinline__ int team_claim(const TeamCtx& tc, int ph) {
+    __shared__ int s_item;
+    __syncthreads();
+    if (threadIdx.x == 0) s_item = atomicAdd(tc.ctr + 2 * ph, 1);
+    __syncthreads();
+    return s_item;
+}
+
+// Publish one finished item of phase ph (of `items`); the block that finishes
+// the last item advances the completed-phase marker.
+__device__ __forceinline__ void team_done(const TeamCtx& tc, int ph, int items) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(tc.ctr + 2 * ph + 1, 1) == items - 1) atomicMax(tc.ctr + kTeamCounters - 2, ph + 1);
+    }
+}
+
+// Phases completed so far (the same value on all threads).
+__device__ __forceinline__ int team_progress(const TeamCtx& tc) {
+    __shared__ int s_prog;
+    __syncthreads();
+    if (threadIdx.x == 0) s_prog = *(const volatile int*)(tc.ctr + kTeamCounters - 2);
+    __syncthreads();
+    return s_prog;
+}
+
+// Wait until `items` items of phase ph are done; false on timeout.
+__device__ __forceinline__ bool team_wait(const TeamCtx& tc, int ph, int items) {
+    __shared__ int s_ok;
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        const volatile int* d = tc.ctr + 2 * ph + 1;
+        if (*d < items) {
+            const long long t0 = team_clock();
+            for (unsigned it = 0; *d < items; ++it) {
+                if ((it & 63) == 63 && team_clock() - t0 > tc.limit_ns) {
+                    ok = 0;
+                    atomicCAS(tc.err, 0, 3 /* TTG_ETIMEOUT */);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// Lower 64×64 block `item` of C[rest×rest] -= P·Pᵀ, P rest×nb (nb <= 32).
+// Blocks are numbered column by column over the lower triangle.
+__device__ inline void team_syrk_block(int rest, int nb, const double* P, int ldp, double* C, int ldc, int item, double* smem) {
+    double(*As)[kTeamBlock] = reinterpret_cast<double(*)[kTeamBlock]>(smem);
+    double(*Bs)[kTeamBlock] = reinterpret_cast<double(*)[kTeamBlock]>(smem + kPanel * kTeamBlock);
+    const int nbm = (rest + kTeamBlock - 1) / kTeamBlock;
+    int bj = 0, r = item;
+    while (r >= nbm - bj) {
+        r -= nbm - bj;
+        ++bj;
+    }
+    const int bi = bj + r;
+    const int m0 = bi * kTeamBlock, n0 = bj * kTeamBlock;
+    for (int e = threadIdx.x; e < kPanel * kTeamBlock; e += kThreads) {
+        const int i = e % kTeamBlock, kk = e / kTeamBlock;
+        As[kk][i] = (m0 + i < rest && kk < nb) ? ldcg(P + m0 + i + (size_t)kk * ldp) : 0.0;
+        Bs[kk][i] = (n0 + i < rest && kk < nb) ? ldcg(P + n0 + i + (size_t)kk * ldp) : 0.0;
+    }
+    __syncthreads();
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    double acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+#pragma unroll 8
+    for (int kk = 0; kk < kPanel; ++kk) {
+        double x[4], y[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) x[a] = As[kk][tx + 16 * a];
+#pragma unroll
+        for (int b = 0; b < 4; ++b) y[b] = Bs[kk][ty + 16 * b];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) acc[a][b] = fma(x[a], y[b], acc[a][b]);
+    }
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        const int gj = n0 + ty + 16 * b;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int gi = m0 + tx + 16 * a;
+            if (gi < rest && gj < rest && gi >= gj) {
+                double* q = C + gi + (size_t)gj * ldc;
+                *q = ldcg(q) - acc[a][b];
+            }
+        }
+    }
+}
+
+// Team lower Cholesky of the FP64 tile A[n×n] (lda); requires
+// team_fits(n, W32 != nullptr).  With an FP32 source (W32 != nullptr) the
+// team first widens the lower triangle of W32 (ldw) into A and at the end
+// rounds the factor back into W32.  Returns 0, the 1-based failing column, or
+// -1 after a timeout.  The result is the same for any number of blocks: every
+// item computes the same arithmetic whoever runs it.
+__device__ inline int potrf_l_f64_team(int n, double* A, int lda, double* smem, const TeamCtx& tc, float* W32, int ldw) {
+    double* Ls = smem + kBK * kBM + kBK * kBNP;
+    int ph = 0;
+    const int copy_items = (n + kTeamCopyRows - 1) / kTeamCopyRows;
+    if (W32) {
+        for (int it = team_claim(tc, ph); it < copy_items; it = team_claim(tc, ph)) {
+            const int r0 = it * kTeamCopyRows, r1 = min(n, r0 + kTeamCopyRows), rows = r1 - r0;
+            for (long e = threadIdx.x; e < (long)rows * n; e += kThreads) {
+                const int i = r0 + (int)(e % rows), j = (int)(e / rows);
+                A[i + (size_t)j * lda] = i >= j ? (double)__ldcg(W32 + i + (size_t)j * ldw) : 0.0;
+            }
+            team_done(tc, ph, copy_items);
+        }
+        if (!team_wait(tc, ph, copy_items)) return -1;
+        ++ph;
+    }
+    for (int p = 0; p < n; p += kPanel, ph += 3) {
+        // Panels that the team has already finished are skipped by late blocks.
+        if (team_progress(tc) >= ph + 3) continue;
+        const int nb = min(kPanel, n - p);
+        double* Dpp = A + p + (size_t)p * lda;
+        if (team_claim(tc, ph) == 0) {
+            if (threadIdx.x < 32) {
+                const int info = potrf_diag32_warp(Dpp, lda, nb);
+                if (threadIdx.x == 0 && info) atomicExch(tc.ctr + kTeamCounters - 1, p + info);
+            }
+            team_done(tc, ph, 1);
+        }
+        if (!team_wait(tc, ph, 1)) return -1;
+        {
+            const int info = *(const volatile int*)(tc.ctr + kTeamCounters - 1);
+            if (info) return info;
+        }
+        const int rest = n - p - nb;
+        if (rest <= 0) continue;
+        load_panel_block<double>(Dpp, lda, nb, Ls);
+        const int pitems = (rest + kTeamPanelRows - 1) / kTeamPanelRows;
+        for (int it = team_claim(tc, ph + 1); it < pitems; it = team_claim(tc, ph + 1)) {
+            const int r0 = p + nb + it * kTeamPanelRows;
+            trsm_rows_panel<double>(A + (size_t)p * lda, lda, r0, min(n, r0 + kTeamPanelRows), nb, Ls, 1.0);
+            team_done(tc, ph + 1, pitems);
+        }
+        if (!team_wait(tc, ph + 1, pitems)) return -1;
+        const int nbm = (rest + kTeamBlock - 1) / kTeamBlock;
+        const int citems = nbm * (nbm + 1) / 2;
+        const double* P = A + (p + nb) + (size_t)p * lda;
+        double* C = A + (p + nb) + (size_t)(p + nb) * lda;
+        for (int it = team_claim(tc, ph + 2); it < citems; it = team_claim(tc, ph + 2)) {
+            team_syrk_block(rest, nb, P, lda, C, lda, it, smem);
+            team_done(tc, ph + 2, citems);
+        }
+        if (!team_wait(tc, ph + 2, citems)) return -1;
+    }
+    if (W32) {
+        for (int it = team_claim(tc, ph); it < copy_items; it = team_claim(tc, ph)) {
+            const int r0 = it * kTeamCopyRows, r1 = min(n, r0 + kTeamCopyRows), rows = r1 - r0;
+            for (long e = threadIdx.x; e < (long)rows * n; e += kThreads) {
+                const int i = r0 + (int)(e % rows), j = (int)(e / rows);
+                if (i >= j) W32[i + (size_t)j * ldw] = (float)__ldcg(A + i + (size_t)j * lda);
+            }
+            team_done(tc, ph, copy_items);
+        }
+        if (!team_wait(tc, ph, copy_items)) return -1;
+    }
+    return 0;
+}
+
 }  // namespace ttg

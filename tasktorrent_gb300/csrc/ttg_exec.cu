@@ -20,10 +20,14 @@
 
 namespace ttg {
 
-// One part of an FP64 tile task on the whole block.  Returns POTRF's info (0 = ok).
-__device__ int run_op_f64(const ttg_op& op, int part, int parts, double* smem) {
+static_assert(kTeamCounters == kTeamStride, "team counter block size");
+
+// One part of an FP64 tile task on the whole block.  Returns POTRF's info (0 =
+// ok).  A POTRF with a team counter block is factored by all its parts.
+__device__ int run_op_f64(const ttg_op& op, int part, int parts, double* smem, int* team, int* err, long long limit_ns) {
     switch (op.kind) {
         case TTG_OP_POTRF_L:
+            if (team) return potrf_l_f64_team(op.n, (double*)op.c, op.ldc, smem, TeamCtx{team, limit_ns, err}, nullptr, 0);
             return potrf_l_f64(op.n, (double*)op.c, op.ldc, smem);
         case TTG_OP_TRSM_RLTN:
             trsm_rltn_f64(op.m, op.n, op.alpha, (const double*)op.a, op.lda, (double*)op.c, op.ldc, smem, part, parts);
@@ -50,8 +54,8 @@ __device__ int run_op_f64(const ttg_op& op, int part, int parts, double* smem) {
 
 __global__ void __launch_bounds__(kThreads, 1) exec_kernel(ExecParams p) {
     extern __shared__ __align__(128) double smem_f64[];
-    executor_loop(p, smem_f64, [](const ttg_op& op, int part, int parts, double* smem) {
-        return run_op_f64(op, part, parts, smem);
+    executor_loop(p, smem_f64, [&](const ttg_op& op, int part, int parts, double* smem, int* team) {
+        return run_op_f64(op, part, parts, smem, team, p.err, p.timeout_ns);
     });
 }
 
@@ -148,6 +152,9 @@ void ttg_graph_free(ttg_ctx* c) {
     dev_free(g.count);
     dev_free(g.runs);
     dev_free(g.parts);
+    dev_free(g.team_ctr);
+    dev_free(g.team_slot);
+    g.n_team = 0;
     dev_free(g.part_next);
     dev_free(g.part_done);
     dev_free(g.succ_ptr);
@@ -236,9 +243,15 @@ extern "C" uint64_t ttg_graph_generation(const ttg_ctx* c) { return c ? c->graph
 
 // Blocks that share one task: explicit op.parts, else one per 128×128 output
 // block (lower blocks for SYRK) up to 16, TRSM by 128-row slices up to 8;
-// POTRF and no-op tasks are never split.
-int ttg_task_parts(const ttg_op& op) {
+// POTRF (with team) by n/32 blocks up to 16 for n >= 128; no-op tasks and,
+// without team, POTRF are never split.
+int ttg_task_parts(const ttg_op& op, bool team) {
     auto cdiv = [](long a, long b) { return (int)((a + b - 1) / b); };
+    if (op.kind == TTG_OP_POTRF_L) {
+        if (!team || !team_fits(op.n, op.prec == TTG_PREC_MIXED)) return 1;
+        if (op.parts > 0) return std::min(op.parts, 64);
+        return op.n >= 128 ? std::min(16, op.n / 32) : 1;
+    }
     // Tensor-core updates of the mixed path: exactly one 128×256 output block
     // per part (lower-triangle blocks only for SYRK).
     if (op.prec == TTG_PREC_MIXED && op.flags == 2 && (op.kind == TTG_OP_GEMM_NT || op.kind == TTG_OP_SYRK_LN)) {
@@ -372,7 +385,12 @@ extern "C" ttg_status ttg_graph_upload(ttg_ctx* c, const ttg_graph_desc* gd) {
     int n_levels = 1;
     assign_levels(n, gd->priority, runnable, level, &n_levels);
     std::vector<int> parts(n, 1);
-    for (int t = 0; t < n; ++t) parts[t] = ttg_task_parts(gd->ops[t]);
+    std::vector<int> team_slot(n, -1);
+    int n_team = 0;
+    for (int t = 0; t < n; ++t) {
+        parts[t] = ttg_task_parts(gd->ops[t], true);
+        if (gd->ops[t].kind == TTG_OP_POTRF_L && parts[t] > 1) team_slot[t] = n_team++;
+    }
 
     // Queue layout: level queues sized by runnable unbound tasks per level,
     // bound queues by runnable tasks bound to each worker.
@@ -442,6 +460,9 @@ extern "C" ttg_status ttg_graph_upload(ttg_ctx* c, const ttg_graph_desc* gd) {
     ALLOC(bq_head, W * 2);             // head + initial tail
     ALLOC(bq_tail, W);
     if (c->trace) ALLOC(trace, 3 * (size_t)std::max(1, n));
+    ALLOC(team_slot, n);
+    if (n_team) ALLOC(team_ctr, (size_t)n_team * kTeamStride);
+    g.n_team = n_team;
 #undef ALLOC
     TTG_CUDA_TRY(cudaMemcpy(g.ops, gd->ops, sizeof(ttg_op) * n, cudaMemcpyHostToDevice));
     TTG_CUDA_TRY(cudaMemcpy(g.init, gd->init_count, sizeof(int) * n, cudaMemcpyHostToDevice));
@@ -449,6 +470,7 @@ extern "C" ttg_status ttg_graph_upload(ttg_ctx* c, const ttg_graph_desc* gd) {
     if (n_edges) TTG_CUDA_TRY(cudaMemcpy(g.succ_idx, gd->succ_idx, sizeof(int32_t) * n_edges, cudaMemcpyHostToDevice));
     TTG_CUDA_TRY(cudaMemcpy(g.level, level.data(), n, cudaMemcpyHostToDevice));
     TTG_CUDA_TRY(cudaMemcpy(g.parts, parts.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    TTG_CUDA_TRY(cudaMemcpy(g.team_slot, team_slot.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
     TTG_CUDA_TRY(cudaMemcpy(g.bind, bind.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
     TTG_CUDA_TRY(cudaMemcpy(g.runnable, runnable.data(), n, cudaMemcpyHostToDevice));
     TTG_CUDA_TRY(cudaMemcpy(g.qinit, qinit.data(), sizeof(int) * qinit.size(), cudaMemcpyHostToDevice));
@@ -479,6 +501,7 @@ ttg_status ttg_reset_state(ttg_ctx* c, cudaStream_t s) {
     TTG_CUDA_TRY(cudaMemcpyAsync(g.bq_tail, g.bq_head + W, sizeof(int) * W, cudaMemcpyDeviceToDevice, s));
     TTG_CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int) * 8, s));
     if (g.trace) TTG_CUDA_TRY(cudaMemsetAsync(g.trace, 0, sizeof(long long) * 3 * std::max(1, n), s));
+    if (g.n_team) TTG_CUDA_TRY(cudaMemsetAsync(g.team_ctr, 0, sizeof(int) * (size_t)g.n_team * kTeamStride, s));
     return TTG_OK;
 }
 
@@ -514,6 +537,8 @@ static ExecParams ttg_make_params(ttg_ctx* c) {
     p.err_info = c->status + 3;
     p.trace = (long long*)g.trace;
     p.timeout_ns = (long long)(c->timeout_s * 1e9);
+    p.team_ctr = g.team_ctr;
+    p.team_slot = g.team_slot;
     return p;
 }
 

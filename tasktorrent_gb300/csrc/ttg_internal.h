@@ -41,6 +41,9 @@ struct DevGraph {
     int* bq_head = nullptr;
     int* bq_tail = nullptr;
     long long* trace = nullptr;
+    int n_team = 0;             // POTRF tasks factored by a team of blocks
+    int* team_ctr = nullptr;    // kTeamStride words per team task
+    int* team_slot = nullptr;   // per task: team counter block or -1
 };
 
 struct ttg_ctx {
@@ -70,7 +73,9 @@ ttg_status ttg_ctx_init_device(ttg_ctx* c);
 ttg_status ttg_reset_state(ttg_ctx* c, cudaStream_t s);
 ttg_status ttg_launch_executor(ttg_ctx* c, const ttg::ExecParams& p, cudaStream_t s);
 void ttg_graph_free(ttg_ctx* c);
-int ttg_task_parts(const ttg_op& op);
+// Blocks that share one task.  team: a POTRF may be split over a team of
+// blocks (needs a team counter block at run time).
+int ttg_task_parts(const ttg_op& op, bool team = false);
 
 // Lower tiles of the miniapp matrix 1/((i-j)^2+1) (ttg_gen.cu).
 ttg_status ttg_gen_miniapp_tiles(ttg_ctx* c, const int32_t* h_bs, int32_t nb, double* d_tiles, void* stream);

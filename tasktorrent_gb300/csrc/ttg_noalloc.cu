@@ -111,7 +111,7 @@ __device__ int run_op_f64_noalloc(const ttg_op& op, int part, int parts, double*
 __global__ void __launch_bounds__(ttg::kThreads, 1) exec_kernel_noalloc(ttg::ExecParams p, RunStatus* st) {
     extern __shared__ __align__(128) double smem_na[];
     if (threadIdx.x == 0) atomicMin(&st->start, (unsigned long long)ttg::globaltimer());
-    ttg::executor_loop(p, smem_na, [](const ttg_op& op, int part, int parts, double* smem) {
+    ttg::executor_loop(p, smem_na, [](const ttg_op& op, int part, int parts, double* smem, int*) {
         return run_op_f64_noalloc(op, part, parts, smem);
     });
     if (threadIdx.x == 0) atomicMax(&st->end, (unsigned long long)ttg::globaltimer());
@@ -347,6 +347,8 @@ extern "C" ttg_status ttg_run_graph_noalloc(int device, const ttg_graph_desc* gd
         p.err_info = &dst->err_info;
         p.trace = nullptr;
         p.timeout_ns = (long long)((timeout_s > 0 ? timeout_s : 10.0) * 1e9);
+        p.team_ctr = nullptr;  // POTRF tasks run on one block here
+        p.team_slot = nullptr;
         void* args[] = {(void*)&p, (void*)&dst};
         TTG_CUDA_CHECK(cudaLaunchCooperativeKernel((const void*)exec_kernel_noalloc, dim3(W), dim3(ttg::kThreads), args,
                                                    ttg::kF64SmemDoubles * sizeof(double), s));

@@ -75,9 +75,20 @@ struct ttg_solver {
     DevBuf<float> A32;
     bool dense_valid = false;
     double anorm_inf = 0.0;
-    // Inverted diagonal tiles of the current factor.
-    DevBuf<double> inv64;
-    DevBuf<float> inv32;
+    // Operands of the sweeps for the current factor: L_ii⁻ᵀ and L_ii⁻¹
+    // (compact diagonal tiles at doff) and the transposed off-diagonal tiles
+    // (L_ijᵀ at off[i + j·nb], ld bs[j]).
+    DevBuf<double> inv64, linv64, lt64;
+    DevBuf<float> inv32, linv32, lt32;
+    int64_t dsize = 0;  // elements of the compact diagonal
+    DevBuf<int64_t> d_doff;
+    DevBuf<int> d_strip_pre, d_step_fwd, d_step_bwd;
+    DevBuf<int> d_sweep_ctr;  // per sweep direction: claim, ready[nb], applied[strips]
+    DevBuf<int> d_err;        // sweep timeout flag (zeroed per solve)
+    int n_strips = 0;
+    DevBuf<TransposeDesc> d_tdesc_off, d_tdesc_diag;
+    DevBuf<int64_t> d_tsub_off, d_tsub_diag;
+    int n_tdesc_off = 0, n_tdesc_diag = 0;
     // Work vectors (N × 16).
     DevBuf<double> B, X, R, D, W, T1, T2, P;
     DevBuf<float> f1, f2, f3;
@@ -87,25 +98,86 @@ struct ttg_solver {
     int sweep_grid64 = 0, sweep_grid32 = 0, sweep_grid_mix = 0;
 };
 
+template <class T>
+static constexpr int sweep_smem_bytes() {
+    return kChunk * kMaxRhs * (int)sizeof(T);
+}
+
+template <class T, class TM>
+static ttg_status sweep_grid(ttg_solver* S, int* grid) {
+    const int smem = sweep_smem_bytes<T>();
+    TTG_CUDA_CHECK(cudaFuncSetAttribute(sweep_kernel<T, TM>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    int per = 0;
+    TTG_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep_kernel<T, TM>, 256, smem));
+    *grid = std::max(1, per) * S->ctx->sms;
+    return TTG_OK;
+}
+
 static ttg_status solver_init(ttg_solver* S) {
     TTG_CUDA_CHECK(cudaSetDevice(S->ctx->device));
-    int per = 0;
-    TTG_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep_forward<double, double>, 256, 0));
-    S->sweep_grid64 = std::max(1, per) * S->ctx->sms;
-    TTG_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep_forward<float, float>, 256, 0));
-    S->sweep_grid32 = std::max(1, per) * S->ctx->sms;
-    TTG_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep_forward<double, float>, 256, 0));
-    S->sweep_grid_mix = std::max(1, per) * S->ctx->sms;
-    int per_b = 0;
-    TTG_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_b, sweep_backward<double, double>, 256, 0));
-    S->sweep_grid64 = std::min(S->sweep_grid64, std::max(1, per_b) * S->ctx->sms);
-    TTG_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_b, sweep_backward<float, float>, 256, 0));
-    S->sweep_grid32 = std::min(S->sweep_grid32, std::max(1, per_b) * S->ctx->sms);
-    TTG_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_b, sweep_backward<double, float>, 256, 0));
-    S->sweep_grid_mix = std::min(S->sweep_grid_mix, std::max(1, per_b) * S->ctx->sms);
+    ttg_status st;
+    if ((st = sweep_grid<double, double>(S, &S->sweep_grid64)) != TTG_OK) return st;
+    if ((st = sweep_grid<float, float>(S, &S->sweep_grid32)) != TTG_OK) return st;
+    if ((st = sweep_grid<double, float>(S, &S->sweep_grid_mix)) != TTG_OK) return st;
     const int smem = kF64SmemDoubles * (int)sizeof(double);
     TTG_CUDA_CHECK(cudaFuncSetAttribute(invert_diag_tiles<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     TTG_CUDA_CHECK(cudaFuncSetAttribute(invert_diag_tiles<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    return TTG_OK;
+}
+
+// Host tables of the sweeps (strips, item counts per step) and of the tile
+// transposes.
+static ttg_status solver_tables(ttg_solver* S, const int* bs, const int64_t* off) {
+    const int nb = S->nb;
+    std::vector<int64_t> doff(nb, 0);
+    int64_t d = 0;
+    for (int i = 0; i < nb; ++i) {
+        doff[i] = d;
+        d += (int64_t)bs[i] * bs[i];
+    }
+    S->dsize = d;
+    std::vector<int> sp(nb + 1, 0);
+    for (int i = 0; i < nb; ++i) sp[i + 1] = sp[i] + (bs[i] + kStrip - 1) / kStrip;
+    S->n_strips = sp[nb];
+    std::vector<int> fwd(nb + 1, 0), bwd(nb + 1, 0);
+    for (int st = 0; st < nb; ++st) {
+        const int i = st, ib = nb - 1 - st;
+        const int64_t nf = (int64_t)(sp[i + 1] - sp[i]) + (sp[nb] - sp[i + 1]);
+        const int64_t nbk = (int64_t)(sp[ib + 1] - sp[ib]) + sp[ib];
+        if ((int64_t)fwd[st] + nf > INT32_MAX || (int64_t)bwd[st] + nbk > INT32_MAX) return TTG_EINVAL;
+        fwd[st + 1] = fwd[st] + (int)nf;
+        bwd[st + 1] = bwd[st] + (int)nbk;
+    }
+    std::vector<TransposeDesc> to, td;
+    std::vector<int64_t> so(1, 0), sd(1, 0);
+    for (int j = 0; j < nb; ++j) {
+        for (int i = j + 1; i < nb; ++i) {
+            const int64_t o = off[i + (size_t)j * nb];
+            to.push_back({o, o, bs[i], bs[j]});
+            so.push_back(so.back() + (int64_t)((bs[i] + 31) / 32) * ((bs[j] + 31) / 32));
+        }
+        td.push_back({doff[j], doff[j], bs[j], bs[j]});
+        sd.push_back(sd.back() + (int64_t)((bs[j] + 31) / 32) * ((bs[j] + 31) / 32));
+    }
+    S->n_tdesc_off = (int)to.size();
+    S->n_tdesc_diag = (int)td.size();
+    ttg_status st;
+    if ((st = S->d_doff.ensure(nb)) != TTG_OK || (st = S->d_strip_pre.ensure(nb + 1)) != TTG_OK ||
+        (st = S->d_step_fwd.ensure(nb + 1)) != TTG_OK || (st = S->d_step_bwd.ensure(nb + 1)) != TTG_OK ||
+        (st = S->d_sweep_ctr.ensure(2 * (size_t)(2 + nb + S->n_strips))) != TTG_OK || (st = S->d_err.ensure(1)) != TTG_OK ||
+        (st = S->d_tdesc_off.ensure(std::max<size_t>(1, to.size()))) != TTG_OK ||
+        (st = S->d_tdesc_diag.ensure(td.size())) != TTG_OK || (st = S->d_tsub_off.ensure(so.size())) != TTG_OK ||
+        (st = S->d_tsub_diag.ensure(sd.size())) != TTG_OK)
+        return st;
+    TTG_CUDA_CHECK(cudaMemcpy(S->d_doff.p, doff.data(), sizeof(int64_t) * nb, cudaMemcpyHostToDevice));
+    TTG_CUDA_CHECK(cudaMemcpy(S->d_strip_pre.p, sp.data(), sizeof(int) * (nb + 1), cudaMemcpyHostToDevice));
+    TTG_CUDA_CHECK(cudaMemcpy(S->d_step_fwd.p, fwd.data(), sizeof(int) * (nb + 1), cudaMemcpyHostToDevice));
+    TTG_CUDA_CHECK(cudaMemcpy(S->d_step_bwd.p, bwd.data(), sizeof(int) * (nb + 1), cudaMemcpyHostToDevice));
+    if (!to.empty())
+        TTG_CUDA_CHECK(cudaMemcpy(S->d_tdesc_off.p, to.data(), sizeof(TransposeDesc) * to.size(), cudaMemcpyHostToDevice));
+    TTG_CUDA_CHECK(cudaMemcpy(S->d_tdesc_diag.p, td.data(), sizeof(TransposeDesc) * td.size(), cudaMemcpyHostToDevice));
+    TTG_CUDA_CHECK(cudaMemcpy(S->d_tsub_off.p, so.data(), sizeof(int64_t) * so.size(), cudaMemcpyHostToDevice));
+    TTG_CUDA_CHECK(cudaMemcpy(S->d_tsub_diag.p, sd.data(), sizeof(int64_t) * sd.size(), cudaMemcpyHostToDevice));
     return TTG_OK;
 }
 
@@ -145,7 +217,7 @@ ttg_status ttg_solver_create(ttg_ctx* ctx, int N, int nb, const int* bs, const i
     S->lay.displ = S->d_displ.p;
     S->lay.nb = nb;
     S->lay.N = N;
-    if ((st = solver_init(S)) != TTG_OK) {
+    if ((st = solver_init(S)) != TTG_OK || (st = solver_tables(S, bs, off)) != TTG_OK) {
         ttg_solver_destroy(S);
         return st;
     }
@@ -156,14 +228,24 @@ ttg_status ttg_solver_create(ttg_ctx* ctx, int N, int nb, const int* bs, const i
 void ttg_solver_destroy(ttg_solver* S) {
     if (!S) return;
     cudaSetDevice(S->ctx->device);
-    for (auto* b : {&S->A64, &S->inv64, &S->B, &S->X, &S->R, &S->D, &S->W, &S->T1, &S->T2, &S->P, &S->Vd, &S->part, &S->colv,
+    for (auto* b : {&S->A64, &S->inv64, &S->linv64, &S->lt64, &S->B, &S->X, &S->R, &S->D, &S->W, &S->T1, &S->T2, &S->P, &S->Vd, &S->part, &S->colv,
                     &S->coefA, &S->coefB})
         b->release();
-    for (auto* b : {&S->A32, &S->inv32, &S->f1, &S->f2, &S->f3, &S->Vf}) b->release();
+    for (auto* b : {&S->A32, &S->inv32, &S->linv32, &S->lt32, &S->f1, &S->f2, &S->f3, &S->Vf}) b->release();
     S->d_off.release();
     S->d_bs.release();
     S->d_displ.release();
     S->d_rowblk.release();
+    S->d_doff.release();
+    S->d_strip_pre.release();
+    S->d_step_fwd.release();
+    S->d_step_bwd.release();
+    S->d_sweep_ctr.release();
+    S->d_err.release();
+    S->d_tdesc_off.release();
+    S->d_tdesc_diag.release();
+    S->d_tsub_off.release();
+    S->d_tsub_diag.release();
     delete S;
 }
 
@@ -194,32 +276,61 @@ static ttg_status ensure_dense(ttg_solver* S, const double* pristine, cudaStream
     return TTG_OK;
 }
 
-ttg_status ttg_solver_factor_done(ttg_solver* S, const double* L64, const float* L32, cudaStream_t s) {
+// Sweep operands of a new factor: L_ii⁻ᵀ (TRSM of the identity), L_ii⁻¹ (its
+// transpose) and the transposed off-diagonal tiles.
+template <class TM>
+static ttg_status prepare_operands(ttg_solver* S, const TM* L, DevBuf<TM>& inv, DevBuf<TM>& linv, DevBuf<TM>& lt,
+                                   cudaStream_t s) {
     const int parts = 8;
     const int smem = kF64SmemDoubles * (int)sizeof(double);
-    dim3 grid(S->nb, parts);
     ttg_status st;
-    if (S->mixed) {
-        if ((st = S->inv32.ensure(S->elems)) != TTG_OK) return st;
-        invert_diag_tiles<float><<<grid, kThreads, smem, s>>>(S->lay, L32, S->inv32.p, parts);
-    } else {
-        if ((st = S->inv64.ensure(S->elems)) != TTG_OK) return st;
-        invert_diag_tiles<double><<<grid, kThreads, smem, s>>>(S->lay, L64, S->inv64.p, parts);
-    }
+    if ((st = inv.ensure(S->dsize)) != TTG_OK || (st = linv.ensure(S->dsize)) != TTG_OK || (st = lt.ensure(S->elems)) != TTG_OK)
+        return st;
+    invert_diag_tiles<TM><<<dim3(S->nb, parts), kThreads, smem, s>>>(S->lay, S->d_doff.p, L, inv.p, parts);
+    transpose_tiles<TM><<<S->ctx->sms * 8, 256, 0, s>>>(S->d_tdesc_diag.p, S->d_tsub_diag.p, S->n_tdesc_diag, inv.p, linv.p);
+    if (S->n_tdesc_off > 0)
+        transpose_tiles<TM><<<S->ctx->sms * 8, 256, 0, s>>>(S->d_tdesc_off.p, S->d_tsub_off.p, S->n_tdesc_off, L, lt.p);
     TTG_CUDA_CHECK(cudaGetLastError());
     return TTG_OK;
 }
 
+ttg_status ttg_solver_factor_done(ttg_solver* S, const double* L64, const float* L32, cudaStream_t s) {
+    if (S->mixed) return prepare_operands<float>(S, L32, S->inv32, S->linv32, S->lt32, s);
+    return prepare_operands<double>(S, L64, S->inv64, S->linv64, S->lt64, s);
+}
+
 namespace {
 
+// R (scratch, overwritten) -> Y = L⁻¹ R -> X = L⁻ᵀ Y (Y overwritten): the
+// forward and the backward sweep, one launch each.
 template <class T, class TM>
-ttg_status sweeps(ttg_solver* S, const TM* L, const TM* inv, T* R, T* Y, T* X, int nrhs, int grid, cudaStream_t s) {
-    // R (scratch, overwritten) -> Y = L⁻¹ R -> X = L⁻ᵀ Y (Y overwritten).
-    TileLayout lay = S->lay;
-    void* fa[] = {(void*)&lay, (void*)&L, (void*)&inv, (void*)&R, (void*)&Y, (void*)&nrhs};
-    TTG_CUDA_CHECK(cudaLaunchCooperativeKernel((const void*)sweep_forward<T, TM>, dim3(grid), dim3(256), fa, 0, s));
-    void* ba[] = {(void*)&lay, (void*)&L, (void*)&inv, (void*)&Y, (void*)&X, (void*)&nrhs};
-    TTG_CUDA_CHECK(cudaLaunchCooperativeKernel((const void*)sweep_backward<T, TM>, dim3(grid), dim3(256), ba, 0, s));
+ttg_status sweeps(ttg_solver* S, const TM* L, const TM* LT, const TM* Linv, const TM* invT, T* R, T* Y, T* X, int nrhs, int grid,
+                  cudaStream_t s) {
+    const size_t region = 2 + S->nb + S->n_strips;
+    TTG_CUDA_CHECK(cudaMemsetAsync(S->d_sweep_ctr.p, 0, sizeof(int) * 2 * region, s));
+    SweepArgs a;
+    a.off = S->d_off.p;
+    a.doff = S->d_doff.p;
+    a.bs = S->d_bs.p;
+    a.displ = S->d_displ.p;
+    a.strip_pre = S->d_strip_pre.p;
+    a.nb = S->nb;
+    a.N = S->N;
+    a.nrhs = nrhs;
+    a.err = S->d_err.p;
+    a.timeout_ns = (long long)(std::max(1.0, S->ctx->timeout_s) * 1e9);
+    const int smem = sweep_smem_bytes<T>();
+    for (int dir = 0; dir < 2; ++dir) {
+        int* ctr = S->d_sweep_ctr.p + dir * region;
+        a.claim = ctr;
+        a.ready = ctr + 2;
+        a.applied = ctr + 2 + S->nb;
+        a.backward = dir;
+        a.step_start = dir ? S->d_step_bwd.p : S->d_step_fwd.p;
+        if (dir == 0) sweep_kernel<T, TM><<<grid, 256, smem, s>>>(a, L, Linv, R, Y);
+        else sweep_kernel<T, TM><<<grid, 256, smem, s>>>(a, LT, invT, Y, X);
+        TTG_CUDA_CHECK(cudaGetLastError());
+    }
     return TTG_OK;
 }
 
@@ -303,7 +414,7 @@ ttg_status gmres_cycle(ttg_solver* S, const float* L32, int nrhs, int m, double 
     if ((st = colreduce<double>(S, S->R.p, nullptr, nrhs, 1, rn.data(), s)) != TTG_OK) return st;
     for (int q = 0; q < nrhs; ++q) inv[q] = rn[q] > 0 ? 1.0 / rn[q] : 0.0;
     if ((st = axpby<double, TG>(S, inv, S->R.p, nullptr, t1, nrhs, s)) != TTG_OK) return st;
-    if ((st = sweeps<TG, float>(S, L32, S->inv32.p, t1, t2, V, nrhs, grid, s)) != TTG_OK) return st;
+    if ((st = sweeps<TG, float>(S, L32, S->lt32.p, S->linv32.p, S->inv32.p, t1, t2, V, nrhs, grid, s)) != TTG_OK) return st;
     std::vector<double> beta(nrhs);
     if ((st = colreduce<TG>(S, V, V, nrhs, 0, beta.data(), s)) != TTG_OK) return st;
     std::vector<double> scale(nrhs);
@@ -323,7 +434,8 @@ ttg_status gmres_cycle(ttg_solver* S, const float* L32, int nrhs, int m, double 
         TG* w = V + blk * (k + 1);
         // w = M⁻¹ (A v_k)
         if ((st = matmul<TG>(S, A, vk, nullptr, t1, t3, nrhs, 0, s)) != TTG_OK) return st;
-        if ((st = sweeps<TG, float>(S, L32, S->inv32.p, t1, t2, w, nrhs, grid, s)) != TTG_OK) return st;
+        if ((st = sweeps<TG, float>(S, L32, S->lt32.p, S->linv32.p, S->inv32.p, t1, t2, w, nrhs, grid, s)) != TTG_OK)
+            return st;
         // Modified Gram-Schmidt.
         for (int j = 0; j <= k; ++j) {
             std::vector<double> d(nrhs), neg(nrhs);
@@ -424,6 +536,7 @@ ttg_status ttg_solver_solve(ttg_solver* S, const double* pristine, const double*
     if ((st = S->part.ensure(128 * kMaxRhs)) != TTG_OK || (st = S->colv.ensure(kMaxRhs)) != TTG_OK ||
         (st = S->coefA.ensure(kMaxRhs)) != TTG_OK || (st = S->coefB.ensure(kMaxRhs)) != TTG_OK)
         return st;
+    TTG_CUDA_CHECK(cudaMemsetAsync(S->d_err.p, 0, sizeof(int), s));
     clk.mark("buffers");
     if ((st = ensure_dense(S, pristine, s)) != TTG_OK) return st;
     clk.mark("dense copies of A");
@@ -437,7 +550,8 @@ ttg_status ttg_solver_solve(ttg_solver* S, const double* pristine, const double*
     if (!S->mixed) {
         // FP64 direct: X = L⁻ᵀ L⁻¹ B.
         TTG_CUDA_CHECK(cudaMemcpyAsync(S->R.p, S->B.p, sizeof(double) * blk, cudaMemcpyDeviceToDevice, s));
-        if ((st = sweeps<double, double>(S, L64, S->inv64.p, S->R.p, S->T1.p, S->X.p, nrhs, S->sweep_grid64, s)) != TTG_OK)
+        if ((st = sweeps<double, double>(S, L64, S->lt64.p, S->linv64.p, S->inv64.p, S->R.p, S->T1.p, S->X.p, nrhs,
+                                         S->sweep_grid64, s)) != TTG_OK)
             return st;
         clk.mark("FP64 sweeps");
         if ((st = backward_errors(S, nrhs, s, be, rn)) != TTG_OK) return st;
@@ -447,7 +561,8 @@ ttg_status ttg_solver_solve(ttg_solver* S, const double* pristine, const double*
         // x0 = M⁻¹ b (FP32 sweeps).
         std::vector<double> one(nrhs, 1.0);
         if ((st = axpby<double, float>(S, one, S->B.p, nullptr, S->f1.p, nrhs, s)) != TTG_OK) return st;
-        if ((st = sweeps<float, float>(S, L32, S->inv32.p, S->f1.p, S->f2.p, S->f3.p, nrhs, S->sweep_grid32, s)) != TTG_OK)
+        if ((st = sweeps<float, float>(S, L32, S->lt32.p, S->linv32.p, S->inv32.p, S->f1.p, S->f2.p, S->f3.p, nrhs,
+                                       S->sweep_grid32, s)) != TTG_OK)
             return st;
         if ((st = axpby<float, double>(S, one, S->f3.p, nullptr, S->X.p, nrhs, s)) != TTG_OK) return st;
         clk.mark("x0 = M^-1 b (FP32 sweeps)");
@@ -483,7 +598,10 @@ ttg_status ttg_solver_solve(ttg_solver* S, const double* pristine, const double*
     r.bwd_err = be.empty() ? 0.0 : *std::max_element(be.begin(), be.end());
     r.anorm_inf = S->anorm_inf;
     TTG_CUDA_CHECK(cudaMemcpyAsync(d_X, S->X.p, sizeof(double) * blk, cudaMemcpyDeviceToDevice, s));
+    int h_err = 0;
+    TTG_CUDA_CHECK(cudaMemcpyAsync(&h_err, S->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     TTG_CUDA_CHECK(cudaStreamSynchronize(s));
+    if (h_err) r.status = TTG_ETIMEOUT;  // a sweep gave up waiting: X is not valid
     if (rep) *rep = r;
     return r.status;
 }

@@ -208,6 +208,37 @@ def test_potrf_kernel(ctx, n):
     assert np.linalg.norm(got @ got.T - A) <= 1e-14 * n * np.linalg.norm(A)
 
 
+@pytest.mark.parametrize("n", [128, 300, 512, 1000])
+@pytest.mark.parametrize("parts", [2, 5, 16, 64])
+def test_potrf_team_matches_one_block(ctx, n, parts):
+    """A POTRF shared by a team of blocks gives the single-block factor bit for bit."""
+    import torch
+    rng = np.random.default_rng(n + parts)
+    G = rng.standard_normal((n, n))
+    A = G @ G.T / n + np.eye(n)
+    out = []
+    for p in (1, parts):
+        dA, pA = _colmajor(A)
+        torch.cuda.synchronize()
+        st, rep = run_single(ctx, t.Op(kind=t.OP_POTRF_L, m=n, n=n, ldc=n, parts=p, c=pA))
+        assert st == t.TTG_OK
+        out.append(_back(dA, (n, n)))
+    assert np.array_equal(np.tril(out[0]), np.tril(out[1]))
+    L = np.linalg.cholesky(A)
+    assert np.linalg.norm(np.tril(out[1]) - L) <= 1e-13 * np.linalg.norm(L)
+
+
+def test_potrf_team_not_positive_definite(ctx):
+    import torch
+    n = 300
+    A = np.eye(n) * 2.0
+    A[201, 201] = -1.0
+    dA, pA = _colmajor(A)
+    torch.cuda.synchronize()
+    st, rep = run_single(ctx, t.Op(kind=t.OP_POTRF_L, m=n, n=n, ldc=n, parts=8, c=pA))
+    assert st == t.TTG_ENOTPD and rep.info == 202 and rep.error_task == 0
+
+
 def test_potrf_not_positive_definite(ctx):
     import torch
     n = 70

@@ -34,6 +34,29 @@ def test_fp64_direct_solve(ctx, b, nb, alpha, nrhs):
     p.close()
 
 
+@pytest.mark.parametrize("b,nb,upper,nrhs", [(100, 7, 150, 5), (70, 9, 139, 16), (200, 3, 260, 2)])
+def test_fp64_direct_solve_ragged_tiles(ctx, b, nb, upper, nrhs):
+    """Irregular tile sizes: strips that end mid-tile, tiles narrower than a strip."""
+    p = t.CholPlan(ctx, b, nb, kind=2, matrix=1, alpha=1e-2, seed=3, upper_block_size=upper)
+    A = p.input_A()
+    B = rhs(p.N, nrhs, seed=4)
+    st, rep, X = p.solve_host(B)
+    assert st == t.TTG_OK, t.strerror(st)
+    assert rep.bwd_err <= 1e-14 and bwd_err(A, X, B) <= 1e-14
+    p.close()
+
+
+def test_mixed_ragged_tiles_fp32_updates(ctx):
+    p = t.CholPlan(ctx, 90, 8, kind=2, matrix=1, alpha=1e-4, seed=5, upper_block_size=170, precision=t.PREC_MIXED,
+                   mixed_kind=1)
+    A = p.input_A()
+    B = rhs(p.N, 7, seed=6)
+    st, rep, X = p.solve_host(B)
+    assert st == t.TTG_OK, t.strerror(st)
+    assert bwd_err(A, X, B) <= BWD
+    p.close()
+
+
 def test_mixed_factor_is_fp32_accurate(ctx):
     p = t.CholPlan(ctx, 64, 8, kind=2, matrix=1, alpha=1.0, seed=0, precision=t.PREC_MIXED, mixed_kind=1)
     st, rep = p.factor()
