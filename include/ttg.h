@@ -148,6 +148,17 @@ ttg_status ttg_task_record(ttg_ctx* ctx, int32_t* h_runs, int32_t* h_final_count
  * global timer relative to the earliest start, and the worker (block) id. */
 ttg_status ttg_trace(ttg_ctx* ctx, int64_t* h_start_ns, int64_t* h_end_ns, int32_t* h_worker);
 
+/* Extension: priorities for a graph from the longest path (in estimated
+ * device time: flops over the per-block rate of each task kind, shared by the
+ * task's parts) from each task to the end of the graph.  out[n_tasks]; higher
+ * runs first, as ttg_graph_desc.priority.  TTG_EINVAL for a cyclic graph. */
+ttg_status ttg_critical_path_priority(const ttg_graph_desc* g, double* out);
+
+/* Per-task busy time of the last run (opts.trace): the durations of all its
+ * parts added up, in ns.  A task shared by P blocks that ran together shows
+ * about P times its span. */
+ttg_status ttg_trace_busy(ttg_ctx* ctx, int64_t* h_busy_ns);
+
 /* Number of persistent workers the context launches. */
 int ttg_workers(const ttg_ctx* ctx);
 

@@ -28,7 +28,9 @@ typedef struct ttg_chol_args {
     int32_t verb;             /* --verb                                            */
     int32_t block_size;       /* --block_size                                      */
     int32_t num_blocks;       /* --num_blocks                                      */
-    int32_t kind;             /* --kind: 0 none, 1 row, 2 critical path, 3 cp+row   */
+    int32_t kind;             /* --kind: 0 none, 1 row, 2 critical path, 3 cp+row;
+                                 4 (extension): longest remaining path in
+                                 estimated device time (ttg_critical_path_priority) */
     int32_t accumulate;       /* --accumulate                                      */
     int32_t upper_block_size; /* --upper_block_size (-1 = block_size)              */
     int32_t matrix;           /* 0: 1/((i-j)^2+1) (the miniapp's); 1: G·Gᵀ/N + αI    */
@@ -94,6 +96,13 @@ int32_t ttg_chol_plan_remedy(const ttg_chol_plan* plan);
 
 /* Per-kind device busy time (ms) of the last run (needs ctx trace). */
 ttg_status ttg_chol_plan_kind_times(ttg_chol_plan* plan, double* potrf_ms, double* trsm_ms, double* gemm_ms, double* accu_ms);
+/* Per-task record of the last factorisation run on a context created with
+ * opts.trace: one CSV line "name,start_ns,end_ns,worker,busy_ns" per device
+ * task: the task name of the captured Taskflow (e.g. "POTRF_3"), first start
+ * and release times relative to the earliest start, the releasing worker, and
+ * the task's part durations added up.  The timeline view of the reference's Logger output
+ * (tasktorrent/src/util.hpp Logger, written by 2d_cholesky with -log). */
+ttg_status ttg_chol_plan_trace_dump(ttg_chol_plan* plan, const char* path);
 
 /* ------------------------------------------------------------------ solve */
 
@@ -120,8 +129,9 @@ typedef struct ttg_solve_report {
     double anorm_inf;   /* ‖A‖∞                                                        */
     double factor_ms;   /* factorisation (device events; 0 for ttg_chol_plan_solve)     */
     double solve_ms;    /* solve and refinement (host clock)                           */
-    int32_t remedy;     /* mixed factor: 0 BF16 updates, 1 BF16 with a diagonal shift,
-                           2 FP32 updates (after the BF16 factor lost definiteness)    */
+    int32_t remedy;     /* mixed factor: 0 BF16 updates; after a loss of definiteness
+                           2 FP32 updates, 3 FP32 updates on A + 16·2^-24·diag(A),
+                           1 BF16 updates on A + 8·2^-8·diag(A)                      */
 } ttg_solve_report;
 
 /* d_B, d_X: device N×nrhs column-major (ld N). */

@@ -94,6 +94,8 @@ SIGNATURES = {
     "ttg_run": (_STATUS, [_P, _P, ctypes.POINTER(Report)]),
     "ttg_task_record": (_STATUS, [_P, _P, _P]),
     "ttg_trace": (_STATUS, [_P, _P, _P, _P]),
+    "ttg_trace_busy": (_STATUS, [_P, _P]),
+    "ttg_critical_path_priority": (_STATUS, [_P, _P]),
     "ttg_workers": (ctypes.c_int, [_P]),
     "ttg_graph_generation": (ctypes.c_uint64, [_P]),
     "ttg_gen_gram_tiles": (_STATUS, [_P, _I32, _P, _I32, ctypes.c_double, ctypes.c_uint32, _P, _P]),
@@ -121,6 +123,7 @@ SIGNATURES = {
     "ttg_chol_plan_tiles": (_P, [_P, _P]),
     "ttg_chol_plan_dump_dag": (_STATUS, [_P, ctypes.c_char_p]),
     "ttg_chol_plan_kind_times": (_STATUS, [_P, _P, _P, _P, _P]),
+    "ttg_chol_plan_trace_dump": (_STATUS, [_P, ctypes.c_char_p]),
     "ttg_chol_plan_remedy": (ctypes.c_int32, [_P]),
     "ttg_chol_dag_dump": (_STATUS, [ctypes.POINTER(CholArgs), ctypes.c_char_p]),
     "ttg_gemm_dag_dump": (_STATUS, [ctypes.POINTER(GemmArgs), ctypes.c_char_p]),
@@ -233,6 +236,25 @@ class Context:
         check(lib().ttg_trace(self.h, _ptr(s), _ptr(e), _ptr(w)), "ttg_trace")
         return s, e, w
 
+    def trace_busy(self, n):
+        b = np.zeros(n, dtype=np.int64)
+        check(lib().ttg_trace_busy(self.h, _ptr(b)), "ttg_trace_busy")
+        return b
+
+
+def critical_path_priority(ops, succ_ptr, succ_idx):
+    """Longest remaining path (estimated device µs) of every task of a graph
+    (host computation, no device needed).  Returns (status, priorities)."""
+    n = len(ops)
+    ops_arr = (Op * max(1, n))(*ops)
+    sp = np.ascontiguousarray(succ_ptr, dtype=np.int64)
+    si = np.ascontiguousarray(succ_idx if len(succ_idx) else [0], dtype=np.int32)
+    g = GraphDesc(n, ops_arr, None, None, None, sp.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                  si.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
+    out = np.zeros(max(1, n), dtype=np.float64)
+    st = lib().ttg_critical_path_priority(ctypes.byref(g), _ptr(out))
+    return st, out[:n]
+
 
 def dag_edges_from_lists(n, succ_lists):
     ptr = np.zeros(n + 1, dtype=np.int64)
@@ -336,6 +358,10 @@ class CholPlan:
         else:
             st = lib().ttg_chol_solve_host(self.h, _ptr(B), _ptr(X), ctypes.byref(o), ctypes.byref(rep), None)
         return st, rep, X
+
+    def trace_dump(self, path):
+        """Per-task timeline of the last run (context created with trace=True)."""
+        check(lib().ttg_chol_plan_trace_dump(self.h, path.encode()), "ttg_chol_plan_trace_dump")
 
     def kind_times(self):
         v = [ctypes.c_double() for _ in range(4)]

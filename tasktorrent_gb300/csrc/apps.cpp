@@ -86,7 +86,9 @@ static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry, bool tc, std::uni
     const ttg_chol_args& a = P->args;
     const int nb = P->nb, n_threads = a.n_threads;
     const bool accumulate = a.accumulate != 0;
-    const int pk = a.kind;
+    // kind 4 (extension): capture with the kind-3 priorities, then replace
+    // them by the longest remaining path of each device task.
+    const int pk = a.kind == 4 ? 3 : a.kind;
     const bool mixed = a.precision == TTG_PREC_MIXED;
     auto block = [P](int i, int j) { return P->tiles + P->off[i + (size_t)j * P->nb]; };
     auto lda = [P](int i) { return std::max(1, P->bs[i]); };
@@ -131,6 +133,7 @@ static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry, bool tc, std::uni
     }
 
     tp_out.reset(new Threadpool_shared(n_threads, a.verb, "Wk_Chol_0_"));
+    tp_out->set_critical_path_priority(a.kind == 4);
     Threadpool_shared& tp = *tp_out;
     if (!dry) tp.set_context(P->ctx);
     Taskflow<int> potrf(&tp, a.verb);
@@ -390,8 +393,7 @@ extern "C" ttg_status ttg_chol_plan_factor(ttg_chol_plan* P, void* stream, ttg_r
     return chol_factor_from(P, stream, rep, 0);
 }
 
-// Factorisation starting at attempt `first_attempt` of the mixed chain
-// (0 BF16, 1 BF16 + shift, 2 FP32 updates).
+// Factorisation starting at attempt `first_attempt` of the mixed chain.
 static ttg_status chol_factor_from(ttg_chol_plan* P, void* stream, ttg_report* rep, size_t first_attempt) {
     if (!P) return TTG_EINVAL;
     TTG_CUDA_CHECK(cudaSetDevice(P->ctx->device));
@@ -402,10 +404,13 @@ static ttg_status chol_factor_from(ttg_chol_plan* P, void* stream, ttg_report* r
         return s;
     }
     // Mixed: BF16 tensor-core updates when available.  A trailing diagonal
-    // block that loses positive definiteness (TTG_ENOTPD) is handled by a
-    // retry with a relative diagonal shift of a few BF16 units, then by FP32
-    // updates; iterative refinement always solves the unshifted system.
-    // Retries start from the restored input (a failed run overwrote it).
+    // block that loses positive definiteness (TTG_ENOTPD) means the update
+    // precision is too low for the matrix's conditioning (BF16 rounding of
+    // the panels perturbs A by about 2^-9·‖A‖): retry with FP32 updates, then
+    // FP32 updates on A + 16·2^-24·diag(A), and last BF16 updates on A +
+    // 8·2^-8·diag(A).  A shifted factor only preconditions: refinement always
+    // solves the unshifted system.  Retries start from the restored input (a
+    // failed run overwrote it).
     const bool tc = ttg_mixed_has_tc(P->mixed);
     struct Attempt {
         Threadpool_shared* tp;
@@ -414,13 +419,11 @@ static ttg_status chol_factor_from(ttg_chol_plan* P, void* stream, ttg_report* r
         int remedy;
     };
     std::vector<Attempt> plan;
-    if (tc) {
-        plan.push_back({P->tp.get(), 0.0, true, 0});
-        plan.push_back({P->tp.get(), 8.0 * 0.00390625, true, 1});
-        plan.push_back({P->tp32.get(), 0.0, false, 2});
-    } else {
-        plan.push_back({P->tp.get(), 0.0, false, 0});
-    }
+    Threadpool_shared* tp32 = tc ? P->tp32.get() : P->tp.get();
+    if (tc) plan.push_back({P->tp.get(), 0.0, true, 0});
+    plan.push_back({tp32, 0.0, false, 2});
+    plan.push_back({tp32, 16.0 * 5.9604644775390625e-08, false, 3});
+    if (tc) plan.push_back({P->tp.get(), 8.0 * 0.00390625, true, 1});
     ttg_status s = TTG_OK;
     float total_ms = 0.f;
     for (size_t a = std::min(first_attempt, plan.size() - 1); a < plan.size(); ++a) {
@@ -556,31 +559,10 @@ extern "C" ttg_status ttg_chol_posv(ttg_chol_plan* P, const double* d_B, double*
     ttg_report fr{};
     st = ttg_chol_plan_factor(P, stream, &fr);
     if (st != TTG_OK) return st;
-    float factor_ms = fr.elapsed_ms;
-    double solve_ms = 0.0;
-    if (P->mixed && P->remedy == 1) {
-        // A shifted factor is a weaker preconditioner: give refinement a few
-        // steps, and if it stalls refactor with FP32 updates and start over.
-        ttg_solve_opts quick = *o;
-        quick.max_outer = std::min(o->max_outer > 0 ? o->max_outer : 10, 3);
-        ttg_solve_report r1{};
-        st = ttg_chol_plan_solve(P, d_B, d_X, &quick, &r1, stream);
-        solve_ms += r1.solve_ms;
-        if (st != TTG_ENOCONV) {
-            r1.factor_ms = factor_ms;
-            if (rep) *rep = r1;
-            return st;
-        }
-        st = ttg_chol_plan_restore(P, stream);
-        if (st != TTG_OK) return st;
-        st = chol_factor_from(P, stream, &fr, 2);
-        if (st != TTG_OK) return st;
-        factor_ms += fr.elapsed_ms;
-    }
+    const float factor_ms = fr.elapsed_ms;
     ttg_solve_report r{};
     st = ttg_chol_plan_solve(P, d_B, d_X, o, &r, stream);
     r.factor_ms = factor_ms;
-    r.solve_ms += solve_ms;
     if (rep) *rep = r;
     return st;
 }
@@ -650,6 +632,25 @@ extern "C" ttg_status ttg_chol_plan_kind_times(ttg_chol_plan* P, double* potrf_m
     if (trsm_ms) *trsm_ms = t[1];
     if (gemm_ms) *gemm_ms = t[2];
     if (accu_ms) *accu_ms = t[3];
+    return TTG_OK;
+}
+
+extern "C" ttg_status ttg_chol_plan_trace_dump(ttg_chol_plan* P, const char* path) {
+    if (!P || !path) return TTG_EINVAL;
+    const auto& nodes = P->tp->device_task_nodes();
+    const int nd = (int)nodes.size();
+    std::vector<int64_t> s(nd), e(nd), busy(nd);
+    std::vector<int32_t> w(nd);
+    ttg_status st = ttg_trace(P->ctx, s.data(), e.data(), w.data());
+    if (st == TTG_OK) st = ttg_trace_busy(P->ctx, busy.data());
+    if (st != TTG_OK) return st;
+    FILE* f = fopen(path, "w");
+    if (!f) return TTG_EINVAL;
+    fprintf(f, "name,start_ns,end_ns,worker,busy_ns\n");
+    for (int d = 0; d < nd; ++d)
+        fprintf(f, "%s,%lld,%lld,%d,%lld\n", P->tp->node_name(nodes[d]).c_str(), (long long)s[d], (long long)e[d], w[d],
+                (long long)busy[d]);
+    fclose(f);
     return TTG_OK;
 }
 

@@ -23,7 +23,13 @@
 
 namespace ttg {
 
-constexpr int kMaxLevels = 32;
+// Priority levels: kMaxLevels FIFO queues, scanned 32 at a time by the lanes
+// of warp 0 (kLevelGroups loads per lane, issued together).
+constexpr int kMaxLevels = 128;
+constexpr int kLevelGroups = kMaxLevels / 32;
+// Trace words per task: first-part start, release time, releasing worker,
+// summed part durations (ns of the global timer).
+constexpr int kTraceWords = 4;
 // Counter words per team task (the POTRF tasks shared by several blocks).
 constexpr int kTeamStride = 256;
 
@@ -55,7 +61,7 @@ struct ExecParams {
     int* err;               // first error status
     int* err_task;
     int* err_info;
-    long long* trace;       // [3 * n_tasks] start, end, worker; or null
+    long long* trace;       // [kTraceWords * n_tasks] start, end, worker, busy; or null
     long long timeout_ns;
     int* team_ctr;          // kTeamStride words per team task, zero at launch; or null
     const int* team_slot;   // per task: its team counter block, -1 if none; or null
@@ -124,22 +130,37 @@ __device__ inline int claim_task(const ExecParams& p) {
                 return task;
             }
         }
-        int h = 0, t = 0;
-        if (lane < p.n_levels) {
-            h = ld_volatile(p.q_head + lane * 32);
-            t = ld_volatile(p.q_tail + lane * 32);
+        int hs[kLevelGroups], ts[kLevelGroups];
+#pragma unroll
+        for (int g = 0; g < kLevelGroups; ++g) {
+            const int l = g * 32 + lane;
+            hs[g] = ts[g] = 0;
+            if (l < p.n_levels) {
+                hs[g] = ld_volatile(p.q_head + l * 32);
+                ts[g] = ld_volatile(p.q_tail + l * 32);
+            }
         }
-        const unsigned mask = __ballot_sync(0xffffffffu, lane < p.n_levels && h < t);
+        unsigned mask = 0;
+        int grp = 0, h = 0;
+#pragma unroll
+        for (int g = kLevelGroups - 1; g >= 0; --g) {
+            const unsigned m = __ballot_sync(0xffffffffu, g * 32 + lane < p.n_levels && hs[g] < ts[g]);
+            if (m) {
+                mask = m;
+                grp = g;
+                h = hs[g];
+            }
+        }
         if (mask) {
-            const int lvl = __ffs(mask) - 1;
+            const int lvl = grp * 32 + __ffs(mask) - 1;
             int got = -1;
-            if (lane == lvl) {
+            if (lane == (lvl & 31)) {
                 if (atomicCAS(p.q_head + lvl * 32, h, h + 1) == h) {
                     got = wait_slot(p, p.qbuf + p.q_off[lvl] + h);
                     if (got < 0) got = -2;
                 }
             }
-            got = __shfl_sync(0xffffffffu, got, lvl);
+            got = __shfl_sync(0xffffffffu, got, lvl & 31);
             if (got == -2) return -1;
             if (got >= 0) {
                 __threadfence();
@@ -219,22 +240,30 @@ __device__ inline void fulfil_successors(const ExecParams& p, int t) {
     }
 }
 
-// The persistent kernel body: `RunOp(op, part, parts, smem, team)` runs one
-// part of a tile task on the whole block and returns 0 or an error info (POTRF
-// failing column); team is the task's team counter block or null.  The block that finishes the last part of a task fulfils
-// its successors.
+// The persistent kernel body: `RunOp(op, part, parts, smem, team, fin)` runs
+// one part of a tile task on the whole block and returns 0 or an error info
+// (POTRF failing column); team is the task's team counter block or null.  The
+// block that finishes the last part of a task fulfils its successors — except
+// for team tasks, whose parts set *fin (shared, -1 on entry) to 1 in the block
+// that completed the work and to 0 elsewhere: that block fulfils at once, and
+// parts that start later find nothing left to do.
 template <class RunOp>
 __device__ void executor_loop(const ExecParams& p, double* smem, RunOp run_op) {
-    __shared__ int s_task, s_part, s_info, s_last;
+    __shared__ int s_task, s_part, s_info, s_last, s_fin;
+    long long t_part = 0;  // thread 0: start of the current part (trace)
     for (;;) {
         if (threadIdx.x < 32) {
             const int t = claim_task(p);
             if (threadIdx.x == 0) {
                 s_task = t;
+                s_fin = -1;
                 if (t >= 0) {
                     const int part = atomicAdd(p.part_next + t, 1);
                     s_part = part;
-                    if (part == 0 && p.trace) p.trace[3 * (size_t)t] = globaltimer();
+                    if (p.trace) {
+                        t_part = globaltimer();
+                        if (part == 0) p.trace[kTraceWords * (size_t)t] = t_part;
+                    }
                 }
             }
         }
@@ -248,22 +277,24 @@ __device__ void executor_loop(const ExecParams& p, double* smem, RunOp run_op) {
             const int slot = p.team_slot[t];
             if (slot >= 0) team = p.team_ctr + (size_t)slot * kTeamStride;
         }
-        const int info = run_op(op, s_part, nparts, smem, team);
+        const int info = run_op(op, s_part, nparts, smem, team, &s_fin);
         __syncthreads();
         if (threadIdx.x == 0) {
             s_info = info;
             __threadfence();  // release this part's writes (after bar.sync)
             const int finished = atomicAdd(p.part_done + t, 1);
-            s_last = finished == nparts - 1;
+            s_last = s_fin >= 0 ? s_fin == 1 : finished == nparts - 1;
             if (s_last) __threadfence();  // acquire the other parts' writes
+            if (p.trace) atomicAdd((unsigned long long*)(p.trace + kTraceWords * (size_t)t + 3),
+                                   (unsigned long long)(globaltimer() - t_part));
         }
         __syncwarp();
         if (threadIdx.x < 32) {
             if (threadIdx.x == 0 && s_info != 0) set_error(p, TTG_ENOTPD, t, s_info);
             if (s_last) {
                 if (threadIdx.x == 0 && p.trace) {
-                    p.trace[3 * (size_t)t + 1] = globaltimer();
-                    p.trace[3 * (size_t)t + 2] = blockIdx.x;
+                    p.trace[kTraceWords * (size_t)t + 1] = globaltimer();
+                    p.trace[kTraceWords * (size_t)t + 2] = blockIdx.x;
                 }
                 fulfil_successors(p, t);
             }

@@ -324,13 +324,19 @@ __device__ __forceinline__ int team_claim(const TeamCtx& tc, int ph) {
 }
 
 // Publish one finished item of phase ph (of `items`); the block that finishes
-// the last item advances the completed-phase marker.
-__device__ __forceinline__ void team_done(const TeamCtx& tc, int ph, int items) {
+// the last item advances the completed-phase marker.  Returns (on every
+// thread) whether this item completed the phase.
+__device__ __forceinline__ bool team_done(const TeamCtx& tc, int ph, int items) {
+    __shared__ int s_last;
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
-        if (atomicAdd(tc.ctr + 2 * ph + 1, 1) == items - 1) atomicMax(tc.ctr + kTeamCounters - 2, ph + 1);
+        const bool last = atomicAdd(tc.ctr + 2 * ph + 1, 1) == items - 1;
+        if (last) atomicMax(tc.ctr + kTeamCounters - 2, ph + 1);
+        s_last = last;
     }
+    __syncthreads();
+    return s_last != 0;
 }
 
 // Phases completed so far (the same value on all threads).
@@ -421,10 +427,15 @@ __device__ inline void team_syrk_block(int rest, int nb, const double* P, int ld
 // team_fits(n, W32 != nullptr).  With an FP32 source (W32 != nullptr) the
 // team first widens the lower triangle of W32 (ldw) into A and at the end
 // rounds the factor back into W32.  Returns 0, the 1-based failing column, or
-// -1 after a timeout.  The result is the same for any number of blocks: every
-// item computes the same arithmetic whoever runs it.
-__device__ inline int potrf_l_f64_team(int n, double* A, int lda, double* smem, const TeamCtx& tc, float* W32, int ldw) {
+// -1 after a timeout.  *finisher (shared) is set to 1 in the one block that
+// completed the factorisation (or found the failing column), else 0: that
+// block releases the task's successors at once, whether or not the other
+// parts of the team have run yet.  The result is the same for any number of
+// blocks: every item computes the same arithmetic whoever runs it.
+__device__ inline int potrf_l_f64_team(int n, double* A, int lda, double* smem, const TeamCtx& tc, float* W32, int ldw,
+                                       int* finisher) {
     double* Ls = smem + kBK * kBM + kBK * kBNP;
+    if (threadIdx.x == 0) *finisher = 0;
     int ph = 0;
     const int copy_items = (n + kTeamCopyRows - 1) / kTeamCopyRows;
     if (W32) {
@@ -445,11 +456,18 @@ __device__ inline int potrf_l_f64_team(int n, double* A, int lda, double* smem, 
         const int nb = min(kPanel, n - p);
         double* Dpp = A + p + (size_t)p * lda;
         if (team_claim(tc, ph) == 0) {
+            __shared__ int s_bad;
             if (threadIdx.x < 32) {
                 const int info = potrf_diag32_warp(Dpp, lda, nb);
-                if (threadIdx.x == 0 && info) atomicExch(tc.ctr + kTeamCounters - 1, p + info);
+                if (threadIdx.x == 0) {
+                    s_bad = info != 0;
+                    if (info) atomicExch(tc.ctr + kTeamCounters - 1, p + info);
+                }
             }
             team_done(tc, ph, 1);
+            // The factorisation ends here after a failure, or after the last
+            // panel when there is no FP32 copy to write.
+            if (threadIdx.x == 0 && (s_bad || (p + nb >= n && !W32))) *finisher = 1;
         }
         if (!team_wait(tc, ph, 1)) return -1;
         {
@@ -483,7 +501,7 @@ __device__ inline int potrf_l_f64_team(int n, double* A, int lda, double* smem, 
                 const int i = r0 + (int)(e % rows), j = (int)(e / rows);
                 if (i >= j) W32[i + (size_t)j * ldw] = (float)__ldcg(A + i + (size_t)j * lda);
             }
-            team_done(tc, ph, copy_items);
+            if (team_done(tc, ph, copy_items) && threadIdx.x == 0) *finisher = 1;
         }
         if (!team_wait(tc, ph, copy_items)) return -1;
     }

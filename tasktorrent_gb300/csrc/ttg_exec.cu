@@ -24,10 +24,12 @@ static_assert(kTeamCounters == kTeamStride, "team counter block size");
 
 // One part of an FP64 tile task on the whole block.  Returns POTRF's info (0 =
 // ok).  A POTRF with a team counter block is factored by all its parts.
-__device__ int run_op_f64(const ttg_op& op, int part, int parts, double* smem, int* team, int* err, long long limit_ns) {
+__device__ int run_op_f64(const ttg_op& op, int part, int parts, double* smem, int* team, int* fin, int* err,
+                          long long limit_ns) {
     switch (op.kind) {
         case TTG_OP_POTRF_L:
-            if (team) return potrf_l_f64_team(op.n, (double*)op.c, op.ldc, smem, TeamCtx{team, limit_ns, err}, nullptr, 0);
+            if (team)
+                return potrf_l_f64_team(op.n, (double*)op.c, op.ldc, smem, TeamCtx{team, limit_ns, err}, nullptr, 0, fin);
             return potrf_l_f64(op.n, (double*)op.c, op.ldc, smem);
         case TTG_OP_TRSM_RLTN:
             trsm_rltn_f64(op.m, op.n, op.alpha, (const double*)op.a, op.lda, (double*)op.c, op.ldc, smem, part, parts);
@@ -54,8 +56,8 @@ __device__ int run_op_f64(const ttg_op& op, int part, int parts, double* smem, i
 
 __global__ void __launch_bounds__(kThreads, 1) exec_kernel(ExecParams p) {
     extern __shared__ __align__(128) double smem_f64[];
-    executor_loop(p, smem_f64, [&](const ttg_op& op, int part, int parts, double* smem, int* team) {
-        return run_op_f64(op, part, parts, smem, team, p.err, p.timeout_ns);
+    executor_loop(p, smem_f64, [&](const ttg_op& op, int part, int parts, double* smem, int* team, int* fin) {
+        return run_op_f64(op, part, parts, smem, team, fin, p.err, p.timeout_ns);
     });
 }
 
@@ -291,6 +293,73 @@ int ttg_task_parts(const ttg_op& op, bool team) {
     return std::max(1, auto_parts);
 }
 
+// Estimated duration (µs) of a task on this executor: its flops over the
+// per-block rate of its kernel times the blocks that share it, plus a fixed
+// cost for claiming and releasing it.
+static double task_cost_us(const ttg_op& op) {
+    const double m = op.m, n = op.n, k = op.k;
+    const int parts = ttg_task_parts(op, true);
+    const bool mixed = op.prec == TTG_PREC_MIXED;
+    double flops = 0.0, rate = 1.0, par = parts;  // rate in flops per µs per block
+    switch (op.kind) {
+        case TTG_OP_POTRF_L:
+            flops = n * n * n / 3.0;
+            rate = 4.0e3;
+            par = std::min(parts, 8) * 0.5 + 0.5;  // team phases are short and synchronised
+            break;
+        case TTG_OP_TRSM_RLTN:
+            flops = m * n * n;
+            rate = mixed ? 5.0e4 : 5.0e3;
+            break;
+        case TTG_OP_SYRK_LN:
+            flops = n * n * k;
+            rate = mixed ? (op.flags == 2 ? 3.0e6 : 2.0e5) : 7.5e3;
+            break;
+        case TTG_OP_GEMM_NT:
+        case TTG_OP_GEMM_NN:
+            flops = 2.0 * m * n * k;
+            rate = mixed ? (op.flags == 2 ? 3.0e6 : 2.0e5) : 7.5e3;
+            break;
+        case TTG_OP_GEADD:
+            flops = m * n;
+            rate = 5.0e4;
+            break;
+        default:
+            break;
+    }
+    return 2.0 + flops / (rate * std::max(1.0, par));
+}
+
+extern "C" ttg_status ttg_critical_path_priority(const ttg_graph_desc* gd, double* out) {
+    if (!gd || !out || gd->n_tasks < 0 || (gd->n_tasks > 0 && (!gd->ops || !gd->succ_ptr))) return TTG_EINVAL;
+    const int n = gd->n_tasks;
+    std::vector<int> indeg(n, 0);
+    for (int t = 0; t < n; ++t)
+        for (int64_t e = gd->succ_ptr[t]; e < gd->succ_ptr[t + 1]; ++e) {
+            const int s = gd->succ_idx[e];
+            if (s < 0 || s >= n) return TTG_EINVAL;
+            ++indeg[s];
+        }
+    // Kahn's order, then the longest remaining path in reverse order.
+    std::vector<int> order;
+    order.reserve(n);
+    for (int t = 0; t < n; ++t)
+        if (indeg[t] == 0) order.push_back(t);
+    for (size_t h = 0; h < order.size(); ++h) {
+        const int t = order[h];
+        for (int64_t e = gd->succ_ptr[t]; e < gd->succ_ptr[t + 1]; ++e)
+            if (--indeg[gd->succ_idx[e]] == 0) order.push_back(gd->succ_idx[e]);
+    }
+    if ((int)order.size() != n) return TTG_EINVAL;  // a cycle
+    for (int h = n - 1; h >= 0; --h) {
+        const int t = order[h];
+        double best = 0.0;
+        for (int64_t e = gd->succ_ptr[t]; e < gd->succ_ptr[t + 1]; ++e) best = std::max(best, out[gd->succ_idx[e]]);
+        out[t] = task_cost_us(gd->ops[t]) + best;
+    }
+    return TTG_OK;
+}
+
 // Priority levels: distinct priorities ranked from high to low; more than
 // kMaxLevels distinct values are split into kMaxLevels equal-count groups.
 static void assign_levels(int n, const double* prio, const std::vector<uint8_t>& runnable, std::vector<uint8_t>& level,
@@ -459,7 +528,7 @@ extern "C" ttg_status ttg_graph_upload(ttg_ctx* c, const ttg_graph_desc* gd) {
     ALLOC(bq_off, W + 1);
     ALLOC(bq_head, W * 2);             // head + initial tail
     ALLOC(bq_tail, W);
-    if (c->trace) ALLOC(trace, 3 * (size_t)std::max(1, n));
+    if (c->trace) ALLOC(trace, kTraceWords * (size_t)std::max(1, n));
     ALLOC(team_slot, n);
     if (n_team) ALLOC(team_ctr, (size_t)n_team * kTeamStride);
     g.n_team = n_team;
@@ -500,7 +569,7 @@ ttg_status ttg_reset_state(ttg_ctx* c, cudaStream_t s) {
     TTG_CUDA_TRY(cudaMemsetAsync(g.bq_head, 0, sizeof(int) * W, s));
     TTG_CUDA_TRY(cudaMemcpyAsync(g.bq_tail, g.bq_head + W, sizeof(int) * W, cudaMemcpyDeviceToDevice, s));
     TTG_CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(int) * 8, s));
-    if (g.trace) TTG_CUDA_TRY(cudaMemsetAsync(g.trace, 0, sizeof(long long) * 3 * std::max(1, n), s));
+    if (g.trace) TTG_CUDA_TRY(cudaMemsetAsync(g.trace, 0, sizeof(long long) * kTraceWords * std::max(1, n), s));
     if (g.n_team) TTG_CUDA_TRY(cudaMemsetAsync(g.team_ctr, 0, sizeof(int) * (size_t)g.n_team * kTeamStride, s));
     return TTG_OK;
 }
@@ -617,25 +686,44 @@ extern "C" ttg_status ttg_task_record(ttg_ctx* c, int32_t* h_runs, int32_t* h_fi
     return TTG_OK;
 }
 
-extern "C" ttg_status ttg_trace(ttg_ctx* c, int64_t* h_start, int64_t* h_end, int32_t* h_worker) {
+static ttg_status read_trace(ttg_ctx* c, std::vector<long long>& tr, long long* t0) {
     if (!c || !c->uploaded || !c->g.trace) return TTG_ESTATE;
     TTG_CUDA_TRY(cudaSetDevice(c->device));
     const int n = c->g.n_tasks;
-    std::vector<long long> tr(3 * (size_t)n);
-    TTG_CUDA_TRY(cudaMemcpy(tr.data(), c->g.trace, sizeof(long long) * 3 * n, cudaMemcpyDeviceToHost));
-    long long t0 = 0;
+    tr.resize(kTraceWords * (size_t)n);
+    TTG_CUDA_TRY(cudaMemcpy(tr.data(), c->g.trace, sizeof(long long) * kTraceWords * n, cudaMemcpyDeviceToHost));
     bool any = false;
+    *t0 = 0;
     for (int t = 0; t < n; ++t)
-        if (tr[3 * t] > 0 && (!any || tr[3 * t] < t0)) {
-            t0 = tr[3 * t];
+        if (tr[kTraceWords * t] > 0 && (!any || tr[kTraceWords * t] < *t0)) {
+            *t0 = tr[kTraceWords * t];
             any = true;
         }
+    return TTG_OK;
+}
+
+extern "C" ttg_status ttg_trace(ttg_ctx* c, int64_t* h_start, int64_t* h_end, int32_t* h_worker) {
+    std::vector<long long> tr;
+    long long t0;
+    ttg_status st = read_trace(c, tr, &t0);
+    if (st != TTG_OK) return st;
+    const int n = c->g.n_tasks;
     for (int t = 0; t < n; ++t) {
-        const bool ran = tr[3 * t] > 0;
-        if (h_start) h_start[t] = ran ? tr[3 * t] - t0 : -1;
-        if (h_end) h_end[t] = ran ? tr[3 * t + 1] - t0 : -1;
-        if (h_worker) h_worker[t] = ran ? (int32_t)tr[3 * t + 2] : -1;
+        const long long* w = tr.data() + kTraceWords * (size_t)t;
+        const bool ran = w[0] > 0;
+        if (h_start) h_start[t] = ran ? w[0] - t0 : -1;
+        if (h_end) h_end[t] = ran ? w[1] - t0 : -1;
+        if (h_worker) h_worker[t] = ran ? (int32_t)w[2] : -1;
     }
+    return TTG_OK;
+}
+
+extern "C" ttg_status ttg_trace_busy(ttg_ctx* c, int64_t* h_busy_ns) {
+    std::vector<long long> tr;
+    long long t0;
+    ttg_status st = read_trace(c, tr, &t0);
+    if (st != TTG_OK) return st;
+    for (int t = 0; t < c->g.n_tasks; ++t) h_busy_ns[t] = tr[kTraceWords * (size_t)t + 3];
     return TTG_OK;
 }
 

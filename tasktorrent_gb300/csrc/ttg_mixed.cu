@@ -54,12 +54,13 @@ __device__ inline void rows_to_bf16(const float* W, int ldw, int r0, int r1, int
     }
 }
 
-__device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem, int* team, tc::TcShared* tsh, uint8_t* ring,
-                             const CUtensorMap* tmap, int* err, long long limit_ns) {
+__device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem, int* team, int* fin, tc::TcShared* tsh,
+                             uint8_t* ring, const CUtensorMap* tmap, int* err, long long limit_ns) {
     if (op.prec == TTG_PREC_F64) {
         switch (op.kind) {
             case TTG_OP_POTRF_L:
-                if (team) return potrf_l_f64_team(op.n, (double*)op.c, op.ldc, smem, TeamCtx{team, limit_ns, err}, nullptr, 0);
+                if (team)
+                    return potrf_l_f64_team(op.n, (double*)op.c, op.ldc, smem, TeamCtx{team, limit_ns, err}, nullptr, 0, fin);
                 return potrf_l_f64(op.n, (double*)op.c, op.ldc, smem);
             case TTG_OP_TRSM_RLTN:
                 trsm_rltn_f64(op.m, op.n, op.alpha, (const double*)op.a, op.lda, (double*)op.c, op.ldc, smem, part, parts);
@@ -90,7 +91,7 @@ __device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem,
             const int n = op.n;
             float* W = (float*)op.c;
             double* D = (double*)op.aux;
-            if (team) return potrf_l_f64_team(n, D, n, smem, TeamCtx{team, limit_ns, err}, W, op.ldc);
+            if (team) return potrf_l_f64_team(n, D, n, smem, TeamCtx{team, limit_ns, err}, W, op.ldc, fin);
             for (long e = threadIdx.x; e < (long)n * n; e += kThreads) {
                 const int i = (int)(e % n), j = (int)(e / n);
                 D[e] = i >= j ? (double)ldcg(W + i + (size_t)j * op.ldc) : 0.0;
@@ -159,8 +160,8 @@ __global__ void __launch_bounds__(kThreads, 1) exec_kernel_mixed(ExecParams p, c
     uint8_t* ring = reinterpret_cast<uint8_t*>(((uintptr_t)smem_mx + 1023) & ~(uintptr_t)1023);
     if (g.has_tc) tc::tc_setup(&tsh);
     const CUtensorMap* tmap = &g.tmap;
-    executor_loop(p, smem_mx, [&](const ttg_op& op, int part, int parts, double* smem, int* team) {
-        return run_op_mixed(op, part, parts, smem, team, &tsh, ring, tmap, p.err, p.timeout_ns);
+    executor_loop(p, smem_mx, [&](const ttg_op& op, int part, int parts, double* smem, int* team, int* fin) {
+        return run_op_mixed(op, part, parts, smem, team, fin, &tsh, ring, tmap, p.err, p.timeout_ns);
     });
     if (g.has_tc) tc::tc_teardown(&tsh, p.timeout_ns);
 }

@@ -111,7 +111,7 @@ __device__ int run_op_f64_noalloc(const ttg_op& op, int part, int parts, double*
 __global__ void __launch_bounds__(ttg::kThreads, 1) exec_kernel_noalloc(ttg::ExecParams p, RunStatus* st) {
     extern __shared__ __align__(128) double smem_na[];
     if (threadIdx.x == 0) atomicMin(&st->start, (unsigned long long)ttg::globaltimer());
-    ttg::executor_loop(p, smem_na, [](const ttg_op& op, int part, int parts, double* smem, int*) {
+    ttg::executor_loop(p, smem_na, [](const ttg_op& op, int part, int parts, double* smem, int*, int*) {
         return run_op_f64_noalloc(op, part, parts, smem);
     });
     if (threadIdx.x == 0) atomicMax(&st->end, (unsigned long long)ttg::globaltimer());

@@ -198,6 +198,9 @@ class Threadpool_shared {
         return ctx_;
     }
     void set_trace(bool on) { trace_ = on ? 1 : 0; }
+    // Extension: replace the captured priorities by the longest remaining
+    // path of each device task (ttg_critical_path_priority).
+    void set_critical_path_priority(bool on) { cp_prio_ = on; }
     const ttg_report& report() const { return report_; }
     ttg_status status() const { return report_.status; }
     double capture_seconds() const { return capture_s_; }
@@ -399,6 +402,15 @@ class Threadpool_shared {
         g_bind_ = std::move(bind);
         g_ptr_ = std::move(ptr);
         g_idx_ = std::move(idx);
+        if (cp_prio_) {
+            ttg_graph_desc g{};
+            g.n_tasks = (int32_t)g_ops_.size();
+            g.ops = g_ops_.data();
+            g.succ_ptr = g_ptr_.data();
+            g.succ_idx = g_idx_.data();
+            if (ttg_critical_path_priority(&g, g_prio_.data()) != TTG_OK)
+                throw std::runtime_error("Threadpool_shared: critical-path priorities failed");
+        }
         upload();
         uploaded_ = true;
     }
@@ -476,6 +488,7 @@ class Threadpool_shared {
     std::vector<ttg_op> g_ops_;
     std::vector<int32_t> g_init_, g_bind_, g_idx_;
     std::vector<double> g_prio_;
+    bool cp_prio_ = false;
     std::vector<int64_t> g_ptr_;
     uint64_t graph_gen_ = 0;
 };

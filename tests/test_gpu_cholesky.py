@@ -96,6 +96,23 @@ def test_repeated_factorisations_are_identical(ctx):
     p.close()
 
 
+@pytest.mark.parametrize("prec,mk", [(None, 0), ("mixed", 1), ("mixed", 0)])
+def test_critical_path_priorities_same_factor(ctx, tmp_path, prec, mk):
+    """Priority kind 4 (longest remaining path) changes the order, not the DAG or the bits."""
+    kw = dict(precision=t.PREC_MIXED, mixed_kind=mk) if prec else {}
+    outs, dags = [], []
+    for kind in (2, 4):
+        p = t.CholPlan(ctx, 128, 6, kind=kind, matrix=1, alpha=1.0, seed=2, **kw)
+        st, _ = p.factor()
+        assert st == t.TTG_OK
+        outs.append(p.factor_L())
+        p.dump_dag(str(tmp_path / ("k%d" % kind)))
+        dags.append((tmp_path / ("k%d.tasks.csv" % kind)).read_text() + (tmp_path / ("k%d.edges.csv" % kind)).read_text())
+        p.close()
+    assert np.array_equal(outs[0], outs[1])
+    assert dags[0] == dags[1]
+
+
 def test_not_positive_definite_is_reported(ctx):
     p = t.CholPlan(ctx, 16, 4, matrix=1, alpha=-1.0, seed=0)
     st, rep = p.factor()
