@@ -48,6 +48,10 @@ enum {
 
 const char* ttg_strerror(ttg_status s);
 
+/* Text of the last CUDA runtime error behind a TTG_ECUDA / TTG_ENOMEM status
+ * (the failing call and its source location), or an empty string. */
+const char* ttg_last_cuda_error(void);
+
 /* ------------------------------------------------------------------ tasks */
 
 /* Tile operation of one task.  The reference task bodies call BLAS/LAPACK on
@@ -60,7 +64,11 @@ enum {
     TTG_OP_SYRK_LN = 3,   /* lower(c[n×n]) <- alpha a·aᵀ + beta c, a[n×k] (cblas_dsyrk L,N) */
     TTG_OP_GEMM_NT = 4,   /* c[m×n] <- alpha a·bᵀ + beta c, a[m×k], b[n×k] (cblas_dgemm N,T) */
     TTG_OP_GEMM_NN = 5,   /* c[m×n] <- alpha a·b + beta c, a[m×k], b[k×n]  (cblas_dgemm N,N) */
-    TTG_OP_GEADD = 6      /* c[m×n] <- alpha a + beta c  (tile accumulation)          */
+    TTG_OP_GEADD = 6,     /* c[m×n] <- alpha a + beta c  (tile accumulation)          */
+    TTG_OP_TRSM_RLNN = 7, /* c[m×n] <- alpha c · a⁻¹, a[n×n] lower non-unit (cblas_dtrsm R,L,N,N):
+                             the backward step of a block solve with row-vector RHS */
+    TTG_OP_CONVERT = 8    /* c[m×n] <- alpha a + beta c with a and c of either precision:
+                             flags bit 0 = a is float, bit 1 = c is float (prec F64) */
 };
 
 /* Arithmetic of one task. */
@@ -161,6 +169,12 @@ ttg_status ttg_trace_busy(ttg_ctx* ctx, int64_t* h_busy_ns);
 
 /* Number of persistent workers the context launches. */
 int ttg_workers(const ttg_ctx* ctx);
+
+/* Extension: change the number of persistent blocks of a context (1 ..
+ * the resident maximum; 0 = the maximum).  A change drops the uploaded graph
+ * (its queues are laid out per worker): upload again before the next launch
+ * (the graph generation changes, so plans do so by themselves). */
+ttg_status ttg_set_workers(ttg_ctx* ctx, int32_t workers);
 
 /* Identifier of the graph currently uploaded to the context (changes with
  * every successful ttg_graph_upload): a host-side owner of a graph compares

@@ -17,7 +17,7 @@ BIN_DIR = os.path.join(HERE, "bin")
 # Status codes (include/ttg.h)
 TTG_OK, TTG_EINVAL, TTG_ECUDA, TTG_ETIMEOUT, TTG_EOVERCOUNT, TTG_ENOTPD, TTG_ENOMEM, TTG_ESTATE, TTG_EUNDERRUN, TTG_ENOCONV = range(10)
 # Tile operations
-OP_NOP, OP_POTRF_L, OP_TRSM_RLTN, OP_SYRK_LN, OP_GEMM_NT, OP_GEMM_NN, OP_GEADD = range(7)
+OP_NOP, OP_POTRF_L, OP_TRSM_RLTN, OP_SYRK_LN, OP_GEMM_NT, OP_GEMM_NN, OP_GEADD, OP_TRSM_RLNN, OP_CONVERT = range(9)
 PREC_F64, PREC_MIXED = 0, 1
 
 
@@ -86,6 +86,7 @@ _STATUS = ctypes.c_int
 SIGNATURES = {
     # include/ttg.h
     "ttg_strerror": (ctypes.c_char_p, [ctypes.c_int]),
+    "ttg_last_cuda_error": (ctypes.c_char_p, []),
     "ttg_create": (_STATUS, [ctypes.POINTER(_P), ctypes.POINTER(Opts)]),
     "ttg_destroy": (_STATUS, [_P]),
     "ttg_graph_upload": (_STATUS, [_P, ctypes.POINTER(GraphDesc)]),
@@ -97,6 +98,7 @@ SIGNATURES = {
     "ttg_trace_busy": (_STATUS, [_P, _P]),
     "ttg_critical_path_priority": (_STATUS, [_P, _P]),
     "ttg_workers": (ctypes.c_int, [_P]),
+    "ttg_set_workers": (_STATUS, [_P, _I32]),
     "ttg_graph_generation": (ctypes.c_uint64, [_P]),
     "ttg_gen_gram_tiles": (_STATUS, [_P, _I32, _P, _I32, ctypes.c_double, ctypes.c_uint32, _P, _P]),
     "ttg_gen_uniform": (_STATUS, [_P, ctypes.c_int64, ctypes.c_uint32, ctypes.c_uint32, _P, _P]),

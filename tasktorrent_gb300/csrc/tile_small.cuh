@@ -1,0 +1,178 @@
+// tile_small.cuh — row-vector forms of the tile operations, for the block
+// triangular solves of the batched path: the right-hand sides are kept as
+// m × N row blocks (m = number of right-hand sides, m <= kSmallM), so the
+// forward solve L y = b is y_iᵀ = (b_iᵀ − Σ_j y_jᵀ L_ijᵀ) L_ii⁻ᵀ and the
+// backward solve Lᵀ x = y is x_iᵀ = (y_iᵀ − Σ_j x_jᵀ L_ji) L_ii⁻¹: GEMM_NT,
+// TRSM_RLTN, GEMM_NN and TRSM_RLNN tasks with m rows.
+//
+// The 128×128-block kernels of tile_f64.cuh would spend a whole block row on
+// each of these few rows; here every thread owns output columns and the
+// block's threads share the k loop, so the work is the m·n·k the operation
+// needs.  T is double (FP64 tasks) or float (FP32 tasks of the mixed path).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "tile_f64.cuh"
+
+namespace ttg {
+
+constexpr int kSmallM = 16;
+constexpr int kSmallKC = 16;              // k rows staged per pass
+constexpr int kSmallBPad = kThreads + 1;  // staged B row (conflict-free stores)
+// Shared memory (elements of T) used by the small-m kernels.
+constexpr int kSmallSmem = kSmallKC * kSmallBPad + kSmallKC * kSmallM + kPanel * (kPanel + 1) + kPanel;
+
+// C[m×n] (columns [j0, j1)) <- alpha·A·op(B) + beta·C, m <= kSmallM; A is m×k
+// (lda).  op(B)(kk, j) = B[j + kk·ldb] (NT) or B[kk + j·ldb] (NN).  Thread t
+// owns columns j0 + t, j0 + t + kThreads, ...; k is staged kSmallKC rows at a
+// time through shared memory (coalesced loads for both layouts).
+template <class T, bool B_NN>
+__device__ void gemm_small_cols(int m, int j0, int j1, int k, T alpha, const T* A, int lda, const T* B, int ldb, T beta, T* C,
+                                int ldc, T* smem) {
+    T* sB = smem;                          // [kSmallKC][kSmallBPad]
+    T* sA = smem + kSmallKC * kSmallBPad;  // [kSmallKC][kSmallM]
+    for (int c0 = j0; c0 < j1; c0 += kThreads) {
+        const int cols = min(kThreads, j1 - c0);
+        const int j = c0 + threadIdx.x;
+        T acc[kSmallM];
+#pragma unroll
+        for (int q = 0; q < kSmallM; ++q) acc[q] = T(0);
+        for (int k0 = 0; k0 < k; k0 += kSmallKC) {
+            const int kc = min(kSmallKC, k - k0);
+            __syncthreads();
+            for (int e = threadIdx.x; e < kSmallKC * cols; e += kThreads) {
+                int kk, jj;
+                if (B_NN) {
+                    kk = e % kSmallKC;
+                    jj = e / kSmallKC;
+                } else {
+                    jj = e % cols;
+                    kk = e / cols;
+                }
+                T v = T(0);
+                if (kk < kc) v = B_NN ? ldcg(B + (k0 + kk) + (size_t)(c0 + jj) * ldb) : ldcg(B + (c0 + jj) + (size_t)(k0 + kk) * ldb);
+                sB[kk * kSmallBPad + jj] = v;
+            }
+            for (int e = threadIdx.x; e < kSmallKC * kSmallM; e += kThreads) {
+                const int q = e % kSmallM, kk = e / kSmallM;
+                sA[e] = (q < m && kk < kc) ? ldcg(A + q + (size_t)(k0 + kk) * lda) : T(0);
+            }
+            __syncthreads();
+            if (threadIdx.x < cols) {
+#pragma unroll
+                for (int kk = 0; kk < kSmallKC; ++kk) {
+                    const T b = sB[kk * kSmallBPad + threadIdx.x];
+#pragma unroll
+                    for (int q = 0; q < kSmallM; ++q)
+                        if (q < m) acc[q] = fma(sA[kk * kSmallM + q], b, acc[q]);
+                }
+            }
+        }
+        if (threadIdx.x < cols) {
+#pragma unroll
+            for (int q = 0; q < kSmallM; ++q) {
+                if (q >= m) break;
+                T* p = C + q + (size_t)j * ldc;
+                T v = alpha * acc[q];
+                if (beta != T(0)) v = fma(beta, ldcg(p), v);
+                *p = v;
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// The part `part` of `parts` of a small-m GEMM: a contiguous range of columns.
+template <class T, bool B_NN>
+__device__ inline void gemm_small_m(int m, int n, int k, T alpha, const T* A, int lda, const T* B, int ldb, T beta, T* C, int ldc,
+                                    T* smem, int part, int parts) {
+    const int per = (n + parts - 1) / parts;
+    const int j0 = min(n, part * per), j1 = min(n, j0 + per);
+    gemm_small_cols<T, B_NN>(m, j0, j1, k, alpha, A, lda, B, ldb, beta, C, ldc, smem);
+}
+
+// B[m×n] <- alpha·B·L⁻ᵀ (TRANS, cblas_dtrsm R,L,T,N) or alpha·B·L⁻¹ (cblas_dtrsm
+// R,L,N,N), L n×n lower non-unit, m <= kSmallM: forward (TRANS) or backward
+// substitution over 32-column panels.  Panel solve: warp w takes rows
+// w, w+8, ...; lane j is column j of the panel, and each solved column is
+// passed to the lanes that still need it by a shuffle.  The rest of the row
+// is then updated by a small-m GEMM with the solved panel.
+template <class T, bool TRANS>
+__device__ void trsm_small_m(int m, int n, T alpha, const T* L, int ldl, T* B, int ldb, T* smem) {
+    T* Ls = smem + kSmallKC * kSmallBPad + kSmallKC * kSmallM;  // [kPanel][kPanel+1]: Ls[c][l] = L(p+c, p+l)
+    T* invd = Ls + kPanel * (kPanel + 1);                      // 1 / L(p+c, p+c)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (alpha != T(1)) {
+        for (int e = threadIdx.x; e < m * n; e += kThreads) {
+            const int q = e % m, j = e / m;
+            B[q + (size_t)j * ldb] = alpha * ldcg(B + q + (size_t)j * ldb);
+        }
+    }
+    const int npan = (n + kPanel - 1) / kPanel;
+    for (int pi = 0; pi < npan; ++pi) {
+        const int p = (TRANS ? pi : npan - 1 - pi) * kPanel;
+        const int nb = min(kPanel, n - p);
+        __syncthreads();
+        load_panel_block<T>(L + p + (size_t)p * ldl, ldl, nb, Ls);
+        if (threadIdx.x < kPanel)
+            invd[threadIdx.x] = (int)threadIdx.x < nb ? T(1) / ldcg(L + (size_t)(p + threadIdx.x) * (ldl + 1)) : T(0);
+        __syncthreads();
+        for (int q = warp; q < m; q += kThreads / 32) {
+            T t = lane < nb ? ldcg(B + q + (size_t)(p + lane) * ldb) : T(0);
+            if (TRANS) {
+                for (int c = 0; c < nb; ++c) {
+                    const T x = __shfl_sync(0xffffffffu, t, c) * invd[c];
+                    if (lane == c) t = x;
+                    else if (lane > c) t = fma(-Ls[lane * (kPanel + 1) + c], x, t);
+                }
+            } else {
+                for (int c = nb - 1; c >= 0; --c) {
+                    const T x = __shfl_sync(0xffffffffu, t, c) * invd[c];
+                    if (lane == c) t = x;
+                    else if (lane < c) t = fma(-Ls[c * (kPanel + 1) + lane], x, t);
+                }
+            }
+            if (lane < nb) B[q + (size_t)(p + lane) * ldb] = t;
+        }
+        __syncthreads();
+        if (TRANS) {
+            // Columns right of the panel: B[:, p+nb:] -= X · L[p+nb:, p:p+nb]ᵀ.
+            if (p + nb < n)
+                gemm_small_cols<T, false>(m, 0, n - p - nb, nb, T(-1), B + (size_t)p * ldb, ldb, L + (p + nb) + (size_t)p * ldl,
+                                          ldl, T(1), B + (size_t)(p + nb) * ldb, ldb, smem);
+        } else {
+            // Columns left of the panel: B[:, :p] -= X · L[p:p+nb, :p].
+            if (p > 0) gemm_small_cols<T, true>(m, 0, p, nb, T(-1), B + (size_t)p * ldb, ldb, L + p, ldl, T(1), B, ldb, smem);
+        }
+    }
+    __syncthreads();
+}
+
+// Rows [r0, r1) of part `part` of a TRSM, as successive groups of kSmallM
+// rows (the row-vector kernel above; used for m <= kSmallM, and for
+// TRSM_RLNN of any size).
+template <class T, bool TRANS>
+__device__ inline void trsm_rows_small(int m, int n, T alpha, const T* L, int ldl, T* B, int ldb, T* smem, int part, int parts) {
+    const int per = (m + parts - 1) / parts;
+    const int r0 = min(m, part * per), r1 = min(m, r0 + per);
+    for (int q0 = r0; q0 < r1; q0 += kSmallM) trsm_small_m<T, TRANS>(min(kSmallM, r1 - q0), n, alpha, L, ldl, B + q0, ldb, smem);
+}
+
+// C[m×n] <- alpha·A + beta·C with A and C of either precision (TTG_OP_CONVERT:
+// flags bit 0: A is float, bit 1: C is float); parts split the elements.
+__device__ inline void convert_tile(int m, int n, double alpha, const void* A, int lda, double beta, void* C, int ldc, int flags,
+                                    int part, int parts) {
+    const bool af = flags & 1, cf = flags & 2;
+    for (long e = threadIdx.x + (long)part * kThreads; e < (long)m * n; e += (long)kThreads * parts) {
+        const int i = (int)(e % m), j = (int)(e / m);
+        const size_t ia = i + (size_t)j * lda, ic = i + (size_t)j * ldc;
+        const double a = af ? (double)__ldcg((const float*)A + ia) : __ldcg((const double*)A + ia);
+        double v = alpha * a;
+        if (beta != 0.0) v = fma(beta, cf ? (double)__ldcg((const float*)C + ic) : __ldcg((const double*)C + ic), v);
+        if (cf) ((float*)C)[ic] = (float)v;
+        else ((double*)C)[ic] = v;
+    }
+    __syncthreads();
+}
+
+}  // namespace ttg

@@ -15,6 +15,7 @@
 
 #include "../../include/ttg.h"
 #include "exec.cuh"
+#include "op_runner.cuh"
 #include "tile_f64.cuh"
 #include "ttg_internal.h"
 
@@ -26,32 +27,11 @@ static_assert(kTeamCounters == kTeamStride, "team counter block size");
 // ok).  A POTRF with a team counter block is factored by all its parts.
 __device__ int run_op_f64(const ttg_op& op, int part, int parts, double* smem, int* team, int* fin, int* err,
                           long long limit_ns) {
-    switch (op.kind) {
-        case TTG_OP_POTRF_L:
-            if (team)
-                return potrf_l_f64_team(op.n, (double*)op.c, op.ldc, smem, TeamCtx{team, limit_ns, err}, nullptr, 0, fin);
-            return potrf_l_f64(op.n, (double*)op.c, op.ldc, smem);
-        case TTG_OP_TRSM_RLTN:
-            trsm_rltn_f64(op.m, op.n, op.alpha, (const double*)op.a, op.lda, (double*)op.c, op.ldc, smem, part, parts);
-            return 0;
-        case TTG_OP_SYRK_LN:
-            gemm_f64<false, true>(op.n, op.n, op.k, op.alpha, (const double*)op.a, op.lda, (const double*)op.a, op.lda,
-                                  op.beta, (double*)op.c, op.ldc, smem, part, parts);
-            return 0;
-        case TTG_OP_GEMM_NT:
-            gemm_f64<false, false>(op.m, op.n, op.k, op.alpha, (const double*)op.a, op.lda, (const double*)op.b, op.ldb,
-                                   op.beta, (double*)op.c, op.ldc, smem, part, parts);
-            return 0;
-        case TTG_OP_GEMM_NN:
-            gemm_f64<true, false>(op.m, op.n, op.k, op.alpha, (const double*)op.a, op.lda, (const double*)op.b, op.ldb,
-                                  op.beta, (double*)op.c, op.ldc, smem, part, parts);
-            return 0;
-        case TTG_OP_GEADD:
-            geadd_f64(op.m, op.n, op.alpha, (const double*)op.a, op.lda, op.beta, (double*)op.c, op.ldc, part, parts);
-            return 0;
-        default:
-            return 0;
+    if (op.kind == TTG_OP_POTRF_L) {
+        if (team) return potrf_l_f64_team(op.n, (double*)op.c, op.ldc, smem, TeamCtx{team, limit_ns, err}, nullptr, 0, fin);
+        return potrf_l_f64(op.n, (double*)op.c, op.ldc, smem);
     }
+    return run_op_plain<double>(op, part, parts, smem);
 }
 
 __global__ void __launch_bounds__(kThreads, 1) exec_kernel(ExecParams p) {
@@ -214,7 +194,7 @@ ttg_status ttg_ctx_init_device(ttg_ctx* c) {
     TTG_CUDA_TRY(cudaMallocHost((void**)&c->h_status, sizeof(int) * 8));
     TTG_CUDA_TRY(cudaEventCreate(&c->ev0));
     TTG_CUDA_TRY(cudaEventCreate(&c->ev1));
-    const int smem = kF64SmemDoubles * (int)sizeof(double);
+    const int smem = kPlainSmemDoubles * (int)sizeof(double);
     TTG_CUDA_TRY(cudaFuncSetAttribute(exec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     // Workers of a bound queue wait for their own block, so every block must
     // be resident: the executor is a cooperative launch and its size is
@@ -240,6 +220,22 @@ extern "C" ttg_status ttg_destroy(ttg_ctx* c) {
 }
 
 extern "C" int ttg_workers(const ttg_ctx* c) { return c ? c->workers : 0; }
+
+extern "C" ttg_status ttg_set_workers(ttg_ctx* c, int32_t w) {
+    if (!c || w < 0) return TTG_EINVAL;
+    int maxw = c->max_workers_f64;
+    const int mx = ttg_mixed_max_workers(c);
+    if (mx > 0) maxw = std::min(maxw, mx);
+    const int nw = w == 0 ? maxw : std::min(w, maxw);
+    if (nw != c->workers) {
+        // The queue layout of an uploaded graph depends on the worker count:
+        // the graph must be uploaded again (owners see a new generation).
+        c->workers = nw;
+        c->uploaded = false;
+        c->graph_gen += 1;
+    }
+    return TTG_OK;
+}
 
 extern "C" uint64_t ttg_graph_generation(const ttg_ctx* c) { return c ? c->graph_gen : 0; }
 
@@ -279,10 +275,12 @@ int ttg_task_parts(const ttg_op& op, bool team) {
             break;
         }
         case TTG_OP_TRSM_RLTN:
+        case TTG_OP_TRSM_RLNN:
             max_parts = std::max(1, cdiv(op.m, 16));
             auto_parts = std::min(8, std::max(1, cdiv(op.m, 128)));
             break;
         case TTG_OP_GEADD:
+        case TTG_OP_CONVERT:
             max_parts = std::max(1, cdiv((long)op.m * op.n, 256));
             auto_parts = std::min(8, std::max(1, cdiv((long)op.m * op.n, 65536)));
             break;
@@ -411,7 +409,7 @@ extern "C" ttg_status ttg_graph_upload(ttg_ctx* c, const ttg_graph_desc* gd) {
     for (int t = 0; t < n; ++t) {
         if (gd->init_count[t] < 0 || gd->succ_ptr[t] > gd->succ_ptr[t + 1]) return TTG_EINVAL;
         const int k = gd->ops[t].kind;
-        if (k < TTG_OP_NOP || k > TTG_OP_GEADD) return TTG_EINVAL;
+        if (k < TTG_OP_NOP || k > TTG_OP_CONVERT) return TTG_EINVAL;
         if (gd->ops[t].prec != TTG_PREC_F64 && gd->ops[t].prec != TTG_PREC_MIXED) return TTG_EINVAL;
     }
     if (n > 0 && gd->succ_ptr[0] != 0) return TTG_EINVAL;
@@ -630,13 +628,46 @@ extern "C" ttg_status ttg_launch(ttg_ctx* c, void* stream) {
     return TTG_OK;
 }
 
+cudaError_t ttg_launch_cooperative(const void* fn, int grid, int block, void** args, size_t smem, cudaStream_t s) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelExC(&cfg, fn, args);
+}
+
 ttg_status ttg_launch_executor(ttg_ctx* c, const ExecParams& p, cudaStream_t s) {
     if (c->g_mixed) return ttg_launch_mixed(c, p, s);
-    const int smem = kF64SmemDoubles * (int)sizeof(double);
+    const int smem = kPlainSmemDoubles * (int)sizeof(double);
     void* args[] = {(void*)&p};
-    TTG_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)exec_kernel, dim3(c->workers), dim3(kThreads), args, smem, s));
+    TTG_CUDA_TRY(ttg_launch_cooperative((const void*)exec_kernel, c->workers, kThreads, args, smem, s));
     return TTG_OK;
 }
+
+ttg_status ttg_enqueue_run(ttg_ctx* c, cudaStream_t s) {
+    if (!c->uploaded) return TTG_ESTATE;
+    ttg_status st = ttg_reset_state(c, s);
+    if (st != TTG_OK) return st;
+    if (c->g.n_runnable > 0) {
+        ExecParams p = ttg_make_params(c);
+        st = ttg_launch_executor(c, p, s);
+    }
+    return st;
+}
+
+ttg_status ttg_mark_launched(ttg_ctx* c, cudaStream_t s) {
+    c->stream = s;
+    c->launched = true;
+    return TTG_OK;
+}
+
+cudaEvent_t ttg_event(ttg_ctx* c, int which) { return which ? c->ev1 : c->ev0; }
 
 extern "C" ttg_status ttg_wait(ttg_ctx* c, ttg_report* rep) {
     if (!c) return TTG_EINVAL;

@@ -72,6 +72,16 @@ void ttg_set_last_cuda_error(cudaError_t e, const char* expr, const char* file, 
 ttg_status ttg_ctx_init_device(ttg_ctx* c);
 ttg_status ttg_reset_state(ttg_ctx* c, cudaStream_t s);
 ttg_status ttg_launch_executor(ttg_ctx* c, const ttg::ExecParams& p, cudaStream_t s);
+// A cooperative launch (every block resident) through cudaLaunchKernelEx, so
+// that it can also be recorded into a CUDA graph.
+cudaError_t ttg_launch_cooperative(const void* fn, int grid, int block, void** args, size_t smem, cudaStream_t s);
+// Enqueue the counter/queue reset and the executor launch of the uploaded
+// graph on s (no events): the body of a recorded CUDA graph.
+ttg_status ttg_enqueue_run(ttg_ctx* c, cudaStream_t s);
+// After a recorded graph holding ttg_enqueue_run was launched on s between
+// the context's events: let ttg_wait collect the run.
+ttg_status ttg_mark_launched(ttg_ctx* c, cudaStream_t s);
+cudaEvent_t ttg_event(ttg_ctx* c, int which);
 void ttg_graph_free(ttg_ctx* c);
 // Blocks that share one task.  team: a POTRF may be split over a team of
 // blocks (needs a team counter block at run time).
@@ -88,6 +98,9 @@ ttg_status ttg_gen_gemm_tiles(ttg_ctx* c, int32_t N, int32_t b, int32_t inputs, 
 ttg_status ttg_mixed_init(ttg_ctx* c);
 void ttg_mixed_free(ttg_ctx* c);
 ttg_status ttg_launch_mixed(ttg_ctx* c, const ttg::ExecParams& p, cudaStream_t s);
+// Graphs without tensor-core tasks (no plan tensor map in the launch).
+void ttg_mixed_no_tc(ttg_ctx* c);
+int ttg_mixed_max_workers(const ttg_ctx* c);
 
 #define TTG_CUDA_CHECK(expr)                                                            \
     do {                                                                                \

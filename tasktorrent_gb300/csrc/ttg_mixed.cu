@@ -18,6 +18,7 @@
 
 #include "../../include/ttg.h"
 #include "exec.cuh"
+#include "op_runner.cuh"
 #include "tile_bf16_tc.cuh"
 #include "tile_f64.cuh"
 #include "ttg_internal.h"
@@ -57,32 +58,12 @@ __device__ inline void rows_to_bf16(const float* W, int ldw, int r0, int r1, int
 __device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem, int* team, int* fin, tc::TcShared* tsh,
                              uint8_t* ring, const CUtensorMap* tmap, int* err, long long limit_ns) {
     if (op.prec == TTG_PREC_F64) {
-        switch (op.kind) {
-            case TTG_OP_POTRF_L:
-                if (team)
-                    return potrf_l_f64_team(op.n, (double*)op.c, op.ldc, smem, TeamCtx{team, limit_ns, err}, nullptr, 0, fin);
-                return potrf_l_f64(op.n, (double*)op.c, op.ldc, smem);
-            case TTG_OP_TRSM_RLTN:
-                trsm_rltn_f64(op.m, op.n, op.alpha, (const double*)op.a, op.lda, (double*)op.c, op.ldc, smem, part, parts);
-                return 0;
-            case TTG_OP_SYRK_LN:
-                gemm_f64<false, true>(op.n, op.n, op.k, op.alpha, (const double*)op.a, op.lda, (const double*)op.a, op.lda,
-                                      op.beta, (double*)op.c, op.ldc, smem, part, parts);
-                return 0;
-            case TTG_OP_GEMM_NT:
-                gemm_f64<false, false>(op.m, op.n, op.k, op.alpha, (const double*)op.a, op.lda, (const double*)op.b, op.ldb,
-                                       op.beta, (double*)op.c, op.ldc, smem, part, parts);
-                return 0;
-            case TTG_OP_GEMM_NN:
-                gemm_f64<true, false>(op.m, op.n, op.k, op.alpha, (const double*)op.a, op.lda, (const double*)op.b, op.ldb,
-                                      op.beta, (double*)op.c, op.ldc, smem, part, parts);
-                return 0;
-            case TTG_OP_GEADD:
-                geadd_f64(op.m, op.n, op.alpha, (const double*)op.a, op.lda, op.beta, (double*)op.c, op.ldc, part, parts);
-                return 0;
-            default:
-                return 0;
+        if (op.kind == TTG_OP_POTRF_L) {
+            if (team)
+                return potrf_l_f64_team(op.n, (double*)op.c, op.ldc, smem, TeamCtx{team, limit_ns, err}, nullptr, 0, fin);
+            return potrf_l_f64(op.n, (double*)op.c, op.ldc, smem);
         }
+        return run_op_plain<double>(op, part, parts, smem);
     }
     float* fsm = reinterpret_cast<float*>(smem);
     switch (op.kind) {
@@ -109,9 +90,10 @@ __device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem,
             return info;
         }
         case TTG_OP_TRSM_RLTN:
+            if (op.flags != kMixedBF16) return run_op_plain<float>(op, part, parts, fsm);
             trsm_rltn_tile<float>(op.m, op.n, (float)op.alpha, (const float*)op.a, op.lda, (float*)op.c, op.ldc, fsm, part,
                                   parts);
-            if (op.flags == kMixedBF16) {
+            {
                 // Publish this row slice as the tile's BF16 panel copy.
                 const MixedTables* tb = (const MixedTables*)op.aux;
                 const int per = ((op.m + parts - 1) / parts + 15) / 16 * 16;
@@ -137,22 +119,15 @@ __device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem,
                 if (!ok && threadIdx.x == 0) atomicCAS(err, 0, TTG_ETIMEOUT);
                 return 0;
             }
-            if (op.kind == TTG_OP_GEMM_NT) {
-                gemm_tile<float, false, false>(op.m, op.n, op.k, (float)op.alpha, (const float*)op.a, op.lda, (const float*)op.b,
-                                               op.ldb, (float)op.beta, (float*)op.c, op.ldc, fsm, part, parts);
-                return 0;
-            }
-            gemm_tile<float, false, true>(op.n, op.n, op.k, (float)op.alpha, (const float*)op.a, op.lda, (const float*)op.a,
-                                          op.lda, (float)op.beta, (float*)op.c, op.ldc, fsm, part, parts);
-            return 0;
+            return run_op_plain<float>(op, part, parts, fsm);
         default:
-            return 0;
+            return run_op_plain<float>(op, part, parts, fsm);
     }
 }
 
 // Dynamic shared memory: the FP64/FP32 tile kernels use the front, the
 // tensor-core ring (1024-aligned) the rest; both are never live together.
-constexpr int kMixedSmemBytes = tc::kSmemBytes > kF64SmemDoubles * 8 ? tc::kSmemBytes : kF64SmemDoubles * 8;
+constexpr int kMixedSmemBytes = tc::kSmemBytes > kPlainSmemDoubles * 8 ? tc::kSmemBytes : kPlainSmemDoubles * 8;
 
 __global__ void __launch_bounds__(kThreads, 1) exec_kernel_mixed(ExecParams p, const __grid_constant__ MixedGlobals g) {
     extern __shared__ __align__(1024) double smem_mx[];
@@ -230,6 +205,12 @@ ttg_status ttg_mixed_init(ttg_ctx* c) {
     return TTG_OK;
 }
 
+void ttg_mixed_no_tc(ttg_ctx* c) {
+    if (c->mixed) ((MixedCtx*)c->mixed)->globals.has_tc = 0;
+}
+
+int ttg_mixed_max_workers(const ttg_ctx* c) { return c->mixed ? ((const MixedCtx*)c->mixed)->max_workers : 0; }
+
 void ttg_mixed_free(ttg_ctx* c) {
     delete (MixedCtx*)c->mixed;
     c->mixed = nullptr;
@@ -240,7 +221,7 @@ ttg_status ttg_launch_mixed(ttg_ctx* c, const ExecParams& p, cudaStream_t s) {
     if (!m || c->workers > m->max_workers) return TTG_EINVAL;
     const int smem = kMixedSmemBytes;
     void* args[] = {(void*)&p, (void*)&m->globals};
-    TTG_CUDA_CHECK(cudaLaunchCooperativeKernel((const void*)exec_kernel_mixed, dim3(c->workers), dim3(kThreads), args, smem, s));
+    TTG_CUDA_CHECK(ttg_launch_cooperative((const void*)exec_kernel_mixed, c->workers, kThreads, args, smem, s));
     return TTG_OK;
 }
 
