@@ -79,6 +79,16 @@ class SolveReport(ctypes.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class BatchArgs(ctypes.Structure):
+    _fields_ = [("n_systems", ctypes.c_int32), ("sizes", ctypes.POINTER(ctypes.c_int32)), ("tile", ctypes.c_int32),
+                ("precision", ctypes.c_int32), ("nrhs", ctypes.c_int32), ("ir_steps", ctypes.c_int32),
+                ("seed", ctypes.c_uint32), ("alpha", ctypes.c_double), ("priority", ctypes.c_int32)]
+
+
+class BatchReport(ctypes.Structure):
+    _fields_ = [("run", Report), ("tasks", ctypes.c_int64), ("flops", ctypes.c_double)]
+
+
 # Every symbol the public headers declare, with its ctypes signature.
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32
@@ -99,6 +109,16 @@ SIGNATURES = {
     "ttg_critical_path_priority": (_STATUS, [_P, _P]),
     "ttg_workers": (ctypes.c_int, [_P]),
     "ttg_set_workers": (_STATUS, [_P, _I32]),
+    # include/ttg_batch.h
+    "ttg_batch_create": (_STATUS, [_P, ctypes.POINTER(BatchArgs), ctypes.POINTER(_P)]),
+    "ttg_batch_destroy": (None, [_P]),
+    "ttg_batch_generate": (_STATUS, [_P, _P]),
+    "ttg_batch_set_system": (_STATUS, [_P, _I32, _P, _P, _P]),
+    "ttg_batch_run": (_STATUS, [_P, _P, ctypes.POINTER(BatchReport)]),
+    "ttg_batch_get_x": (_STATUS, [_P, _I32, _P]),
+    "ttg_batch_backward_errors": (_STATUS, [_P, _P, _P]),
+    "ttg_batch_autotune": (_STATUS, [_P, ctypes.POINTER(BatchArgs), _P, _I32, _P, _I32, _I32, _P, _P,
+                                     ctypes.POINTER(ctypes.c_double)]),
     "ttg_graph_generation": (ctypes.c_uint64, [_P]),
     "ttg_gen_gram_tiles": (_STATUS, [_P, _I32, _P, _I32, ctypes.c_double, ctypes.c_uint32, _P, _P]),
     "ttg_gen_uniform": (_STATUS, [_P, ctypes.c_int64, ctypes.c_uint32, ctypes.c_uint32, _P, _P]),
@@ -428,3 +448,68 @@ class GemmPlan:
             self.close()
         except Exception:
             pass
+
+
+class Batch:
+    """Many independent SPD factor-and-solve systems in one executor launch
+    (include/ttg_batch.h).  sizes: N_i; precision PREC_F64, or PREC_MIXED
+    (FP32 factor and ir_steps refinement rounds in the same launch)."""
+
+    def __init__(self, ctx, sizes, tile, precision=PREC_F64, nrhs=1, ir_steps=2, seed=3, alpha=1.0, priority=0,
+                 generate=True):
+        self.ctx = ctx
+        self.sizes = np.ascontiguousarray(sizes, dtype=np.int32)
+        self.nrhs = nrhs
+        self.args = BatchArgs(len(self.sizes), self.sizes.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), tile, precision,
+                              nrhs, ir_steps, seed, alpha, priority)
+        h = _P()
+        check(lib().ttg_batch_create(ctx.h, ctypes.byref(self.args), ctypes.byref(h)), "ttg_batch_create")
+        self.h = h
+        if generate:
+            check(lib().ttg_batch_generate(self.h, None), "ttg_batch_generate")
+
+    def set_system(self, i, A=None, B=None):
+        n = int(self.sizes[i])
+        A = None if A is None else np.asfortranarray(A, dtype=np.float64)
+        B = None if B is None else np.asfortranarray(np.asarray(B, dtype=np.float64).reshape(n, -1))
+        check(lib().ttg_batch_set_system(self.h, i, _ptr(A), _ptr(B), None), "ttg_batch_set_system")
+
+    def run(self, stream=None):
+        rep = BatchReport()
+        st = lib().ttg_batch_run(self.h, stream, ctypes.byref(rep))
+        return st, rep
+
+    def x(self, i):
+        out = np.zeros((int(self.sizes[i]), self.nrhs), order="F")
+        check(lib().ttg_batch_get_x(self.h, i, _ptr(out)), "ttg_batch_get_x")
+        return out
+
+    def backward_errors(self):
+        out = np.zeros(len(self.sizes))
+        check(lib().ttg_batch_backward_errors(self.h, _ptr(out), None), "ttg_batch_backward_errors")
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ttg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_autotune(ctx, sizes, tiles, workers, precision=PREC_F64, nrhs=1, ir_steps=2, seed=3, alpha=1.0, max_sample=400):
+    """Fastest (tile, workers) for a batch of these sizes; returns (tile, workers, ms per system)."""
+    sizes = np.ascontiguousarray(sizes, dtype=np.int32)
+    a = BatchArgs(len(sizes), sizes.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), 0, precision, nrhs, ir_steps, seed,
+                  alpha, 0)
+    tl = np.ascontiguousarray(tiles, dtype=np.int32)
+    wk = np.ascontiguousarray(workers, dtype=np.int32)
+    bt, bw, ms = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_double()
+    check(lib().ttg_batch_autotune(ctx.h, ctypes.byref(a), _ptr(tl), len(tl), _ptr(wk), len(wk), max_sample,
+                                   ctypes.byref(bt), ctypes.byref(bw), ctypes.byref(ms)), "ttg_batch_autotune")
+    return bt.value, bw.value, ms.value
+
