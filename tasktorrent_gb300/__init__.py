@@ -89,6 +89,26 @@ class BatchReport(ctypes.Structure):
     _fields_ = [("run", Report), ("tasks", ctypes.c_int64), ("flops", ctypes.c_double)]
 
 
+class ServeArgs(ctypes.Structure):
+    _fields_ = [("n_requests", ctypes.c_int32), ("rate", ctypes.c_double), ("n_min", ctypes.c_int32), ("n_max", ctypes.c_int32),
+                ("alpha", ctypes.c_double), ("seed", ctypes.c_uint32), ("followup_frac", ctypes.c_double),
+                ("precision", ctypes.c_int32), ("ir_steps", ctypes.c_int32), ("nrhs", ctypes.c_int32), ("lanes", ctypes.c_int32),
+                ("max_batch", ctypes.c_int32), ("hbm_budget_gb", ctypes.c_double), ("tol", ctypes.c_double),
+                ("keep_results", ctypes.c_int32)]
+
+
+class ServeReport(ctypes.Structure):
+    _fields_ = [("completed", ctypes.c_int32), ("factorisations", ctypes.c_int32), ("followups", ctypes.c_int32),
+                ("followup_misses", ctypes.c_int32), ("evictions", ctypes.c_int32), ("launches", ctypes.c_int32),
+                ("retries", ctypes.c_int32), ("unconverged", ctypes.c_int32), ("wall_s", ctypes.c_double),
+                ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double), ("mean_ms", ctypes.c_double),
+                ("max_ms", ctypes.c_double), ("solves_per_s", ctypes.c_double), ("tflops", ctypes.c_double),
+                ("worst_bwd_err", ctypes.c_double), ("peak_gb", ctypes.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 # Every symbol the public headers declare, with its ctypes signature.
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32
@@ -109,6 +129,13 @@ SIGNATURES = {
     "ttg_critical_path_priority": (_STATUS, [_P, _P]),
     "ttg_workers": (ctypes.c_int, [_P]),
     "ttg_set_workers": (_STATUS, [_P, _I32]),
+    # include/ttg_serve.h
+    "ttg_serve_tile": (_I32, [_I32]),
+    "ttg_serve_create": (_STATUS, [ctypes.c_int, ctypes.POINTER(ServeArgs), ctypes.POINTER(_P)]),
+    "ttg_serve_destroy": (None, [_P]),
+    "ttg_serve_run": (_STATUS, [_P, ctypes.POINTER(ServeReport), _P]),
+    "ttg_serve_request": (_STATUS, [_P, _I32, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "ttg_serve_get_x": (_STATUS, [_P, _I32, _P]),
     # include/ttg_batch.h
     "ttg_batch_create": (_STATUS, [_P, ctypes.POINTER(BatchArgs), ctypes.POINTER(_P)]),
     "ttg_batch_destroy": (None, [_P]),
@@ -512,4 +539,50 @@ def batch_autotune(ctx, sizes, tiles, workers, precision=PREC_F64, nrhs=1, ir_st
     check(lib().ttg_batch_autotune(ctx.h, ctypes.byref(a), _ptr(tl), len(tl), _ptr(wk), len(wk), max_sample,
                                    ctypes.byref(bt), ctypes.byref(bw), ctypes.byref(ms)), "ttg_batch_autotune")
     return bt.value, bw.value, ms.value
+
+
+class Serve:
+    """The request loop of include/ttg_serve.h (a Poisson stream of
+    factor-and-solve and follow-up requests over `lanes` executors)."""
+
+    def __init__(self, n_requests, rate, n_min=64, n_max=8192, alpha=1e-4, seed=2, followup_frac=0.3,
+                 precision=PREC_MIXED, ir_steps=4, nrhs=1, lanes=2, max_batch=16, hbm_budget_gb=180.0, tol=1e-14,
+                 keep_results=False, device=0):
+        self.args = ServeArgs(n_requests, rate, n_min, n_max, alpha, seed, followup_frac, precision, ir_steps, nrhs, lanes,
+                              max_batch, hbm_budget_gb, tol, 1 if keep_results else 0)
+        self.nrhs = nrhs
+        h = _P()
+        check(lib().ttg_serve_create(device, ctypes.byref(self.args), ctypes.byref(h)), "ttg_serve_create")
+        self.h = h
+
+    def run(self):
+        rep = ServeReport()
+        lat = np.zeros(self.args.n_requests)
+        st = lib().ttg_serve_run(self.h, ctypes.byref(rep), _ptr(lat))
+        return st, rep, lat
+
+    def request(self, i):
+        n, tile, fo, ir = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        sa, sb = ctypes.c_uint32(), ctypes.c_uint32()
+        arr, be = ctypes.c_double(), ctypes.c_double()
+        check(lib().ttg_serve_request(self.h, i, ctypes.byref(n), ctypes.byref(tile), ctypes.byref(sa), ctypes.byref(sb),
+                                      ctypes.byref(arr), ctypes.byref(fo), ctypes.byref(be), ctypes.byref(ir)), "ttg_serve_request")
+        return {"n": n.value, "tile": tile.value, "seed_a": sa.value, "seed_b": sb.value, "arrival_s": arr.value,
+                "followup_of": fo.value, "bwd_err": be.value, "ir_steps": ir.value}
+
+    def x(self, i):
+        out = np.zeros((self.request(i)["n"], self.nrhs), order="F")
+        check(lib().ttg_serve_get_x(self.h, i, _ptr(out)), "ttg_serve_get_x")
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ttg_serve_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 

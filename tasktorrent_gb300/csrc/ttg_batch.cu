@@ -1,27 +1,6 @@
 // ttg_batch.cu — many independent SPD factor-and-solve systems in one launch
-// of the persistent executor (include/ttg_batch.h).
-//
-// The device graph is built directly (no Taskflow capture: a batch holds up
-// to millions of tasks).  Per system it is the DAG of the reference's
-// 2d_cholesky flows with accumulate = false (2d_cholesky.cpp:316-551):
-//   potrf(j)      indegree 1                 -> trsm(i,j), i > j
-//   trsm(i,j)     indegree 1 + (j > 0)        -> gemm{j,i,m} (j<m<i), gemm{j,m,i} (m>=i)
-//   gemm{k,i,j}   indegree (i==j ? 1 : 2) + (k > 0)
-//                 -> gemm{k+1,i,j} if k < j-1, else potrf(i) if i == j, else trsm(i,j)
-// followed by the block solves of its right-hand sides (row blocks, ld nrhs):
-//   forward   fs(i) = TRSM_RLTN on block i after fu(i,i-1) and potrf(i);
-//             fu(i,j) = GEMM_NT  X_i -= X_j·L_ijᵀ, chained over j = 0..i-1;
-//   backward  bs(i) = TRSM_RLNN on block i after bu(i,i+1) (or fs(nb-1));
-//             bu(i,j) = GEMM_NN  X_i -= X_j·L_ji, chained over j = nb-1..i+1.
-// fs(nb-1) depends, through the forward chains, on every forward task, so no
-// backward update overwrites a block that a forward update still reads.
-// Every block's updates are chained in a fixed order, so each system's
-// result is the same whatever else shares the launch.
-// The mixed variant converts the FP64 input tiles to FP32 working tiles with
-// CONVERT tasks, factors them (FP64 diagonal POTRF through an FP64 scratch
-// tile, FP32 TRSM and updates), solves in FP32, and runs ir_steps rounds of
-// refinement: r = b − A·x (FP64 input tiles, row-vector GEMMs chained over
-// the tile row), d = (L̃L̃ᵀ)⁻¹ r in FP32, x += d.
+// of the persistent executor (include/ttg_batch.h), and the construction of
+// their device task graphs (batch_graph.h, which describes the DAG).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -32,34 +11,10 @@
 #include "../../include/ttg.h"
 #include "../../include/ttg_batch.h"
 #include "../../include/ttg_philox.h"
+#include "batch_graph.h"
 #include "ttg_internal.h"
 
 namespace {
-
-struct SysInfo {
-    int N = 0, nb = 0, tile = 0;
-    int64_t tile_base = 0;  // element offset of the system's tiles
-    int64_t vec_base = 0;   // element offset of its nrhs × N row blocks
-    int bs(int i) const { return i < nb - 1 ? tile : N - (nb - 1) * tile; }
-    int displ(int i) const { return i * tile; }
-    // Packed lower tiles, column by column: tile (i, j), i >= j.  Tile
-    // columns c < j are full width (c < nb - 1) with N − c·tile rows.
-    int64_t off(int i, int j) const {
-        return (int64_t)tile * ((int64_t)j * N - (int64_t)tile * j * (j - 1) / 2) + (int64_t)(i - j) * tile * bs(j);
-    }
-    int64_t elems() const { return off(nb - 1, nb - 1) + (int64_t)bs(nb - 1) * bs(nb - 1); }
-};
-
-// Graph under construction.
-struct Builder {
-    std::vector<ttg_op> ops;
-    std::vector<std::pair<int32_t, int32_t>> edges;
-    int add(const ttg_op& op) {
-        ops.push_back(op);
-        return (int)ops.size() - 1;
-    }
-    void edge(int a, int b) { edges.emplace_back(a, b); }
-};
 
 ttg_op make_op(int kind, int prec, int m, int n, int k, const void* a, int lda, const void* b, int ldb, void* c, int ldc,
                double alpha, double beta, int flags = 0, void* aux = nullptr) {
@@ -174,44 +129,18 @@ __global__ void batch_bwd_kernel(const int* __restrict__ Ns, const int* __restri
 
 }  // namespace
 
-struct ttg_batch {
-    ttg_ctx* ctx = nullptr;
-    ttg_batch_args a{};
-    std::vector<int32_t> sizes;
-    std::vector<SysInfo> sys;
-    bool mixed = false;
-    int64_t tile_elems = 0, vec_elems = 0;
-    double* A64 = nullptr;  // FP64 input tiles (full diagonal tiles)
-    double* W64 = nullptr;  // FP64: factor tiles; mixed: FP64 scratch of the diagonal POTRFs
-    float* W32 = nullptr;   // mixed: FP32 working tiles
-    double *B = nullptr, *X = nullptr, *R = nullptr;
-    float* D32 = nullptr;
-    Builder g;
-    std::vector<double> prio;
-    std::vector<int32_t> init;
-    std::vector<int64_t> ptr;
-    std::vector<int32_t> idx;
-    uint64_t gen = 0;  // context graph generation of our upload
-    cudaGraphExec_t gexec = nullptr;
-    cudaStream_t gstream = nullptr;  // the stream the graph was recorded on
-    cudaStream_t own = nullptr;      // used for a NULL stream (the legacy stream cannot be recorded)
-    int gworkers = 0;
-    double flops = 0.0;
-};
+namespace ttg {
+namespace batch {
 
-namespace {
 
 // Factor DAG of one system (FP64 in place on W64, or mixed: CONVERT tasks,
-// FP32 working tiles, FP64 POTRF scratch); returns the potrf and trsm ids
-// the solve depends on.
-void build_factor(ttg_batch* b, const SysInfo& S, std::vector<int>& potrf, std::vector<int>& trsm) {
-    Builder& g = b->g;
+// FP32 working tiles, FP64 POTRF scratch); fills the potrf and trsm ids the
+// solve depends on.
+static void build_factor(Graph& g, const System& S, std::vector<int>& potrf, std::vector<int>& trsm) {
     const int nb = S.nb;
-    const bool mx = b->mixed;
+    const bool mx = S.mixed;
     const int prec = mx ? TTG_PREC_MIXED : TTG_PREC_F64;
-    auto W = [&](int i, int j) -> void* {
-        return mx ? (void*)(b->W32 + S.tile_base + S.off(i, j)) : (void*)(b->W64 + S.tile_base + S.off(i, j));
-    };
+    auto W = [&](int i, int j) -> void* { return mx ? (void*)(S.W32 + S.off(i, j)) : (void*)(S.W64 + S.off(i, j)); };
     auto T = [&](int i, int j) { return i + j * nb; };
     auto G = [&](int k, int i, int j) { return ((size_t)k * nb + i) * nb + j; };
     potrf.assign(nb, -1);
@@ -219,7 +148,7 @@ void build_factor(ttg_batch* b, const SysInfo& S, std::vector<int>& potrf, std::
     std::vector<int> gemm((size_t)nb * nb * nb, -1), cvt((size_t)nb * nb, -1);
     for (int j = 0; j < nb; ++j) {
         potrf[j] = g.add(make_op(TTG_OP_POTRF_L, prec, S.bs(j), S.bs(j), 0, nullptr, 0, nullptr, 0, W(j, j), S.bs(j), 1.0, 0.0, 0,
-                                 mx ? (void*)(b->W64 + S.tile_base + S.off(j, j)) : nullptr));
+                                 mx ? (void*)(S.D64 + (size_t)j * S.tile * S.tile) : nullptr));
         for (int i = j + 1; i < nb; ++i)
             trsm[T(i, j)] = g.add(make_op(TTG_OP_TRSM_RLTN, prec, S.bs(i), S.bs(j), 0, W(j, j), S.bs(j), nullptr, 0, W(i, j),
                                           S.bs(i), 1.0, 0.0, mx ? 1 : 0));
@@ -233,8 +162,8 @@ void build_factor(ttg_batch* b, const SysInfo& S, std::vector<int>& potrf, std::
     if (mx)
         for (int j = 0; j < nb; ++j)
             for (int i = j; i < nb; ++i)
-                cvt[T(i, j)] = g.add(make_op(TTG_OP_CONVERT, TTG_PREC_F64, S.bs(i), S.bs(j), 0, b->A64 + S.tile_base + S.off(i, j),
-                                             S.bs(i), nullptr, 0, W(i, j), S.bs(i), 1.0, 0.0, 2));
+                cvt[T(i, j)] = g.add(make_op(TTG_OP_CONVERT, TTG_PREC_F64, S.bs(i), S.bs(j), 0, S.A64 + S.off(i, j), S.bs(i), nullptr,
+                                             0, W(i, j), S.bs(i), 1.0, 0.0, 2));
     for (int j = 0; j < nb; ++j) {
         for (int i = j + 1; i < nb; ++i) {
             g.edge(potrf[j], trsm[T(i, j)]);
@@ -258,17 +187,16 @@ void build_factor(ttg_batch* b, const SysInfo& S, std::vector<int>& potrf, std::
 
 // Block solve L Lᵀ x = v in place on the row blocks V (ld nrhs) with the
 // factor tiles (FP32 when f32).  pre[i]: a task that must precede any access
-// to block i (or -1).  Returns the final task of every block.
-std::vector<int> build_solve(ttg_batch* b, const SysInfo& S, void* V, bool f32, const std::vector<int>& potrf,
+// to block i (or -1); potrf / trsm: the factor's tasks (empty for a resident
+// factor).  Returns the final task of every block.
+static std::vector<int> build_solve(Graph& g, const System& S, void* V, bool f32, const std::vector<int>& potrf,
                              const std::vector<int>& trsm, const std::vector<int>& pre) {
-    Builder& g = b->g;
-    const int nb = S.nb, nr = b->a.nrhs;
+    const int nb = S.nb, nr = S.nrhs;
     const int prec = f32 ? TTG_PREC_MIXED : TTG_PREC_F64;
     const size_t es = f32 ? sizeof(float) : sizeof(double);
-    auto Vb = [&](int i) { return (void*)((char*)V + es * ((size_t)S.vec_base + (size_t)S.displ(i) * nr)); };
-    auto F = [&](int i, int j) -> const void* {
-        return f32 ? (const void*)(b->W32 + S.tile_base + S.off(i, j)) : (const void*)(b->W64 + S.tile_base + S.off(i, j));
-    };
+    const bool dep = !potrf.empty();
+    auto Vb = [&](int i) { return (void*)((char*)V + es * (size_t)S.displ(i) * nr); };
+    auto F = [&](int i, int j) -> const void* { return f32 ? (const void*)(S.W32 + S.off(i, j)) : (const void*)(S.W64 + S.off(i, j)); };
     auto T = [&](int i, int j) { return i + j * nb; };
     std::vector<int> fs(nb), fu((size_t)nb * nb, -1), bsv(nb), bu((size_t)nb * nb, -1);
     for (int i = 0; i < nb; ++i) {
@@ -283,18 +211,18 @@ std::vector<int> build_solve(ttg_batch* b, const SysInfo& S, void* V, bool f32, 
     }
     for (int i = 0; i < nb; ++i) {
         if (pre[i] >= 0) g.edge(pre[i], i == 0 ? fs[0] : fu[T(i, 0)]);
-        g.edge(potrf[i], fs[i]);
+        if (dep) g.edge(potrf[i], fs[i]);
         if (i > 0) g.edge(fu[T(i, i - 1)], fs[i]);
         for (int j = 0; j < i; ++j) {
             const int t = fu[T(i, j)];
             g.edge(fs[j], t);
-            g.edge(trsm[T(i, j)], t);
+            if (dep) g.edge(trsm[T(i, j)], t);
             if (j > 0) g.edge(fu[T(i, j - 1)], t);
         }
         if (i == nb - 1) {
             g.edge(fs[i], bsv[i]);
         } else {
-            g.edge(fs[nb - 1], bu[T(i, nb - 1)]);  // every forward task is done (see the header)
+            g.edge(fs[nb - 1], bu[T(i, nb - 1)]);  // every forward task is done (see batch_graph.h)
             g.edge(fs[i], bu[T(i, nb - 1)]);
             for (int j = nb - 1; j > i; --j) {
                 const int t = bu[T(i, j)];
@@ -307,59 +235,105 @@ std::vector<int> build_solve(ttg_batch* b, const SysInfo& S, void* V, bool f32, 
     return bsv;
 }
 
-void build_system(ttg_batch* b, const SysInfo& S) {
-    Builder& g = b->g;
-    const int nb = S.nb, nr = b->a.nrhs;
+void add_system(Graph& g, const System& S) {
+    const int nb = S.nb, nr = S.nrhs;
     std::vector<int> potrf, trsm;
-    build_factor(b, S, potrf, trsm);
-    if (!b->mixed) {
-        build_solve(b, S, b->X, false, potrf, trsm, std::vector<int>(nb, -1));
+    if (!S.factored) build_factor(g, S, potrf, trsm);
+    if (!S.mixed) {
+        // FP64: the solve runs in place on X (a copy of B made before the launch).
+        build_solve(g, S, S.X, false, potrf, trsm, std::vector<int>(nb, -1));
         return;
     }
-    auto vec = [&](auto* base, int i) { return base + S.vec_base + (size_t)S.displ(i) * nr; };
+    auto vec = [&](auto* base, int i) { return base + (size_t)S.displ(i) * nr; };
     // x0: d = b (FP32), solve, x = d.
     std::vector<int> pre(nb), last(nb);
     for (int i = 0; i < nb; ++i)
-        pre[i] = g.add(make_op(TTG_OP_CONVERT, TTG_PREC_F64, nr, S.bs(i), 0, vec(b->B, i), nr, nullptr, 0, vec(b->D32, i), nr, 1.0,
-                               0.0, 2));
-    std::vector<int> done = build_solve(b, S, b->D32, true, potrf, trsm, pre);
+        pre[i] = g.add(make_op(TTG_OP_CONVERT, TTG_PREC_F64, nr, S.bs(i), 0, vec(S.B, i), nr, nullptr, 0, vec(S.D32, i), nr, 1.0, 0.0, 2));
+    std::vector<int> done = build_solve(g, S, S.D32, true, potrf, trsm, pre);
     for (int i = 0; i < nb; ++i) {
-        last[i] = g.add(make_op(TTG_OP_CONVERT, TTG_PREC_F64, nr, S.bs(i), 0, vec(b->D32, i), nr, nullptr, 0, vec(b->X, i), nr, 1.0,
-                                0.0, 1));
+        last[i] = g.add(make_op(TTG_OP_CONVERT, TTG_PREC_F64, nr, S.bs(i), 0, vec(S.D32, i), nr, nullptr, 0, vec(S.X, i), nr, 1.0, 0.0, 1));
         g.edge(done[i], last[i]);
     }
-    for (int step = 0; step < b->a.ir_steps; ++step) {
+    for (int step = 0; step < S.ir_steps; ++step) {
         const int xb = g.add(nop());  // x is complete
         for (int i = 0; i < nb; ++i) g.edge(last[i], xb);
         const int rb = g.add(nop());  // every row's residual has read x
         std::vector<int> dcv(nb);
         for (int i = 0; i < nb; ++i) {
             // r_i = b_i − Σ_j A_ij x_j, chained over j.
-            int prev = g.add(make_op(TTG_OP_CONVERT, TTG_PREC_F64, nr, S.bs(i), 0, vec(b->B, i), nr, nullptr, 0, vec(b->R, i), nr, 1.0,
-                                     0.0, 0));
+            int prev = g.add(make_op(TTG_OP_CONVERT, TTG_PREC_F64, nr, S.bs(i), 0, vec(S.B, i), nr, nullptr, 0, vec(S.R, i), nr, 1.0, 0.0, 0));
             g.edge(xb, prev);
             for (int j = 0; j < nb; ++j) {
                 const bool low = j <= i;
-                const double* Aij = b->A64 + S.tile_base + (low ? S.off(i, j) : S.off(j, i));
-                const int t = g.add(make_op(low ? TTG_OP_GEMM_NT : TTG_OP_GEMM_NN, TTG_PREC_F64, nr, S.bs(i), S.bs(j), vec(b->X, j),
-                                            nr, Aij, low ? S.bs(i) : S.bs(j), vec(b->R, i), nr, -1.0, 1.0));
+                const double* Aij = S.A64 + (low ? S.off(i, j) : S.off(j, i));
+                const int t = g.add(make_op(low ? TTG_OP_GEMM_NT : TTG_OP_GEMM_NN, TTG_PREC_F64, nr, S.bs(i), S.bs(j), vec(S.X, j), nr,
+                                            Aij, low ? S.bs(i) : S.bs(j), vec(S.R, i), nr, -1.0, 1.0));
                 g.edge(prev, t);
                 prev = t;
             }
             g.edge(prev, rb);
-            dcv[i] = g.add(make_op(TTG_OP_CONVERT, TTG_PREC_F64, nr, S.bs(i), 0, vec(b->R, i), nr, nullptr, 0, vec(b->D32, i), nr,
-                                   1.0, 0.0, 2));
+            dcv[i] = g.add(make_op(TTG_OP_CONVERT, TTG_PREC_F64, nr, S.bs(i), 0, vec(S.R, i), nr, nullptr, 0, vec(S.D32, i), nr, 1.0, 0.0, 2));
             g.edge(prev, dcv[i]);
         }
-        done = build_solve(b, S, b->D32, true, potrf, trsm, dcv);
+        done = build_solve(g, S, S.D32, true, potrf, trsm, dcv);
         for (int i = 0; i < nb; ++i) {
-            last[i] = g.add(make_op(TTG_OP_CONVERT, TTG_PREC_F64, nr, S.bs(i), 0, vec(b->D32, i), nr, nullptr, 0, vec(b->X, i), nr,
-                                    1.0, 1.0, 1));
+            last[i] = g.add(make_op(TTG_OP_CONVERT, TTG_PREC_F64, nr, S.bs(i), 0, vec(S.D32, i), nr, nullptr, 0, vec(S.X, i), nr, 1.0, 1.0, 1));
             g.edge(done[i], last[i]);
             g.edge(rb, last[i]);
         }
     }
 }
+
+ttg_status Graph::finish(bool critical_path) {
+    const int n = (int)ops.size();
+    init.assign(n, 0);
+    ptr.assign(n + 1, 0);
+    for (auto& e : edges) {
+        ++ptr[e.first + 1];
+        ++init[e.second];
+    }
+    for (int t = 0; t < n; ++t) ptr[t + 1] += ptr[t];
+    idx.resize(edges.size());
+    {
+        std::vector<int64_t> fill(ptr.begin(), ptr.end() - 1);
+        for (auto& e : edges) idx[fill[e.first]++] = e.second;
+    }
+    edges.clear();
+    prio.assign(n, 0.0);
+    if (critical_path) {
+        ttg_graph_desc d = desc();
+        return ttg_critical_path_priority(&d, prio.data());
+    }
+    return TTG_OK;
+}
+
+}  // namespace batch
+}  // namespace ttg
+
+using namespace ttg::batch;
+
+struct ttg_batch {
+    ttg_ctx* ctx = nullptr;
+    ttg_batch_args a{};
+    std::vector<int32_t> sizes;
+    std::vector<System> sys;
+    bool mixed = false;
+    int64_t tile_elems = 0, vec_elems = 0;
+    double* A64 = nullptr;  // FP64 input tiles of all systems (full diagonal tiles)
+    double* W64 = nullptr;  // FP64: factor tiles; mixed: FP64 scratch of the diagonal POTRFs
+    float* W32 = nullptr;   // mixed: FP32 working tiles
+    double *B = nullptr, *X = nullptr, *R = nullptr;
+    float* D32 = nullptr;
+    Graph g;
+    uint64_t gen = 0;  // context graph generation of our upload
+    cudaGraphExec_t gexec = nullptr;
+    cudaStream_t gstream = nullptr;  // the stream the graph was recorded on
+    cudaStream_t own = nullptr;      // used for a NULL stream (the legacy stream cannot be recorded)
+    int gworkers = 0;
+    double flops = 0.0;
+};
+
+namespace {
 
 template <class P>
 ttg_status dev_alloc(P** p, size_t count) {
@@ -371,13 +345,7 @@ ttg_status dev_alloc(P** p, size_t count) {
 }
 
 ttg_status batch_upload(ttg_batch* b) {
-    ttg_graph_desc d{};
-    d.n_tasks = (int32_t)b->g.ops.size();
-    d.ops = b->g.ops.data();
-    d.init_count = b->init.data();
-    d.priority = b->prio.data();
-    d.succ_ptr = b->ptr.data();
-    d.succ_idx = b->idx.data();
+    ttg_graph_desc d = b->g.desc();
     ttg_status st = ttg_graph_upload(b->ctx, &d);
     if (st != TTG_OK) return st;
     b->gen = ttg_graph_generation(b->ctx);
@@ -439,16 +407,18 @@ extern "C" ttg_status ttg_batch_create(ttg_ctx* ctx, const ttg_batch_args* args,
     b->a.sizes = b->sizes.data();
     b->mixed = args->precision == TTG_PREC_MIXED;
     b->sys.resize(args->n_systems);
+    std::vector<int64_t> tb(args->n_systems), vb(args->n_systems);
     for (int s = 0; s < args->n_systems; ++s) {
-        SysInfo& S = b->sys[s];
-        S.N = b->sizes[s];
-        S.tile = std::min(args->tile, S.N);
-        S.nb = (S.N + S.tile - 1) / S.tile;
-        S.tile_base = b->tile_elems;
-        S.vec_base = b->vec_elems;
+        System& S = b->sys[s];
+        S.set_size(b->sizes[s], args->tile);
+        S.mixed = b->mixed;
+        S.nrhs = args->nrhs;
+        S.ir_steps = args->ir_steps;
+        tb[s] = b->tile_elems;
+        vb[s] = b->vec_elems;
         b->tile_elems += (S.elems() + 31) / 32 * 32;  // the next system starts 256-byte aligned
         b->vec_elems += ((int64_t)S.N * args->nrhs + 31) / 32 * 32;
-        b->flops += (double)S.N * S.N * S.N / 3.0;
+        b->flops += S.flops();
     }
     ttg_status st;
     if ((st = dev_alloc(&b->A64, b->tile_elems)) != TTG_OK || (st = dev_alloc(&b->W64, b->tile_elems)) != TTG_OK ||
@@ -458,34 +428,23 @@ extern "C" ttg_status ttg_batch_create(ttg_ctx* ctx, const ttg_batch_args* args,
         ttg_batch_destroy(b);
         return st;
     }
-    for (const SysInfo& S : b->sys) build_system(b, S);
-    // CSR successors and indegrees.
-    const int n = (int)b->g.ops.size();
-    b->init.assign(n, 0);
-    b->ptr.assign(n + 1, 0);
-    for (auto& e : b->g.edges) {
-        ++b->ptr[e.first + 1];
-        ++b->init[e.second];
-    }
-    for (int t = 0; t < n; ++t) b->ptr[t + 1] += b->ptr[t];
-    b->idx.resize(b->g.edges.size());
-    {
-        std::vector<int64_t> fill(b->ptr.begin(), b->ptr.end() - 1);
-        for (auto& e : b->g.edges) b->idx[fill[e.first]++] = e.second;
-    }
-    b->g.edges.clear();
-    b->g.edges.shrink_to_fit();
-    b->prio.assign(n, 0.0);
-    if (args->priority == 0) {
-        ttg_graph_desc d{};
-        d.n_tasks = n;
-        d.ops = b->g.ops.data();
-        d.succ_ptr = b->ptr.data();
-        d.succ_idx = b->idx.data();
-        if ((st = ttg_critical_path_priority(&d, b->prio.data())) != TTG_OK) {
-            ttg_batch_destroy(b);
-            return st;
+    for (int s = 0; s < args->n_systems; ++s) {
+        System& S = b->sys[s];
+        S.A64 = b->A64 + tb[s];
+        S.W64 = b->W64 + tb[s];
+        S.B = b->B + vb[s];
+        S.X = b->X + vb[s];
+        if (b->mixed) {
+            S.D64 = b->W64 + tb[s];  // nb·tile² <= the system's tile elements
+            S.W32 = b->W32 + tb[s];
+            S.R = b->R + vb[s];
+            S.D32 = b->D32 + vb[s];
         }
+        add_system(b->g, S);
+    }
+    if ((st = b->g.finish(args->priority == 0)) != TTG_OK) {
+        ttg_batch_destroy(b);
+        return st;
     }
     if ((st = batch_upload(b)) != TTG_OK) {
         ttg_batch_destroy(b);
@@ -511,11 +470,10 @@ extern "C" ttg_status ttg_batch_generate(ttg_batch* b, void* stream) {
     cudaStream_t s = (cudaStream_t)stream;
     std::vector<int32_t> bs;
     for (size_t i = 0; i < b->sys.size(); ++i) {
-        const SysInfo& S = b->sys[i];
+        const System& S = b->sys[i];
         bs.assign(S.nb, 0);
         for (int t = 0; t < S.nb; ++t) bs[t] = S.bs(t);
-        ttg_status st = ttg_gen_gram_tiles(b->ctx, S.N, bs.data(), S.nb, b->a.alpha, b->a.seed + (uint32_t)i, b->A64 + S.tile_base,
-                                           stream);
+        ttg_status st = ttg_gen_gram_tiles(b->ctx, S.N, bs.data(), S.nb, b->a.alpha, b->a.seed + (uint32_t)i, S.A64, stream);
         if (st != TTG_OK) return st;
     }
     const int n = (int)b->sys.size();
@@ -523,7 +481,7 @@ extern "C" ttg_status ttg_batch_generate(ttg_batch* b, void* stream) {
     std::vector<int64_t> vb(n);
     for (int i = 0; i < n; ++i) {
         Ns[i] = b->sys[i].N;
-        vb[i] = b->sys[i].vec_base;
+        vb[i] = b->sys[i].B - b->B;
     }
     int* dN = nullptr;
     int64_t* dV = nullptr;
@@ -549,7 +507,7 @@ extern "C" ttg_status ttg_batch_set_system(ttg_batch* b, int32_t i, const double
     if (!b || i < 0 || i >= (int)b->sys.size()) return TTG_EINVAL;
     TTG_CUDA_CHECK(cudaSetDevice(b->ctx->device));
     cudaStream_t s = (cudaStream_t)stream;
-    const SysInfo& S = b->sys[i];
+    const System& S = b->sys[i];
     const int nr = b->a.nrhs;
     if (h_A) {
         std::vector<double> t(S.elems());
@@ -563,14 +521,14 @@ extern "C" ttg_status ttg_batch_set_system(ttg_batch* b, int32_t i, const double
                         T[r + (size_t)c * S.bs(ii)] = h_A[gr + (size_t)gc * S.N];
                     }
             }
-        TTG_CUDA_CHECK(cudaMemcpyAsync(b->A64 + S.tile_base, t.data(), sizeof(double) * t.size(), cudaMemcpyHostToDevice, s));
+        TTG_CUDA_CHECK(cudaMemcpyAsync(S.A64, t.data(), sizeof(double) * t.size(), cudaMemcpyHostToDevice, s));
         TTG_CUDA_CHECK(cudaStreamSynchronize(s));
     }
     if (h_B) {
         std::vector<double> v((size_t)S.N * nr);
         for (int q = 0; q < nr; ++q)
             for (int r = 0; r < S.N; ++r) v[q + (size_t)r * nr] = h_B[r + (size_t)q * S.N];
-        TTG_CUDA_CHECK(cudaMemcpyAsync(b->B + S.vec_base, v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice, s));
+        TTG_CUDA_CHECK(cudaMemcpyAsync(S.B, v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice, s));
         TTG_CUDA_CHECK(cudaStreamSynchronize(s));
     }
     return TTG_OK;
@@ -607,10 +565,10 @@ extern "C" ttg_status ttg_batch_run(ttg_batch* b, void* stream, ttg_batch_report
 extern "C" ttg_status ttg_batch_get_x(ttg_batch* b, int32_t i, double* h_X) {
     if (!b || !h_X || i < 0 || i >= (int)b->sys.size()) return TTG_EINVAL;
     TTG_CUDA_CHECK(cudaSetDevice(b->ctx->device));
-    const SysInfo& S = b->sys[i];
+    const System& S = b->sys[i];
     const int nr = b->a.nrhs;
     std::vector<double> v((size_t)S.N * nr);
-    TTG_CUDA_CHECK(cudaMemcpy(v.data(), b->X + S.vec_base, sizeof(double) * v.size(), cudaMemcpyDeviceToHost));
+    TTG_CUDA_CHECK(cudaMemcpy(v.data(), S.X, sizeof(double) * v.size(), cudaMemcpyDeviceToHost));
     for (int q = 0; q < nr; ++q)
         for (int r = 0; r < S.N; ++r) h_X[r + (size_t)q * S.N] = v[q + (size_t)r * nr];
     return TTG_OK;
@@ -626,8 +584,8 @@ extern "C" ttg_status ttg_batch_backward_errors(ttg_batch* b, double* h_err, voi
     for (int i = 0; i < n; ++i) {
         Ns[i] = b->sys[i].N;
         tl[i] = b->sys[i].tile;
-        tb[i] = b->sys[i].tile_base;
-        vb[i] = b->sys[i].vec_base;
+        tb[i] = b->sys[i].A64 - b->A64;
+        vb[i] = b->sys[i].B - b->B;
     }
     int *dN = nullptr, *dT = nullptr;
     int64_t *dTB = nullptr, *dVB = nullptr;

@@ -119,6 +119,21 @@ ttg_status dev_alloc(T** p, size_t count) {
     return TTG_OK;
 }
 
+// Grow-only buffer of the device graph (see DevGraph::cap).
+template <class T>
+ttg_status dev_reserve(DevGraph& g, T** p, size_t count) {
+    if (count == 0) count = 1;
+    size_t& cap = g.cap[(const void*)p];
+    if (*p && cap >= count) return TTG_OK;
+    if (*p) cudaFree((void*)*p);
+    *p = nullptr;
+    cap = 0;
+    const size_t want = std::max(count, count + count / 2);
+    TTG_CUDA_TRY(cudaMalloc((void**)p, want * sizeof(T)));
+    cap = want;
+    return TTG_OK;
+}
+
 template <class T>
 void dev_free(T*& p) {
     if (p) cudaFree((void*)p);
@@ -402,7 +417,10 @@ extern "C" ttg_status ttg_graph_upload(ttg_ctx* c, const ttg_graph_desc* gd) {
     if (!c || !gd || gd->n_tasks < 0 || (gd->n_tasks > 0 && (!gd->ops || !gd->init_count || !gd->succ_ptr)))
         return TTG_EINVAL;
     TTG_CUDA_TRY(cudaSetDevice(c->device));
-    ttg_graph_free(c);
+    // The buffers are reused below: let a run still in flight finish first.
+    if (c->launched && c->stream) TTG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->uploaded = false;
+    c->launched = false;
     const int n = gd->n_tasks;
     const int64_t n_edges = n > 0 ? gd->succ_ptr[n] : 0;
     if (n_edges > 0 && !gd->succ_idx) return TTG_EINVAL;
@@ -499,10 +517,10 @@ extern "C" ttg_status ttg_graph_upload(ttg_ctx* c, const ttg_graph_desc* gd) {
     g.q_total = q_off[kMaxLevels];
     g.bq_total = bq_off[W];
     ttg_status st;
-#define ALLOC(ptr, cnt)                                 \
-    if ((st = dev_alloc(&g.ptr, (cnt))) != TTG_OK) {    \
-        ttg_graph_free(c);                              \
-        return st;                                      \
+#define ALLOC(ptr, cnt)                                    \
+    if ((st = dev_reserve(g, &g.ptr, (cnt))) != TTG_OK) {  \
+        ttg_graph_free(c);                                 \
+        return st;                                         \
     }
     ALLOC(ops, n);
     ALLOC(init, n);
@@ -646,8 +664,22 @@ ttg_status ttg_launch_executor(ttg_ctx* c, const ExecParams& p, cudaStream_t s) 
     if (c->g_mixed) return ttg_launch_mixed(c, p, s);
     const int smem = kPlainSmemDoubles * (int)sizeof(double);
     void* args[] = {(void*)&p};
-    TTG_CUDA_TRY(ttg_launch_cooperative((const void*)exec_kernel, c->workers, kThreads, args, smem, s));
+    TTG_CUDA_TRY(ttg_launch_executor_kernel(c, (const void*)exec_kernel, args, smem, s));
     return TTG_OK;
+}
+
+// The executor kernel needs every block resident only when a task is bound
+// to a block (its bound queue waits for that block); without bound tasks any
+// resident subset makes progress, and a context may launch it as a plain
+// kernel so that it shares the GPU with another context's executor.
+cudaError_t ttg_launch_executor_kernel(ttg_ctx* c, const void* fn, void** args, size_t smem, cudaStream_t s) {
+    if (c->coop || c->g.has_bound) return ttg_launch_cooperative(fn, c->workers, kThreads, args, smem, s);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(c->workers);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
 ttg_status ttg_enqueue_run(ttg_ctx* c, cudaStream_t s) {

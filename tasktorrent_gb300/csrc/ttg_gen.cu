@@ -35,18 +35,13 @@ __global__ void gen_qgauss_kernel(int8_t* G, int N, int ldg, uint32_t seed) {
     }
 }
 
-// One 64×64 block of the lower tile (ti, tj): 256 threads, 4×4 outputs each,
-// K staged 64 bytes (16 words) at a time.
-__global__ void gram_tiles_kernel(const int8_t* __restrict__ G, int N, int ldg, const int* __restrict__ blk,
-                                  const int* __restrict__ displ, const int64_t* __restrict__ off, int nb,
-                                  const int* __restrict__ work, int n_work, double alpha, double* tiles) {
+// One 64×64 block of a tile T (ld bi) of A = G·Gᵀ/N + αI: rows r0.. of the
+// tile (global row gi0 = first row of the block), columns c0.. (global gj0);
+// 256 threads, 4×4 outputs each, K staged 64 bytes (16 words) at a time.
+__device__ void gram_block(const int8_t* __restrict__ G, int N, int ldg, int gi0, int gj0, int r0, int c0, int bi, int bj,
+                           double alpha, double* T) {
     __shared__ int Gi[64][17];
     __shared__ int Gj[64][17];
-    const int w = blockIdx.x;
-    if (w >= n_work) return;
-    const int ti = work[4 * w + 0], tj = work[4 * w + 1], r0 = work[4 * w + 2], c0 = work[4 * w + 3];
-    const int bi = blk[ti], bj = blk[tj];
-    const int gi0 = displ[ti] + r0, gj0 = displ[tj] + c0;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     int acc[4][4] = {};
     const int* G32 = reinterpret_cast<const int*>(G);
@@ -74,7 +69,6 @@ __global__ void gram_tiles_kernel(const int8_t* __restrict__ G, int N, int ldg, 
         __syncthreads();
     }
     const double scale = 256.0 * (double)N;
-    double* T = tiles + off[ti + (int64_t)tj * nb];
 #pragma unroll
     for (int r = 0; r < 4; ++r)
 #pragma unroll
@@ -82,10 +76,42 @@ __global__ void gram_tiles_kernel(const int8_t* __restrict__ G, int N, int ldg, 
             const int lr = r0 + tx + 16 * r, lc = c0 + ty + 16 * c;
             if (lr < bi && lc < bj) {
                 double v = __ddiv_rn((double)acc[r][c], scale);
-                if (displ[ti] + lr == displ[tj] + lc) v = __dadd_rn(v, alpha);
+                if (gi0 - r0 + lr == gj0 - c0 + lc) v = __dadd_rn(v, alpha);
                 T[lr + (int64_t)lc * bi] = v;
             }
         }
+}
+
+// One 64×64 block of the lower tile (ti, tj) from a work list.
+__global__ void gram_tiles_kernel(const int8_t* __restrict__ G, int N, int ldg, const int* __restrict__ blk,
+                                  const int* __restrict__ displ, const int64_t* __restrict__ off, int nb,
+                                  const int* __restrict__ work, int n_work, double alpha, double* tiles) {
+    const int w = blockIdx.x;
+    if (w >= n_work) return;
+    const int ti = work[4 * w + 0], tj = work[4 * w + 1], r0 = work[4 * w + 2], c0 = work[4 * w + 3];
+    gram_block(G, N, ldg, displ[ti] + r0, displ[tj] + c0, r0, c0, blk[ti], blk[tj], alpha, tiles + off[ti + (int64_t)tj * nb]);
+}
+
+// nrhs × n row block (ld nrhs): element (q, r) = entry (r, q) of the
+// column-major n × nrhs N(0,1) array of (seed, stream 1).
+__global__ void rhs_rows_kernel(int n, int nrhs, uint32_t seed, double* B) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n * nrhs; e += gridDim.x * blockDim.x) {
+        const int r = e % n, q = e / n;
+        B[q + (int64_t)r * nrhs] = ttg_normal_at((uint64_t)e, seed, TTG_STREAM_RHS);
+    }
+}
+
+// Uniform tiles of size `tile` (a multiple of 64, or >= N), the last one
+// ragged: block (x, y) of the grid is the 64×64 block at global rows 64y,
+// columns 64x; blocks above the diagonal tiles return.
+__global__ void gram_grid_kernel(const int8_t* __restrict__ G, int N, int ldg, int tile, double alpha, double* tiles) {
+    const int gr = blockIdx.y * 64, gc = blockIdx.x * 64;
+    const int ti = gr / tile, tj = gc / tile;
+    if (ti < tj || gr >= N || gc >= N) return;
+    const int nb = (N + tile - 1) / tile;
+    auto bs = [&](int i) { return i < nb - 1 ? tile : N - (nb - 1) * tile; };
+    const int64_t off = (int64_t)tile * ((int64_t)tj * N - (int64_t)tile * tj * (tj - 1) / 2) + (int64_t)(ti - tj) * tile * bs(tj);
+    gram_block(G, N, ldg, gr, gc, gr - ti * tile, gc - tj * tile, bs(ti), bs(tj), alpha, tiles + off);
 }
 
 __global__ void gen_uniform_kernel(double* out, int64_t count, uint32_t seed, uint32_t stream) {
@@ -262,3 +288,25 @@ extern "C" ttg_status ttg_gen_normal(ttg_ctx* c, int64_t count, uint32_t seed, u
     TTG_CUDA_CHECK(cudaGetLastError());
     return TTG_OK;
 }
+
+ttg_status ttg_gen_gram_async(ttg_ctx* c, int n, int tile, double alpha, uint32_t seed, double* d_tiles, cudaStream_t s) {
+    if (!c || n <= 0 || n > 131072 || tile <= 0 || (tile < n && tile % 64 != 0) || !d_tiles) return TTG_EINVAL;
+    const int ldg = (n + 63) / 64 * 64;
+    int8_t* G = nullptr;
+    TTG_CUDA_CHECK(cudaMallocAsync((void**)&G, (size_t)n * ldg, s));
+    TTG_CUDA_CHECK(cudaMemsetAsync(G, 0, (size_t)n * ldg, s));
+    gen_qgauss_kernel<<<c->sms * 8, 256, 0, s>>>(G, n, ldg, seed);
+    const int nB = (n + 63) / 64;
+    gram_grid_kernel<<<dim3(nB, nB), 256, 0, s>>>(G, n, ldg, tile < n ? tile : n, alpha, d_tiles);
+    TTG_CUDA_CHECK(cudaGetLastError());
+    TTG_CUDA_CHECK(cudaFreeAsync(G, s));
+    return TTG_OK;
+}
+
+ttg_status ttg_gen_rhs_rows_async(int n, int nrhs, uint32_t seed, double* d_B, cudaStream_t s) {
+    if (n <= 0 || nrhs < 1 || !d_B) return TTG_EINVAL;
+    rhs_rows_kernel<<<std::min(1024, (n * nrhs + 255) / 256), 256, 0, s>>>(n, nrhs, seed, d_B);
+    TTG_CUDA_CHECK(cudaGetLastError());
+    return TTG_OK;
+}
+

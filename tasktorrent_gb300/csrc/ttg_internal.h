@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <unordered_map>
+
 #include "../../include/ttg.h"
 
 namespace ttg {
@@ -44,6 +46,10 @@ struct DevGraph {
     int n_team = 0;             // POTRF tasks factored by a team of blocks
     int* team_ctr = nullptr;    // kTeamStride words per team task
     int* team_slot = nullptr;   // per task: team counter block or -1
+    // Capacity (elements) of each buffer above, keyed by the field's address:
+    // a new upload reuses buffers that are large enough, so uploading a graph
+    // frees nothing (cudaFree would wait for the whole device).
+    std::unordered_map<const void*, size_t> cap;
 };
 
 struct ttg_ctx {
@@ -56,6 +62,8 @@ struct ttg_ctx {
     bool uploaded = false;
     bool launched = false;
     bool g_mixed = false;     // the uploaded graph has mixed-precision tasks
+    bool coop = true;         // cooperative launches (off: graphs without bound tasks may
+                              // start while other kernels hold part of the GPU)
     uint64_t graph_gen = 0;   // incremented by every successful upload
     int pending_host = 0;     // tasks that will never become ready
     bool overcount_host = false;
@@ -78,6 +86,8 @@ cudaError_t ttg_launch_cooperative(const void* fn, int grid, int block, void** a
 // Enqueue the counter/queue reset and the executor launch of the uploaded
 // graph on s (no events): the body of a recorded CUDA graph.
 ttg_status ttg_enqueue_run(ttg_ctx* c, cudaStream_t s);
+// Cooperative, or plain when c->coop is off and the graph has no bound tasks.
+cudaError_t ttg_launch_executor_kernel(ttg_ctx* c, const void* fn, void** args, size_t smem, cudaStream_t s);
 // After a recorded graph holding ttg_enqueue_run was launched on s between
 // the context's events: let ttg_wait collect the run.
 ttg_status ttg_mark_launched(ttg_ctx* c, cudaStream_t s);
@@ -89,6 +99,14 @@ int ttg_task_parts(const ttg_op& op, bool team = false);
 
 // Lower tiles of the miniapp matrix 1/((i-j)^2+1) (ttg_gen.cu).
 ttg_status ttg_gen_miniapp_tiles(ttg_ctx* c, const int32_t* h_bs, int32_t nb, double* d_tiles, void* stream);
+
+// Lower tiles (uniform tile, a multiple of 64 or >= n, the last ragged) of
+// A = G·Gᵀ/n + αI as ttg_gen_gram_tiles, enqueued on s without waiting
+// (stream-ordered scratch).
+ttg_status ttg_gen_gram_async(ttg_ctx* c, int n, int tile, double alpha, uint32_t seed, double* d_tiles, cudaStream_t s);
+// Right-hand sides as an nrhs × n row block (ld nrhs), entry (r, q) of the
+// column-major N(0,1) array of (seed, stream 1); enqueued on s.
+ttg_status ttg_gen_rhs_rows_async(int n, int nrhs, uint32_t seed, double* d_B, cudaStream_t s);
 
 // Block-GEMM inputs in tile layout (ttg_gen.cu).
 ttg_status ttg_gen_gemm_tiles(ttg_ctx* c, int32_t N, int32_t b, int32_t inputs, uint32_t seed, double* d_A, double* d_B,

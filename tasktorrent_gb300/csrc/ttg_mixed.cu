@@ -221,7 +221,7 @@ ttg_status ttg_launch_mixed(ttg_ctx* c, const ExecParams& p, cudaStream_t s) {
     if (!m || c->workers > m->max_workers) return TTG_EINVAL;
     const int smem = kMixedSmemBytes;
     void* args[] = {(void*)&p, (void*)&m->globals};
-    TTG_CUDA_CHECK(ttg_launch_cooperative((const void*)exec_kernel_mixed, c->workers, kThreads, args, smem, s));
+    TTG_CUDA_CHECK(ttg_launch_executor_kernel(c, (const void*)exec_kernel_mixed, args, smem, s));
     return TTG_OK;
 }
 
