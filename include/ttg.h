@@ -52,6 +52,11 @@ const char* ttg_strerror(ttg_status s);
  * (the failing call and its source location), or an empty string. */
 const char* ttg_last_cuda_error(void);
 
+/* Kernels this library has launched in the process so far (executor runs,
+ * solver, generator and conversion kernels; a replayed CUDA graph counts its
+ * kernels again).  Differences bracket a region of work. */
+int64_t ttg_kernel_launches(void);
+
 /* ------------------------------------------------------------------ tasks */
 
 /* Tile operation of one task.  The reference task bodies call BLAS/LAPACK on

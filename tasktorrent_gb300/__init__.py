@@ -117,6 +117,7 @@ SIGNATURES = {
     # include/ttg.h
     "ttg_strerror": (ctypes.c_char_p, [ctypes.c_int]),
     "ttg_last_cuda_error": (ctypes.c_char_p, []),
+    "ttg_kernel_launches": (ctypes.c_int64, []),
     "ttg_create": (_STATUS, [ctypes.POINTER(_P), ctypes.POINTER(Opts)]),
     "ttg_destroy": (_STATUS, [_P]),
     "ttg_graph_upload": (_STATUS, [_P, ctypes.POINTER(GraphDesc)]),

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -92,6 +93,10 @@ void ttg_set_last_cuda_error(cudaError_t e, const char* expr, const char* file, 
 }
 
 extern "C" const char* ttg_last_cuda_error(void) { return g_last_cuda; }
+
+static std::atomic<long long> g_launches{0};
+void ttg_note_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+extern "C" int64_t ttg_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
 
 extern "C" const char* ttg_strerror(ttg_status s) {
     switch (s) {
@@ -664,6 +669,7 @@ ttg_status ttg_launch_executor(ttg_ctx* c, const ExecParams& p, cudaStream_t s) 
     if (c->g_mixed) return ttg_launch_mixed(c, p, s);
     const int smem = kPlainSmemDoubles * (int)sizeof(double);
     void* args[] = {(void*)&p};
+    ttg_note_launch();
     TTG_CUDA_TRY(ttg_launch_executor_kernel(c, (const void*)exec_kernel, args, smem, s));
     return TTG_OK;
 }
@@ -707,6 +713,7 @@ extern "C" ttg_status ttg_wait(ttg_ctx* c, ttg_report* rep) {
     TTG_CUDA_TRY(cudaSetDevice(c->device));
     DevGraph& g = c->g;
     // status[4..6] <- ran, pending, bad
+    ttg_note_launch();
     summarize_kernel<<<std::max(1, std::min(256, (g.n_tasks + 255) / 256)), 256, 0, c->stream>>>(
         g.runs, g.count, g.runnable, g.n_tasks, c->status + 4);
     TTG_CUDA_TRY(cudaGetLastError());
@@ -803,8 +810,10 @@ extern "C" ttg_status ttg_measure_fp64_peak(ttg_ctx* c, double ms, double* tflop
     int iters = 2000;
     float t = 0.f;
     for (int pass = 0; pass < 2; ++pass) {
+        ttg_note_launch();
         fp64_peak_kernel<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
         cudaEventRecord(e0);
+        ttg_note_launch();
         fp64_peak_kernel<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
         cudaEventRecord(e1);
         cudaEventSynchronize(e1);

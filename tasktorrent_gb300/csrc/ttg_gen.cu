@@ -173,6 +173,7 @@ ttg_status ttg_gen_gemm_tiles(ttg_ctx* c, int32_t N, int32_t b, int32_t inputs, 
                               void* stream) {
     if (!c || N <= 0 || b <= 0 || N % b != 0 || !d_A || !d_B) return TTG_EINVAL;
     TTG_CUDA_CHECK(cudaSetDevice(c->device));
+    ttg_note_launch();
     gemm_tiles_kernel<<<c->sms * 8, 256, 0, (cudaStream_t)stream>>>(N, b, inputs, seed, d_A, d_B);
     TTG_CUDA_CHECK(cudaGetLastError());
     TTG_CUDA_CHECK(cudaStreamSynchronize((cudaStream_t)stream));
@@ -196,6 +197,7 @@ ttg_status ttg_gen_miniapp_tiles(ttg_ctx* c, const int32_t* h_bs, int32_t nb, do
     TTG_CUDA_CHECK(cudaMemcpyAsync(d_displ, displ.data(), sizeof(int) * (nb + 1), cudaMemcpyHostToDevice, s));
     TTG_CUDA_CHECK(cudaMemcpyAsync(d_off, off.data(), sizeof(int64_t) * nb * nb, cudaMemcpyHostToDevice, s));
     dim3 grid(8, nb, nb);
+    ttg_note_launch();
     miniapp_tiles_kernel<<<grid, 256, 0, s>>>(d_blk, d_displ, d_off, nb, d_tiles);
     TTG_CUDA_CHECK(cudaGetLastError());
     TTG_CUDA_CHECK(cudaStreamSynchronize(s));
@@ -254,9 +256,12 @@ extern "C" ttg_status ttg_gen_gram_tiles(ttg_ctx* c, int32_t n, const int32_t* h
         cudaMemcpyAsync(d_displ, displ.data(), sizeof(int) * (nb + 1), cudaMemcpyHostToDevice, s);
         cudaMemcpyAsync(d_off, off.data(), sizeof(int64_t) * nb * nb, cudaMemcpyHostToDevice, s);
         cudaMemcpyAsync(d_work, work.data(), sizeof(int) * work.size(), cudaMemcpyHostToDevice, s);
+        ttg_note_launch();
         gen_qgauss_kernel<<<c->sms * 8, 256, 0, s>>>(G, n, ldg, seed);
-        if (n_work > 0)
+        if (n_work > 0) {
+            ttg_note_launch();
             gram_tiles_kernel<<<n_work, 256, 0, s>>>(G, n, ldg, d_blk, d_displ, d_off, nb, d_work, n_work, alpha, d_tiles);
+        }
         if ((e = cudaGetLastError()) != cudaSuccess) fail(e, "gram kernels");
         // Host vectors above must outlive the async copies.
         if (st == TTG_OK && (e = cudaStreamSynchronize(s)) != cudaSuccess) fail(e, "sync");
@@ -274,6 +279,7 @@ extern "C" ttg_status ttg_gen_uniform(ttg_ctx* c, int64_t count, uint32_t seed, 
     if (!c || count < 0 || (count > 0 && !d_out)) return TTG_EINVAL;
     if (count == 0) return TTG_OK;
     TTG_CUDA_CHECK(cudaSetDevice(c->device));
+    ttg_note_launch();
     gen_uniform_kernel<<<c->sms * 8, 256, 0, (cudaStream_t)stream>>>(d_out, count, seed, stream_id);
     TTG_CUDA_CHECK(cudaGetLastError());
     return TTG_OK;
@@ -284,6 +290,7 @@ extern "C" ttg_status ttg_gen_normal(ttg_ctx* c, int64_t count, uint32_t seed, u
     if (!c || count < 0 || (count > 0 && !d_out)) return TTG_EINVAL;
     if (count == 0) return TTG_OK;
     TTG_CUDA_CHECK(cudaSetDevice(c->device));
+    ttg_note_launch();
     gen_normal_kernel<<<c->sms * 8, 256, 0, (cudaStream_t)stream>>>(d_out, count, seed, stream_id);
     TTG_CUDA_CHECK(cudaGetLastError());
     return TTG_OK;
@@ -295,8 +302,10 @@ ttg_status ttg_gen_gram_async(ttg_ctx* c, int n, int tile, double alpha, uint32_
     int8_t* G = nullptr;
     TTG_CUDA_CHECK(cudaMallocAsync((void**)&G, (size_t)n * ldg, s));
     TTG_CUDA_CHECK(cudaMemsetAsync(G, 0, (size_t)n * ldg, s));
+    ttg_note_launch();
     gen_qgauss_kernel<<<c->sms * 8, 256, 0, s>>>(G, n, ldg, seed);
     const int nB = (n + 63) / 64;
+    ttg_note_launch();
     gram_grid_kernel<<<dim3(nB, nB), 256, 0, s>>>(G, n, ldg, tile < n ? tile : n, alpha, d_tiles);
     TTG_CUDA_CHECK(cudaGetLastError());
     TTG_CUDA_CHECK(cudaFreeAsync(G, s));
@@ -305,6 +314,7 @@ ttg_status ttg_gen_gram_async(ttg_ctx* c, int n, int tile, double alpha, uint32_
 
 ttg_status ttg_gen_rhs_rows_async(int n, int nrhs, uint32_t seed, double* d_B, cudaStream_t s) {
     if (n <= 0 || nrhs < 1 || !d_B) return TTG_EINVAL;
+    ttg_note_launch();
     rhs_rows_kernel<<<std::min(1024, (n * nrhs + 255) / 256), 256, 0, s>>>(n, nrhs, seed, d_B);
     TTG_CUDA_CHECK(cudaGetLastError());
     return TTG_OK;

@@ -77,6 +77,8 @@ struct ttg_ctx {
 };
 
 void ttg_set_last_cuda_error(cudaError_t e, const char* expr, const char* file, int line);
+// Count one kernel launch of this library (ttg_kernel_launches).
+void ttg_note_launch(int n = 1);
 ttg_status ttg_ctx_init_device(ttg_ctx* c);
 ttg_status ttg_reset_state(ttg_ctx* c, cudaStream_t s);
 ttg_status ttg_launch_executor(ttg_ctx* c, const ttg::ExecParams& p, cudaStream_t s);

@@ -221,6 +221,7 @@ ttg_status ttg_launch_mixed(ttg_ctx* c, const ExecParams& p, cudaStream_t s) {
     if (!m || c->workers > m->max_workers) return TTG_EINVAL;
     const int smem = kMixedSmemBytes;
     void* args[] = {(void*)&p, (void*)&m->globals};
+    ttg_note_launch();
     TTG_CUDA_CHECK(ttg_launch_executor_kernel(c, (const void*)exec_kernel_mixed, args, smem, s));
     return TTG_OK;
 }
@@ -395,17 +396,20 @@ ttg_op ttg_mixed_update_op(ttg_mixed_state* m, int k, int i, int j, bool tc) {
 
 ttg_status ttg_mixed_prepare(ttg_mixed_state* m, void* stream, double shift, bool tc) {
     cudaStream_t s = (cudaStream_t)stream;
+    ttg_note_launch();
     convert_f64_to_f32<<<m->ctx->sms * 8, 256, 0, s>>>(m->tiles64, m->w32, m->elems);
     TTG_CUDA_CHECK(cudaGetLastError());
     if (shift > 0) {
         for (int j = 0; j < m->nb; ++j) {
             const int64_t o = m->off[j + (size_t)j * m->nb];
+            ttg_note_launch();
             shift_diagonal<<<(m->bs[j] + 255) / 256, 256, 0, s>>>(m->w32 + o, m->bs[j], shift);
         }
         TTG_CUDA_CHECK(cudaGetLastError());
     }
     MixedCtx* mc = (MixedCtx*)m->ctx->mixed;
     if (m->kind == 0 && tc) {
+        ttg_note_launch();
         block_row_scales<<<m->nb, 256, 0, s>>>(m->tiles64, m->diag_off, m->b, m->nb, m->rowscale);
         TTG_CUDA_CHECK(cudaGetLastError());
         mc->globals = m->globals;
@@ -416,6 +420,7 @@ ttg_status ttg_mixed_prepare(ttg_mixed_state* m, void* stream, double shift, boo
 }
 
 const double* ttg_mixed_factor_tiles(ttg_mixed_state* m) {
+    ttg_note_launch();
     convert_f32_to_f64<<<m->ctx->sms * 8, 256>>>(m->w32, m->tiles64, m->elems);
     if (cudaStreamSynchronize(nullptr) != cudaSuccess) return nullptr;
     return m->tiles64;

@@ -345,7 +345,9 @@ ttg_status dispatch(ttg_serve* s, Lane& L, std::deque<int>& queue) {
     for (int k = 0; k < n; ++k) slices = std::max(slices, (s->req[L.reqs[k]].N + kRowsPerBlock - 1) / kRowsPerBlock);
     TTG_CUDA_CHECK(cudaMemcpyAsync(L.d_items, L.h_items, sizeof(BwdItem) * n, cudaMemcpyHostToDevice, L.s));
     TTG_CUDA_CHECK(cudaMemsetAsync(L.d_acc, 0, sizeof(unsigned long long) * 33 * n, L.s));
+    ttg_note_launch();
     serve_bwd_partial<<<dim3(n, slices), kRowsPerBlock, 0, L.s>>>(L.d_items);
+    ttg_note_launch();
     serve_bwd_final<<<1, 128, 0, L.s>>>(L.d_items, n, L.d_err);
     TTG_CUDA_CHECK(cudaGetLastError());
     TTG_CUDA_CHECK(cudaMemcpyAsync(L.h_err, L.d_err, sizeof(double) * n, cudaMemcpyDeviceToHost, L.s));

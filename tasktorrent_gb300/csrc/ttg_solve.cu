@@ -259,12 +259,15 @@ static ttg_status ensure_dense(ttg_solver* S, const double* pristine, cudaStream
     const size_t NN = (size_t)S->N * S->N;
     ttg_status st = S->A64.ensure(NN);
     if (st != TTG_OK) return st;
+    ttg_note_launch();
     dense_from_tiles<double, double><<<S->ctx->sms * 8, 256, 0, s>>>(S->lay, S->d_rowblk.p, pristine, S->A64.p);
     if (S->mixed) {
         if ((st = S->A32.ensure(NN)) != TTG_OK) return st;
+        ttg_note_launch();
         dense_from_tiles<double, float><<<S->ctx->sms * 8, 256, 0, s>>>(S->lay, S->d_rowblk.p, pristine, S->A32.p);
     }
     if ((st = S->T1.ensure(S->N)) != TTG_OK) return st;
+    ttg_note_launch();
     row_abs_sums<double><<<(S->N + 255) / 256, 256, 0, s>>>(S->N, S->A64.p, S->T1.p);
     TTG_CUDA_CHECK(cudaGetLastError());
     std::vector<double> rs(S->N);
@@ -286,10 +289,14 @@ static ttg_status prepare_operands(ttg_solver* S, const TM* L, DevBuf<TM>& inv, 
     ttg_status st;
     if ((st = inv.ensure(S->dsize)) != TTG_OK || (st = linv.ensure(S->dsize)) != TTG_OK || (st = lt.ensure(S->elems)) != TTG_OK)
         return st;
+    ttg_note_launch();
     invert_diag_tiles<TM><<<dim3(S->nb, parts), kThreads, smem, s>>>(S->lay, S->d_doff.p, L, inv.p, parts);
+    ttg_note_launch();
     transpose_tiles<TM><<<S->ctx->sms * 8, 256, 0, s>>>(S->d_tdesc_diag.p, S->d_tsub_diag.p, S->n_tdesc_diag, inv.p, linv.p);
-    if (S->n_tdesc_off > 0)
+    if (S->n_tdesc_off > 0) {
+        ttg_note_launch();
         transpose_tiles<TM><<<S->ctx->sms * 8, 256, 0, s>>>(S->d_tdesc_off.p, S->d_tsub_off.p, S->n_tdesc_off, L, lt.p);
+    }
     TTG_CUDA_CHECK(cudaGetLastError());
     return TTG_OK;
 }
@@ -327,8 +334,14 @@ ttg_status sweeps(ttg_solver* S, const TM* L, const TM* LT, const TM* Linv, cons
         a.applied = ctr + 2 + S->nb;
         a.backward = dir;
         a.step_start = dir ? S->d_step_bwd.p : S->d_step_fwd.p;
-        if (dir == 0) sweep_kernel<T, TM><<<grid, 256, smem, s>>>(a, L, Linv, R, Y);
-        else sweep_kernel<T, TM><<<grid, 256, smem, s>>>(a, LT, invT, Y, X);
+        if (dir == 0) {
+            ttg_note_launch();
+            sweep_kernel<T, TM><<<grid, 256, smem, s>>>(a, L, Linv, R, Y);
+        }
+        else {
+            ttg_note_launch();
+            sweep_kernel<T, TM><<<grid, 256, smem, s>>>(a, LT, invT, Y, X);
+        }
         TTG_CUDA_CHECK(cudaGetLastError());
     }
     return TTG_OK;
@@ -339,7 +352,9 @@ template <class T>
 ttg_status matmul(ttg_solver* S, const T* A, const T* X, const T* B, T* Y, T* P, int nrhs, int mode, cudaStream_t s) {
     const int splits = 4;
     dim3 grid((S->N + 127) / 128, splits);
+    ttg_note_launch();
     dense_matmul_partial<T><<<grid, 256, 0, s>>>(S->N, A, X, nrhs, P, splits);
+    ttg_note_launch();
     reduce_partials<T><<<S->ctx->sms * 4, 256, 0, s>>>(S->N, nrhs, P, splits, B, Y, mode);
     TTG_CUDA_CHECK(cudaGetLastError());
     return TTG_OK;
@@ -349,7 +364,9 @@ ttg_status matmul(ttg_solver* S, const T* A, const T* X, const T* B, T* Y, T* P,
 template <class T>
 ttg_status colreduce(ttg_solver* S, const T* X, const T* Y, int nrhs, int kind, double* host, cudaStream_t s) {
     const int blocks = 128;
+    ttg_note_launch();
     column_reduce_partial<T><<<blocks, 256, 0, s>>>(S->N, nrhs, X, Y, kind, S->part.p);
+    ttg_note_launch();
     column_reduce_final<<<1, 32, 0, s>>>(nrhs, blocks, S->part.p, kind, S->colv.p);
     TTG_CUDA_CHECK(cudaGetLastError());
     TTG_CUDA_CHECK(cudaMemcpyAsync(host, S->colv.p, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s));
@@ -363,6 +380,7 @@ ttg_status axpby(ttg_solver* S, const std::vector<double>& a, const TX* X, const
                  cudaStream_t s) {
     TTG_CUDA_CHECK(cudaMemcpyAsync(S->coefA.p, a.data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, s));
     if (b) TTG_CUDA_CHECK(cudaMemcpyAsync(S->coefB.p, b->data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, s));
+    ttg_note_launch();
     column_axpby<TX, TY><<<S->ctx->sms * 4, 256, 0, s>>>(S->N, nrhs, S->coefA.p, X, b ? S->coefB.p : nullptr, Y);
     TTG_CUDA_CHECK(cudaGetLastError());
     return TTG_OK;
