@@ -155,6 +155,64 @@ def _tasks(nb):
     return nb + nb * (nb - 1) // 2 + (nb - 1) * nb * (nb + 1) // 6
 
 
+def run_batched(ctx, args):
+    """cfg4: many independent SPD systems (N log-uniform in [32, 2048], A_i from
+    seed 3 + i, one right-hand side each) in one executor launch replayed as a
+    CUDA graph; tile size and worker count from the autotuner; FP64 plain and
+    FP32 factor + in-launch refinement."""
+    import numpy as np
+    import tasktorrent_gb300 as t
+    rng = np.random.default_rng(3)
+    sizes = np.exp(rng.uniform(np.log(32), np.log(2048), args.batch_n)).astype(np.int32)
+    out = {"systems": int(args.batch_n), "sizes": "log-uniform [32, 2048] (numpy default_rng(3))",
+           "flops_total": float(np.sum(sizes.astype(np.float64) ** 3) / 3.0)}
+    for name, prec in (("fp64", t.PREC_F64), ("mixed", t.PREC_MIXED)):
+        tile, workers, _ = t.batch_autotune(ctx, sizes, [64, 128, 256], [0, t.lib().ttg_workers(ctx.h) // 2],
+                                            precision=prec, ir_steps=2, max_sample=300)
+        b = t.Batch(ctx, sizes, tile, precision=prec, nrhs=1, ir_steps=2, seed=3, alpha=1.0)
+        b.run()
+        ms = []
+        for _ in range(3):
+            st, rep = b.run()
+            if st != t.TTG_OK:
+                raise RuntimeError("batch run failed: %s" % t.strerror(st))
+            ms.append(rep.run.elapsed_ms)
+        errs = b.backward_errors()
+        best = min(ms)
+        out[name] = {"tile": tile, "workers": workers, "ms_per_batch": ms, "systems_per_s": args.batch_n / (best * 1e-3),
+                     "tflops": rep.flops / (best * 1e-3) / 1e12, "tasks": int(rep.tasks), "worst_bwd_err": float(errs.max()),
+                     "ir_steps": 2 if prec == t.PREC_MIXED else 0}
+        b.close()
+        t.check(t.lib().ttg_set_workers(ctx.h, 0), "reset workers")
+    out["speedup_mixed_vs_fp64"] = min(out["fp64"]["ms_per_batch"]) / min(out["mixed"]["ms_per_batch"])
+    return out
+
+
+def run_serving(args, local):
+    """cfg5: a Poisson stream of factor-and-solve requests (N log-uniform in
+    [64, 8192], A = G·Gᵀ/N + 1e-4·I, 30% follow-up right-hand sides on a
+    resident factor) over two executor lanes sharing the GPU, admission by an
+    180 GB HBM budget; p50/p99 latency and solves/s per arrival rate, mixed
+    (FP32 factor + FP64-residual refinement) and plain FP64."""
+    import tasktorrent_gb300 as t
+    out = {"requests_per_rate": args.serve_n, "n_range": [64, 8192], "alpha": 1e-4, "followup_frac": 0.3,
+           "hbm_budget_gb": 180.0, "lanes": 2}
+    for name, prec in (("mixed", t.PREC_MIXED), ("fp64", t.PREC_F64)):
+        rows = []
+        for rate in args.serve_rates:
+            s = t.Serve(args.serve_n, rate=rate, n_min=64, n_max=8192, alpha=1e-4, seed=2, followup_frac=0.3, precision=prec,
+                        ir_steps=4, lanes=2, max_batch=16, hbm_budget_gb=180.0, device=local)
+            st, rep, _ = s.run()
+            s.close()
+            if st != t.TTG_OK:
+                raise RuntimeError("serving failed: %s" % t.strerror(st))
+            d = rep.as_dict()
+            d["rate"] = rate
+            rows.append(d)
+        out[name] = rows
+    return out
+
+
 def run_ours(args, world, rank, local):
     import ctypes
     import numpy as np
@@ -203,6 +261,7 @@ def run_ours(args, world, rank, local):
     times, reps, kernel_ms = [], [], []
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
+        launches0 = lib.ttg_kernel_launches()
         w0 = time.perf_counter()
         for _ in range(args.steps):
             ms, rep = posv(plan)
@@ -211,6 +270,7 @@ def run_ours(args, world, rank, local):
             kernel_ms.append(rep.factor_ms)
         torch.cuda.synchronize()
         wall = time.perf_counter() - w0
+        gpu_launches = int(lib.ttg_kernel_launches() - launches0)
     barrier(world)
     step_ms = allmax(world, statistics.mean(times))
     value = world * flops / (step_ms * 1e-3) / 1e12
@@ -281,6 +341,10 @@ def run_ours(args, world, rank, local):
                               "gmres_prec": ra.gmres_prec, "remedy": ra.remedy, "bwd_err": ra.bwd_err})
             pa.close()
         extra["mixed_per_alpha"] = per_alpha
+    if not args.quick and not args.no_batched:
+        extra["batched"] = run_batched(ctx, args)
+    if not args.quick and not args.no_serving:
+        extra["serving"] = run_serving(args, local)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -307,7 +371,7 @@ def run_ours(args, world, rank, local):
                              "frac": achieved / bf16_peak, "traffic": None,
                              "kernel": "exec_kernel_mixed (one launch per factorisation); achieved = N^3/3 / its duration",
                              "peak_source": "measured: MEASURED_PEAKS.json bf16_tflops (burst)"},
-                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": None, "clocks": clk.summary()}
+                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches, "clocks": clk.summary()}
         line.update(extra)
         print(json.dumps(line))
     ctx.close()
@@ -330,7 +394,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", dest="no_cpu_baseline", action="store_true")
     ap.add_argument("--nrhs", type=int, default=16)
     ap.add_argument("--tol", type=float, default=1e-14)
-    ap.add_argument("--quick", action="store_true", help="skip the FP64 and per-alpha comparison runs")
+    ap.add_argument("--quick", action="store_true", help="skip the FP64, per-alpha, batched and serving runs")
+    ap.add_argument("--no-batched", dest="no_batched", action="store_true")
+    ap.add_argument("--no-serving", dest="no_serving", action="store_true")
+    ap.add_argument("--batch-n", dest="batch_n", type=int, default=10000)
+    ap.add_argument("--serve-n", dest="serve_n", type=int, default=600)
+    ap.add_argument("--serve-rates", dest="serve_rates", type=lambda s: [float(x) for x in s.split(",")],
+                    default=[100.0, 1000.0, 10000.0])
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
