@@ -445,7 +445,11 @@ class Threadpool_shared {
         if (verb_ > 0)
             printf("[%s] device run: %lld tasks, %.3f ms, status %s\n", basename_.c_str(), (long long)report_.tasks_run,
                    report_.elapsed_ms, ttg_strerror(s));
-        if (s != TTG_OK && s != TTG_EUNDERRUN) printf("Error: device executor: %s\n", ttg_strerror(s));
+        // On stderr (stdout carries the application's own output).  A tile that
+        // is not positive definite is reported by the status; callers that
+        // retry with a remedy (the mixed Cholesky plan) see it only at verb > 0.
+        if (s != TTG_OK && s != TTG_EUNDERRUN && (s != TTG_ENOTPD || verb_ > 0))
+            fprintf(stderr, "Error: device executor: %s\n", ttg_strerror(s));
         if (logger_) fill_logger(t0, t1);
         return s;
     }
