@@ -89,8 +89,8 @@ typedef struct ttg_op {
     int32_t lda, ldb, ldc;
     int32_t parts;     /* blocks that share the task: 0 = chosen by the executor
                           (one per 128×128 output block, up to 16; TRSM by
-                          128-row slices; POTRF: a team of n/32 blocks up to
-                          16 for n >= 128, else 1), else that many (POTRF:
+                          128-row slices; POTRF: a team of n/16 blocks up to
+                          32 for n >= 128, else 1), else that many (POTRF:
                           up to 64; the factor is the same for any count)   */
     int32_t flags;     /* reserved, 0                         */
     double alpha, beta;

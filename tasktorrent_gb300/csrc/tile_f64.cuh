@@ -295,7 +295,6 @@ __device__ __forceinline__ void geadd_f64(int m, int n, double alpha, const doub
 constexpr int kTeamCounters = 256;
 constexpr int kTeamPanelRows = 32;  // rows per panel item
 constexpr int kTeamCopyRows = 128;  // rows per widen / narrow item
-constexpr int kTeamBlock = 64;      // trailing-update block
 
 // Phases of potrf_l_f64_team on an n×n tile; the team form needs
 // 2·phases + 2 <= kTeamCounters.
@@ -372,69 +371,155 @@ __device__ __forceinline__ bool team_wait(const TeamCtx& tc, int ph, int items) 
     return s_ok != 0;
 }
 
-// Lower 64×64 block `item` of C[rest×rest] -= P·Pᵀ, P rest×nb (nb <= 32).
-// Blocks are numbered column by column over the lower triangle.
-__device__ inline void team_syrk_block(int rest, int nb, const double* P, int ldp, double* C, int ldc, int item, double* smem) {
-    double(*As)[kTeamBlock] = reinterpret_cast<double(*)[kTeamBlock]>(smem);
-    double(*Bs)[kTeamBlock] = reinterpret_cast<double(*)[kTeamBlock]>(smem + kPanel * kTeamBlock);
-    const int nbm = (rest + kTeamBlock - 1) / kTeamBlock;
-    int bj = 0, r = item;
-    while (r >= nbm - bj) {
-        r -= nbm - bj;
-        ++bj;
+// Shared-memory layout of the team POTRF (doubles): the 32×32 diagonal block
+// L (ld 33), its inverse X (ld 33), 1/L_cc, and two 32×33 work panels.
+constexpr int kTS = 0, kTX = 1056, kTInv = 2112, kTW1 = 2144, kTW2 = 3200, kTeamSmemDoubles = 4256;
+static_assert(kTeamSmemDoubles <= kF64SmemDoubles, "team POTRF shared memory");
+
+// Lower Cholesky of the nb×nb (nb <= 32) diagonal block at D (ld) in shared
+// memory S (ld 33) by warps 0-3: column c's pivot is taken by warp c % 4
+// (one rsqrt: l_cc = d·d^-1/2, the column scaled by d^-1/2, kept in inv[c]),
+// then warp w updates the columns j > c with j % 4 == w (lane = row).  Every
+// FP64 operation of a GB300 warp costs ~65 cycles whatever its active lanes,
+// so the column updates are spread over the four sub-partitions.  Returns 0
+// or the 1-based failing column; S and inv hold the factor.
+__device__ inline int team_diag_factor(const double* D, int ld, int nb, double* S, double* inv) {
+    __shared__ int s_info;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int e = threadIdx.x; e < 32 * 32; e += kThreads) {
+        const int i = e & 31, j = e >> 5;
+        S[i * 33 + j] = (i < nb && j < nb && i >= j) ? ldcg(D + i + (size_t)j * ld) : 0.0;
     }
-    const int bi = bj + r;
-    const int m0 = bi * kTeamBlock, n0 = bj * kTeamBlock;
-    for (int e = threadIdx.x; e < kPanel * kTeamBlock; e += kThreads) {
-        const int i = e % kTeamBlock, kk = e / kTeamBlock;
-        As[kk][i] = (m0 + i < rest && kk < nb) ? ldcg(P + m0 + i + (size_t)kk * ldp) : 0.0;
-        Bs[kk][i] = (n0 + i < rest && kk < nb) ? ldcg(P + n0 + i + (size_t)kk * ldp) : 0.0;
-    }
+    if (threadIdx.x == 0) s_info = 0;
     __syncthreads();
-    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    double acc[4][4];
-#pragma unroll
-    for (int a = 0; a < 4; ++a)
-#pragma unroll
-        for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
-#pragma unroll 8
-    for (int kk = 0; kk < kPanel; ++kk) {
-        double x[4], y[4];
-#pragma unroll
-        for (int a = 0; a < 4; ++a) x[a] = As[kk][tx + 16 * a];
-#pragma unroll
-        for (int b = 0; b < 4; ++b) y[b] = Bs[kk][ty + 16 * b];
-#pragma unroll
-        for (int a = 0; a < 4; ++a)
-#pragma unroll
-            for (int b = 0; b < 4; ++b) acc[a][b] = fma(x[a], y[b], acc[a][b]);
-    }
-#pragma unroll
-    for (int b = 0; b < 4; ++b) {
-        const int gj = n0 + ty + 16 * b;
-#pragma unroll
-        for (int a = 0; a < 4; ++a) {
-            const int gi = m0 + tx + 16 * a;
-            if (gi < rest && gj < rest && gi >= gj) {
-                double* q = C + gi + (size_t)gj * ldc;
-                *q = ldcg(q) - acc[a][b];
+    for (int c = 0; c < nb; ++c) {
+        if (warp == (c & 3)) {
+            const double d = S[c * 33 + c];
+            if (!(d > 0.0)) {
+                if (lane == 0) s_info = c + 1;
+            } else {
+                const double y = rsqrt(d);
+                if (lane == c) {
+                    S[c * 33 + c] = d * y;
+                    inv[c] = y;
+                } else if (lane > c && lane < nb) {
+                    S[lane * 33 + c] *= y;
+                }
             }
         }
+        __syncthreads();
+        if (s_info) break;
+        if (warp < 4)
+            for (int j = c + 1 + ((warp - c - 1) & 3); j < nb; j += 4)
+                if (lane >= j && lane < nb) S[lane * 33 + j] = fma(-S[lane * 33 + c], S[j * 33 + c], S[lane * 33 + j]);
+        __syncthreads();
     }
+    return s_info;
+}
+
+// X = L⁻¹ (lower, ld 33) from the factor S and inv (1/L_ii) by warps 0-3:
+// row i of X is finished by warp i % 4, then warp w subtracts L_ji·X_i from
+// its rows j > i (lane = column).
+__device__ inline void team_diag_inverse(const double* S, const double* inv, int nb, double* X) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int e = threadIdx.x; e < 32 * 32; e += kThreads) {
+        const int j = e >> 5, c = e & 31;
+        X[j * 33 + c] = (j == c && j < nb) ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    for (int i = 0; i < nb; ++i) {
+        if (warp == (i & 3) && lane <= i) X[i * 33 + lane] *= inv[i];
+        __syncthreads();
+        if (warp < 4)
+            for (int j = i + 1 + ((warp - i - 1) & 3); j < nb; j += 4)
+                if (lane <= i) X[j * 33 + lane] = fma(-S[j * 33 + i], X[i * 33 + lane], X[j * 33 + lane]);
+        __syncthreads();
+    }
+}
+
+// Rows [r0, r0 + rows) (rows <= 32) of the panel P (columns 0..nb-1, ld) <-
+// P · L⁻ᵀ = P · Xᵀ: thread (r, g) computes columns g, g+8, g+16, g+24.
+__device__ inline void team_panel_rows(double* P, int ld, int r0, int rows, int nb, const double* X, double* W) {
+    for (int e = threadIdx.x; e < 32 * 32; e += kThreads) {
+        const int r = e & 31, c = e >> 5;
+        W[r * 33 + c] = (r < rows && c < nb) ? ldcg(P + r0 + r + (size_t)c * ld) : 0.0;
+    }
+    __syncthreads();
+    const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
+    double acc[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int j = g + 8 * k;
+        double a = 0.0;
+        for (int c = 0; c <= j && c < nb; ++c) a = fma(W[r * 33 + c], X[j * 33 + c], a);
+        acc[k] = a;
+    }
+    if (r < rows) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int j = g + 8 * k;
+            if (j < nb) P[r0 + r + (size_t)j * ld] = acc[k];
+        }
+    }
+    __syncthreads();
+}
+
+// Lower 32×32 block `item` (column by column over the lower triangle) of
+// C[rest×rest] -= Q·Qᵀ, Q rest×nb (nb <= 32, ld).
+__device__ inline void team_syrk_block32(int rest, int nb, const double* Q, int ld, double* C, int item, double* W1, double* W2) {
+    const int mb = (rest + 31) / 32;
+    int bj = 0, rr = item;
+    while (rr >= mb - bj) {
+        rr -= mb - bj;
+        ++bj;
+    }
+    const int bi = bj + rr;
+    const int m0 = bi * 32, n0 = bj * 32;
+    for (int e = threadIdx.x; e < 32 * 32; e += kThreads) {
+        const int r = e & 31, c = e >> 5;
+        W1[r * 33 + c] = (m0 + r < rest && c < nb) ? ldcg(Q + m0 + r + (size_t)c * ld) : 0.0;
+        W2[r * 33 + c] = (n0 + r < rest && c < nb) ? ldcg(Q + n0 + r + (size_t)c * ld) : 0.0;
+    }
+    __syncthreads();
+    const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
+    const bool diag = bi == bj;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int j = g + 8 * k;
+        const int gi = m0 + r, gj = n0 + j;
+        if (gi < rest && gj < rest && (!diag || r >= j)) {
+            double a = 0.0;
+#pragma unroll 8
+            for (int c = 0; c < kPanel; ++c) a = fma(W1[r * 33 + c], W2[j * 33 + c], a);
+            double* q = C + gi + (size_t)gj * ld;
+            *q = ldcg(q) - a;
+        }
+    }
+    __syncthreads();
 }
 
 // Team lower Cholesky of the FP64 tile A[n×n] (lda); requires
 // team_fits(n, W32 != nullptr).  With an FP32 source (W32 != nullptr) the
 // team first widens the lower triangle of W32 (ldw) into A and at the end
-// rounds the factor back into W32.  Returns 0, the 1-based failing column, or
-// -1 after a timeout.  *finisher (shared) is set to 1 in the one block that
-// completed the factorisation (or found the failing column), else 0: that
-// block releases the task's successors at once, whether or not the other
-// parts of the team have run yet.  The result is the same for any number of
-// blocks: every item computes the same arithmetic whoever runs it.
+// rounds the factor back into W32.  Per 32-column panel: the diagonal block
+// (one block, team_diag_factor), the panel rows in 32-row items (each block
+// that takes one first inverts the diagonal block for itself), the trailing
+// lower 32×32 blocks.  Returns 0, the 1-based failing column, or -1 after a
+// timeout.  *finisher (shared) is set to 1 in the one block that completed
+// the factorisation (or found the failing column), else 0: that block
+// releases the task's successors at once, whether or not the other parts of
+// the team have run yet.  The result is the same for any number of blocks:
+// every item computes the same arithmetic whoever runs it.
 __device__ inline int potrf_l_f64_team(int n, double* A, int lda, double* smem, const TeamCtx& tc, float* W32, int ldw,
                                        int* finisher) {
-    double* Ls = smem + kBK * kBM + kBK * kBNP;
+    double* S = smem + kTS;
+    double* X = smem + kTX;
+    double* inv = smem + kTInv;
+    double* W1 = smem + kTW1;
+    double* W2 = smem + kTW2;
+    // An empty tile has no phases: its parts complete as ordinary parts
+    // (*finisher keeps the executor's -1).
+    if (n <= 0) return 0;
     if (threadIdx.x == 0) *finisher = 0;
     int ph = 0;
     const int copy_items = (n + kTeamCopyRows - 1) / kTeamCopyRows;
@@ -457,12 +542,16 @@ __device__ inline int potrf_l_f64_team(int n, double* A, int lda, double* smem, 
         double* Dpp = A + p + (size_t)p * lda;
         if (team_claim(tc, ph) == 0) {
             __shared__ int s_bad;
-            if (threadIdx.x < 32) {
-                const int info = potrf_diag32_warp(Dpp, lda, nb);
-                if (threadIdx.x == 0) {
-                    s_bad = info != 0;
-                    if (info) atomicExch(tc.ctr + kTeamCounters - 1, p + info);
+            const int info = team_diag_factor(Dpp, lda, nb, S, inv);
+            if (info == 0) {
+                for (int e = threadIdx.x; e < 32 * 32; e += kThreads) {
+                    const int i = e & 31, j = e >> 5;
+                    if (i < nb && j <= i) Dpp[i + (size_t)j * lda] = S[i * 33 + j];
                 }
+            }
+            if (threadIdx.x == 0) {
+                s_bad = info != 0;
+                if (info) atomicExch(tc.ctr + kTeamCounters - 1, p + info);
             }
             team_done(tc, ph, 1);
             // The factorisation ends here after a failure, or after the last
@@ -476,20 +565,33 @@ __device__ inline int potrf_l_f64_team(int n, double* A, int lda, double* smem, 
         }
         const int rest = n - p - nb;
         if (rest <= 0) continue;
-        load_panel_block<double>(Dpp, lda, nb, Ls);
         const int pitems = (rest + kTeamPanelRows - 1) / kTeamPanelRows;
+        bool have_inverse = false;
         for (int it = team_claim(tc, ph + 1); it < pitems; it = team_claim(tc, ph + 1)) {
+            if (!have_inverse) {
+                // The factored diagonal block and 1/L_ii (this block may not
+                // be the one that factored it), then its inverse.
+                for (int e = threadIdx.x; e < 32 * 32; e += kThreads) {
+                    const int i = e & 31, j = e >> 5;
+                    S[i * 33 + j] = (i < nb && j < nb && i >= j) ? ldcg(Dpp + i + (size_t)j * lda) : 0.0;
+                }
+                __syncthreads();
+                if (threadIdx.x < nb) inv[threadIdx.x] = 1.0 / S[threadIdx.x * 33 + threadIdx.x];
+                __syncthreads();
+                team_diag_inverse(S, inv, nb, X);
+                have_inverse = true;
+            }
             const int r0 = p + nb + it * kTeamPanelRows;
-            trsm_rows_panel<double>(A + (size_t)p * lda, lda, r0, min(n, r0 + kTeamPanelRows), nb, Ls, 1.0);
+            team_panel_rows(A + (size_t)p * lda, lda, r0, min(kTeamPanelRows, n - r0), nb, X, W1);
             team_done(tc, ph + 1, pitems);
         }
         if (!team_wait(tc, ph + 1, pitems)) return -1;
-        const int nbm = (rest + kTeamBlock - 1) / kTeamBlock;
-        const int citems = nbm * (nbm + 1) / 2;
-        const double* P = A + (p + nb) + (size_t)p * lda;
+        const int mb = (rest + 31) / 32;
+        const int citems = mb * (mb + 1) / 2;
+        const double* Q = A + (p + nb) + (size_t)p * lda;
         double* C = A + (p + nb) + (size_t)(p + nb) * lda;
         for (int it = team_claim(tc, ph + 2); it < citems; it = team_claim(tc, ph + 2)) {
-            team_syrk_block(rest, nb, P, lda, C, lda, it, smem);
+            team_syrk_block32(rest, nb, Q, lda, C, it, W1, W2);
             team_done(tc, ph + 2, citems);
         }
         if (!team_wait(tc, ph + 2, citems)) return -1;

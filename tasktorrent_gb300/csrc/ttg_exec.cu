@@ -261,14 +261,14 @@ extern "C" uint64_t ttg_graph_generation(const ttg_ctx* c) { return c ? c->graph
 
 // Blocks that share one task: explicit op.parts, else one per 128×128 output
 // block (lower blocks for SYRK) up to 16, TRSM by 128-row slices up to 8;
-// POTRF (with team) by n/32 blocks up to 16 for n >= 128; no-op tasks and,
+// POTRF (with team) by n/16 blocks up to 32 for n >= 128; no-op tasks and,
 // without team, POTRF are never split.
 int ttg_task_parts(const ttg_op& op, bool team) {
     auto cdiv = [](long a, long b) { return (int)((a + b - 1) / b); };
     if (op.kind == TTG_OP_POTRF_L) {
         if (!team || !team_fits(op.n, op.prec == TTG_PREC_MIXED)) return 1;
         if (op.parts > 0) return std::min(op.parts, 64);
-        return op.n >= 128 ? std::min(16, op.n / 32) : 1;
+        return op.n >= 128 ? std::min(32, op.n / 16) : 1;
     }
     // Tensor-core updates of the mixed path: exactly one 128×256 output block
     // per part (lower-triangle blocks only for SYRK).
@@ -479,7 +479,10 @@ extern "C" ttg_status ttg_graph_upload(ttg_ctx* c, const ttg_graph_desc* gd) {
     int n_team = 0;
     for (int t = 0; t < n; ++t) {
         parts[t] = ttg_task_parts(gd->ops[t], true);
-        if (gd->ops[t].kind == TTG_OP_POTRF_L && parts[t] > 1) team_slot[t] = n_team++;
+        // Every POTRF that fits runs the team code, a team of one included, so
+        // the factor does not depend on how many blocks share it.
+        if (gd->ops[t].kind == TTG_OP_POTRF_L && team_fits(gd->ops[t].n, gd->ops[t].prec == TTG_PREC_MIXED))
+            team_slot[t] = n_team++;
     }
 
     // Queue layout: level queues sized by runnable unbound tasks per level,

@@ -228,6 +228,16 @@ def test_potrf_team_matches_one_block(ctx, n, parts):
     assert np.linalg.norm(np.tril(out[1]) - L) <= 1e-13 * np.linalg.norm(L)
 
 
+@pytest.mark.parametrize("parts", [0, 1, 4])
+def test_empty_potrf_releases_its_successor(ctx, parts):
+    """A 0×0 diagonal tile (ragged tilings can produce one) still completes."""
+    ops = [t.Op(kind=t.OP_POTRF_L, m=0, n=0, ldc=1, parts=parts), t.Op(kind=t.OP_NOP)]
+    ptr, idx = t.dag_edges_from_lists(2, [[1], []])
+    t.check(ctx.upload(ops, np.array([0, 1], np.int32), ptr, idx), "upload")
+    st, rep = ctx.run()
+    assert st == t.TTG_OK and rep.tasks_run == 2
+
+
 def test_potrf_team_not_positive_definite(ctx):
     import torch
     n = 300
