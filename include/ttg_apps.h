@@ -37,7 +37,9 @@ typedef struct ttg_chol_args {
     double alpha;
     uint32_t seed;
     int32_t precision;        /* TTG_PREC_F64 or TTG_PREC_MIXED                     */
-    int32_t mixed_kind;       /* mixed path: 0 = BF16 updates, 1 = FP32 updates       */
+    int32_t mixed_kind;       /* mixed path: 0 = BF16 tensor-core updates, 1 = FP32
+                                 updates, 2 = split-BF16 tensor-core updates (three
+                                 BF16 slices per operand, FP32-level accuracy)      */
 } ttg_chol_args;
 
 typedef struct ttg_chol_plan ttg_chol_plan;
@@ -130,8 +132,8 @@ typedef struct ttg_solve_report {
     double factor_ms;   /* factorisation (device events; 0 for ttg_chol_plan_solve)     */
     double solve_ms;    /* solve and refinement (host clock)                           */
     int32_t remedy;     /* mixed factor: 0 BF16 updates; after a loss of definiteness
-                           2 FP32 updates, 3 FP32 updates on A + 16·2^-24·diag(A),
-                           1 BF16 updates on A + 8·2^-8·diag(A)                      */
+                           4 split-BF16 updates, 2 FP32 updates, 3 FP32 updates on
+                           A + 16·2^-24·diag(A), 1 BF16 updates on A + 8·2^-8·diag(A) */
 } ttg_solve_report;
 
 /* d_B, d_X: device N×nrhs column-major (ld N). */

@@ -71,6 +71,7 @@ struct ttg_chol_plan {
     double* pristine = nullptr;  // input copy
     std::unique_ptr<Threadpool_shared> tp;    // the plan's graph (FP64, or mixed with BF16 updates when available)
     std::unique_ptr<Threadpool_shared> tp32;  // mixed plans with tensor cores: the same graph with FP32 updates
+    std::unique_ptr<Threadpool_shared> tpx3;  // ... and with split-BF16 updates (mixed_kind 0)
     int remedy = 0;                           // last mixed factorisation: 0 none, 1 diagonal shift, 2 FP32 updates
     std::vector<int> kind_of_dev;  // per device task: 0 potrf, 1 trsm, 2 gemm, 3 accu, -1 other
     std::vector<double*> tmp;      // accumulate-flow temporaries (device)
@@ -82,7 +83,7 @@ struct ttg_chol_plan {
     long solver_gen = -1;  // factorisation the solver's inverted tiles belong to
 };
 
-static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry, bool tc, std::unique_ptr<Threadpool_shared>& tp_out) {
+static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry, int upd, std::unique_ptr<Threadpool_shared>& tp_out) {
     const ttg_chol_args& a = P->args;
     const int nb = P->nb, n_threads = a.n_threads;
     const bool accumulate = a.accumulate != 0;
@@ -142,7 +143,7 @@ static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry, bool tc, std::uni
     Taskflow<Key3> accu(&tp, a.verb);
 
     potrf.set_task([&](int j) {
-             if (mixed) gpu::record_op(ttg_mixed_potrf_op(P->mixed, j, tc));
+             if (mixed) gpu::record_op(ttg_mixed_potrf_op(P->mixed, j, upd));
              else gpu::LAPACKE_dpotrf(gpu::LAPACK_COL_MAJOR, 'L', P->bs[j], block(j, j), lda(j));
          })
         .set_fulfill([&](int j) {
@@ -155,7 +156,7 @@ static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry, bool tc, std::uni
 
     trsm.set_task([&](Key2 ij) {
             const int i = ij[0], j = ij[1];
-            if (mixed) gpu::record_op(ttg_mixed_trsm_op(P->mixed, i, j, tc));
+            if (mixed) gpu::record_op(ttg_mixed_trsm_op(P->mixed, i, j, upd));
             else
                 gpu::cblas_dtrsm(gpu::CblasColMajor, gpu::CblasRight, gpu::CblasLower, gpu::CblasTrans, gpu::CblasNonUnit,
                                  P->bs[i], P->bs[j], 1.0, block(j, j), lda(j), block(i, j), lda(i));
@@ -175,7 +176,7 @@ static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry, bool tc, std::uni
             double* C = accumulate ? tmp_of[{k, i, j}] : block(i, j);
             const double beta = accumulate ? 0.0 : 1.0;
             if (mixed) {
-                gpu::record_op(ttg_mixed_update_op(P->mixed, k, i, j, tc));
+                gpu::record_op(ttg_mixed_update_op(P->mixed, k, i, j, upd));
             } else if (i == j) {
                 gpu::cblas_dsyrk(gpu::CblasColMajor, gpu::CblasLower, gpu::CblasNoTrans, P->bs[i], P->bs[k], -1.0, block(i, k),
                                  lda(i), beta, C, lda(i));
@@ -265,12 +266,17 @@ extern "C" ttg_status ttg_chol_plan_create(ttg_ctx* ctx, const ttg_chol_args* ar
     TTG_CUDA_CHECK(cudaMalloc((void**)&P->tiles, sizeof(double) * std::max<int64_t>(1, P->elems)));
     TTG_CUDA_CHECK(cudaMalloc((void**)&P->pristine, sizeof(double) * std::max<int64_t>(1, P->elems)));
     if (args->precision == TTG_PREC_MIXED) {
-        ttg_status s = ttg_mixed_state_create(ctx, P->N, P->nb, P->bs.data(), P->off.data(), P->tiles, args->mixed_kind, &P->mixed);
+        if (args->mixed_kind < 0 || args->mixed_kind > 2) return TTG_EINVAL;
+        ttg_status s = ttg_mixed_state_create(ctx, P->N, P->nb, P->bs.data(), P->off.data(), P->tiles,
+                                              args->mixed_kind == 1 ? 1 : 0, &P->mixed);
         if (s != TTG_OK) return s;
     }
+    // Graphs: the first attempt's update arithmetic, then the remedies'.
     const bool tc = P->mixed && ttg_mixed_has_tc(P->mixed);
-    ttg_status s = chol_build_graph(P.get(), false, tc, P->tp);
-    if (s == TTG_OK && tc) s = chol_build_graph(P.get(), false, false, P->tp32);
+    const int first = !tc ? TTG_UPD_FP32 : (args->mixed_kind == 2 ? TTG_UPD_BF16X3 : TTG_UPD_BF16);
+    ttg_status s = chol_build_graph(P.get(), false, first, P->tp);
+    if (s == TTG_OK && tc) s = chol_build_graph(P.get(), false, TTG_UPD_FP32, P->tp32);
+    if (s == TTG_OK && tc && first == TTG_UPD_BF16) s = chol_build_graph(P.get(), false, TTG_UPD_BF16X3, P->tpx3);
     if (s != TTG_OK) {
         ttg_chol_plan_destroy(P.release());
         return s;
@@ -294,7 +300,7 @@ extern "C" ttg_status ttg_chol_dag_dump(const ttg_chol_args* args, const char* p
     P.nb = args->num_blocks;
     P.off.assign((size_t)P.nb * P.nb, 0);
     P.elems = ttg_tile_layout(P.bs.data(), P.nb, P.off.data());
-    ttg_status s = chol_build_graph(&P, true, false, P.tp);
+    ttg_status s = chol_build_graph(&P, true, TTG_UPD_FP32, P.tp);
     if (s != TTG_OK) return s;
     P.tp->dump_dag(prefix);
     return TTG_OK;
@@ -305,6 +311,7 @@ extern "C" ttg_status ttg_chol_plan_destroy(ttg_chol_plan* P) {
     cudaSetDevice(P->ctx->device);
     P->tp.reset();
     P->tp32.reset();
+    P->tpx3.reset();
     for (double* t : P->tmp) cudaFree(t);
     if (P->tiles) cudaFree(P->tiles);
     if (P->pristine) cudaFree(P->pristine);
@@ -406,24 +413,27 @@ static ttg_status chol_factor_from(ttg_chol_plan* P, void* stream, ttg_report* r
     // Mixed: BF16 tensor-core updates when available.  A trailing diagonal
     // block that loses positive definiteness (TTG_ENOTPD) means the update
     // precision is too low for the matrix's conditioning (BF16 rounding of
-    // the panels perturbs A by about 2^-9·‖A‖): retry with FP32 updates, then
-    // FP32 updates on A + 16·2^-24·diag(A), and last BF16 updates on A +
+    // the panels perturbs A by about 2^-9·‖A‖): retry with split-BF16
+    // tensor-core updates (FP32-level accuracy), then FP32 updates, then FP32
+    // updates on A + 16·2^-24·diag(A), and last BF16 updates on A +
     // 8·2^-8·diag(A).  A shifted factor only preconditions: refinement always
     // solves the unshifted system.  Retries start from the restored input (a
     // failed run overwrote it).
     const bool tc = ttg_mixed_has_tc(P->mixed);
+    const bool first_x3 = P->args.mixed_kind == 2;
     struct Attempt {
         Threadpool_shared* tp;
         double shift;
-        bool tc;
+        int upd;
         int remedy;
     };
     std::vector<Attempt> plan;
     Threadpool_shared* tp32 = tc ? P->tp32.get() : P->tp.get();
-    if (tc) plan.push_back({P->tp.get(), 0.0, true, 0});
-    plan.push_back({tp32, 0.0, false, 2});
-    plan.push_back({tp32, 16.0 * 5.9604644775390625e-08, false, 3});
-    if (tc) plan.push_back({P->tp.get(), 8.0 * 0.00390625, true, 1});
+    if (tc && !first_x3) plan.push_back({P->tp.get(), 0.0, TTG_UPD_BF16, 0});
+    if (tc) plan.push_back({first_x3 ? P->tp.get() : P->tpx3.get(), 0.0, TTG_UPD_BF16X3, 4});
+    plan.push_back({tp32, 0.0, TTG_UPD_FP32, 2});
+    plan.push_back({tp32, 16.0 * 5.9604644775390625e-08, TTG_UPD_FP32, 3});
+    if (tc && !first_x3) plan.push_back({P->tp.get(), 8.0 * 0.00390625, TTG_UPD_BF16, 1});
     ttg_status s = TTG_OK;
     float total_ms = 0.f;
     for (size_t a = std::min(first_attempt, plan.size() - 1); a < plan.size(); ++a) {
@@ -431,7 +441,7 @@ static ttg_status chol_factor_from(ttg_chol_plan* P, void* stream, ttg_report* r
             s = ttg_chol_plan_restore(P, stream);
             if (s != TTG_OK) return s;
         }
-        s = ttg_mixed_prepare(P->mixed, stream, plan[a].shift, plan[a].tc);
+        s = ttg_mixed_prepare(P->mixed, stream, plan[a].shift, plan[a].upd);
         if (s != TTG_OK) return s;
         s = plan[a].tp->replay(stream);
         const ttg_report r = plan[a].tp->report();

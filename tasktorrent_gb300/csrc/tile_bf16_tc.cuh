@@ -190,16 +190,32 @@ __device__ inline void tc_teardown(TcShared* sh, long long limit_ns) {
 // One 128×256 block of C += f·Â·B̂ᵀ over K = k (multiple of 64).  All
 // threads of the block call it; returns false if a wait timed out.
 // lower: only elements with (row0 + r) >= (col0 + c) are updated.
+// Slice pairs of a split product (slice 0 = hi, 1 = mid, 2 = lo of each
+// operand): the six products whose terms reach 2^-16 of hi·hi, smallest
+// first — mid·mid, hi·lo, lo·hi, hi·mid, mid·hi, hi·hi.
+__device__ __forceinline__ int split_pair_a(int p) { return p == 0 ? 1 : (p == 2 ? 2 : (p == 4 ? 1 : 0)); }
+__device__ __forceinline__ int split_pair_b(int p) { return p == 0 ? 1 : (p == 1 ? 2 : (p == 3 ? 1 : 0)); }
+
+// C[block] += f · Σ A_slotA · B_slotBᵀ.  split = 1: one BF16 product;
+// split = 3: the operands are stored as three BF16 slices (slot + s·stride,
+// s = 0, 1, 2) and the six products of split_pair_* accumulate in the same
+// FP32 TMEM accumulator, which gives FP32-level accuracy.
 __device__ inline bool tc_gemm_block(TcShared* sh, uint8_t* ring, const CUtensorMap* map, int slotA, int slotB, int row0,
-                                     int col0, int k, float f, float* C, int ldc, int m, int n, bool lower, long long limit_ns) {
+                                     int col0, int k, float f, float* C, int ldc, int m, int n, bool lower, long long limit_ns,
+                                     int split = 1, int stride = 0) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ksteps = k / kBK;
+    const int npairs = split == 3 ? 6 : 1;
+    const int total = npairs * ksteps;
     bool ok = !sh->failed;
     if (threadIdx.x == 0 && ok) {
         // Producer: K slabs of A (128 rows) and B (two boxes of 128 rows).
         fence_proxy_async_global();  // panel tiles were written by other blocks' generic stores
         uint32_t p = sh->produced;
-        for (int ks = 0; ks < ksteps; ++ks, ++p) {
+        for (int g = 0; g < total; ++g, ++p) {
+            const int ks = g % ksteps, pr = g / ksteps;
+            const int sa = slotA + (split == 3 ? split_pair_a(pr) * stride : 0);
+            const int sb = slotB + (split == 3 ? split_pair_b(pr) * stride : 0);
             const int s = p % kStages;
             if (!mbar_wait(&sh->empty[s], ((p / kStages) & 1) ^ 1, limit_ns)) {
                 sh->failed = 1;
@@ -207,9 +223,9 @@ __device__ inline bool tc_gemm_block(TcShared* sh, uint8_t* ring, const CUtensor
             }
             uint8_t* st = ring + (size_t)s * kStageBytes;
             mbar_expect_tx(&sh->full[s], kStageBytes);
-            tma_load_3d(st, map, &sh->full[s], ks * kBK, row0, slotA);
-            tma_load_3d(st + kStageBytesA, map, &sh->full[s], ks * kBK, col0, slotB);
-            tma_load_3d(st + kStageBytesA + kStageBytesB / 2, map, &sh->full[s], ks * kBK, col0 + 128, slotB);
+            tma_load_3d(st, map, &sh->full[s], ks * kBK, row0, sa);
+            tma_load_3d(st + kStageBytesA, map, &sh->full[s], ks * kBK, col0, sb);
+            tma_load_3d(st + kStageBytesA + kStageBytesB / 2, map, &sh->full[s], ks * kBK, col0 + 128, sb);
         }
         sh->produced = p;
     } else if (threadIdx.x == 32 && ok) {
@@ -217,7 +233,7 @@ __device__ inline bool tc_gemm_block(TcShared* sh, uint8_t* ring, const CUtensor
         const uint32_t idesc = idesc_bf16_f32(kBM, kBN);
         uint32_t c = sh->consumed;
         bool good = true;
-        for (int ks = 0; ks < ksteps; ++ks, ++c) {
+        for (int g = 0; g < total; ++g, ++c) {
             const int s = c % kStages;
             if (!mbar_wait(&sh->full[s], (c / kStages) & 1, limit_ns)) {
                 sh->failed = 1;
@@ -231,7 +247,7 @@ __device__ inline bool tc_gemm_block(TcShared* sh, uint8_t* ring, const CUtensor
             for (int kk = 0; kk < kBK / 16; ++kk) {
                 const uint64_t ad = smem_desc_kmajor_sw128(a0 + kk * 32);
                 const uint64_t bd = smem_desc_kmajor_sw128(b0 + kk * 32);
-                umma_bf16(sh->tmem_base, ad, bd, idesc, (ks > 0 || kk > 0) ? 1u : 0u);
+                umma_bf16(sh->tmem_base, ad, bd, idesc, (g > 0 || kk > 0) ? 1u : 0u);
             }
             umma_commit(&sh->empty[s]);
         }

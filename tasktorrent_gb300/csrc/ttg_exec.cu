@@ -272,7 +272,7 @@ int ttg_task_parts(const ttg_op& op, bool team) {
     }
     // Tensor-core updates of the mixed path: exactly one 128×256 output block
     // per part (lower-triangle blocks only for SYRK).
-    if (op.prec == TTG_PREC_MIXED && op.flags == 2 && (op.kind == TTG_OP_GEMM_NT || op.kind == TTG_OP_SYRK_LN)) {
+    if (op.prec == TTG_PREC_MIXED && op.flags >= 2 && (op.kind == TTG_OP_GEMM_NT || op.kind == TTG_OP_SYRK_LN)) {
         const int bm = cdiv(op.m, 128), bn = cdiv(op.n, 256);
         if (op.kind == TTG_OP_GEMM_NT) return std::max(1, bm * bn);
         int cnt = 0;
@@ -331,12 +331,12 @@ static double task_cost_us(const ttg_op& op) {
             break;
         case TTG_OP_SYRK_LN:
             flops = n * n * k;
-            rate = mixed ? (op.flags == 2 ? 3.0e6 : 2.0e5) : 7.5e3;
+            rate = mixed ? (op.flags == 2 ? 3.0e6 : (op.flags == 3 ? 5.0e5 : 2.0e5)) : 7.5e3;
             break;
         case TTG_OP_GEMM_NT:
         case TTG_OP_GEMM_NN:
             flops = 2.0 * m * n * k;
-            rate = mixed ? (op.flags == 2 ? 3.0e6 : 2.0e5) : 7.5e3;
+            rate = mixed ? (op.flags == 2 ? 3.0e6 : (op.flags == 3 ? 5.0e5 : 2.0e5)) : 7.5e3;
             break;
         case TTG_OP_GEADD:
             flops = m * n;

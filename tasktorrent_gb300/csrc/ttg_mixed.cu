@@ -27,15 +27,16 @@
 namespace ttg {
 
 // Mixed-op variants carried in ttg_op::flags.
-enum { kMixedF32 = 1, kMixedBF16 = 2 };
+enum { kMixedF32 = 1, kMixedBF16 = 2, kMixedBF16x3 = 3 };
 
 // Device tables of the BF16 path: panel copies (one b×b K-major slot per lower
 // tile), the scale of each slot, and the power-of-two scale of each block row.
 struct MixedTables {
-    __nv_bfloat16* b16;
+    __nv_bfloat16* b16;      // 3 slices of n_slots slots (hi, mid, lo)
     float* slot_scale;
     const float* rowscale;
     int b;
+    int n_slots;
 };
 
 // Kernel parameters of the mixed executor (the tensor map must live in the
@@ -47,6 +48,26 @@ struct __align__(64) MixedGlobals {
 
 // Rows [r0, r1) of the FP32 tile W (column-major, ldw, n columns) to the
 // K-major BF16 slot dst (row r at dst + r·b), multiplied by inv.
+// The same rows as three BF16 slices hi + mid + lo = v (dst + s·slice), each
+// the BF16 rounding of what the previous slices leave of v: together they
+// hold v to FP32 accuracy.
+__device__ inline void rows_to_bf16x3(const float* W, int ldw, int r0, int r1, int n, __nv_bfloat16* dst, size_t slice, int b,
+                                      float inv) {
+    const long total = (long)(r1 - r0) * n;
+    for (long e = threadIdx.x; e < total; e += kThreads) {
+        const int r = r0 + (int)(e / n), c = (int)(e % n);
+        const float v = __ldcg(W + r + (size_t)c * ldw) * inv;
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        const float r1v = v - __bfloat162float(h);
+        const __nv_bfloat16 mi = __float2bfloat16_rn(r1v);
+        const __nv_bfloat16 lo = __float2bfloat16_rn(r1v - __bfloat162float(mi));
+        const size_t o = (size_t)r * b + c;
+        dst[o] = h;
+        dst[slice + o] = mi;
+        dst[2 * slice + o] = lo;
+    }
+}
+
 __device__ inline void rows_to_bf16(const float* W, int ldw, int r0, int r1, int n, __nv_bfloat16* dst, int b, float inv) {
     const long total = (long)(r1 - r0) * n;
     for (long e = threadIdx.x; e < total; e += kThreads) {
@@ -90,7 +111,7 @@ __device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem,
             return info;
         }
         case TTG_OP_TRSM_RLTN:
-            if (op.flags != kMixedBF16) return run_op_plain<float>(op, part, parts, fsm);
+            if (op.flags < kMixedBF16) return run_op_plain<float>(op, part, parts, fsm);
             trsm_rltn_tile<float>(op.m, op.n, (float)op.alpha, (const float*)op.a, op.lda, (float*)op.c, op.ldc, fsm, part,
                                   parts);
             {
@@ -100,7 +121,12 @@ __device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem,
                 const int r0 = min(op.m, part * per), r1 = min(op.m, r0 + per);
                 const float s = tb->rowscale[op.k];
                 __syncthreads();
-                rows_to_bf16((const float*)op.c, op.ldc, r0, r1, op.n, tb->b16 + (size_t)op.ldb * tb->b * tb->b, tb->b, 1.0f / s);
+                const size_t slice = (size_t)tb->n_slots * tb->b * tb->b;
+                if (op.flags == kMixedBF16x3)
+                    rows_to_bf16x3((const float*)op.c, op.ldc, r0, r1, op.n, tb->b16 + (size_t)op.ldb * tb->b * tb->b, slice, tb->b,
+                                   1.0f / s);
+                else
+                    rows_to_bf16((const float*)op.c, op.ldc, r0, r1, op.n, tb->b16 + (size_t)op.ldb * tb->b * tb->b, tb->b, 1.0f / s);
                 if (threadIdx.x == 0 && part == 0) tb->slot_scale[op.ldb] = s;
                 tc::fence_proxy_async_global();
                 __syncthreads();
@@ -108,14 +134,14 @@ __device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem,
             return 0;
         case TTG_OP_SYRK_LN:
         case TTG_OP_GEMM_NT:
-            if (op.flags == kMixedBF16) {
+            if (op.flags >= kMixedBF16) {
                 const MixedTables* tb = (const MixedTables*)op.aux;
                 const bool lower = op.kind == TTG_OP_SYRK_LN;
                 int row0, col0;
                 tc::tc_block_coords(part, op.m, op.n, lower, &row0, &col0);
                 const float f = (float)op.alpha * __ldcg(tb->slot_scale + op.lda) * __ldcg(tb->slot_scale + op.ldb);
                 const bool ok = tc::tc_gemm_block(tsh, ring, tmap, op.lda, op.ldb, row0, col0, op.k, f, (float*)op.c, op.ldc,
-                                                  op.m, op.n, lower, limit_ns);
+                                                  op.m, op.n, lower, limit_ns, op.flags == kMixedBF16x3 ? 3 : 1, tb->n_slots);
                 if (!ok && threadIdx.x == 0) atomicCAS(err, 0, TTG_ETIMEOUT);
                 return 0;
             }
@@ -257,7 +283,7 @@ static ttg_status encode_tmap(ttg_mixed_state* m, int n_slots) {
     }
     auto encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
     const int b = m->b;
-    cuuint64_t dims[3] = {(cuuint64_t)b, (cuuint64_t)b, (cuuint64_t)n_slots};
+    cuuint64_t dims[3] = {(cuuint64_t)b, (cuuint64_t)b, (cuuint64_t)(3 * n_slots)};  // three slices
     cuuint64_t strides[2] = {(cuuint64_t)b * 2, (cuuint64_t)b * b * 2};
     cuuint32_t box[3] = {(cuuint32_t)tc::kBK, 128u, 1u};
     cuuint32_t estr[3] = {1, 1, 1};
@@ -303,8 +329,10 @@ ttg_status ttg_mixed_state_create(ttg_ctx* ctx, int N, int nb, const int* bs, co
     if (e != cudaSuccess) return fail(e, "cudaMalloc w32");
     if (kind == 0) {
         const int n_slots = nb * (nb + 1) / 2;
-        if ((e = cudaMalloc((void**)&m->b16, sizeof(__nv_bfloat16) * m->elems)) != cudaSuccess) return fail(e, "cudaMalloc b16");
-        if ((e = cudaMemset(m->b16, 0, sizeof(__nv_bfloat16) * m->elems)) != cudaSuccess) return fail(e, "memset b16");
+        // Three slices of slots: the BF16 copies (slice 0) and, for split
+        // updates, the two residual slices.
+        if ((e = cudaMalloc((void**)&m->b16, sizeof(__nv_bfloat16) * 3 * m->elems)) != cudaSuccess) return fail(e, "cudaMalloc b16");
+        if ((e = cudaMemset(m->b16, 0, sizeof(__nv_bfloat16) * 3 * m->elems)) != cudaSuccess) return fail(e, "memset b16");
         if ((e = cudaMalloc((void**)&m->slot_scale, sizeof(float) * n_slots)) != cudaSuccess) return fail(e, "cudaMalloc");
         if ((e = cudaMalloc((void**)&m->rowscale, sizeof(float) * nb)) != cudaSuccess) return fail(e, "cudaMalloc");
         if ((e = cudaMalloc((void**)&m->diag_off, sizeof(int64_t) * nb)) != cudaSuccess) return fail(e, "cudaMalloc");
@@ -312,7 +340,7 @@ ttg_status ttg_mixed_state_create(ttg_ctx* ctx, int N, int nb, const int* bs, co
         std::vector<int64_t> doff(nb);
         for (int i = 0; i < nb; ++i) doff[i] = off[i + (size_t)i * nb];
         cudaMemcpy(m->diag_off, doff.data(), sizeof(int64_t) * nb, cudaMemcpyHostToDevice);
-        MixedTables t{m->b16, m->slot_scale, m->rowscale, m->b};
+        MixedTables t{m->b16, m->slot_scale, m->rowscale, m->b, n_slots};
         cudaMemcpy(m->tables, &t, sizeof(t), cudaMemcpyHostToDevice);
         ttg_status st = encode_tmap(m, n_slots);
         if (st != TTG_OK) {
@@ -337,17 +365,17 @@ void ttg_mixed_state_destroy(ttg_mixed_state* m) {
 
 bool ttg_mixed_has_tc(const ttg_mixed_state* m) { return m && m->kind == 0; }
 
-static ttg_op mixed_op(const ttg_mixed_state* m, int kind, bool tc) {
+static ttg_op mixed_op(const ttg_mixed_state* m, int kind, int upd) {
     ttg_op op{};
     op.kind = kind;
     op.prec = TTG_PREC_MIXED;
-    op.flags = (tc && m->kind == 0) ? kMixedBF16 : kMixedF32;
+    op.flags = m->kind != 0 || upd == TTG_UPD_FP32 ? kMixedF32 : (upd == TTG_UPD_BF16X3 ? kMixedBF16x3 : kMixedBF16);
     op.alpha = 1.0;
     return op;
 }
 
-ttg_op ttg_mixed_potrf_op(ttg_mixed_state* m, int j, bool tc) {
-    ttg_op op = mixed_op(m, TTG_OP_POTRF_L, tc);
+ttg_op ttg_mixed_potrf_op(ttg_mixed_state* m, int j, int upd) {
+    ttg_op op = mixed_op(m, TTG_OP_POTRF_L, upd);
     const int64_t o = m->off[j + (size_t)j * m->nb];
     op.m = op.n = m->bs[j];
     op.c = m->w32 + o;
@@ -356,15 +384,15 @@ ttg_op ttg_mixed_potrf_op(ttg_mixed_state* m, int j, bool tc) {
     return op;
 }
 
-ttg_op ttg_mixed_trsm_op(ttg_mixed_state* m, int i, int j, bool tc) {
-    ttg_op op = mixed_op(m, TTG_OP_TRSM_RLTN, tc);
+ttg_op ttg_mixed_trsm_op(ttg_mixed_state* m, int i, int j, int upd) {
+    ttg_op op = mixed_op(m, TTG_OP_TRSM_RLTN, upd);
     op.m = m->bs[i];
     op.n = m->bs[j];
     op.a = m->w32 + m->off[j + (size_t)j * m->nb];
     op.lda = std::max(1, m->bs[j]);
     op.c = m->w32 + m->off[i + (size_t)j * m->nb];
     op.ldc = std::max(1, m->bs[i]);
-    if (op.flags == kMixedBF16) {
+    if (op.flags >= kMixedBF16) {
         op.aux = m->tables;
         op.ldb = slot_of(m, i, j);  // BF16 slot written by this task
         op.k = i;                   // block row: its power-of-two scale
@@ -372,8 +400,8 @@ ttg_op ttg_mixed_trsm_op(ttg_mixed_state* m, int i, int j, bool tc) {
     return op;
 }
 
-ttg_op ttg_mixed_update_op(ttg_mixed_state* m, int k, int i, int j, bool tc) {
-    ttg_op op = mixed_op(m, i == j ? TTG_OP_SYRK_LN : TTG_OP_GEMM_NT, tc);
+ttg_op ttg_mixed_update_op(ttg_mixed_state* m, int k, int i, int j, int upd) {
+    ttg_op op = mixed_op(m, i == j ? TTG_OP_SYRK_LN : TTG_OP_GEMM_NT, upd);
     op.m = m->bs[i];
     op.n = m->bs[j];
     op.k = m->bs[k];
@@ -381,7 +409,7 @@ ttg_op ttg_mixed_update_op(ttg_mixed_state* m, int k, int i, int j, bool tc) {
     op.beta = 1.0;
     op.c = m->w32 + m->off[i + (size_t)j * m->nb];
     op.ldc = std::max(1, m->bs[i]);
-    if (op.flags == kMixedBF16) {
+    if (op.flags >= kMixedBF16) {
         op.aux = m->tables;
         op.lda = slot_of(m, i, k);
         op.ldb = slot_of(m, j, k);
@@ -394,7 +422,8 @@ ttg_op ttg_mixed_update_op(ttg_mixed_state* m, int k, int i, int j, bool tc) {
     return op;
 }
 
-ttg_status ttg_mixed_prepare(ttg_mixed_state* m, void* stream, double shift, bool tc) {
+ttg_status ttg_mixed_prepare(ttg_mixed_state* m, void* stream, double shift, int upd) {
+    const bool tc = upd != TTG_UPD_FP32;
     cudaStream_t s = (cudaStream_t)stream;
     ttg_note_launch();
     convert_f64_to_f32<<<m->ctx->sms * 8, 256, 0, s>>>(m->tiles64, m->w32, m->elems);

@@ -13,21 +13,26 @@
 
 struct ttg_mixed_state;
 
-// kind: 0 = BF16 updates on tensor cores, 1 = FP32 updates.
+// Trailing-update arithmetic of a mixed graph: FP32 on the CUDA cores, BF16
+// on the tensor cores, or split BF16 (three BF16 slices per operand, six
+// products, FP32-level accuracy) on the tensor cores.
+enum { TTG_UPD_FP32 = 0, TTG_UPD_BF16 = 1, TTG_UPD_BF16X3 = 2 };
+
+// kind: 0 = tensor-core updates available (BF16 and split BF16), 1 = FP32 updates only.
 ttg_status ttg_mixed_state_create(ttg_ctx* ctx, int N, int nb, const int* bs, const int64_t* off, double* tiles64, int kind,
                                   ttg_mixed_state** out);
 void ttg_mixed_state_destroy(ttg_mixed_state* m);
-// Whether the state has the BF16 tensor-core variant (kind 0).
+// Whether the state has the tensor-core variants (kind 0).
 bool ttg_mixed_has_tc(const ttg_mixed_state* m);
-// Tile operations of the three task kinds; tc selects the BF16 tensor-core
-// variant (kind 0 states only), otherwise FP32 updates.
-ttg_op ttg_mixed_potrf_op(ttg_mixed_state* m, int j, bool tc);
-ttg_op ttg_mixed_trsm_op(ttg_mixed_state* m, int i, int j, bool tc);
-ttg_op ttg_mixed_update_op(ttg_mixed_state* m, int k, int i, int j, bool tc);
+// Tile operations of the three task kinds with update arithmetic upd
+// (TTG_UPD_*; the tensor-core ones need a kind 0 state, else FP32).
+ttg_op ttg_mixed_potrf_op(ttg_mixed_state* m, int j, int upd);
+ttg_op ttg_mixed_trsm_op(ttg_mixed_state* m, int i, int j, int upd);
+ttg_op ttg_mixed_update_op(ttg_mixed_state* m, int k, int i, int j, int upd);
 // Convert the FP64 input tiles (tiles64) to the FP32 working tiles, adding
-// shift·|a_ii| to every diagonal entry (shift 0: none), and select the
-// tensor-core variant (tc) for the next run.
-ttg_status ttg_mixed_prepare(ttg_mixed_state* m, void* stream, double shift, bool tc);
+// shift·|a_ii| to every diagonal entry (shift 0: none), for a run with
+// update arithmetic upd.
+ttg_status ttg_mixed_prepare(ttg_mixed_state* m, void* stream, double shift, int upd);
 // The low-precision factor as FP64 tiles (converted into tiles64).
 const double* ttg_mixed_factor_tiles(ttg_mixed_state* m);
 // The FP32 factor tiles (same layout as tiles64).

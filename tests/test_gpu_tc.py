@@ -49,7 +49,7 @@ def test_remedy_chain_on_ill_conditioned_input(ctx):
     p = t.CholPlan(ctx, 128, 8, kind=2, matrix=1, alpha=1e-8, seed=2, precision=t.PREC_MIXED, mixed_kind=0)
     st, rep = p.factor()
     assert st == t.TTG_OK
-    assert t.lib().ttg_chol_plan_remedy(p.h) in (0, 1, 2, 3)
+    assert t.lib().ttg_chol_plan_remedy(p.h) in (0, 1, 2, 3, 4)
     L = p.factor_L()
     assert np.isfinite(L).all()
     p.close()
@@ -80,4 +80,35 @@ def test_bf16_gmres_ir_to_fp64_backward_error(ctx, alpha, max_outer):
     assert rep.bwd_err <= BWD and bwd_err(A, X, B) <= 2 * BWD
     Xref = np.linalg.solve(A, B)
     assert rel(X, Xref) <= max(1e-12, 1e-15 * np.linalg.cond(A) * 100)
+    p.close()
+
+
+@pytest.mark.parametrize("b,nb", [(128, 3), (256, 2), (512, 3)])
+def test_split_bf16_factor_is_fp32_accurate(ctx, b, nb):
+    """Split-BF16 updates (three BF16 slices, six tensor-core products) give a
+    factor as accurate as FP32 updates, far better than plain BF16."""
+    errs = {}
+    for mk in (0, 1, 2):
+        p = t.CholPlan(ctx, b, nb, kind=2, matrix=1, alpha=1.0, seed=4, precision=t.PREC_MIXED, mixed_kind=mk)
+        st, rep = p.factor()
+        assert st == t.TTG_OK, t.strerror(st)
+        assert rep.tasks_run == rep.tasks_total and rep.bad_runs == 0
+        A = p.input_A()
+        errs[mk] = rel(p.factor_L() @ p.factor_L().T, A)
+        p.close()
+    assert errs[2] < 1e-5, errs
+    assert errs[2] < errs[0] / 30, errs
+    assert errs[2] < 10 * errs[1], errs
+
+
+def test_split_bf16_refines_an_ill_conditioned_system(ctx):
+    """alpha = 1e-4: plain BF16 loses definiteness; split BF16 (first attempt
+    of mixed_kind 2) factors it and GMRES-IR reaches FP64 backward error."""
+    p = t.CholPlan(ctx, 128, 8, kind=2, matrix=1, alpha=1e-4, seed=2, precision=t.PREC_MIXED, mixed_kind=2)
+    A = p.input_A()
+    B = orc.normals(0, p.N * 4, 9, 1).reshape(p.N, 4, order="F")
+    st, rep, X = p.solve_host(B, tol=BWD, max_outer=10, restart=30)
+    assert st == t.TTG_OK, rep.as_dict()
+    assert rep.remedy == 4
+    assert rep.bwd_err <= BWD and bwd_err(A, X, B) <= 2 * BWD
     p.close()
