@@ -6,7 +6,9 @@
 Workload (one step): solve A X = B to backward error ≤ 1e-14 per column with
 A = G·Gᵀ/N + αI (N = 32768, tile 512, 45,760 tasks, α = 1e-4, seed 2) and 16
 right-hand sides, through ttg_chol_posv: the mixed-precision tiled Cholesky
-(BF16 trailing updates on the tensor cores, FP32 TRSM, FP64 diagonal POTRF;
+(BF16 trailing updates on the tensor cores — by default split into three BF16
+terms per operand, six products, for FP32-level updates (--mixed-kind 2) —
+FP32 TRSM, FP64 diagonal POTRF;
 one persistent-kernel launch of the task graph captured from the Taskflow<K>
 drop-in) followed by GMRES-based iterative refinement with FP64 residuals.
 Inputs (4.4 GB of FP64 lower tiles) are resident in HBM and larger than L2.
@@ -251,9 +253,10 @@ def run_ours(args, world, rank, local):
             raise RuntimeError("posv failed: %s (%s)" % (t.strerror(st), rep.as_dict()))
         return e0.elapsed_time(e1), rep
 
-    # Headline: mixed precision (BF16 tensor-core updates) + GMRES-IR at alpha.
+    # Headline: mixed precision (BF16 tensor-core updates, split into three
+    # BF16 terms by default) + GMRES-IR at alpha.
     plan = t.CholPlan(ctx, args.block, nb, n_threads=16, kind=args.kind, matrix=1, alpha=args.alpha,
-                      seed=args.seed + rank, precision=t.PREC_MIXED, mixed_kind=0)
+                      seed=args.seed + rank, precision=t.PREC_MIXED, mixed_kind=args.mixed_kind)
     n_tasks, capture_s = plan.tasks()
     for _ in range(args.warmup):
         posv(plan)
@@ -331,15 +334,18 @@ def run_ours(args, world, rank, local):
         extra["fwd_err_vs_fp64"] = fwd
         p64.close()
         # The three conditionings of the workload (one step each).
+        # mixed_kind 0: plain BF16 first (remedies on loss of definiteness);
+        # 2: split BF16 (FP32-level updates on the tensor cores).
         per_alpha = []
-        for a in (1.0, 1e-4, 1e-8):
-            pa = t.CholPlan(ctx, args.block, nb, n_threads=16, kind=args.kind, matrix=1, alpha=a, seed=args.seed + rank,
-                            precision=t.PREC_MIXED, mixed_kind=0)
-            posv(pa)
-            msa, ra = posv(pa)
-            per_alpha.append({"alpha": a, "ms": msa, "factor_ms": ra.factor_ms, "outer": ra.outer, "inner": ra.inner,
-                              "gmres_prec": ra.gmres_prec, "remedy": ra.remedy, "bwd_err": ra.bwd_err})
-            pa.close()
+        for mk in (0, 2):
+            for a in (1.0, 1e-4, 1e-8):
+                pa = t.CholPlan(ctx, args.block, nb, n_threads=16, kind=args.kind, matrix=1, alpha=a, seed=args.seed + rank,
+                                precision=t.PREC_MIXED, mixed_kind=mk)
+                posv(pa)
+                msa, ra = posv(pa)
+                per_alpha.append({"mixed_kind": mk, "alpha": a, "ms": msa, "factor_ms": ra.factor_ms, "outer": ra.outer,
+                                  "inner": ra.inner, "gmres_prec": ra.gmres_prec, "remedy": ra.remedy, "bwd_err": ra.bwd_err})
+                pa.close()
         extra["mixed_per_alpha"] = per_alpha
     if not args.quick and not args.no_batched:
         extra["batched"] = run_batched(ctx, args)
@@ -359,8 +365,11 @@ def run_ours(args, world, rank, local):
                 "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "bf16",
                 "data": "synthetic: A = G*G^T/N + alpha*I, G quantised N(0,1) (Philox-4x32-10, seed %d); B iid N(0,1)" % args.seed,
-                "config": {"workload": "tiled Cholesky + solve, mixed precision (BF16 tensor-core updates, FP32 TRSM, FP64 "
-                                       "diagonal POTRF) + GMRES-IR to backward error <= %g" % args.tol,
+                "config": {"workload": "tiled Cholesky + solve, mixed precision (BF16 tensor-core updates, %s; FP32 TRSM, FP64 "
+                                       "diagonal POTRF) + GMRES-IR to backward error <= %g" % (
+                                           {0: "plain BF16 first", 1: "FP32 updates", 2: "split into three BF16 terms"}[args.mixed_kind],
+                                           args.tol),
+                           "mixed_kind": args.mixed_kind,
                            "matrix_size": N, "block_size": args.block, "nrhs": nrhs, "alpha": args.alpha, "tasks": n_tasks,
                            "l2": "inputs larger than L2 (%.1f GB of FP64 tiles)" % (elems * 8 / 1e9), "capture_s": capture_s,
                            "wall_s_timed": wall},
@@ -393,6 +402,8 @@ def main():
     ap.add_argument("--alpha", type=float, default=1e-4)
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--kind", type=int, default=2)
+    ap.add_argument("--mixed-kind", dest="mixed_kind", type=int, default=2,
+                    help="0: BF16 updates (remedies on loss of definiteness); 2: split BF16; 1: FP32")
     ap.add_argument("--cpu-n", dest="cpu_n", type=int, default=16384)
     ap.add_argument("--cpu-b", dest="cpu_b", type=int, default=512)
     ap.add_argument("--no-e2e", dest="no_e2e", action="store_true")
