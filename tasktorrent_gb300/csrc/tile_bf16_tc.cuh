@@ -208,6 +208,17 @@ __device__ inline bool tc_gemm_block(TcShared* sh, uint8_t* ring, const CUtensor
     const int npairs = split == 3 ? 6 : 1;
     const int total = npairs * ksteps;
     bool ok = !sh->failed;
+    if (threadIdx.x >= 64) {
+        // Warps 2-7 are idle during the main loop: bring this block's part of
+        // C into L2 (one 128-byte line per 32 rows of a column) so that the
+        // epilogue's reads hit.
+        const int rows = min(kBM, m - row0), lines = (rows + 31) >> 5;
+        for (int e = threadIdx.x - 64; e < kBN * lines; e += (int)blockDim.x - 64) {
+            const int c = e / lines, gc = col0 + c, gr = row0 + 32 * (e % lines);
+            if (gc < n && (!lower || row0 + rows - 1 >= gc))
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(C + gr + (size_t)gc * ldc)));
+        }
+    }
     if (threadIdx.x == 0 && ok) {
         // Producer: K slabs of A (128 rows) and B (two boxes of 128 rows).
         fence_proxy_async_global();  // panel tiles were written by other blocks' generic stores
@@ -279,13 +290,19 @@ __device__ inline bool tc_gemm_block(TcShared* sh, uint8_t* ring, const CUtensor
             uint32_t v[32];
             tmem_ld32(sh->tmem_base + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, v);
             if (gr < m) {
+                // All 32 reads first (independent, in flight together), then
+                // the 32 writes: one memory round trip per chunk, not 32.
+                float cv[32];
+                float* p = C + gr + (size_t)(col0 + c0) * ldc;
 #pragma unroll
                 for (int j = 0; j < 32; ++j) {
                     const int gc = col0 + c0 + j;
-                    if (gc < n && (!lower || gr >= gc)) {
-                        float* p = C + gr + (size_t)gc * ldc;
-                        *p = fmaf(f, __uint_as_float(v[j]), __ldcg(p));
-                    }
+                    cv[j] = (gc < n && (!lower || gr >= gc)) ? __ldcg(p + (size_t)j * ldc) : 0.0f;
+                }
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const int gc = col0 + c0 + j;
+                    if (gc < n && (!lower || gr >= gc)) p[(size_t)j * ldc] = fmaf(f, __uint_as_float(v[j]), cv[j]);
                 }
             }
         }
