@@ -38,8 +38,10 @@ struct TileLayout {
 // L_ijᵀ (backward update), so every operand is read with coalesced column
 // segments.
 //
-// Items are claimed in processing order (step by step, diagonal items first)
-// from one counter, and each waits for exactly what it reads: a diagonal item
+// Items are claimed from one counter in processing order: step by step, the
+// diagonal items first, then the update items, the strips nearest the
+// diagonal (which the next step's diagonal items wait for) first.  Each item
+// waits for exactly what it reads: a diagonal item
 // of step s for every strip of its block row to have received s updates, an
 // update item for the step's diagonal items and for its own strip to have
 // received the s earlier updates.  Everything an item waits for was claimed
@@ -62,6 +64,7 @@ struct SweepArgs {
     int* claim;                // item counter
     int* err;                  // nonzero after a timeout
     long long timeout_ns;
+    long long* trace;          // per item: claimed, inputs ready, done (ns), SM; nullptr = off
 };
 
 __device__ __forceinline__ long long sweep_clock() {
@@ -70,14 +73,29 @@ __device__ __forceinline__ long long sweep_clock() {
     return t;
 }
 
+// Shared memory of a sweep block: the staged vector chunk (kChunk × kMaxRhs
+// T, reused for the warp partials).
+template <class T, class TM>
+__host__ __device__ constexpr int sweep_smem_bytes() {
+    return kChunk * kMaxRhs * (int)sizeof(T);
+}
+
 // out[0:rows, q] (mode 0: =, 1: -=) Σ_c M[r + c·ldm] · V[c + q·ldv], rows <=
 // kStrip, on the whole block (256 threads).  Warp w takes columns w, w+8, ...
 // of each staged chunk, lane l rows 2l and 2l+1; the eight warp partials are
-// added in warp order.  smem: kChunk·kMaxRhs T.
+// added in warp order.
+//
+// An item is a chain of memory round trips unless many loads are in flight:
+// V is staged kStage values per thread at a time, with FP32 operands the
+// next U columns of M are loaded while the current U are used (FP64
+// accumulators leave no registers for that), and the output rows are read
+// together before they are written.
 template <class T, class TM>
 __device__ void strip_gemv(int rows, int kc, const TM* __restrict__ M, int ldm, const T* V, int ldv, int nrhs, T* out,
-                           int ldo, int mode, T* smem) {
+                           int ldo, int mode, unsigned char* smem_raw) {
     constexpr int U = 8;
+    constexpr int kStage = sizeof(T) == 4 ? 16 : 4;
+    T* smem = reinterpret_cast<T*>(smem_raw);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int ra = 2 * lane, rb = 2 * lane + 1;
     const bool oka = ra < rows, okb = rb < rows;
@@ -86,21 +104,34 @@ __device__ void strip_gemv(int rows, int kc, const TM* __restrict__ M, int ldm, 
     for (int q = 0; q < kMaxRhs; ++q) acc0[q] = acc1[q] = T(0);
     for (int c0 = 0; c0 < kc; c0 += kChunk) {
         const int kcc = min(kChunk, kc - c0);
+        const int total = kcc * kMaxRhs;
         __syncthreads();
-        for (int e = threadIdx.x; e < kcc * kMaxRhs; e += blockDim.x) {
-            const int c = e % kcc, q = e / kcc;
-            smem[c * kMaxRhs + q] = q < nrhs ? ldcg(V + (c0 + c) + (size_t)q * ldv) : T(0);
+        for (int e0 = threadIdx.x; e0 < total; e0 += (int)blockDim.x * kStage) {
+            T tmp[kStage];
+#pragma unroll
+            for (int j = 0; j < kStage; ++j) {
+                const int e = e0 + j * (int)blockDim.x;
+                const int c = e % kcc, q = e / kcc;
+                tmp[j] = (e < total && q < nrhs) ? ldcg(V + (c0 + c) + (size_t)q * ldv) : T(0);
+            }
+#pragma unroll
+            for (int j = 0; j < kStage; ++j) {
+                const int e = e0 + j * (int)blockDim.x;
+                if (e < total) smem[(e % kcc) * kMaxRhs + e / kcc] = tmp[j];
+            }
         }
         __syncthreads();
         const TM* Mc = M + (size_t)c0 * ldm;
-        for (int cb = warp; cb < kcc; cb += 8 * U) {
-            TM ma[U], mb[U];
+        TM ma[U], mb[U];
+        auto load = [&](int cb, TM(&xa)[U], TM(&xb)[U]) {
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const int c = cb + 8 * u;
-                ma[u] = (c < kcc && oka) ? Mc[ra + (size_t)c * ldm] : TM(0);
-                mb[u] = (c < kcc && okb) ? Mc[rb + (size_t)c * ldm] : TM(0);
+                xa[u] = (c < kcc && oka) ? Mc[ra + (size_t)c * ldm] : TM(0);
+                xb[u] = (c < kcc && okb) ? Mc[rb + (size_t)c * ldm] : TM(0);
             }
+        };
+        auto use = [&](int cb) {
 #pragma unroll
             for (int u = 0; u < U; ++u) {
                 const int c = cb + 8 * u;
@@ -115,6 +146,24 @@ __device__ void strip_gemv(int rows, int kc, const TM* __restrict__ M, int ldm, 
                     }
                 }
             }
+        };
+        if constexpr (sizeof(T) == 4) {
+            load(warp, ma, mb);
+            for (int cb = warp; cb < kcc; cb += 8 * U) {
+                TM na[U], nb[U];
+                load(cb + 8 * U, na, nb);
+                use(cb);
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    ma[u] = na[u];
+                    mb[u] = nb[u];
+                }
+            }
+        } else {
+            for (int cb = warp; cb < kcc; cb += 8 * U) {
+                load(cb, ma, mb);
+                use(cb);
+            }
         }
     }
     // Warp partials: smem[(w·kMaxRhs + q)·kStrip + r].
@@ -125,14 +174,23 @@ __device__ void strip_gemv(int rows, int kc, const TM* __restrict__ M, int ldm, 
         smem[(warp * kMaxRhs + q) * kStrip + rb] = acc1[q];
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < kStrip * nrhs; e += blockDim.x) {
+    constexpr int kOut = kStrip * kMaxRhs / 256;  // outputs per thread
+    T prev[kOut];
+#pragma unroll
+    for (int j = 0; j < kOut; ++j) {
+        const int e = threadIdx.x + j * (int)blockDim.x;
         const int r = e % kStrip, q = e / kStrip;
-        if (r >= rows) continue;
+        prev[j] = (mode != 0 && r < rows && q < nrhs) ? ldcg(out + r + (size_t)q * ldo) : T(0);
+    }
+#pragma unroll
+    for (int j = 0; j < kOut; ++j) {
+        const int e = threadIdx.x + j * (int)blockDim.x;
+        const int r = e % kStrip, q = e / kStrip;
+        if (r >= rows || q >= nrhs) continue;
         T sum = T(0);
 #pragma unroll
         for (int w = 0; w < 8; ++w) sum += smem[(w * kMaxRhs + q) * kStrip + r];
-        T* o = out + r + (size_t)q * ldo;
-        *o = mode == 0 ? sum : ldcg(o) - sum;
+        out[r + (size_t)q * ldo] = mode == 0 ? sum : prev[j] - sum;
     }
 }
 
@@ -155,7 +213,7 @@ template <class T, class TM>
 __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs a, const TM* __restrict__ Mu, const TM* __restrict__ Md, T* Vin,
                                                     T* Vout) {
     extern __shared__ __align__(16) unsigned char sweep_smem[];
-    T* smem = reinterpret_cast<T*>(sweep_smem);
+    unsigned char* smem = sweep_smem;
     __shared__ int s_item, s_abort;
     const int nb = a.nb, N = a.N;
     const int total = a.step_start[nb];
@@ -165,6 +223,7 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs a, const TM* __res
         __syncthreads();
         const int it = s_item;
         if (it >= total) break;
+        if (a.trace && threadIdx.x == 0) a.trace[4 * (size_t)it] = sweep_clock();
         const int s = upper_index(a.step_start, nb, it);
         const int i = a.backward ? nb - 1 - s : s;
         int u = it - a.step_start[s];
@@ -176,7 +235,7 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs a, const TM* __res
             g = a.strip_pre[i] + u;
         } else {
             u -= Si;
-            g = a.backward ? u : a.strip_pre[i + 1] + u;
+            g = a.backward ? a.strip_pre[i] - 1 - u : a.strip_pre[i + 1] + u;
             k = upper_index(a.strip_pre, nb, g);
         }
         // Wait for the inputs of this item.
@@ -209,6 +268,7 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs a, const TM* __res
             }
             __threadfence();
             s_abort = abort;
+            if (a.trace) a.trace[4 * (size_t)it + 1] = sweep_clock();
         }
         __syncthreads();
         if (s_abort) break;
@@ -227,6 +287,12 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs a, const TM* __res
             __threadfence();
             if (diag) atomicAdd(a.ready + i, 1);
             else atomicExch(a.applied + g, s + 1);
+            if (a.trace) {
+                unsigned sm;
+                asm volatile("mov.u32 %0, %%smid;" : "=r"(sm));
+                a.trace[4 * (size_t)it + 2] = sweep_clock();
+                a.trace[4 * (size_t)it + 3] = sm;
+            }
         }
     }
 }

@@ -86,6 +86,8 @@ struct ttg_solver {
     DevBuf<int> d_sweep_ctr;  // per sweep direction: claim, ready[nb], applied[strips]
     DevBuf<int> d_err;        // sweep timeout flag (zeroed per solve)
     int n_strips = 0;
+    int items_fwd = 0, items_bwd = 0;  // work items of one sweep per direction
+    DevBuf<long long> d_trace;         // sweep timeline (TTG_SWEEP_TRACE)
     DevBuf<TransposeDesc> d_tdesc_off, d_tdesc_diag;
     DevBuf<int64_t> d_tsub_off, d_tsub_diag;
     int n_tdesc_off = 0, n_tdesc_diag = 0;
@@ -98,14 +100,9 @@ struct ttg_solver {
     int sweep_grid64 = 0, sweep_grid32 = 0, sweep_grid_mix = 0;
 };
 
-template <class T>
-static constexpr int sweep_smem_bytes() {
-    return kChunk * kMaxRhs * (int)sizeof(T);
-}
-
 template <class T, class TM>
 static ttg_status sweep_grid(ttg_solver* S, int* grid) {
-    const int smem = sweep_smem_bytes<T>();
+    const int smem = sweep_smem_bytes<T, TM>();
     TTG_CUDA_CHECK(cudaFuncSetAttribute(sweep_kernel<T, TM>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     int per = 0;
     TTG_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep_kernel<T, TM>, 256, smem));
@@ -159,6 +156,8 @@ static ttg_status solver_tables(ttg_solver* S, const int* bs, const int64_t* off
         td.push_back({doff[j], doff[j], bs[j], bs[j]});
         sd.push_back(sd.back() + (int64_t)((bs[j] + 31) / 32) * ((bs[j] + 31) / 32));
     }
+    S->items_fwd = fwd[nb];
+    S->items_bwd = bwd[nb];
     S->n_tdesc_off = (int)to.size();
     S->n_tdesc_diag = (int)td.size();
     ttg_status st;
@@ -308,6 +307,14 @@ ttg_status ttg_solver_factor_done(ttg_solver* S, const double* L64, const float*
 
 namespace {
 
+// TTG_SWEEP_TRACE=<file> appends the timeline of every sweep to <file>: one
+// line per work item (direction, item, claimed, inputs ready, done in ns of
+// the GPU global timer, SM).  A diagnostic: it synchronises after each pair.
+const char* sweep_trace_path() {
+    static const char* p = getenv("TTG_SWEEP_TRACE");
+    return p && *p ? p : nullptr;
+}
+
 // R (scratch, overwritten) -> Y = L⁻¹ R -> X = L⁻ᵀ Y (Y overwritten): the
 // forward and the backward sweep, one launch each.
 template <class T, class TM>
@@ -326,7 +333,13 @@ ttg_status sweeps(ttg_solver* S, const TM* L, const TM* LT, const TM* Linv, cons
     a.nrhs = nrhs;
     a.err = S->d_err.p;
     a.timeout_ns = (long long)(std::max(1.0, S->ctx->timeout_s) * 1e9);
-    const int smem = sweep_smem_bytes<T>();
+    a.trace = nullptr;
+    const size_t n_trace = 4 * ((size_t)S->items_fwd + S->items_bwd);
+    if (sweep_trace_path()) {
+        ttg_status st = S->d_trace.ensure(n_trace);
+        if (st != TTG_OK) return st;
+    }
+    const int smem = sweep_smem_bytes<T, TM>();
     for (int dir = 0; dir < 2; ++dir) {
         int* ctr = S->d_sweep_ctr.p + dir * region;
         a.claim = ctr;
@@ -334,6 +347,7 @@ ttg_status sweeps(ttg_solver* S, const TM* L, const TM* LT, const TM* Linv, cons
         a.applied = ctr + 2 + S->nb;
         a.backward = dir;
         a.step_start = dir ? S->d_step_bwd.p : S->d_step_fwd.p;
+        if (sweep_trace_path()) a.trace = S->d_trace.p + (dir ? 4 * (size_t)S->items_fwd : 0);
         if (dir == 0) {
             ttg_note_launch();
             sweep_kernel<T, TM><<<grid, 256, smem, s>>>(a, L, Linv, R, Y);
@@ -343,6 +357,22 @@ ttg_status sweeps(ttg_solver* S, const TM* L, const TM* LT, const TM* Linv, cons
             sweep_kernel<T, TM><<<grid, 256, smem, s>>>(a, LT, invT, Y, X);
         }
         TTG_CUDA_CHECK(cudaGetLastError());
+    }
+    if (const char* path = sweep_trace_path()) {
+        std::vector<long long> h(n_trace);
+        TTG_CUDA_CHECK(cudaMemcpyAsync(h.data(), S->d_trace.p, sizeof(long long) * n_trace, cudaMemcpyDeviceToHost, s));
+        TTG_CUDA_CHECK(cudaStreamSynchronize(s));
+        if (FILE* f = fopen(path, "a")) {
+            for (int dir = 0; dir < 2; ++dir) {
+                const size_t base = dir ? 4 * (size_t)S->items_fwd : 0;
+                const int n = dir ? S->items_bwd : S->items_fwd;
+                for (int it = 0; it < n; ++it) {
+                    const long long* r = h.data() + base + 4 * (size_t)it;
+                    fprintf(f, "%d,%d,%lld,%lld,%lld,%lld\n", dir, it, r[0], r[1], r[2], r[3]);
+                }
+            }
+            fclose(f);
+        }
     }
     return TTG_OK;
 }
