@@ -30,7 +30,9 @@ typedef struct ttg_chol_args {
     int32_t num_blocks;       /* --num_blocks                                      */
     int32_t kind;             /* --kind: 0 none, 1 row, 2 critical path, 3 cp+row;
                                  4 (extension): longest remaining path in
-                                 estimated device time (ttg_critical_path_priority) */
+                                 estimated device time (ttg_critical_path_priority);
+                                 5 (extension): look-ahead — POTRF, then TRSM and
+                                 the next panel column's updates, then the rest  */
     int32_t accumulate;       /* --accumulate                                      */
     int32_t upper_block_size; /* --upper_block_size (-1 = block_size)              */
     int32_t matrix;           /* 0: 1/((i-j)^2+1) (the miniapp's); 1: G·Gᵀ/N + αI    */

@@ -88,7 +88,10 @@ static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry, int upd, std::uni
     const int nb = P->nb, n_threads = a.n_threads;
     const bool accumulate = a.accumulate != 0;
     // kind 4 (extension): capture with the kind-3 priorities, then replace
-    // them by the longest remaining path of each device task.
+    // them by the longest remaining path of each device task.  kind 5
+    // (extension): look-ahead — three levels, the POTRFs, then the TRSMs and
+    // the updates of the next panel column (GEMM (k, i, k+1)), then the other
+    // updates; within a level tasks run in the order they become ready.
     const int pk = a.kind == 4 ? 3 : a.kind;
     const bool mixed = a.precision == TTG_PREC_MIXED;
     auto block = [P](int i, int j) { return P->tiles + P->off[i + (size_t)j * P->nb]; };
@@ -96,18 +99,21 @@ static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry, int upd, std::uni
     auto block_2_thread = [=](int i, int j) { return (i + j * nb) % n_threads; };
 
     auto potf_block_2_prio = [=](int j) -> double {
+        if (pk == 5) return 3.0;
         if (pk == 3) return (double)(9 * (nb - j) - 1) + 18 * nb * nb;
         if (pk == 2) return (double)(9 * (nb - j) - 1);
         if (pk == 1) return 3.0 * (double)(nb - j);
         return 3.0;
     };
     auto trsm_block_2_prio = [=](Key2 ij) -> double {
+        if (pk == 5) return 2.0;
         if (pk == 3) return (double)((nb - ij[0]) + nb * (9.0 * nb - 9.0 * ij[1] - 2.0) + 9 * nb * nb);
         if (pk == 2) return (double)(9 * (nb - ij[1]) - 2);
         if (pk == 1) return 2.0 * (double)(nb - ij[0]);
         return 2.0;
     };
     auto gemm_block_2_prio = [=](Key3 kij) -> double {
+        if (pk == 5) return kij[2] == kij[0] + 1 ? 2.0 : 1.0;
         if (pk == 3) {
             if (accumulate) return (double)(nb - kij[1]) + nb * (9.0 * nb - 9.0 * kij[2] - 2.0);
             return (double)(nb - kij[1]) + nb * (9.0 * nb - 3.0 * kij[2] - 6.0 * kij[0] - 2.0);

@@ -32,6 +32,10 @@ constexpr int kLevelGroups = kMaxLevels / 32;
 constexpr int kTraceWords = 4;
 // Counter words per team task (the POTRF tasks shared by several blocks).
 constexpr int kTeamStride = 256;
+// 128×256 tensor-core output blocks per part of a mixed-path update: with
+// one, the parts (~25 µs of split-BF16 work) come faster than the queue
+// hands them out well; two measured best at N = 32768, tile 512.
+constexpr int kTcBlocksPerPart = 2;
 
 struct ExecParams {
     const ttg_op* ops;
@@ -101,8 +105,16 @@ __device__ inline int wait_slot(const ExecParams& p, int* slot) {
     }
 }
 
-// Called by all lanes of warp 0.  Returns a claimed task id, or -1 to exit.
-__device__ inline int claim_task(const ExecParams& p) {
+// Called by all lanes of warp 0.  Returns a claimed task id and its part
+// (*part, the same on all lanes), or -1 to exit.
+//
+// A level queue holds one slot per ready task.  The task at the head stays
+// there until its parts are handed out: a block takes a part with an atomic
+// increment of the task's part counter, and the block that takes the last
+// part (or finds none left) advances the head by compare-and-swap.  The
+// contended compare-and-swap thus runs once per task, not once per part.
+// A bound queue holds one slot per part.
+__device__ inline int claim_task(const ExecParams& p, int* part) {
     const int lane = threadIdx.x & 31;
     const int w = blockIdx.x;
     int last_done = -1;
@@ -126,6 +138,9 @@ __device__ inline int claim_task(const ExecParams& p) {
             task = __shfl_sync(0xffffffffu, task, 0);
             if (task == -2) return -1;
             if (task >= 0) {
+                int pt = 0;
+                if (lane == 0) pt = atomicAdd(p.part_next + task, 1);
+                *part = __shfl_sync(0xffffffffu, pt, 0);
                 __threadfence();
                 return task;
             }
@@ -153,20 +168,27 @@ __device__ inline int claim_task(const ExecParams& p) {
         }
         if (mask) {
             const int lvl = grp * 32 + __ffs(mask) - 1;
-            int got = -1;
+            int got = -1, pt = 0;
             if (lane == (lvl & 31)) {
-                if (atomicCAS(p.q_head + lvl * 32, h, h + 1) == h) {
-                    got = wait_slot(p, p.qbuf + p.q_off[lvl] + h);
-                    if (got < 0) got = -2;
+                // Slot h is reserved (h < tail); its producer may still be writing it.
+                const int t = wait_slot(p, p.qbuf + p.q_off[lvl] + h);
+                if (t < 0) {
+                    got = -2;
+                } else {
+                    pt = atomicAdd(p.part_next + t, 1);
+                    const int P = p.parts[t];
+                    if (pt < P) got = t;
+                    if (pt >= P - 1) atomicCAS(p.q_head + lvl * 32, h, h + 1);
                 }
             }
             got = __shfl_sync(0xffffffffu, got, lvl & 31);
             if (got == -2) return -1;
             if (got >= 0) {
+                *part = __shfl_sync(0xffffffffu, pt, lvl & 31);
                 __threadfence();
                 return got;
             }
-            continue;  // lost the race for this slot; rescan at once
+            continue;  // the head task had no part left; rescan at once
         }
         int d = 0, e = 0;
         if (lane == 0) {
@@ -197,7 +219,8 @@ __device__ __forceinline__ void push_ready(const ExecParams& p, int s) {
     // counter at one pushes), so a queue never outgrows the number of tasks
     // assigned to it; the bound checks below only guard against a corrupted
     // graph.
-    // A task of P parts takes P consecutive slots, one per part.
+    // In a bound queue a task of P parts takes P consecutive slots, one per
+    // part; in a level queue it takes one slot.
     if (b >= 0) {
         const int w = b % p.n_workers;
         const int slot = atomicAdd(p.bq_tail + w, P);
@@ -207,10 +230,11 @@ __device__ __forceinline__ void push_ready(const ExecParams& p, int s) {
             set_error(p, TTG_EOVERCOUNT, s, 0);
         }
     } else {
+        // One slot per task: its parts are handed out at the head.
         const int lvl = p.level[s];
-        const int slot = atomicAdd(p.q_tail + lvl * 32, P);
-        if (p.q_off[lvl] + slot + P <= p.q_off[lvl + 1]) {
-            for (int q = 0; q < P; ++q) st_volatile(p.qbuf + p.q_off[lvl] + slot + q, s);
+        const int slot = atomicAdd(p.q_tail + lvl * 32, 1);
+        if (p.q_off[lvl] + slot + 1 <= p.q_off[lvl + 1]) {
+            st_volatile(p.qbuf + p.q_off[lvl] + slot, s);
         } else {
             set_error(p, TTG_EOVERCOUNT, s, 0);
         }
@@ -253,12 +277,12 @@ __device__ void executor_loop(const ExecParams& p, double* smem, RunOp run_op) {
     long long t_part = 0;  // thread 0: start of the current part (trace)
     for (;;) {
         if (threadIdx.x < 32) {
-            const int t = claim_task(p);
+            int part = 0;
+            const int t = claim_task(p, &part);
             if (threadIdx.x == 0) {
                 s_task = t;
                 s_fin = -1;
                 if (t >= 0) {
-                    const int part = atomicAdd(p.part_next + t, 1);
                     s_part = part;
                     if (p.trace) {
                         t_part = globaltimer();

@@ -99,17 +99,26 @@ __device__ void gemm_tile(int m, int n, int k, T alpha, const T* __restrict__ A,
                 }
                 __syncthreads();
             }
+            // Per column: the eight reads of C first (in flight together),
+            // then the eight writes — with a short k the epilogue is
+            // otherwise a chain of 64 memory round trips.
 #pragma unroll
             for (int c = 0; c < 8; ++c) {
                 const int gj = n0 + ty + 16 * c;
+                T cv[8];
+#pragma unroll
+                for (int r = 0; r < 8; ++r) {
+                    const int gi = m0 + tx + 16 * r;
+                    const bool ok = gi < m && gj < n && (!LOWER || gi >= gj);
+                    cv[r] = (ok && beta != T(0)) ? ldcg(C + gi + (size_t)gj * ldc) : T(0);
+                }
 #pragma unroll
                 for (int r = 0; r < 8; ++r) {
                     const int gi = m0 + tx + 16 * r;
                     if (gi < m && gj < n && (!LOWER || gi >= gj)) {
-                        T* p = C + gi + (size_t)gj * ldc;
                         T v = alpha * acc[r][c];
-                        if (beta != T(0)) v = fma(beta, ldcg(p), v);
-                        *p = v;
+                        if (beta != T(0)) v = fma(beta, cv[r], v);
+                        C[gi + (size_t)gj * ldc] = v;
                     }
                 }
             }
@@ -183,6 +192,7 @@ __device__ inline void trsm_rows_panel(T* X, int ldx, int row0, int m, int nb, c
 // Load the nb×nb lower block at L (ldl) into Ls (ld kPanel+1), zero above.
 template <class T>
 __device__ inline void load_panel_block(const T* L, int ldl, int nb, T* Ls) {
+#pragma unroll
     for (int e = threadIdx.x; e < kPanel * kPanel; e += kThreads) {
         const int c = e / kPanel, l = e % kPanel;  // Ls[c][l] = L(c, l)
         Ls[c * (kPanel + 1) + l] = (c < nb && l < nb && l <= c) ? ldcg(L + c + (size_t)l * ldl) : T(0);
@@ -280,26 +290,39 @@ __device__ __forceinline__ void geadd_f64(int m, int n, double alpha, const doub
 // ------------------------------------------------------------------------
 // Team POTRF: one diagonal tile factored by several blocks of the executor.
 //
-// The factorisation runs as a sequence of phases; for every 32-column panel:
-// the 32×32 diagonal block (one warp), the panel rows below it (32-row
-// items), and the lower 64×64 blocks of the trailing update.  Every block
-// that holds a part of the task claims items of the current phase from a
-// per-task counter and then waits until all items of the phase are done.  A
-// block never waits for a part that has not started — whoever is present does
-// the work — so the team cannot deadlock, and a single block alone factors
-// the whole tile.  Waits are bounded by limit_ns.
+// The tile is cut into P×P blocks of 32×32 (P = ceil(n/32)), and the
+// factorisation into items over the lower blocks:
+//   D(j)       factor the diagonal block (j,j) and invert it,
+//   R(j, i)    panel block (i,j) <- A_ij · L_jj⁻ᵀ            (i > j),
+//   T(p, i, j) trailing update A_ij -= L_ip · L_jpᵀ           (i >= j > p).
+// One state byte per block counts what it has received: block (i,j) holds
+// state p after the updates of panels 0..p-1, and j+1 once it is final (D or
+// R done).  Every item waits only for the blocks it reads and writes — D(j)
+// for state(j,j) = j; R(j,i) for state(j,j) = j+1 and state(i,j) = j;
+// T(p,i,j) for state(i,p) = state(j,p) = p+1 and state(i,j) = p — so the next
+// panel starts as soon as its own blocks are ready (look-ahead) and the
+// updates of every block are applied in panel order (deterministic result).
 //
-// ctr: kTeamCounters ints per task, zero at launch: (claimed, done) per
-// phase; ctr[kTeamCounters - 2] = phases completed; ctr[kTeamCounters - 1] =
-// the first failing column.
+// Blocks of the team claim items from one counter in a fixed order, segment
+// by segment: seg(j) = D(j), R(j,·), T(j-1,·,j+1), T(j,·,j+1), then the rest
+// of panel j-1's trailing update T(j-1,·,>=j+2).  The next panel's critical
+// items come before the bulk of the previous trailing update, and everything
+// an item waits for is claimed before it by a block that is running, so the
+// team cannot deadlock and a single block alone factors the whole tile.
+// Waits are bounded by limit_ns.
+//
+// ctr: kTeamCounters ints per task, zero at launch: [0] items claimed, [1]
+// items done, [2] first failing column (1-based), then the state bytes of
+// the lower blocks ((i,j) at byte i(i+1)/2 + j).
 constexpr int kTeamCounters = 256;
-constexpr int kTeamPanelRows = 32;  // rows per panel item
-constexpr int kTeamCopyRows = 128;  // rows per widen / narrow item
+constexpr int kTeamHeader = 8;  // ints before the state bytes
 
-// Phases of potrf_l_f64_team on an n×n tile; the team form needs
-// 2·phases + 2 <= kTeamCounters.
-__host__ __device__ inline int team_phases(int n, bool widen) { return 3 * ((n + kPanel - 1) / kPanel) + (widen ? 2 : 0); }
-__host__ __device__ inline bool team_fits(int n, bool widen) { return 2 * team_phases(n, widen) + 2 <= kTeamCounters; }
+__host__ __device__ inline int team_blocks(int n) { return (n + kPanel - 1) / kPanel; }
+// The team form needs one state byte per lower block.
+__host__ __device__ inline bool team_fits(int n) {
+    const int P = team_blocks(n);
+    return P * (P + 1) / 2 <= (kTeamCounters - kTeamHeader) * 4;
+}
 
 struct TeamCtx {
     int* ctr;
@@ -313,87 +336,126 @@ __device__ __forceinline__ long long team_clock() {
     return t;
 }
 
-// Claim the next item of phase ph (the same value on all threads).
-__device__ __forceinline__ int team_claim(const TeamCtx& tc, int ph) {
-    __shared__ int s_item;
-    __syncthreads();
-    if (threadIdx.x == 0) s_item = atomicAdd(tc.ctr + 2 * ph, 1);
-    __syncthreads();
-    return s_item;
+// One item of the order above: kind 0 D(p), 1 R(p, bi), 2 T(p, bi, bj); kind
+// -1 past the last item.
+struct TeamItem {
+    int kind, p, bi, bj;
+};
+
+__host__ __device__ inline int team_segment_items(int P, int j) {
+    const int m = P - 1 - j;
+    return 1 + 2 * m + (j >= 1 ? m + m * (m - 1) / 2 : 0);
 }
 
-// Publish one finished item of phase ph (of `items`); the block that finishes
-// the last item advances the completed-phase marker.  Returns (on every
-// thread) whether this item completed the phase.
-__device__ __forceinline__ bool team_done(const TeamCtx& tc, int ph, int items) {
-    __shared__ int s_last;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        const bool last = atomicAdd(tc.ctr + 2 * ph + 1, 1) == items - 1;
-        if (last) atomicMax(tc.ctr + kTeamCounters - 2, ph + 1);
-        s_last = last;
+__host__ __device__ inline int team_total_items(int P) {
+    int t = 0;
+    for (int j = 0; j < P; ++j) t += team_segment_items(P, j);
+    return t;
+}
+
+__host__ __device__ inline TeamItem team_item(int P, int idx) {
+    for (int j = 0; j < P; ++j) {
+        const int m = P - 1 - j;
+        const int cnt = team_segment_items(P, j);
+        if (idx >= cnt) {
+            idx -= cnt;
+            continue;
+        }
+        int k = idx;
+        if (k < 1) return {0, j, j, j};
+        k -= 1;
+        if (k < m) return {1, j, j + 1 + k, j};
+        k -= m;
+        if (j >= 1) {
+            if (k < m) return {2, j - 1, j + 1 + k, j + 1};
+            k -= m;
+        }
+        if (k < m) return {2, j, j + 1 + k, j + 1};
+        k -= m;
+        int bj = j + 2;
+        while (k >= P - bj) {
+            k -= P - bj;
+            ++bj;
+        }
+        return {2, j - 1, bj + k, bj};
     }
-    __syncthreads();
-    return s_last != 0;
+    return {-1, 0, 0, 0};
 }
 
-// Phases completed so far (the same value on all threads).
-__device__ __forceinline__ int team_progress(const TeamCtx& tc) {
-    __shared__ int s_prog;
-    __syncthreads();
-    if (threadIdx.x == 0) s_prog = *(const volatile int*)(tc.ctr + kTeamCounters - 2);
-    __syncthreads();
-    return s_prog;
+__device__ __forceinline__ volatile unsigned char* team_state(const TeamCtx& tc, int bi, int bj) {
+    return reinterpret_cast<volatile unsigned char*>(tc.ctr + kTeamHeader) + bi * (bi + 1) / 2 + bj;
 }
 
-// Wait until `items` items of phase ph are done; false on timeout.
-__device__ __forceinline__ bool team_wait(const TeamCtx& tc, int ph, int items) {
-    __shared__ int s_ok;
+// Thread 0 waits until every (state, value) pair holds (a null state is no
+// condition); the outcome is returned on all threads: 0, the failing column
+// after another block found the tile not positive definite, or -1 after a
+// timeout.
+__device__ inline int team_wait_states(const TeamCtx& tc, volatile unsigned char* s0, int v0, volatile unsigned char* s1,
+                                       int v1, volatile unsigned char* s2, int v2) {
+    __shared__ int s_res;
     if (threadIdx.x == 0) {
-        int ok = 1;
-        const volatile int* d = tc.ctr + 2 * ph + 1;
-        if (*d < items) {
+        auto ready = [&]() { return (!s0 || *s0 >= v0) && (!s1 || *s1 >= v1) && (!s2 || *s2 >= v2); };
+        int res = 0;
+        if (!ready()) {
             const long long t0 = team_clock();
-            for (unsigned it = 0; *d < items; ++it) {
-                if ((it & 63) == 63 && team_clock() - t0 > tc.limit_ns) {
-                    ok = 0;
-                    atomicCAS(tc.err, 0, 3 /* TTG_ETIMEOUT */);
-                    break;
+            for (unsigned it = 0;; ++it) {
+                if (ready()) break;
+                if ((it & 63) == 63) {
+                    const int bad = *(const volatile int*)(tc.ctr + 2);
+                    if (bad) {
+                        res = bad;
+                        break;
+                    }
+                    if (team_clock() - t0 > tc.limit_ns) {
+                        res = -1;
+                        atomicCAS(tc.err, 0, 3 /* TTG_ETIMEOUT */);
+                        break;
+                    }
                 }
-                __nanosleep(64);
+                __nanosleep(32);
             }
         }
         __threadfence();
-        s_ok = ok;
+        s_res = res;
     }
     __syncthreads();
-    return s_ok != 0;
+    return s_res;
 }
 
-// Shared-memory layout of the team POTRF (doubles): the 32×32 diagonal block
-// L (ld 33), its inverse X (ld 33), 1/L_cc, and two 32×33 work panels.
+// Publish a block: its writes (all threads, before the call) are made
+// visible, then its state is set.
+__device__ __forceinline__ void team_publish(volatile unsigned char* st, int v) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        *st = (unsigned char)v;
+    }
+}
+
+// Shared-memory layout of the team POTRF (doubles): a 32×32 block S (ld 33),
+// the inverse X of a diagonal block (ld 33), 1/L_cc, and two 32×33 work
+// blocks.
 constexpr int kTS = 0, kTX = 1056, kTInv = 2112, kTW1 = 2144, kTW2 = 3200, kTeamSmemDoubles = 4256;
 static_assert(kTeamSmemDoubles <= kF64SmemDoubles, "team POTRF shared memory");
 
-// Lower Cholesky of the nb×nb (nb <= 32) diagonal block at D (ld) in shared
-// memory S (ld 33) by warps 0-3: column c's pivot is taken by warp c % 4
-// (one rsqrt: l_cc = d·d^-1/2, the column scaled by d^-1/2, kept in inv[c]),
-// then warp w updates the columns j > c with j % 4 == w (lane = row).  Every
-// FP64 operation of a GB300 warp costs ~65 cycles whatever its active lanes,
-// so the column updates are spread over the four sub-partitions.  Returns 0
-// or the 1-based failing column; S and inv hold the factor.
-__device__ inline int team_diag_factor(const double* D, int ld, int nb, double* S, double* inv) {
+// Lower Cholesky of the nb×nb (nb <= 32) block in S (ld 33) and, one column
+// behind it, the inverse X = L⁻¹ (X starts as the identity).  Factor, warps
+// 0-3: column c's pivot is taken by warp c % 4 (one rsqrt: l_cc = d·d^-1/2,
+// the column scaled by d^-1/2, kept in inv[c]), then warp w updates the
+// columns j > c with j % 4 == w (lane = row).  Inverse, warps 4-7, row i as
+// soon as column i of L is final: row i of X is scaled by inv[i], then the
+// rows j > i (j % 4 == w - 4) subtract L_ji·X_i (lane = column).  Every FP64
+// operation of a GB300 warp costs ~65 cycles whatever its active lanes, so
+// the work is spread over the four sub-partitions twice.  Returns 0 or the
+// 1-based failing column.
+__device__ inline int team_factor_invert(int nb, double* S, double* X, double* inv) {
     __shared__ int s_info;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int e = threadIdx.x; e < 32 * 32; e += kThreads) {
-        const int i = e & 31, j = e >> 5;
-        S[i * 33 + j] = (i < nb && j < nb && i >= j) ? ldcg(D + i + (size_t)j * ld) : 0.0;
-    }
     if (threadIdx.x == 0) s_info = 0;
     __syncthreads();
-    for (int c = 0; c < nb; ++c) {
-        if (warp == (c & 3)) {
+    for (int c = 0; c <= nb; ++c) {
+        const int i = c - 1;  // row of X finished in this step
+        if (c < nb && warp == (c & 3)) {
             const double d = S[c * 33 + c];
             if (!(d > 0.0)) {
                 if (lane == 0) s_info = c + 1;
@@ -406,12 +468,19 @@ __device__ inline int team_diag_factor(const double* D, int ld, int nb, double* 
                     S[lane * 33 + c] *= y;
                 }
             }
+        } else if (i >= 0 && warp == 4 + (i & 3) && lane <= i) {
+            X[i * 33 + lane] *= inv[i];
         }
         __syncthreads();
         if (s_info) break;
-        if (warp < 4)
-            for (int j = c + 1 + ((warp - c - 1) & 3); j < nb; j += 4)
-                if (lane >= j && lane < nb) S[lane * 33 + j] = fma(-S[lane * 33 + c], S[j * 33 + c], S[lane * 33 + j]);
+        if (warp < 4) {
+            if (c < nb)
+                for (int j = c + 1 + ((warp - c - 1) & 3); j < nb; j += 4)
+                    if (lane >= j && lane < nb) S[lane * 33 + j] = fma(-S[lane * 33 + c], S[j * 33 + c], S[lane * 33 + j]);
+        } else if (i >= 0) {
+            for (int j = i + 1 + ((warp - 4 - i - 1) & 3); j < nb; j += 4)
+                if (lane <= i) X[j * 33 + lane] = fma(-S[j * 33 + i], X[i * 33 + lane], X[j * 33 + lane]);
+        }
         __syncthreads();
     }
     return s_info;
@@ -437,79 +506,53 @@ __device__ inline void team_diag_inverse(const double* S, const double* inv, int
     }
 }
 
-// Rows [r0, r0 + rows) (rows <= 32) of the panel P (columns 0..nb-1, ld) <-
-// P · L⁻ᵀ = P · Xᵀ: thread (r, g) computes columns g, g+8, g+16, g+24.
-__device__ inline void team_panel_rows(double* P, int ld, int r0, int rows, int nb, const double* X, double* W) {
+// Block of the tile (rows × cols at row r0, column c0) into W (ld 33), from
+// the FP32 source when `wide` (the first touch of a block in the mixed path)
+// else from A; lower_only keeps the lower triangle of a diagonal block.
+__device__ inline void team_load_block(double* W, const double* A, int lda, const float* W32, int ldw, bool wide, int r0, int c0,
+                                       int rows, int cols, bool lower_only) {
+#pragma unroll
     for (int e = threadIdx.x; e < 32 * 32; e += kThreads) {
         const int r = e & 31, c = e >> 5;
-        W[r * 33 + c] = (r < rows && c < nb) ? ldcg(P + r0 + r + (size_t)c * ld) : 0.0;
+        double v = 0.0;
+        if (r < rows && c < cols && (!lower_only || r >= c))
+            v = wide ? (double)__ldcg(W32 + (r0 + r) + (size_t)(c0 + c) * ldw) : ldcg(A + (r0 + r) + (size_t)(c0 + c) * lda);
+        W[r * 33 + c] = v;
     }
-    __syncthreads();
-    const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
-    double acc[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const int j = g + 8 * k;
-        double a = 0.0;
-        for (int c = 0; c <= j && c < nb; ++c) a = fma(W[r * 33 + c], X[j * 33 + c], a);
-        acc[k] = a;
-    }
-    if (r < rows) {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const int j = g + 8 * k;
-            if (j < nb) P[r0 + r + (size_t)j * ld] = acc[k];
-        }
-    }
-    __syncthreads();
 }
 
-// Lower 32×32 block `item` (column by column over the lower triangle) of
-// C[rest×rest] -= Q·Qᵀ, Q rest×nb (nb <= 32, ld).
-__device__ inline void team_syrk_block32(int rest, int nb, const double* Q, int ld, double* C, int item, double* W1, double* W2) {
-    const int mb = (rest + 31) / 32;
-    int bj = 0, rr = item;
-    while (rr >= mb - bj) {
-        rr -= mb - bj;
-        ++bj;
-    }
-    const int bi = bj + rr;
-    const int m0 = bi * 32, n0 = bj * 32;
+// Block (rows × cols at r0, c0) from W (ld 33) into A and, when W32 is set,
+// rounded into the FP32 tile (a final factor block of the mixed path).
+__device__ inline void team_store_block(const double* W, double* A, int lda, float* W32, int ldw, int r0, int c0, int rows, int cols,
+                                        bool lower_only) {
     for (int e = threadIdx.x; e < 32 * 32; e += kThreads) {
         const int r = e & 31, c = e >> 5;
-        W1[r * 33 + c] = (m0 + r < rest && c < nb) ? ldcg(Q + m0 + r + (size_t)c * ld) : 0.0;
-        W2[r * 33 + c] = (n0 + r < rest && c < nb) ? ldcg(Q + n0 + r + (size_t)c * ld) : 0.0;
-    }
-    __syncthreads();
-    const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
-    const bool diag = bi == bj;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const int j = g + 8 * k;
-        const int gi = m0 + r, gj = n0 + j;
-        if (gi < rest && gj < rest && (!diag || r >= j)) {
-            double a = 0.0;
-#pragma unroll 8
-            for (int c = 0; c < kPanel; ++c) a = fma(W1[r * 33 + c], W2[j * 33 + c], a);
-            double* q = C + gi + (size_t)gj * ld;
-            *q = ldcg(q) - a;
+        if (r < rows && c < cols && (!lower_only || r >= c)) {
+            const double v = W[r * 33 + c];
+            A[(r0 + r) + (size_t)(c0 + c) * lda] = v;
+            if (W32) W32[(r0 + r) + (size_t)(c0 + c) * ldw] = (float)v;
         }
     }
-    __syncthreads();
 }
 
-// Team lower Cholesky of the FP64 tile A[n×n] (lda); requires
-// team_fits(n, W32 != nullptr).  With an FP32 source (W32 != nullptr) the
-// team first widens the lower triangle of W32 (ldw) into A and at the end
-// rounds the factor back into W32.  Per 32-column panel: the diagonal block
-// (one block, team_diag_factor), the panel rows in 32-row items (each block
-// that takes one first inverts the diagonal block for itself), the trailing
-// lower 32×32 blocks.  Returns 0, the 1-based failing column, or -1 after a
-// timeout.  *finisher (shared) is set to 1 in the one block that completed
-// the factorisation (or found the failing column), else 0: that block
-// releases the task's successors at once, whether or not the other parts of
-// the team have run yet.  The result is the same for any number of blocks:
-// every item computes the same arithmetic whoever runs it.
+// Where a diagonal block's inverse is kept for the R items of its panel: the
+// strictly upper h×h corner of the FP64 scratch tile (rows 0..h-1, columns
+// n-h..n-1, h = n/2), which the factorisation never touches.  Element k of the
+// P inverses (32×32 each, ld 32) -> A offset; usable when h² >= P·1024.
+__device__ __forceinline__ size_t team_xoff(int n, int lda, int k) {
+    const int h = n / 2;
+    return (size_t)(k % h) + (size_t)(n - h + k / h) * lda;
+}
+
+// Team lower Cholesky of the FP64 tile A[n×n] (lda); requires team_fits(n).
+// With an FP32 source (W32 != nullptr, the mixed path) A is FP64 scratch:
+// the first item that touches a block reads it from W32 (ldw), and every
+// final block is also rounded back into W32.  Returns 0, the 1-based failing
+// column, or -1 after a timeout.  *finisher (shared) is set to 1 in the one
+// block that completed the last item (or found the failing column), else 0:
+// that block releases the task's successors at once, whether or not the other
+// parts of the team have run yet.  The result is the same for any number of
+// blocks: every item computes the same arithmetic whoever runs it.
 __device__ inline int potrf_l_f64_team(int n, double* A, int lda, double* smem, const TeamCtx& tc, float* W32, int ldw,
                                        int* finisher) {
     double* S = smem + kTS;
@@ -517,95 +560,135 @@ __device__ inline int potrf_l_f64_team(int n, double* A, int lda, double* smem, 
     double* inv = smem + kTInv;
     double* W1 = smem + kTW1;
     double* W2 = smem + kTW2;
-    // An empty tile has no phases: its parts complete as ordinary parts
+    __shared__ int s_item, s_xpanel;
+    // An empty tile has no items: its parts complete as ordinary parts
     // (*finisher keeps the executor's -1).
     if (n <= 0) return 0;
-    if (threadIdx.x == 0) *finisher = 0;
-    int ph = 0;
-    const int copy_items = (n + kTeamCopyRows - 1) / kTeamCopyRows;
-    if (W32) {
-        for (int it = team_claim(tc, ph); it < copy_items; it = team_claim(tc, ph)) {
-            const int r0 = it * kTeamCopyRows, r1 = min(n, r0 + kTeamCopyRows), rows = r1 - r0;
-            for (long e = threadIdx.x; e < (long)rows * n; e += kThreads) {
-                const int i = r0 + (int)(e % rows), j = (int)(e / rows);
-                A[i + (size_t)j * lda] = i >= j ? (double)__ldcg(W32 + i + (size_t)j * ldw) : 0.0;
-            }
-            team_done(tc, ph, copy_items);
-        }
-        if (!team_wait(tc, ph, copy_items)) return -1;
-        ++ph;
+    const int P = team_blocks(n);
+    const int total = team_total_items(P);
+    // The mixed path keeps each diagonal inverse for the panel's R items; the
+    // FP64 path (A is the caller's tile) recomputes it in every block.
+    const bool keep_x = W32 != nullptr && (long)(n / 2) * (n / 2) >= (long)P * 1024;
+    if (threadIdx.x == 0) {
+        *finisher = 0;
+        s_xpanel = -1;
     }
-    for (int p = 0; p < n; p += kPanel, ph += 3) {
-        // Panels that the team has already finished are skipped by late blocks.
-        if (team_progress(tc) >= ph + 3) continue;
-        const int nb = min(kPanel, n - p);
-        double* Dpp = A + p + (size_t)p * lda;
-        if (team_claim(tc, ph) == 0) {
-            __shared__ int s_bad;
-            const int info = team_diag_factor(Dpp, lda, nb, S, inv);
-            if (info == 0) {
-                for (int e = threadIdx.x; e < 32 * 32; e += kThreads) {
-                    const int i = e & 31, j = e >> 5;
-                    if (i < nb && j <= i) Dpp[i + (size_t)j * lda] = S[i * 33 + j];
-                }
-            }
-            if (threadIdx.x == 0) {
-                s_bad = info != 0;
-                if (info) atomicExch(tc.ctr + kTeamCounters - 1, p + info);
-            }
-            team_done(tc, ph, 1);
-            // The factorisation ends here after a failure, or after the last
-            // panel when there is no FP32 copy to write.
-            if (threadIdx.x == 0 && (s_bad || (p + nb >= n && !W32))) *finisher = 1;
+    auto rows_of = [&](int b) { return min(kPanel, n - kPanel * b); };
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const int bad = *(const volatile int*)(tc.ctr + 2);
+            s_item = bad ? -1 - bad : atomicAdd(tc.ctr, 1);
         }
-        if (!team_wait(tc, ph, 1)) return -1;
-        {
-            const int info = *(const volatile int*)(tc.ctr + kTeamCounters - 1);
-            if (info) return info;
-        }
-        const int rest = n - p - nb;
-        if (rest <= 0) continue;
-        const int pitems = (rest + kTeamPanelRows - 1) / kTeamPanelRows;
-        bool have_inverse = false;
-        for (int it = team_claim(tc, ph + 1); it < pitems; it = team_claim(tc, ph + 1)) {
-            if (!have_inverse) {
-                // The factored diagonal block and 1/L_ii (this block may not
-                // be the one that factored it), then its inverse.
-                for (int e = threadIdx.x; e < 32 * 32; e += kThreads) {
-                    const int i = e & 31, j = e >> 5;
-                    S[i * 33 + j] = (i < nb && j < nb && i >= j) ? ldcg(Dpp + i + (size_t)j * lda) : 0.0;
+        __syncthreads();
+        const int idx = s_item;
+        if (idx < 0) return -1 - idx;  // another block found the failing column
+        if (idx >= total) break;
+        const TeamItem itm = team_item(P, idx);
+        const int p = itm.p, bi = itm.bi, bj = itm.bj;
+        if (itm.kind == 0) {
+            // D(p): factor and invert the diagonal block.
+            const int nb = rows_of(p);
+            const int w = team_wait_states(tc, team_state(tc, p, p), p, nullptr, 0, nullptr, 0);
+            if (w) return w;
+            team_load_block(S, A, lda, W32, ldw, W32 && p == 0, kPanel * p, kPanel * p, nb, nb, true);
+            for (int e = threadIdx.x; e < 32 * 32; e += kThreads) {
+                const int j = e >> 5, c = e & 31;
+                X[j * 33 + c] = (j == c && j < nb) ? 1.0 : 0.0;
+            }
+            __syncthreads();
+            const int info = team_factor_invert(nb, S, X, inv);
+            if (info) {
+                if (threadIdx.x == 0) {
+                    atomicCAS(tc.ctr + 2, 0, kPanel * p + info);
+                    *finisher = 1;
                 }
                 __syncthreads();
-                if (threadIdx.x < nb) inv[threadIdx.x] = 1.0 / S[threadIdx.x * 33 + threadIdx.x];
+                return kPanel * p + info;
+            }
+            team_store_block(S, A, lda, W32, ldw, kPanel * p, kPanel * p, nb, nb, true);
+            if (keep_x)
+                for (int e = threadIdx.x; e < 32 * 32; e += kThreads) {
+                    const int r = e & 31, c = e >> 5;
+                    A[team_xoff(n, lda, p * 1024 + e)] = X[r * 33 + c];
+                }
+            // With the inverse kept, every R item uses these same bits; else
+            // every R item recomputes it (the same way, whichever block).
+            if (threadIdx.x == 0) s_xpanel = keep_x ? p : -1;
+            team_publish(team_state(tc, p, p), p + 1);
+        } else if (itm.kind == 1) {
+            // R(p, bi): panel block (bi, p) <- A_ip · L_pp⁻ᵀ = A_ip · Xᵀ.
+            const int nb = rows_of(p), rb = rows_of(bi);
+            const int w = team_wait_states(tc, team_state(tc, p, p), p + 1, team_state(tc, bi, p), p, nullptr, 0);
+            if (w) return w;
+            if (s_xpanel != p) {
+                if (keep_x) {
+                    for (int e = threadIdx.x; e < 32 * 32; e += kThreads) {
+                        const int r = e & 31, c = e >> 5;
+                        X[r * 33 + c] = ldcg(A + team_xoff(n, lda, p * 1024 + e));
+                    }
+                } else {
+                    team_load_block(S, A, lda, nullptr, 0, false, kPanel * p, kPanel * p, nb, nb, true);
+                    __syncthreads();
+                    if (threadIdx.x < nb) inv[threadIdx.x] = 1.0 / S[threadIdx.x * 33 + threadIdx.x];
+                    __syncthreads();
+                    team_diag_inverse(S, inv, nb, X);
+                }
                 __syncthreads();
-                team_diag_inverse(S, inv, nb, X);
-                have_inverse = true;
+                if (threadIdx.x == 0) s_xpanel = p;
             }
-            const int r0 = p + nb + it * kTeamPanelRows;
-            team_panel_rows(A + (size_t)p * lda, lda, r0, min(kTeamPanelRows, n - r0), nb, X, W1);
-            team_done(tc, ph + 1, pitems);
-        }
-        if (!team_wait(tc, ph + 1, pitems)) return -1;
-        const int mb = (rest + 31) / 32;
-        const int citems = mb * (mb + 1) / 2;
-        const double* Q = A + (p + nb) + (size_t)p * lda;
-        double* C = A + (p + nb) + (size_t)(p + nb) * lda;
-        for (int it = team_claim(tc, ph + 2); it < citems; it = team_claim(tc, ph + 2)) {
-            team_syrk_block32(rest, nb, Q, lda, C, it, W1, W2);
-            team_done(tc, ph + 2, citems);
-        }
-        if (!team_wait(tc, ph + 2, citems)) return -1;
-    }
-    if (W32) {
-        for (int it = team_claim(tc, ph); it < copy_items; it = team_claim(tc, ph)) {
-            const int r0 = it * kTeamCopyRows, r1 = min(n, r0 + kTeamCopyRows), rows = r1 - r0;
-            for (long e = threadIdx.x; e < (long)rows * n; e += kThreads) {
-                const int i = r0 + (int)(e % rows), j = (int)(e / rows);
-                if (i >= j) W32[i + (size_t)j * ldw] = (float)__ldcg(A + i + (size_t)j * lda);
+            team_load_block(W1, A, lda, W32, ldw, W32 && p == 0, kPanel * bi, kPanel * p, rb, nb, false);
+            __syncthreads();
+            {
+                const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
+                double acc[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int j = g + 8 * k;
+                    double a = 0.0;
+                    for (int c = 0; c <= j && c < nb; ++c) a = fma(W1[r * 33 + c], X[j * 33 + c], a);
+                    acc[k] = a;
+                }
+                __syncthreads();
+#pragma unroll
+                for (int k = 0; k < 4; ++k) W1[r * 33 + g + 8 * k] = acc[k];
             }
-            if (team_done(tc, ph, copy_items) && threadIdx.x == 0) *finisher = 1;
+            __syncthreads();
+            team_store_block(W1, A, lda, W32, ldw, kPanel * bi, kPanel * p, rb, nb, false);
+            team_publish(team_state(tc, bi, p), p + 1);
+        } else {
+            // T(p, bi, bj): A_ij -= L_ip · L_jpᵀ (lower part of a diagonal block).
+            const int ri = rows_of(bi), rj = rows_of(bj);
+            const int w = team_wait_states(tc, team_state(tc, bi, p), p + 1, team_state(tc, bj, p), p + 1,
+                                           team_state(tc, bi, bj), p);
+            if (w) return w;
+            team_load_block(W1, A, lda, nullptr, 0, false, kPanel * bi, kPanel * p, ri, kPanel, false);
+            team_load_block(W2, A, lda, nullptr, 0, false, kPanel * bj, kPanel * p, rj, kPanel, false);
+            __syncthreads();
+            const bool diag = bi == bj;
+            const bool wide = W32 && p == 0;
+            const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
+            const int gi = kPanel * bi + r;
+            double cv[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int j = g + 8 * k, gj = kPanel * bj + j;
+                const bool ok = r < ri && j < rj && (!diag || r >= j);
+                cv[k] = !ok ? 0.0 : (wide ? (double)__ldcg(W32 + gi + (size_t)gj * ldw) : ldcg(A + gi + (size_t)gj * lda));
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int j = g + 8 * k, gj = kPanel * bj + j;
+                if (r < ri && j < rj && (!diag || r >= j)) {
+                    double a = 0.0;
+#pragma unroll 8
+                    for (int c = 0; c < kPanel; ++c) a = fma(W1[r * 33 + c], W2[j * 33 + c], a);
+                    A[gi + (size_t)gj * lda] = cv[k] - a;
+                }
+            }
+            team_publish(team_state(tc, bi, bj), p + 1);
         }
-        if (!team_wait(tc, ph, copy_items)) return -1;
+        if (threadIdx.x == 0 && atomicAdd(tc.ctr + 1, 1) == total - 1) *finisher = 1;
     }
     return 0;
 }

@@ -266,20 +266,22 @@ extern "C" uint64_t ttg_graph_generation(const ttg_ctx* c) { return c ? c->graph
 int ttg_task_parts(const ttg_op& op, bool team) {
     auto cdiv = [](long a, long b) { return (int)((a + b - 1) / b); };
     if (op.kind == TTG_OP_POTRF_L) {
-        if (!team || !team_fits(op.n, op.prec == TTG_PREC_MIXED)) return 1;
+        if (!team || !team_fits(op.n)) return 1;
         if (op.parts > 0) return std::min(op.parts, 64);
         return op.n >= 128 ? std::min(32, op.n / 16) : 1;
     }
-    // Tensor-core updates of the mixed path: exactly one 128×256 output block
-    // per part (lower-triangle blocks only for SYRK).
+    // Tensor-core updates of the mixed path: kTcBlocksPerPart 128×256 output
+    // blocks per part (lower-triangle blocks only for SYRK), one after the
+    // other in the part's block.
     if (op.prec == TTG_PREC_MIXED && op.flags >= 2 && (op.kind == TTG_OP_GEMM_NT || op.kind == TTG_OP_SYRK_LN)) {
         const int bm = cdiv(op.m, 128), bn = cdiv(op.n, 256);
-        if (op.kind == TTG_OP_GEMM_NT) return std::max(1, bm * bn);
+        const int per = kTcBlocksPerPart;
+        if (op.kind == TTG_OP_GEMM_NT) return std::max(1, cdiv(bm * bn, per));
         int cnt = 0;
         for (int j = 0; j < bn; ++j)
             for (int i = 0; i < bm; ++i)
                 if (i * 128 + 127 >= j * 256) ++cnt;
-        return std::max(1, cnt);
+        return std::max(1, cdiv(cnt, per));
     }
     int auto_parts = 1, max_parts = 1;
     switch (op.kind) {
@@ -481,7 +483,7 @@ extern "C" ttg_status ttg_graph_upload(ttg_ctx* c, const ttg_graph_desc* gd) {
         parts[t] = ttg_task_parts(gd->ops[t], true);
         // Every POTRF that fits runs the team code, a team of one included, so
         // the factor does not depend on how many blocks share it.
-        if (gd->ops[t].kind == TTG_OP_POTRF_L && team_fits(gd->ops[t].n, gd->ops[t].prec == TTG_PREC_MIXED))
+        if (gd->ops[t].kind == TTG_OP_POTRF_L && team_fits(gd->ops[t].n))
             team_slot[t] = n_team++;
     }
 
@@ -494,8 +496,8 @@ extern "C" ttg_status ttg_graph_upload(ttg_ctx* c, const ttg_graph_desc* gd) {
     std::vector<int> qcount(kMaxLevels, 0), bqcount(W, 0);
     for (int t = 0; t < n; ++t) {
         if (!runnable[t]) continue;
-        if (bind[t] >= 0) bqcount[bind[t] % W] += parts[t];
-        else qcount[level[t]] += parts[t];
+        if (bind[t] >= 0) bqcount[bind[t] % W] += parts[t];  // one slot per part
+        else qcount[level[t]] += 1;                           // one slot per task
     }
     std::vector<int> q_off(kMaxLevels + 1, 0), bq_off(W + 1, 0);
     for (int l = 0; l < kMaxLevels; ++l) q_off[l + 1] = q_off[l] + qcount[l];
@@ -506,14 +508,12 @@ extern "C" ttg_status ttg_graph_upload(ttg_ctx* c, const ttg_graph_desc* gd) {
     std::vector<int> tail0(kMaxLevels * 32, 0), btail0(W, 0);
     for (int t = 0; t < n; ++t) {
         if (gd->init_count[t] != 0) continue;
-        for (int q = 0; q < parts[t]; ++q) {
-            if (bind[t] >= 0) {
-                const int w = bind[t] % W;
-                bqinit[bq_off[w] + btail0[w]++] = t;
-            } else {
-                const int l = level[t];
-                qinit[q_off[l] + tail0[l * 32]++] = t;
-            }
+        if (bind[t] >= 0) {
+            const int w = bind[t] % W;
+            for (int q = 0; q < parts[t]; ++q) bqinit[bq_off[w] + btail0[w]++] = t;
+        } else {
+            const int l = level[t];
+            qinit[q_off[l] + tail0[l * 32]++] = t;
         }
     }
 

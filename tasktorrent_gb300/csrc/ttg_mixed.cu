@@ -137,12 +137,20 @@ __device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem,
             if (op.flags >= kMixedBF16) {
                 const MixedTables* tb = (const MixedTables*)op.aux;
                 const bool lower = op.kind == TTG_OP_SYRK_LN;
-                int row0, col0;
-                tc::tc_block_coords(part, op.m, op.n, lower, &row0, &col0);
+                // The part's share of the 128×256 output blocks, in turn.
+                const int nblk = tc::tc_num_blocks(op.m, op.n, lower);
+                const int per = (nblk + parts - 1) / parts;
                 const float f = (float)op.alpha * __ldcg(tb->slot_scale + op.lda) * __ldcg(tb->slot_scale + op.ldb);
-                const bool ok = tc::tc_gemm_block(tsh, ring, tmap, op.lda, op.ldb, row0, col0, op.k, f, (float*)op.c, op.ldc,
-                                                  op.m, op.n, lower, limit_ns, op.flags == kMixedBF16x3 ? 3 : 1, tb->n_slots);
-                if (!ok && threadIdx.x == 0) atomicCAS(err, 0, TTG_ETIMEOUT);
+                for (int b = part * per; b < min(nblk, (part + 1) * per); ++b) {
+                    int row0, col0;
+                    tc::tc_block_coords(b, op.m, op.n, lower, &row0, &col0);
+                    const bool ok = tc::tc_gemm_block(tsh, ring, tmap, op.lda, op.ldb, row0, col0, op.k, f, (float*)op.c, op.ldc,
+                                                      op.m, op.n, lower, limit_ns, op.flags == kMixedBF16x3 ? 3 : 1, tb->n_slots);
+                    if (!ok) {
+                        if (threadIdx.x == 0) atomicCAS(err, 0, TTG_ETIMEOUT);
+                        break;
+                    }
+                }
                 return 0;
             }
             return run_op_plain<float>(op, part, parts, fsm);
