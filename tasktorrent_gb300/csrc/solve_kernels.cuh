@@ -194,6 +194,160 @@ __device__ void strip_gemv(int rows, int kc, const TM* __restrict__ M, int ldm, 
     }
 }
 
+// ------------------------------------------------------------------------
+// Double-float arithmetic for the FP64 Krylov variant: a value is the
+// unevaluated sum hi + lo of two floats.  Products of the high parts are
+// split exactly with an FMA (Dekker's two-product), sums with Knuth's
+// two-sum; the small cross terms are added in FP32.  Relative accuracy is
+// about 2^-46 per operation at FP32 instruction rates (64 times the FP64
+// rate of GB300).  The _rn intrinsics keep the compiler from contracting the
+// error-free steps into FMAs.
+__device__ __forceinline__ void df_split(double x, float& hi, float& lo) {
+    hi = __double2float_rn(x);
+    lo = __double2float_rn(x - (double)hi);
+}
+
+// (sh, sl) += (ah + al)·(xh + xl).
+__device__ __forceinline__ void df_fma(float ah, float al, float xh, float xl, float& sh, float& sl) {
+    const float p = __fmul_rn(ah, xh);
+    float e = fmaf(ah, xh, -p);
+    e = fmaf(ah, xl, e);
+    e = fmaf(al, xh, e);
+    const float s = __fadd_rn(sh, p);
+    const float z = __fsub_rn(s, sh);
+    const float t = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, z)), __fsub_rn(p, z));
+    sl = __fadd_rn(sl, __fadd_rn(t, e));
+    sh = s;
+}
+
+// (sh, sl) += a·(xh + xl) for an FP32 a.
+__device__ __forceinline__ void df_fma1(float a, float xh, float xl, float& sh, float& sl) {
+    const float p = __fmul_rn(a, xh);
+    float e = fmaf(a, xh, -p);
+    e = fmaf(a, xl, e);
+    const float s = __fadd_rn(sh, p);
+    const float z = __fsub_rn(s, sh);
+    const float t = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, z)), __fsub_rn(p, z));
+    sl = __fadd_rn(sl, __fadd_rn(t, e));
+    sh = s;
+}
+
+// (sh, sl) <- the same value with |sl| <= ulp(sh)/2 (fast two-sum).
+__device__ __forceinline__ void df_renorm(float& sh, float& sl) {
+    const float s = __fadd_rn(sh, sl);
+    sl = __fsub_rn(sl, __fsub_rn(s, sh));
+    sh = s;
+}
+
+// strip_gemv for FP64 vectors and an FP32 factor in double-float arithmetic:
+// out[0:rows, q] (mode 0: =, 1: -=) Σ_c M[r + c·ldm] · V[c + q·ldv].  The
+// same thread layout as strip_gemv; V is staged as (hi, lo) float pairs.
+__device__ void strip_gemv_df(int rows, int kc, const float* __restrict__ M, int ldm, const double* V, int ldv, int nrhs,
+                              double* out, int ldo, int mode, unsigned char* smem_raw) {
+    float* vh = reinterpret_cast<float*>(smem_raw);   // [kChunk][kMaxRhs]
+    float* vl = vh + kChunk * kMaxRhs;                  // [kChunk][kMaxRhs]
+    double* part = reinterpret_cast<double*>(smem_raw);  // warp partials (after the chunks)
+    constexpr int kStage = 8;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int ra = 2 * lane, rb = 2 * lane + 1;
+    const bool oka = ra < rows, okb = rb < rows;
+    float h0[kMaxRhs], l0[kMaxRhs], h1[kMaxRhs], l1[kMaxRhs];
+#pragma unroll
+    for (int q = 0; q < kMaxRhs; ++q) h0[q] = l0[q] = h1[q] = l1[q] = 0.0f;
+    for (int c0 = 0; c0 < kc; c0 += kChunk) {
+        const int kcc = min(kChunk, kc - c0);
+        const int total = kcc * kMaxRhs;
+        __syncthreads();
+        for (int e0 = threadIdx.x; e0 < total; e0 += (int)blockDim.x * kStage) {
+            double tmp[kStage];
+#pragma unroll
+            for (int j = 0; j < kStage; ++j) {
+                const int e = e0 + j * (int)blockDim.x;
+                const int c = e % kcc, q = e / kcc;
+                tmp[j] = (e < total && q < nrhs) ? ldcg(V + (c0 + c) + (size_t)q * ldv) : 0.0;
+            }
+#pragma unroll
+            for (int j = 0; j < kStage; ++j) {
+                const int e = e0 + j * (int)blockDim.x;
+                if (e < total) {
+                    float hi, lo;
+                    df_split(tmp[j], hi, lo);
+                    vh[(e % kcc) * kMaxRhs + e / kcc] = hi;
+                    vl[(e % kcc) * kMaxRhs + e / kcc] = lo;
+                }
+            }
+        }
+        __syncthreads();
+        const float* Mc = M + (size_t)c0 * ldm;
+        // The factor values of the next U columns are loaded while the
+        // current U are used (a column is ~350 instructions per thread, so U
+        // columns cover the memory latency).
+        constexpr int U = 4;
+        float ca[U], cb[U];
+        auto load = [&](int cbase, float(&xa)[U], float(&xb)[U]) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int c = cbase + 8 * u;
+                xa[u] = (c < kcc && oka) ? Mc[ra + (size_t)c * ldm] : 0.0f;
+                xb[u] = (c < kcc && okb) ? Mc[rb + (size_t)c * ldm] : 0.0f;
+            }
+        };
+        load(warp, ca, cb);
+        for (int cbase = warp; cbase < kcc; cbase += 8 * U) {
+            float na[U], nb[U];
+            load(cbase + 8 * U, na, nb);
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int c = cbase + 8 * u;
+                if (c < kcc) {
+                    const float* xh = vh + c * kMaxRhs;
+                    const float* xl = vl + c * kMaxRhs;
+#pragma unroll
+                    for (int q = 0; q < kMaxRhs; ++q) {
+                        df_fma1(ca[u], xh[q], xl[q], h0[q], l0[q]);
+                        df_fma1(cb[u], xh[q], xl[q], h1[q], l1[q]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                ca[u] = na[u];
+                cb[u] = nb[u];
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kMaxRhs; ++q) {
+            df_renorm(h0[q], l0[q]);
+            df_renorm(h1[q], l1[q]);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < kMaxRhs; ++q) {
+        part[(warp * kMaxRhs + q) * kStrip + ra] = (double)h0[q] + (double)l0[q];
+        part[(warp * kMaxRhs + q) * kStrip + rb] = (double)h1[q] + (double)l1[q];
+    }
+    __syncthreads();
+    constexpr int kOut = kStrip * kMaxRhs / 256;
+    double prev[kOut];
+#pragma unroll
+    for (int j = 0; j < kOut; ++j) {
+        const int e = threadIdx.x + j * (int)blockDim.x;
+        const int r = e % kStrip, q = e / kStrip;
+        prev[j] = (mode != 0 && r < rows && q < nrhs) ? ldcg(out + r + (size_t)q * ldo) : 0.0;
+    }
+#pragma unroll
+    for (int j = 0; j < kOut; ++j) {
+        const int e = threadIdx.x + j * (int)blockDim.x;
+        const int r = e % kStrip, q = e / kStrip;
+        if (r >= rows || q >= nrhs) continue;
+        double sum = 0.0;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) sum += part[(w * kMaxRhs + q) * kStrip + r];
+        out[r + (size_t)q * ldo] = mode == 0 ? sum : prev[j] - sum;
+    }
+}
+
 // Largest idx with tab[idx] <= v (tab ascending, tab[0] = 0 <= v).
 __device__ __forceinline__ int upper_index(const int* tab, int n, int v) {
     int lo = 0, hi = n;  // tab[lo] <= v < tab[hi] (tab[n] > v)
@@ -275,12 +429,19 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs a, const TM* __res
         const int bk = a.bs[k], bi = a.bs[i];
         const int r0 = (g - a.strip_pre[k]) * kStrip;
         const int rows = min(kStrip, bk - r0);
+        // FP64 vectors with an FP32 factor (the FP64 Krylov variant) are
+        // swept in double-float arithmetic.
+        auto gemv = [&](int rws, int kc, const TM* M, int ldm, const T* V, T* o, int mode) {
+            if constexpr (sizeof(T) == 8 && sizeof(TM) == 4)
+                strip_gemv_df(rws, kc, M, ldm, V, N, a.nrhs, o, N, mode, smem);
+            else
+                strip_gemv<T, TM>(rws, kc, M, ldm, V, N, a.nrhs, o, N, mode, smem);
+        };
         if (diag) {
-            strip_gemv<T, TM>(rows, bi, Md + a.doff[i] + r0, bi, Vin + a.displ[i], N, a.nrhs, Vout + a.displ[i] + r0, N, 0,
-                              smem);
+            gemv(rows, bi, Md + a.doff[i] + r0, bi, Vin + a.displ[i], Vout + a.displ[i] + r0, 0);
         } else {
             const int64_t o = a.backward ? a.off[i + (size_t)k * nb] : a.off[k + (size_t)i * nb];
-            strip_gemv<T, TM>(rows, bi, Mu + o + r0, bk, Vout + a.displ[i], N, a.nrhs, Vin + a.displ[k] + r0, N, 1, smem);
+            gemv(rows, bi, Mu + o + r0, bk, Vout + a.displ[i], Vin + a.displ[k] + r0, 1);
         }
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -411,6 +572,58 @@ __global__ void dense_matmul_partial(int N, const T* __restrict__ A, const T* __
             if (qq < nrhs) P[(size_t)sp * N * nrhs + r + (size_t)qq * N] = acc[q];
         }
     }
+}
+
+// Y = A X partials in double-float arithmetic: A = Ah + Al (two FP32
+// copies, Al = fl32(A - Ah)), X FP64 (split per staged chunk); the same grid
+// and partial layout as dense_matmul_partial<double>.
+__global__ void dense_matmul_df_partial(int N, const float* __restrict__ Ah, const float* __restrict__ Al,
+                                        const double* __restrict__ X, int nrhs, double* P, int splits) {
+    __shared__ __align__(16) float sXh[128 * kMaxRhs], sXl[128 * kMaxRhs];
+    const int rb = blockIdx.x, sp = blockIdx.y;
+    const int r = rb * 128 + (threadIdx.x & 127);
+    const int half = threadIdx.x >> 7;  // two threads per row: rhs halves
+    const int kper = (N + splits - 1) / splits;
+    const int k0 = sp * kper, k1 = min(N, k0 + kper);
+    float sh[kMaxRhs / 2], sl[kMaxRhs / 2];
+#pragma unroll
+    for (int q = 0; q < kMaxRhs / 2; ++q) sh[q] = sl[q] = 0.0f;
+    for (int c0 = k0; c0 < k1; c0 += 128) {
+        const int kc = min(128, k1 - c0);
+        __syncthreads();
+        for (int e = threadIdx.x; e < 128 * kMaxRhs; e += blockDim.x) {
+            const int c = e % 128, q = e / 128;
+            float hi = 0.0f, lo = 0.0f;
+            if (c < kc && q < nrhs) df_split(X[(c0 + c) + (size_t)q * N], hi, lo);
+            sXh[c * kMaxRhs + q] = hi;
+            sXl[c * kMaxRhs + q] = lo;
+        }
+        __syncthreads();
+        if (r < N) {
+            for (int c = 0; c < kc; ++c) {
+                const float ah = Ah[r + (size_t)(c0 + c) * N], al = Al[r + (size_t)(c0 + c) * N];
+                const float* xh = sXh + c * kMaxRhs + half * (kMaxRhs / 2);
+                const float* xl = sXl + c * kMaxRhs + half * (kMaxRhs / 2);
+#pragma unroll
+                for (int q = 0; q < kMaxRhs / 2; ++q) df_fma(ah, al, xh[q], xl[q], sh[q], sl[q]);
+            }
+#pragma unroll
+            for (int q = 0; q < kMaxRhs / 2; ++q) df_renorm(sh[q], sl[q]);
+        }
+    }
+    if (r < N) {
+#pragma unroll
+        for (int q = 0; q < kMaxRhs / 2; ++q) {
+            const int qq = half * (kMaxRhs / 2) + q;
+            if (qq < nrhs) P[(size_t)sp * N * nrhs + r + (size_t)qq * N] = (double)sh[q] + (double)sl[q];
+        }
+    }
+}
+
+// Al = fl32(A - Ah): the low FP32 half of the dense copy.
+__global__ void split_low_half(int64_t n, const double* __restrict__ A, const float* __restrict__ Ah, float* __restrict__ Al) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+        Al[e] = __double2float_rn(A[e] - (double)Ah[e]);
 }
 
 template <class T>

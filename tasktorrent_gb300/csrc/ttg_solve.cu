@@ -73,7 +73,9 @@ struct ttg_solver {
     // Dense copies of the input (rebuilt when the input changes).
     DevBuf<double> A64;
     DevBuf<float> A32;
+    DevBuf<float> A32lo;  // fl32(A - A32): the double-float matvec of FP64 Krylov work
     bool dense_valid = false;
+    bool lo_valid = false;
     double anorm_inf = 0.0;
     // Operands of the sweeps for the current factor: L_ii⁻ᵀ and L_ii⁻¹
     // (compact diagonal tiles at doff) and the transposed off-diagonal tiles
@@ -230,7 +232,7 @@ void ttg_solver_destroy(ttg_solver* S) {
     for (auto* b : {&S->A64, &S->inv64, &S->linv64, &S->lt64, &S->B, &S->X, &S->R, &S->D, &S->W, &S->T1, &S->T2, &S->P, &S->Vd, &S->part, &S->colv,
                     &S->coefA, &S->coefB})
         b->release();
-    for (auto* b : {&S->A32, &S->inv32, &S->linv32, &S->lt32, &S->f1, &S->f2, &S->f3, &S->Vf}) b->release();
+    for (auto* b : {&S->A32, &S->A32lo, &S->inv32, &S->linv32, &S->lt32, &S->f1, &S->f2, &S->f3, &S->Vf}) b->release();
     S->d_off.release();
     S->d_bs.release();
     S->d_displ.release();
@@ -249,7 +251,7 @@ void ttg_solver_destroy(ttg_solver* S) {
 }
 
 void ttg_solver_input_changed(ttg_solver* S) {
-    if (S) S->dense_valid = false;
+    if (S) S->dense_valid = S->lo_valid = false;
 }
 
 // Dense copies of A (FP64, and FP32 for the mixed path) and ‖A‖∞.
@@ -390,6 +392,28 @@ ttg_status matmul(ttg_solver* S, const T* A, const T* X, const T* B, T* Y, T* P,
     return TTG_OK;
 }
 
+// Y = A X in double-float arithmetic from the two FP32 halves of the dense
+// copy (built on first use), for the FP64 Krylov variant.
+ttg_status matmul_df(ttg_solver* S, const double* X, double* Y, int nrhs, cudaStream_t s) {
+    const size_t NN = (size_t)S->N * S->N;
+    ttg_status st;
+    if (!S->lo_valid) {
+        if ((st = S->A32lo.ensure(NN)) != TTG_OK) return st;
+        ttg_note_launch();
+        split_low_half<<<S->ctx->sms * 8, 256, 0, s>>>((int64_t)NN, S->A64.p, S->A32.p, S->A32lo.p);
+        TTG_CUDA_CHECK(cudaGetLastError());
+        S->lo_valid = true;
+    }
+    const int splits = 4;
+    dim3 grid((S->N + 127) / 128, splits);
+    ttg_note_launch();
+    dense_matmul_df_partial<<<grid, 256, 0, s>>>(S->N, S->A32.p, S->A32lo.p, X, nrhs, S->P.p, splits);
+    ttg_note_launch();
+    reduce_partials<double><<<S->ctx->sms * 4, 256, 0, s>>>(S->N, nrhs, S->P.p, splits, nullptr, Y, 0);
+    TTG_CUDA_CHECK(cudaGetLastError());
+    return TTG_OK;
+}
+
 // Per-column reduction to host: kind 0 dot(X, Y), kind 1 max|X|.
 template <class T>
 ttg_status colreduce(ttg_solver* S, const T* X, const T* Y, int nrhs, int kind, double* host, cudaStream_t s) {
@@ -480,8 +504,13 @@ ttg_status gmres_cycle(ttg_solver* S, const float* L32, int nrhs, int m, double 
     for (; k < m; ++k) {
         TG* vk = V + blk * k;
         TG* w = V + blk * (k + 1);
-        // w = M⁻¹ (A v_k)
-        if ((st = matmul<TG>(S, A, vk, nullptr, t1, t3, nrhs, 0, s)) != TTG_OK) return st;
+        // w = M⁻¹ (A v_k); FP64 Krylov vectors take A v_k in double-float
+        // arithmetic (FP32 instruction rate, ~2^-46 accurate).
+        if constexpr (sizeof(TG) == 8) {
+            if ((st = matmul_df(S, (const double*)vk, (double*)t1, nrhs, s)) != TTG_OK) return st;
+        } else {
+            if ((st = matmul<TG>(S, A, vk, nullptr, t1, t3, nrhs, 0, s)) != TTG_OK) return st;
+        }
         if ((st = sweeps<TG, float>(S, L32, S->lt32.p, S->linv32.p, S->inv32.p, t1, t2, w, nrhs, grid, s)) != TTG_OK)
             return st;
         // Modified Gram-Schmidt.
