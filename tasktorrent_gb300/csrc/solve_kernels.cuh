@@ -574,6 +574,103 @@ __global__ void dense_matmul_partial(int N, const T* __restrict__ A, const T* __
     }
 }
 
+// Y = A X partials for FP32 (the FP32 Krylov matvec): a block takes 1024
+// rows and one K split; thread (warp w, lane l) owns rows 128w + 4l .. +3 of
+// the block and all 16 right-hand sides (64 accumulators), reading its four
+// rows of a column with one 16-byte load (scalar loads when N % 4 != 0) and
+// the staged X row as four 16-byte shared-memory loads: 64 FMAs per column
+// against 5 loads.  The next kMmU columns are loaded while the current are
+// used.  Partials P[split] are added by reduce_partials in a fixed order.
+constexpr int kMmRows = 1024, kMmChunk = 256, kMmU = 4;
+__global__ void __launch_bounds__(256, 2) dense_matmul_f32_partial(int N, const float* __restrict__ A, const float* __restrict__ X,
+                                                                   int nrhs, float* P, int splits) {
+    __shared__ __align__(16) float sX[kMmChunk * kMaxRhs];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r0 = blockIdx.x * kMmRows + warp * 128 + 4 * lane;
+    const int sp = blockIdx.y;
+    const int kper = (N + splits - 1) / splits;
+    const int k0 = min(N, sp * kper), k1 = min(N, k0 + kper);
+    const bool vec = (N & 3) == 0 && r0 + 3 < N;
+    float acc[4][kMaxRhs];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int q = 0; q < kMaxRhs; ++q) acc[i][q] = 0.0f;
+    auto load_col = [&](int c) -> float4 {
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        const float* col = A + (size_t)c * N + r0;
+        if (vec) {
+            v = *reinterpret_cast<const float4*>(col);
+        } else {
+            if (r0 < N) v.x = col[0];
+            if (r0 + 1 < N) v.y = col[1];
+            if (r0 + 2 < N) v.z = col[2];
+            if (r0 + 3 < N) v.w = col[3];
+        }
+        return v;
+    };
+    for (int c0 = k0; c0 < k1; c0 += kMmChunk) {
+        const int kc = min(kMmChunk, k1 - c0);
+        __syncthreads();
+        {
+            constexpr int kPer = kMmChunk * kMaxRhs / 256;
+            float tmp[kPer];
+#pragma unroll
+            for (int j = 0; j < kPer; ++j) {
+                const int e = threadIdx.x + 256 * j;
+                const int c = e % kMmChunk, q = e / kMmChunk;
+                tmp[j] = (c < kc && q < nrhs) ? __ldcg(X + (c0 + c) + (size_t)q * N) : 0.0f;
+            }
+#pragma unroll
+            for (int j = 0; j < kPer; ++j) {
+                const int e = threadIdx.x + 256 * j;
+                sX[(e % kMmChunk) * kMaxRhs + e / kMmChunk] = tmp[j];
+            }
+        }
+        __syncthreads();
+        float4 cur[kMmU];
+#pragma unroll
+        for (int u = 0; u < kMmU; ++u) cur[u] = u < kc ? load_col(c0 + u) : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int c = 0; c < kc; c += kMmU) {
+            float4 nxt[kMmU];
+#pragma unroll
+            for (int u = 0; u < kMmU; ++u) nxt[u] = c + kMmU + u < kc ? load_col(c0 + c + kMmU + u) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int u = 0; u < kMmU; ++u) {
+                if (c + u < kc) {
+                    const float4* xv = reinterpret_cast<const float4*>(sX + (c + u) * kMaxRhs);
+                    const float a[4] = {cur[u].x, cur[u].y, cur[u].z, cur[u].w};
+#pragma unroll
+                    for (int j = 0; j < kMaxRhs / 4; ++j) {
+                        const float4 x = xv[j];
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) {
+                            acc[i][4 * j + 0] = fmaf(a[i], x.x, acc[i][4 * j + 0]);
+                            acc[i][4 * j + 1] = fmaf(a[i], x.y, acc[i][4 * j + 1]);
+                            acc[i][4 * j + 2] = fmaf(a[i], x.z, acc[i][4 * j + 2]);
+                            acc[i][4 * j + 3] = fmaf(a[i], x.w, acc[i][4 * j + 3]);
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kMmU; ++u) cur[u] = nxt[u];
+        }
+    }
+    float* out = P + (size_t)sp * N * nrhs;
+#pragma unroll
+    for (int q = 0; q < kMaxRhs; ++q) {
+        if (q >= nrhs) break;
+        if (vec) {
+            *reinterpret_cast<float4*>(out + r0 + (size_t)q * N) = make_float4(acc[0][q], acc[1][q], acc[2][q], acc[3][q]);
+        } else {
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                if (r0 + i < N) out[r0 + i + (size_t)q * N] = acc[i][q];
+        }
+    }
+}
+
 // Y = A X partials in double-float arithmetic: A = Ah + Al (two FP32
 // copies, Al = fl32(A - Ah)), X FP64 (split per staged chunk); the same grid
 // and partial layout as dense_matmul_partial<double>.

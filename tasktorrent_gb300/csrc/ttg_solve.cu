@@ -96,6 +96,7 @@ struct ttg_solver {
     // Work vectors (N × 16).
     DevBuf<double> B, X, R, D, W, T1, T2, P;
     DevBuf<float> f1, f2, f3;
+    DevBuf<float> Pf;  // partials of the FP32 matvec (splits × N × nrhs)
     DevBuf<double> Vd;  // Krylov basis, FP64 variant
     DevBuf<float> Vf;   // Krylov basis, FP32 variant
     DevBuf<double> part, colv, coefA, coefB;
@@ -232,7 +233,7 @@ void ttg_solver_destroy(ttg_solver* S) {
     for (auto* b : {&S->A64, &S->inv64, &S->linv64, &S->lt64, &S->B, &S->X, &S->R, &S->D, &S->W, &S->T1, &S->T2, &S->P, &S->Vd, &S->part, &S->colv,
                     &S->coefA, &S->coefB})
         b->release();
-    for (auto* b : {&S->A32, &S->A32lo, &S->inv32, &S->linv32, &S->lt32, &S->f1, &S->f2, &S->f3, &S->Vf}) b->release();
+    for (auto* b : {&S->A32, &S->A32lo, &S->Pf, &S->inv32, &S->linv32, &S->lt32, &S->f1, &S->f2, &S->f3, &S->Vf}) b->release();
     S->d_off.release();
     S->d_bs.release();
     S->d_displ.release();
@@ -379,9 +380,23 @@ ttg_status sweeps(ttg_solver* S, const TM* L, const TM* LT, const TM* Linv, cons
     return TTG_OK;
 }
 
-// Y = A X (mode 0) or Y = B − A X (mode 2) with the dense copy.
+// Y = A X (mode 0) or Y = B − A X (mode 2) with the dense copy.  FP32: the
+// register-blocked kernel, K split so that the grid fills two blocks per SM.
 template <class T>
 ttg_status matmul(ttg_solver* S, const T* A, const T* X, const T* B, T* Y, T* P, int nrhs, int mode, cudaStream_t s) {
+    if constexpr (sizeof(T) == 4) {
+        const int rowblocks = (S->N + kMmRows - 1) / kMmRows;
+        const int splits = std::max(1, std::min(2 * S->ctx->sms / rowblocks, S->N / kMmChunk));
+        ttg_status st = S->Pf.ensure((size_t)splits * S->N * nrhs);
+        if (st != TTG_OK) return st;
+        dim3 grid(rowblocks, splits);
+        ttg_note_launch();
+        dense_matmul_f32_partial<<<grid, 256, 0, s>>>(S->N, (const float*)A, (const float*)X, nrhs, S->Pf.p, splits);
+        ttg_note_launch();
+        reduce_partials<float><<<S->ctx->sms * 4, 256, 0, s>>>(S->N, nrhs, S->Pf.p, splits, (const float*)B, (float*)Y, mode);
+        TTG_CUDA_CHECK(cudaGetLastError());
+        return TTG_OK;
+    }
     const int splits = 4;
     dim3 grid((S->N + 127) / 128, splits);
     ttg_note_launch();
