@@ -270,18 +270,18 @@ int ttg_task_parts(const ttg_op& op, bool team) {
         if (op.parts > 0) return std::min(op.parts, 64);
         return op.n >= 128 ? std::min(32, op.n / 16) : 1;
     }
-    // Tensor-core updates of the mixed path: kTcBlocksPerPart 128×256 output
-    // blocks per part (lower-triangle blocks only for SYRK), one after the
-    // other in the part's block.
+    // Tensor-core updates of the mixed path: GEMM kTcBlocksPerPart 128×256
+    // output blocks per part, one after the other in the part's block; SYRK
+    // (the diagonal tiles, on the factorisation's critical path) one block
+    // per part, lower-triangle blocks only.
     if (op.prec == TTG_PREC_MIXED && op.flags >= 2 && (op.kind == TTG_OP_GEMM_NT || op.kind == TTG_OP_SYRK_LN)) {
         const int bm = cdiv(op.m, 128), bn = cdiv(op.n, 256);
-        const int per = kTcBlocksPerPart;
-        if (op.kind == TTG_OP_GEMM_NT) return std::max(1, cdiv(bm * bn, per));
+        if (op.kind == TTG_OP_GEMM_NT) return std::max(1, cdiv(bm * bn, kTcBlocksPerPart));
         int cnt = 0;
         for (int j = 0; j < bn; ++j)
             for (int i = 0; i < bm; ++i)
                 if (i * 128 + 127 >= j * 256) ++cnt;
-        return std::max(1, cdiv(cnt, per));
+        return std::max(1, cnt);
     }
     int auto_parts = 1, max_parts = 1;
     switch (op.kind) {
@@ -300,6 +300,9 @@ int ttg_task_parts(const ttg_op& op, bool team) {
         case TTG_OP_TRSM_RLNN:
             max_parts = std::max(1, cdiv(op.m, 16));
             auto_parts = std::min(8, std::max(1, cdiv(op.m, 128)));
+            // The mixed path's FP32 TRSM keeps each part's rows in shared
+            // memory: at most 64 rows per part.
+            if (op.prec == TTG_PREC_MIXED && op.kind == TTG_OP_TRSM_RLTN) auto_parts = std::min(max_parts, std::max(1, cdiv(op.m, 64)));
             break;
         case TTG_OP_GEADD:
         case TTG_OP_CONVERT:

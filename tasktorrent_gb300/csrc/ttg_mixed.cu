@@ -76,6 +76,161 @@ __device__ inline void rows_to_bf16(const float* W, int ldw, int r0, int r1, int
     }
 }
 
+// ------------------------------------------------------------------------
+// FP32 TRSM of the mixed path with the part's rows resident in shared memory.
+//
+// Part `part` owns rows [r0, r0 + rows) (rows <= kTrsmRows) of B (m×n, ldb)
+// and computes B <- alpha·B·L⁻ᵀ (L n×n lower, ldl; cblas_dtrsm R,L,T,N of
+// 2d_cholesky.cpp:479), n <= 512:
+//   Bs[c·64 + r]   the row slice, column-major, 128 KB;
+//   Ls[l·nL + c]   panel p of L: Ls[l·nL + c] = L(c, p + l) for c >= p;
+//   iv[l]          1 / L(p + l, p + l).
+// Per 32-column panel the panel is copied in with 16-byte asynchronous copies
+// (all in flight at once), the panel columns of each row are solved by one
+// thread per row (forward substitution), and the columns right of the panel
+// are updated from shared memory in 4×8 register tiles.  The tile never goes
+// back to global memory between panels: the per-panel GEMMs of the generic
+// kernel were chains of global round trips (≈ 25 µs per 128×128 block).
+constexpr int kTrsmRows = 64;
+constexpr int kTrsmMaxN = 512;
+constexpr int kTrsmSmemBytes = (kTrsmRows * kTrsmMaxN + 32 * kTrsmMaxN + 32) * 4;
+
+__device__ __forceinline__ void cp_async16_mx(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+                 "l"(__cvta_generic_to_global(src))
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all_mx() { asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;" ::: "memory"); }
+
+// The resident form applies: n <= 512, 16-byte aligned operands and column
+// starts, whole 16-byte row groups.
+__device__ __forceinline__ bool trsm_resident_ok(int m, int n, const float* L, int ldl, const float* B, int ldb) {
+    return n > 0 && n <= kTrsmMaxN && (n & 3) == 0 && (m & 3) == 0 && (ldl & 3) == 0 && (ldb & 3) == 0 &&
+           ((uintptr_t)L & 15) == 0 && ((uintptr_t)B & 15) == 0;
+}
+
+// Rows [r0, r0 + rows) (r0 and rows multiples of 4, rows <= 64) solved in
+// shared memory; on return Bs holds the solved slice (also written to B).
+__device__ void trsm_rltn_f32_resident(int n, float alpha, const float* L, int ldl, float* B, int ldb, int r0, int rows,
+                                       float* smem) {
+    float* Bs = smem;
+    float* Ls = smem + kTrsmRows * kTrsmMaxN;
+    float* iv = Ls + 32 * kTrsmMaxN;
+    const int nL = (n + 7) & ~7;
+    const int tid = threadIdx.x;
+    const int q4 = rows >> 2;  // 16-byte groups per column of the slice
+    for (int e = tid; e < n * q4; e += kThreads) {
+        const int c = e / q4, q = e - c * q4;
+        cp_async16_mx(Bs + c * kTrsmRows + 4 * q, B + r0 + 4 * q + (size_t)c * ldb);
+    }
+    cp_async_wait_all_mx();
+    __syncthreads();
+    if (alpha != 1.0f) {
+        for (int e = tid; e < n * kTrsmRows; e += kThreads) Bs[e] *= alpha;
+        __syncthreads();
+    }
+    const int rg = tid & 15, cg = tid >> 4;
+    for (int p = 0; p < n; p += 32) {
+        const int nb = min(32, n - p);
+        const int seg = (n - p) >> 2;  // 16-byte groups of a panel column from row p
+        for (int e = tid; e < nb * seg; e += kThreads) {
+            const int l = e / seg, q = e - l * seg;
+            cp_async16_mx(Ls + l * nL + p + 4 * q, L + p + 4 * q + (size_t)(p + l) * ldl);
+        }
+        cp_async_wait_all_mx();
+        __syncthreads();
+        if (tid < nb) iv[tid] = 1.0f / Ls[tid * nL + p + tid];
+        __syncthreads();
+        if (tid < rows) {
+            float x[32];
+#pragma unroll
+            for (int c = 0; c < 32; ++c) x[c] = c < nb ? Bs[(p + c) * kTrsmRows + tid] : 0.0f;
+#pragma unroll
+            for (int c = 0; c < 32; ++c) {
+                if (c < nb) {
+                    float sum = x[c];
+#pragma unroll
+                    for (int l = 0; l < c; ++l) sum = fmaf(-x[l], Ls[l * nL + p + c], sum);
+                    x[c] = sum * iv[c];
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < 32; ++c)
+                if (c < nb) Bs[(p + c) * kTrsmRows + tid] = x[c];
+        }
+        __syncthreads();
+        // Columns right of the panel: Bs[:, c] -= X_p · L(c, p:p+nb)ᵀ.
+        for (int cb = p + nb + 8 * cg; cb < n; cb += 128) {
+            float acc[4][8];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
+            for (int l = 0; l < nb; ++l) {
+                const float4 xv = *reinterpret_cast<const float4*>(Bs + (p + l) * kTrsmRows + 4 * rg);
+                const float4 la = *reinterpret_cast<const float4*>(Ls + l * nL + cb);
+                const float4 lb = *reinterpret_cast<const float4*>(Ls + l * nL + cb + 4);
+                const float xs[4] = {xv.x, xv.y, xv.z, xv.w};
+                const float ls[8] = {la.x, la.y, la.z, la.w, lb.x, lb.y, lb.z, lb.w};
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(xs[i], ls[j], acc[i][j]);
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                if (cb + j < n) {
+                    float4* o = reinterpret_cast<float4*>(Bs + (cb + j) * kTrsmRows + 4 * rg);
+                    float4 v = *o;
+                    v.x -= acc[0][j];
+                    v.y -= acc[1][j];
+                    v.z -= acc[2][j];
+                    v.w -= acc[3][j];
+                    *o = v;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    for (int e = tid; e < n * q4; e += kThreads) {
+        const int c = e / q4, q = e - c * q4;
+        *reinterpret_cast<float4*>(B + r0 + 4 * q + (size_t)c * ldb) = *reinterpret_cast<const float4*>(Bs + c * kTrsmRows + 4 * q);
+    }
+}
+
+// Rows [r0, r0 + rows) of the resident slice Bs (n columns) as BF16 slices
+// of the K-major slot dst (row r at dst + r·b), times inv: one slice (hi) or
+// three (hi, mid, lo; slice s at dst + s·slice).  Each slice goes through a
+// padded row-major buffer in the panel area, so the slot rows are written
+// with consecutive columns.
+__device__ void publish_bf16_resident(const float* smem, int n, int r0, int rows, __nv_bfloat16* dst, size_t slice, int b, float inv,
+                                      int nslices) {
+    const float* Bs = smem;
+    __nv_bfloat16* T = reinterpret_cast<__nv_bfloat16*>(const_cast<float*>(smem) + kTrsmRows * kTrsmMaxN);
+    constexpr int kTs = kTrsmMaxN + 2;  // row stride (odd number of 4-byte words)
+    for (int sl = 0; sl < nslices; ++sl) {
+        __syncthreads();
+        for (int e = threadIdx.x; e < rows * n; e += kThreads) {
+            const int r = e % rows, c = e / rows;
+            const float v = Bs[c * kTrsmRows + r] * inv;
+            const __nv_bfloat16 h = __float2bfloat16_rn(v);
+            __nv_bfloat16 out = h;
+            if (sl > 0) {
+                const float r1v = v - __bfloat162float(h);
+                const __nv_bfloat16 mi = __float2bfloat16_rn(r1v);
+                out = sl == 1 ? mi : __float2bfloat16_rn(r1v - __bfloat162float(mi));
+            }
+            T[r * kTs + c] = out;
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < rows * n; e += kThreads) {
+            const int r = e / n, c = e - (e / n) * n;
+            dst[(size_t)sl * slice + (size_t)(r0 + r) * b + c] = T[r * kTs + c];
+        }
+    }
+    __syncthreads();
+}
+
 __device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem, int* team, int* fin, tc::TcShared* tsh,
                              uint8_t* ring, const CUtensorMap* tmap, int* err, long long limit_ns) {
     if (op.prec == TTG_PREC_F64) {
@@ -111,6 +266,27 @@ __device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem,
             return info;
         }
         case TTG_OP_TRSM_RLTN:
+            if (trsm_resident_ok(op.m, op.n, (const float*)op.a, op.lda, (const float*)op.c, op.ldc)) {
+                // The part's rows: the same slices as the publish below.
+                const int per = ((op.m + parts - 1) / parts + 15) / 16 * 16;
+                const int r0 = min(op.m, part * per), r1 = min(op.m, r0 + per);
+                if (r1 - r0 <= kTrsmRows) {
+                    if (r1 > r0) trsm_rltn_f32_resident(op.n, (float)op.alpha, (const float*)op.a, op.lda, (float*)op.c, op.ldc, r0,
+                                                        r1 - r0, fsm);
+                    if (op.flags >= kMixedBF16) {
+                        const MixedTables* tb = (const MixedTables*)op.aux;
+                        const float s = tb->rowscale[op.k];
+                        const size_t slice = (size_t)tb->n_slots * tb->b * tb->b;
+                        if (r1 > r0)
+                            publish_bf16_resident(fsm, op.n, r0, r1 - r0, tb->b16 + (size_t)op.ldb * tb->b * tb->b, slice, tb->b,
+                                                  1.0f / s, op.flags == kMixedBF16x3 ? 3 : 1);
+                        if (threadIdx.x == 0 && part == 0) tb->slot_scale[op.ldb] = s;
+                        tc::fence_proxy_async_global();
+                    }
+                    __syncthreads();
+                    return 0;
+                }
+            }
             if (op.flags < kMixedBF16) return run_op_plain<float>(op, part, parts, fsm);
             trsm_rltn_tile<float>(op.m, op.n, (float)op.alpha, (const float*)op.a, op.lda, (float*)op.c, op.ldc, fsm, part,
                                   parts);
@@ -162,6 +338,8 @@ __device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem,
 // Dynamic shared memory: the FP64/FP32 tile kernels use the front, the
 // tensor-core ring (1024-aligned) the rest; both are never live together.
 constexpr int kMixedSmemBytes = tc::kSmemBytes > kPlainSmemDoubles * 8 ? tc::kSmemBytes : kPlainSmemDoubles * 8;
+static_assert(kTrsmSmemBytes <= kMixedSmemBytes, "resident TRSM shared memory");
+static_assert(kTrsmRows * kTrsmMaxN * 4 + kTrsmRows * (kTrsmMaxN + 2) * 2 <= kMixedSmemBytes, "BF16 publish buffer");
 
 __global__ void __launch_bounds__(kThreads, 1) exec_kernel_mixed(ExecParams p, const __grid_constant__ MixedGlobals g) {
     extern __shared__ __align__(1024) double smem_mx[];

@@ -680,6 +680,10 @@ ttg_status ttg_solver_solve(ttg_solver* S, const double* pristine, const double*
             if (st != TTG_OK) return st;
             if (solve_verbose()) fprintf(stderr, "[ttg solve] GMRES(FP%d) %d iterations\n", prec, it);
             clk.mark("GMRES cycle");
+            // An FP32 cycle that used its whole restart length did not reach
+            // its tolerance: the FP32 operators are too coarse for this
+            // matrix, so the next cycles use FP64 Krylov vectors (auto mode).
+            if (o->gmres_prec == 0 && prec == 32 && it >= m) prec = 64;
             r.inner += it;
             r.outer = outer + 1;
             std::vector<double> ones(nrhs, 1.0);
