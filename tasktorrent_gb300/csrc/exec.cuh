@@ -32,10 +32,11 @@ constexpr int kLevelGroups = kMaxLevels / 32;
 constexpr int kTraceWords = 4;
 // Counter words per team task (the POTRF tasks shared by several blocks).
 constexpr int kTeamStride = 256;
-// 128×256 tensor-core output blocks per part of a mixed-path update: with
-// one, the parts (~25 µs of split-BF16 work) come faster than the queue
-// hands them out well; two measured best at N = 32768, tile 512.
-constexpr int kTcBlocksPerPart = 2;
+// 128×256 tensor-core output blocks per part of a mixed-path GEMM update,
+// run back to back in the part's block so that each block's epilogue
+// overlaps the next block's MMAs (split-BF16 factorisation, N = 32768, tile
+// 512: 99.0 ms with 2, 94.5 ms with 4, 95.1 ms with 8).
+constexpr int kTcBlocksPerPart = 4;
 
 struct ExecParams {
     const ttg_op* ops;

@@ -11,13 +11,14 @@
 // update of 2d_cholesky.cpp:490-494 in the mixed-precision path.
 //
 // Data movement and compute:
-//   - one thread issues TMA loads (cp.async.bulk.tensor.3d, 128B swizzle) of
-//     64-wide K slabs into a 4-stage shared-memory ring guarded by mbarriers;
+//   - one thread issues TMA loads (cp.async.bulk.tensor.3d, 64B swizzle) of
+//     32-wide K slabs into a 9-slot shared-memory ring guarded by mbarriers;
 //   - one thread issues tcgen05.mma.cta_group::1.kind::f16 (M=128, N=256,
 //     K=16; BF16 inputs, FP32 accumulator in 256 TMEM columns) and commits
 //     each stage back to the producer with tcgen05.commit;
-//   - all 8 warps read the accumulator with tcgen05.ld.32x32b.x32 (warp w
-//     reads TMEM lanes 32·(w%4)…, columns 128·(w/4)…) and update C.
+//   - warps 4-7 read the accumulator with tcgen05.ld.32x32b.x32 (warp w reads
+//     TMEM lanes 32·(w-4)…) and update C, while the MMAs of the next output
+//     block run into the other of two accumulators (512 TMEM columns).
 // Every wait is bounded: on timeout the block records an error and drains.
 #pragma once
 #include <cuda.h>
@@ -30,25 +31,30 @@ namespace tc {
 
 constexpr int kBM = 128;           // accumulator rows (TMEM lanes)
 constexpr int kBN = 256;           // accumulator columns
-constexpr int kBK = 64;            // K per stage (one 128-byte swizzle row of BF16)
-constexpr int kStages = 4;
-constexpr int kStageBytesA = kBM * kBK * 2;       // 16 KB
-constexpr int kStageBytesB = kBN * kBK * 2;       // 32 KB
-constexpr int kStageBytes = kStageBytesA + kStageBytesB;
-constexpr int kSmemBytes = kStages * kStageBytes + 1024;  // + alignment slack
-constexpr uint32_t kTmemCols = 256;
+constexpr int kBK = 32;            // K per slot (one 64-byte swizzle row of BF16)
+// The ring holds kSlots slots of one K slab each: A (128 rows) then B (256
+// rows) of one BF16 slice.  A plain BF16 K step takes one slot; a split K
+// step takes three consecutive slots (hi, mid, lo) and issues all six slice
+// products from them, so each slice is loaded once per K step.
+constexpr int kSlots = 9;
+constexpr int kSlotBytesA = kBM * kBK * 2;        // 8 KB
+constexpr int kSlotBytesB = kBN * kBK * 2;        // 16 KB
+constexpr int kSlotBytes = kSlotBytesA + kSlotBytesB;
+constexpr int kSmemBytes = kSlots * kSlotBytes + 1024;  // 217 KB + alignment slack
+constexpr uint32_t kTmemCols = 512;  // two 256-column accumulators (double buffer)
 
 // Per-block state kept in shared memory across tasks.
 struct TcShared {
-    uint64_t full[kStages];
-    uint64_t empty[kStages];
-    uint64_t accf;
+    uint64_t full[kSlots];
+    uint64_t empty[kSlots];
+    uint64_t accf[2];    // accumulator b complete (tcgen05.commit of the MMA thread)
+    uint64_t afree[2];   // accumulator b drained (the epilogue warps)
     uint32_t tmem_base;
     uint32_t produced;   // stages produced (producer thread)
     uint32_t consumed;   // stages consumed (MMA thread)
-    uint32_t acc_done;   // accumulations completed (all threads read)
+    uint32_t nacc;       // output blocks accumulated so far (all threads read)
     int failed;          // a bounded wait gave up in this block
-    int acc_ok;          // the current accumulator is complete (block-uniform)
+    int ep_ok;           // the epilogue's accumulator is complete (warps 4-7)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -118,14 +124,14 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-// Shared-memory descriptor of a K-major, 128B-swizzled operand whose rows are
-// 128 bytes and whose 8-row groups are 1024 bytes apart: start address >> 4
+// Shared-memory descriptor of a K-major, 64B-swizzled operand whose rows are
+// 64 bytes and whose 8-row groups are 512 bytes apart: start address >> 4
 // (bits 0-13), leading offset (unused for this layout, 1), stride offset
-// 1024 >> 4 (bits 32-45), version 1 (bits 46-47), layout SWIZZLE_128B = 2
+// 512 >> 4 (bits 32-45), version 1 (bits 46-47), layout SWIZZLE_64B = 4
 // (bits 61-63).
-__device__ __forceinline__ uint64_t smem_desc_kmajor_sw128(uint32_t saddr) {
-    return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) | ((uint64_t)1 << 46) |
-           ((uint64_t)2 << 61);
+__device__ __forceinline__ uint64_t smem_desc_kmajor_sw64(uint32_t saddr) {
+    return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)1 << 16) | ((uint64_t)(512 >> 4) << 32) | ((uint64_t)1 << 46) |
+           ((uint64_t)4 << 61);
 }
 
 __device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
@@ -134,6 +140,13 @@ __device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint6
         "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
         : "memory");
 }
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Named barrier 1 over the 128 threads of warps 4-7 (the epilogue warpgroup).
+__device__ __forceinline__ void epilogue_bar() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
 
 __device__ __forceinline__ void umma_commit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
@@ -155,14 +168,17 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
 // Block setup (all threads): barriers and TMEM.  Call once per kernel.
 __device__ inline void tc_setup(TcShared* sh) {
     if (threadIdx.x == 0) {
-        for (int s = 0; s < kStages; ++s) {
+        for (int s = 0; s < kSlots; ++s) {
             mbar_init(&sh->full[s], 1);
             mbar_init(&sh->empty[s], 1);
         }
-        mbar_init(&sh->accf, 1);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&sh->accf[b], 1);
+            mbar_init(&sh->afree[b], 1);
+        }
         sh->produced = 0;
         sh->consumed = 0;
-        sh->acc_done = 0;
+        sh->nacc = 0;
         sh->failed = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         fence_proxy_async_smem();
@@ -179,7 +195,7 @@ __device__ inline void tc_setup(TcShared* sh) {
 __device__ inline void tc_teardown(TcShared* sh, long long limit_ns) {
     if (threadIdx.x == 0 && sh->failed) {
         for (uint32_t p = sh->consumed; p < sh->produced; ++p)
-            if (!mbar_wait(&sh->full[p % kStages], (p / kStages) & 1, limit_ns)) break;
+            if (!mbar_wait(&sh->full[p % kSlots], (p / kSlots) & 1, limit_ns)) break;
     }
     tc_fence_before();
     __syncthreads();
@@ -195,124 +211,6 @@ __device__ inline void tc_teardown(TcShared* sh, long long limit_ns) {
 // first — mid·mid, hi·lo, lo·hi, hi·mid, mid·hi, hi·hi.
 __device__ __forceinline__ int split_pair_a(int p) { return p == 0 ? 1 : (p == 2 ? 2 : (p == 4 ? 1 : 0)); }
 __device__ __forceinline__ int split_pair_b(int p) { return p == 0 ? 1 : (p == 1 ? 2 : (p == 3 ? 1 : 0)); }
-
-// C[block] += f · Σ A_slotA · B_slotBᵀ.  split = 1: one BF16 product;
-// split = 3: the operands are stored as three BF16 slices (slot + s·stride,
-// s = 0, 1, 2) and the six products of split_pair_* accumulate in the same
-// FP32 TMEM accumulator, which gives FP32-level accuracy.
-__device__ inline bool tc_gemm_block(TcShared* sh, uint8_t* ring, const CUtensorMap* map, int slotA, int slotB, int row0,
-                                     int col0, int k, float f, float* C, int ldc, int m, int n, bool lower, long long limit_ns,
-                                     int split = 1, int stride = 0) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int ksteps = k / kBK;
-    const int npairs = split == 3 ? 6 : 1;
-    const int total = npairs * ksteps;
-    bool ok = !sh->failed;
-    if (threadIdx.x >= 64) {
-        // Warps 2-7 are idle during the main loop: bring this block's part of
-        // C into L2 (one 128-byte line per 32 rows of a column) so that the
-        // epilogue's reads hit.
-        const int rows = min(kBM, m - row0), lines = (rows + 31) >> 5;
-        for (int e = threadIdx.x - 64; e < kBN * lines; e += (int)blockDim.x - 64) {
-            const int c = e / lines, gc = col0 + c, gr = row0 + 32 * (e % lines);
-            if (gc < n && (!lower || row0 + rows - 1 >= gc))
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(C + gr + (size_t)gc * ldc)));
-        }
-    }
-    if (threadIdx.x == 0 && ok) {
-        // Producer: K slabs of A (128 rows) and B (two boxes of 128 rows).
-        fence_proxy_async_global();  // panel tiles were written by other blocks' generic stores
-        uint32_t p = sh->produced;
-        for (int g = 0; g < total; ++g, ++p) {
-            const int ks = g % ksteps, pr = g / ksteps;
-            const int sa = slotA + (split == 3 ? split_pair_a(pr) * stride : 0);
-            const int sb = slotB + (split == 3 ? split_pair_b(pr) * stride : 0);
-            const int s = p % kStages;
-            if (!mbar_wait(&sh->empty[s], ((p / kStages) & 1) ^ 1, limit_ns)) {
-                sh->failed = 1;
-                break;
-            }
-            uint8_t* st = ring + (size_t)s * kStageBytes;
-            mbar_expect_tx(&sh->full[s], kStageBytes);
-            tma_load_3d(st, map, &sh->full[s], ks * kBK, row0, sa);
-            tma_load_3d(st + kStageBytesA, map, &sh->full[s], ks * kBK, col0, sb);
-            tma_load_3d(st + kStageBytesA + kStageBytesB / 2, map, &sh->full[s], ks * kBK, col0 + 128, sb);
-        }
-        sh->produced = p;
-    } else if (threadIdx.x == 32 && ok) {
-        // MMA issuer.
-        const uint32_t idesc = idesc_bf16_f32(kBM, kBN);
-        uint32_t c = sh->consumed;
-        bool good = true;
-        for (int g = 0; g < total; ++g, ++c) {
-            const int s = c % kStages;
-            if (!mbar_wait(&sh->full[s], (c / kStages) & 1, limit_ns)) {
-                sh->failed = 1;
-                good = false;
-                break;
-            }
-            tc_fence_after();
-            const uint32_t a0 = smem_u32(ring + (size_t)s * kStageBytes);
-            const uint32_t b0 = a0 + kStageBytesA;
-#pragma unroll
-            for (int kk = 0; kk < kBK / 16; ++kk) {
-                const uint64_t ad = smem_desc_kmajor_sw128(a0 + kk * 32);
-                const uint64_t bd = smem_desc_kmajor_sw128(b0 + kk * 32);
-                umma_bf16(sh->tmem_base, ad, bd, idesc, (g > 0 || kk > 0) ? 1u : 0u);
-            }
-            umma_commit(&sh->empty[s]);
-        }
-        sh->consumed = c;
-        if (good) umma_commit(&sh->accf);
-    }
-    __syncthreads();
-    // Epilogue: one thread waits for the accumulator; the outcome is
-    // broadcast so that every warp takes the same path (tcgen05.ld is
-    // warp-collective).
-    if (threadIdx.x == 0) {
-        bool have = false;
-        if (!sh->failed) {
-            have = mbar_wait(&sh->accf, sh->acc_done & 1, limit_ns);
-            if (!have) sh->failed = 1;
-        }
-        sh->acc_ok = have ? 1 : 0;
-    }
-    __syncthreads();
-    const bool have = sh->acc_ok != 0;
-    if (have) {
-        tc_fence_after();
-        const int q = warp & 3, h = warp >> 2;
-        const int r = 32 * q + lane;  // accumulator row of this thread
-        const int gr = row0 + r;
-#pragma unroll 1
-        for (int ch = 0; ch < 4; ++ch) {
-            const int c0 = 128 * h + 32 * ch;
-            uint32_t v[32];
-            tmem_ld32(sh->tmem_base + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, v);
-            if (gr < m) {
-                // All 32 reads first (independent, in flight together), then
-                // the 32 writes: one memory round trip per chunk, not 32.
-                float cv[32];
-                float* p = C + gr + (size_t)(col0 + c0) * ldc;
-#pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const int gc = col0 + c0 + j;
-                    cv[j] = (gc < n && (!lower || gr >= gc)) ? __ldcg(p + (size_t)j * ldc) : 0.0f;
-                }
-#pragma unroll
-                for (int j = 0; j < 32; ++j) {
-                    const int gc = col0 + c0 + j;
-                    if (gc < n && (!lower || gr >= gc)) p[(size_t)j * ldc] = fmaf(f, __uint_as_float(v[j]), cv[j]);
-                }
-            }
-        }
-        tc_fence_before();
-    }
-    __syncthreads();
-    if (threadIdx.x == 0 && have) sh->acc_done += 1;
-    __syncthreads();
-    return !sh->failed;
-}
 
 // Number of 128×256 output blocks of an m×n tile (lower: blocks that meet
 // the lower triangle of a square tile), and the coordinates of block b.
@@ -341,6 +239,164 @@ __device__ __forceinline__ void tc_block_coords(int b, int m, int n, bool lower,
         }
     *row0 = 0;
     *col0 = 0;
+}
+
+// C[block] += f · Σ A_slotA · B_slotBᵀ for the output blocks b0 .. b0+nblk-1
+// of the tile (tc_block_coords order).  split = 1: one BF16 product; split =
+// 3: the operands are stored as three BF16 slices (slot + s·stride, s = 0,
+// 1, 2) and the six products of split_pair_* accumulate in the same FP32
+// TMEM accumulator, which gives FP32-level accuracy.
+//
+// Roles: thread 0 loads the K slabs of every block into the ring (TMA),
+// thread 32 issues the MMAs, warps 2-3 prefetch the C blocks into L2, and
+// warps 4-7 (one warpgroup: TMEM lanes 32·(w-4)…) drain the accumulators
+// into C.  Consecutive blocks alternate between the two 256-column
+// accumulators, so block j's epilogue runs while block j+1's MMAs do:
+// accf[b] says accumulator b is complete, afree[b] that it has been read.
+// All threads call it; returns false if a wait timed out.
+__device__ inline bool tc_gemm_blocks(TcShared* sh, uint8_t* ring, const CUtensorMap* map, int slotA, int slotB, int b0, int nblk,
+                                      int k, float f, float* C, int ldc, int m, int n, bool lower, long long limit_ns, int split = 1,
+                                      int stride = 0) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ksteps = k / kBK;
+    const int nsl = split == 3 ? 3 : 1;  // slots (slices) per K step
+    const int npairs = split == 3 ? 6 : 1;
+    const int total = nsl * ksteps;      // slots per output block
+    const uint32_t base = sh->nacc;
+    const bool ok = !sh->failed;
+    if (warp == 2 || warp == 3) {
+        // Bring the C blocks into L2 (one 128-byte line per 32 rows of a
+        // column) so that the epilogue's reads hit.
+        for (int j = 0; j < nblk; ++j) {
+            int row0, col0;
+            tc_block_coords(b0 + j, m, n, lower, &row0, &col0);
+            const int rows = min(kBM, m - row0), lines = (rows + 31) >> 5;
+            for (int e = threadIdx.x - 64; e < kBN * lines; e += 64) {
+                const int c = e / lines, gc = col0 + c, gr = row0 + 32 * (e % lines);
+                if (gc < n && (!lower || row0 + rows - 1 >= gc))
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(__cvta_generic_to_global(C + gr + (size_t)gc * ldc)));
+            }
+        }
+    } else if (threadIdx.x == 0 && ok) {
+        // Producer: K slabs of A (128 rows) and B (two boxes of 128 rows).
+        fence_proxy_async_global();  // panel tiles were written by other blocks' generic stores
+        uint32_t p = sh->produced;
+        for (int j = 0; j < nblk && !sh->failed; ++j) {
+            int row0, col0;
+            tc_block_coords(b0 + j, m, n, lower, &row0, &col0);
+            for (int g = 0; g < total; ++g, ++p) {
+                const int ks = g / nsl, sl = g % nsl;  // K step, slice
+                const int s = p % kSlots;
+                if (!mbar_wait(&sh->empty[s], ((p / kSlots) & 1) ^ 1, limit_ns)) {
+                    sh->failed = 1;
+                    break;
+                }
+                uint8_t* st = ring + (size_t)s * kSlotBytes;
+                mbar_expect_tx(&sh->full[s], kSlotBytes);
+                tma_load_3d(st, map, &sh->full[s], ks * kBK, row0, slotA + sl * stride);
+                tma_load_3d(st + kSlotBytesA, map, &sh->full[s], ks * kBK, col0, slotB + sl * stride);
+                tma_load_3d(st + kSlotBytesA + kSlotBytesB / 2, map, &sh->full[s], ks * kBK, col0 + 128, slotB + sl * stride);
+            }
+        }
+        sh->produced = p;
+    } else if (threadIdx.x == 32 && ok) {
+        // MMA issuer.
+        const uint32_t idesc = idesc_bf16_f32(kBM, kBN);
+        uint32_t c = sh->consumed;
+        bool good = true;
+        for (int j = 0; j < nblk && good; ++j) {
+            const uint32_t gi = base + j;
+            const int buf = gi & 1;
+            // The accumulator's previous block must have been drained.
+            if (!mbar_wait(&sh->afree[buf], ((gi >> 1) & 1) ^ 1, limit_ns)) {
+                sh->failed = 1;
+                good = false;
+                break;
+            }
+            tc_fence_after();
+            const uint32_t dacc = sh->tmem_base + (uint32_t)(kBN * buf);
+            for (int ks = 0; ks < ksteps && good; ++ks, c += nsl) {
+                // The K step's slots (one per slice) must all be loaded.
+                uint32_t sbase[3];
+                for (int sl = 0; sl < nsl; ++sl) {
+                    const uint32_t cs = c + sl;
+                    if (!mbar_wait(&sh->full[cs % kSlots], (cs / kSlots) & 1, limit_ns)) {
+                        sh->failed = 1;
+                        good = false;
+                        break;
+                    }
+                    sbase[sl] = smem_u32(ring + (size_t)(cs % kSlots) * kSlotBytes);
+                }
+                if (!good) break;
+                tc_fence_after();
+                for (int pr = 0; pr < npairs; ++pr) {
+                    const uint32_t a0 = sbase[split == 3 ? split_pair_a(pr) : 0];
+                    const uint32_t bb = sbase[split == 3 ? split_pair_b(pr) : 0] + kSlotBytesA;
+#pragma unroll
+                    for (int kk = 0; kk < kBK / 16; ++kk) {
+                        const uint64_t ad = smem_desc_kmajor_sw64(a0 + kk * 32);
+                        const uint64_t bd = smem_desc_kmajor_sw64(bb + kk * 32);
+                        umma_bf16(dacc, ad, bd, idesc, (ks > 0 || pr > 0 || kk > 0) ? 1u : 0u);
+                    }
+                }
+                for (int sl = 0; sl < nsl; ++sl) umma_commit(&sh->empty[(c + sl) % kSlots]);
+            }
+            if (good) umma_commit(&sh->accf[buf]);
+        }
+        sh->consumed = c;
+    } else if (warp >= 4) {
+        // Epilogue warpgroup: warp w drains TMEM lanes 32·(w-4) (rows of the
+        // block) over all 256 columns.
+        const int q = warp - 4;
+        const int r = 32 * q + lane;
+        for (int j = 0; j < nblk; ++j) {
+            const uint32_t gi = base + j;
+            const int buf = gi & 1;
+            if (threadIdx.x == 128) {
+                bool have = false;
+                if (!sh->failed) {
+                    have = mbar_wait(&sh->accf[buf], (gi >> 1) & 1, limit_ns);
+                    if (!have) sh->failed = 1;
+                }
+                sh->ep_ok = have ? 1 : 0;
+            }
+            epilogue_bar();
+            if (!sh->ep_ok) break;  // the same value in all four warps
+            tc_fence_after();
+            int row0, col0;
+            tc_block_coords(b0 + j, m, n, lower, &row0, &col0);
+            const int gr = row0 + r;
+#pragma unroll 1
+            for (int ch = 0; ch < kBN / 32; ++ch) {
+                const int c0 = 32 * ch;
+                uint32_t v[32];
+                tmem_ld32(sh->tmem_base + ((uint32_t)(32 * q) << 16) + (uint32_t)(kBN * buf + c0), v);
+                if (gr < m) {
+                    // All 32 reads first (independent, in flight together), then
+                    // the 32 writes: one memory round trip per chunk, not 32.
+                    float cv[32];
+                    float* pc = C + gr + (size_t)(col0 + c0) * ldc;
+#pragma unroll
+                    for (int jj = 0; jj < 32; ++jj) {
+                        const int gc = col0 + c0 + jj;
+                        cv[jj] = (gc < n && (!lower || gr >= gc)) ? __ldcg(pc + (size_t)jj * ldc) : 0.0f;
+                    }
+#pragma unroll
+                    for (int jj = 0; jj < 32; ++jj) {
+                        const int gc = col0 + c0 + jj;
+                        if (gc < n && (!lower || gr >= gc)) pc[(size_t)jj * ldc] = fmaf(f, __uint_as_float(v[jj]), cv[jj]);
+                    }
+                }
+            }
+            tc_fence_before();
+            epilogue_bar();  // all four warps have read the accumulator
+            if (threadIdx.x == 128) mbar_arrive(&sh->afree[buf]);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) sh->nacc = base + nblk;
+    __syncthreads();
+    return !sh->failed;
 }
 
 }  // namespace tc

@@ -317,16 +317,11 @@ __device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem,
                 const int nblk = tc::tc_num_blocks(op.m, op.n, lower);
                 const int per = (nblk + parts - 1) / parts;
                 const float f = (float)op.alpha * __ldcg(tb->slot_scale + op.lda) * __ldcg(tb->slot_scale + op.ldb);
-                for (int b = part * per; b < min(nblk, (part + 1) * per); ++b) {
-                    int row0, col0;
-                    tc::tc_block_coords(b, op.m, op.n, lower, &row0, &col0);
-                    const bool ok = tc::tc_gemm_block(tsh, ring, tmap, op.lda, op.ldb, row0, col0, op.k, f, (float*)op.c, op.ldc,
-                                                      op.m, op.n, lower, limit_ns, op.flags == kMixedBF16x3 ? 3 : 1, tb->n_slots);
-                    if (!ok) {
-                        if (threadIdx.x == 0) atomicCAS(err, 0, TTG_ETIMEOUT);
-                        break;
-                    }
-                }
+                const int b0 = min(nblk, part * per), b1 = min(nblk, (part + 1) * per);
+                if (b1 > b0 && !tc::tc_gemm_blocks(tsh, ring, tmap, op.lda, op.ldb, b0, b1 - b0, op.k, f, (float*)op.c, op.ldc, op.m,
+                                                   op.n, lower, limit_ns, op.flags == kMixedBF16x3 ? 3 : 1, tb->n_slots) &&
+                    threadIdx.x == 0)
+                    atomicCAS(err, 0, TTG_ETIMEOUT);
                 return 0;
             }
             return run_op_plain<float>(op, part, parts, fsm);
@@ -474,7 +469,7 @@ static ttg_status encode_tmap(ttg_mixed_state* m, int n_slots) {
     cuuint32_t box[3] = {(cuuint32_t)tc::kBK, 128u, 1u};
     cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = encode(&m->globals.tmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, (void*)m->b16, dims, strides, box, estr,
-                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
         ttg_set_last_cuda_error(cudaErrorInvalidValue, "cuTensorMapEncodeTiled", __FILE__, __LINE__);
