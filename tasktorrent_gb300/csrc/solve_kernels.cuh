@@ -65,6 +65,12 @@ struct SweepArgs {
     int* err;                  // nonzero after a timeout
     long long timeout_ns;
     long long* trace;          // per item: claimed, inputs ready, done (ns), SM; nullptr = off
+    // Folded form (FP32 factors): the update of a block row by the row
+    // processed just before it is folded into W_i = Md_i · Mu(i, prev), so a
+    // step's critical chain is one item.  zready[i]: Z items of row i done.
+    int fold;
+    const int64_t* woff;       // [nb] offset of W_i in Wd (ld bs[i])
+    int* zready;               // [nb]
 };
 
 __device__ __forceinline__ long long sweep_clock() {
@@ -363,14 +369,25 @@ __device__ __forceinline__ int upper_index(const int* tab, int n, int v) {
 // tiles, Md = L_ii⁻¹ (compact diagonal).  Backward: Vin = Y (updated in
 // place), Vout = X, Mu = the transposed tiles (L_ijᵀ at off[i + j·nb], ld
 // bs[j]), Md = L_ii⁻ᵀ.
+//
+// Folded form (a.fold, Wd = W_i at woff[i]): with i the row of step s, p the
+// row of step s-1 and n the row of step s+1, a step's items are
+//   D  (strips of i)  s = 0: Vout_i = Md_i · Vin_i;  s >= 1: Vout_i -= W_i · Vout_p,
+//                     where Vout_i already holds Z_i (ready[i]++);
+//   Z  (strips of n)  Vout_n = Md_n · Vin_n, Vin_n holding the updates of steps
+//                     0 .. s-1 (zready[n]++);
+//   U  (strips of the rows after n)  Vin_k -= Mu(k, i) · Vout_i (applied = s+1).
+// The update of n by i never runs: it is W_n · Vout_i inside n's D items.
 template <class T, class TM>
-__global__ void __launch_bounds__(256) sweep_kernel(SweepArgs a, const TM* __restrict__ Mu, const TM* __restrict__ Md, T* Vin,
-                                                    T* Vout) {
+__global__ void __launch_bounds__(256) sweep_kernel(SweepArgs a, const TM* __restrict__ Mu, const TM* __restrict__ Md,
+                                                    const TM* __restrict__ Wd, T* Vin, T* Vout) {
     extern __shared__ __align__(16) unsigned char sweep_smem[];
     unsigned char* smem = sweep_smem;
     __shared__ int s_item, s_abort;
     const int nb = a.nb, N = a.N;
     const int total = a.step_start[nb];
+    auto row_of = [&](int step) { return a.backward ? nb - 1 - step : step; };
+    auto strips = [&](int row) { return a.strip_pre[row + 1] - a.strip_pre[row]; };
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) s_item = atomicAdd(a.claim, 1);
@@ -379,30 +396,50 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs a, const TM* __res
         if (it >= total) break;
         if (a.trace && threadIdx.x == 0) a.trace[4 * (size_t)it] = sweep_clock();
         const int s = upper_index(a.step_start, nb, it);
-        const int i = a.backward ? nb - 1 - s : s;
+        const int i = row_of(s);
         int u = it - a.step_start[s];
-        const int Si = a.strip_pre[i + 1] - a.strip_pre[i];
-        const bool diag = u < Si;
-        int k, g;  // target block row and its global strip
-        if (diag) {
+        const int Si = strips(i);
+        // kind 0: diagonal (D), 1: next row's Z (folded form), 2: update (U).
+        int kind, k, g;  // target block row and its global strip
+        if (u < Si) {
+            kind = 0;
             k = i;
             g = a.strip_pre[i] + u;
         } else {
             u -= Si;
-            g = a.backward ? a.strip_pre[i] - 1 - u : a.strip_pre[i + 1] + u;
-            k = upper_index(a.strip_pre, nb, g);
+            const int nx = s + 1 < nb ? row_of(s + 1) : -1;
+            const int Sn = (a.fold && nx >= 0) ? strips(nx) : 0;
+            if (u < Sn) {
+                kind = 1;
+                k = nx;
+                g = a.strip_pre[nx] + u;
+            } else {
+                u -= Sn;
+                kind = 2;
+                // Strips of the rows after i (folded: after n), nearest first.
+                const int skip = a.fold ? 1 : 0;
+                g = a.backward ? a.strip_pre[i - skip] - 1 - u : a.strip_pre[i + 1 + skip] + u;
+                k = upper_index(a.strip_pre, nb, g);
+            }
         }
+        const int p = s > 0 ? row_of(s - 1) : -1;
         // Wait for the inputs of this item.
         if (threadIdx.x == 0) {
             int abort = 0;
             const long long t0 = sweep_clock();
             unsigned spin = 0;
             for (;;) {
-                bool ok;
-                if (diag) {
-                    ok = true;
-                    for (int h = a.strip_pre[i]; h < a.strip_pre[i + 1] && ok; ++h)
-                        ok = *(const volatile int*)(a.applied + h) >= s;
+                bool ok = true;
+                if (kind == 0) {
+                    if (a.fold) {
+                        if (s > 0)
+                            ok = *(const volatile int*)(a.zready + i) >= Si && *(const volatile int*)(a.ready + p) >= strips(p);
+                    } else {
+                        for (int h = a.strip_pre[i]; h < a.strip_pre[i + 1] && ok; ++h)
+                            ok = *(const volatile int*)(a.applied + h) >= s;
+                    }
+                } else if (kind == 1) {
+                    for (int h = a.strip_pre[k]; h < a.strip_pre[k + 1] && ok; ++h) ok = *(const volatile int*)(a.applied + h) >= s;
                 } else {
                     ok = *(const volatile int*)(a.ready + i) >= Si && *(const volatile int*)(a.applied + g) >= s;
                 }
@@ -437,8 +474,13 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs a, const TM* __res
             else
                 strip_gemv<T, TM>(rws, kc, M, ldm, V, N, a.nrhs, o, N, mode, smem);
         };
-        if (diag) {
-            gemv(rows, bi, Md + a.doff[i] + r0, bi, Vin + a.displ[i], Vout + a.displ[i] + r0, 0);
+        if (kind == 0) {
+            if (a.fold && s > 0)
+                gemv(rows, a.bs[p], Wd + a.woff[i] + r0, bi, Vout + a.displ[p], Vout + a.displ[i] + r0, 1);
+            else
+                gemv(rows, bi, Md + a.doff[i] + r0, bi, Vin + a.displ[i], Vout + a.displ[i] + r0, 0);
+        } else if (kind == 1) {
+            gemv(rows, bk, Md + a.doff[k] + r0, bk, Vin + a.displ[k], Vout + a.displ[k] + r0, 0);
         } else {
             const int64_t o = a.backward ? a.off[i + (size_t)k * nb] : a.off[k + (size_t)i * nb];
             gemv(rows, bi, Mu + o + r0, bk, Vout + a.displ[i], Vin + a.displ[k] + r0, 1);
@@ -446,7 +488,8 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs a, const TM* __res
         __syncthreads();
         if (threadIdx.x == 0) {
             __threadfence();
-            if (diag) atomicAdd(a.ready + i, 1);
+            if (kind == 0) atomicAdd(a.ready + i, 1);
+            else if (kind == 1) atomicAdd(a.zready + k, 1);
             else atomicExch(a.applied + g, s + 1);
             if (a.trace) {
                 unsigned sm;
@@ -456,6 +499,21 @@ __global__ void __launch_bounds__(256) sweep_kernel(SweepArgs a, const TM* __res
             }
         }
     }
+}
+
+// W_i = A_i · B_i for the folded sweeps (column-major, NN): block (t, q)
+// computes part q of gridDim.y of product t.
+struct WdDesc {
+    int64_t a, b, c;  // offsets into A, B, C
+    int m, n, k;      // C is m×n (ld m), A m×k (ld m), B k×n (ld k)
+};
+
+template <class TM>
+__global__ void wd_gemm_kernel(const WdDesc* __restrict__ d, const TM* A, const TM* B, TM* C) {
+    extern __shared__ __align__(16) unsigned char wd_smem[];
+    const WdDesc w = d[blockIdx.x];
+    gemm_tile<TM, true, false>(w.m, w.n, w.k, TM(1), A + w.a, w.m, B + w.b, w.k, TM(0), C + w.c, w.m,
+                               reinterpret_cast<TM*>(wd_smem), blockIdx.y, gridDim.y);
 }
 
 // Transposes of tiles: dst[doff_t + c + r·rows_t] = src[soff_t + r + c·rows_t]

@@ -250,10 +250,14 @@ __device__ __forceinline__ void tc_block_coords(int b, int m, int n, bool lower,
 // Roles: thread 0 loads the K slabs of every block into the ring (TMA),
 // thread 32 issues the MMAs, warps 2-3 prefetch the C blocks into L2, and
 // warps 4-7 (one warpgroup: TMEM lanes 32·(w-4)…) drain the accumulators
-// into C.  Consecutive blocks alternate between the two 256-column
-// accumulators, so block j's epilogue runs while block j+1's MMAs do:
-// accf[b] says accumulator b is complete, afree[b] that it has been read.
-// All threads call it; returns false if a wait timed out.
+// into C.  Plain BF16: consecutive blocks alternate between the two
+// 256-column accumulators, so block j's epilogue runs while block j+1's MMAs
+// do.  Split: hi·hi accumulates in columns 0-255 and the five smaller
+// products in columns 256-511, added in the epilogue — the small terms are
+// not rounded against the large accumulator (a K step issues all six
+// products), which keeps the update FP32-accurate.  accf[b] says buffer b is
+// complete, afree[b] that it has been read.  All threads call it; returns
+// false if a wait timed out.
 __device__ inline bool tc_gemm_blocks(TcShared* sh, uint8_t* ring, const CUtensorMap* map, int slotA, int slotB, int b0, int nblk,
                                       int k, float f, float* C, int ldc, int m, int n, bool lower, long long limit_ns, int split = 1,
                                       int stride = 0) {
@@ -264,6 +268,9 @@ __device__ inline bool tc_gemm_blocks(TcShared* sh, uint8_t* ring, const CUtenso
     const int total = nsl * ksteps;      // slots per output block
     const uint32_t base = sh->nacc;
     const bool ok = !sh->failed;
+    const bool dbl = split != 3;  // double-buffered accumulators
+    auto buf_of = [&](uint32_t gi) { return dbl ? (int)(gi & 1) : 0; };
+    auto use_of = [&](uint32_t gi) { return dbl ? (gi >> 1) : gi; };
     if (warp == 2 || warp == 3) {
         // Bring the C blocks into L2 (one 128-byte line per 32 rows of a
         // column) so that the epilogue's reads hit.
@@ -306,15 +313,16 @@ __device__ inline bool tc_gemm_blocks(TcShared* sh, uint8_t* ring, const CUtenso
         bool good = true;
         for (int j = 0; j < nblk && good; ++j) {
             const uint32_t gi = base + j;
-            const int buf = gi & 1;
+            const int buf = buf_of(gi);
             // The accumulator's previous block must have been drained.
-            if (!mbar_wait(&sh->afree[buf], ((gi >> 1) & 1) ^ 1, limit_ns)) {
+            if (!mbar_wait(&sh->afree[buf], (use_of(gi) & 1) ^ 1, limit_ns)) {
                 sh->failed = 1;
                 good = false;
                 break;
             }
             tc_fence_after();
             const uint32_t dacc = sh->tmem_base + (uint32_t)(kBN * buf);
+            const uint32_t dsmall = sh->tmem_base + (uint32_t)kBN;  // split: the five smaller products
             for (int ks = 0; ks < ksteps && good; ++ks, c += nsl) {
                 // The K step's slots (one per slice) must all be loaded.
                 uint32_t sbase[3];
@@ -332,11 +340,15 @@ __device__ inline bool tc_gemm_blocks(TcShared* sh, uint8_t* ring, const CUtenso
                 for (int pr = 0; pr < npairs; ++pr) {
                     const uint32_t a0 = sbase[split == 3 ? split_pair_a(pr) : 0];
                     const uint32_t bb = sbase[split == 3 ? split_pair_b(pr) : 0] + kSlotBytesA;
+                    // pair npairs-1 is hi·hi (the only one when not split)
+                    const bool big = pr == npairs - 1;
+                    const uint32_t d = big ? dacc : dsmall;
 #pragma unroll
                     for (int kk = 0; kk < kBK / 16; ++kk) {
                         const uint64_t ad = smem_desc_kmajor_sw64(a0 + kk * 32);
                         const uint64_t bd = smem_desc_kmajor_sw64(bb + kk * 32);
-                        umma_bf16(dacc, ad, bd, idesc, (ks > 0 || pr > 0 || kk > 0) ? 1u : 0u);
+                        const bool acc = big ? (ks > 0 || kk > 0) : (ks > 0 || pr > 0 || kk > 0);
+                        umma_bf16(d, ad, bd, idesc, acc ? 1u : 0u);
                     }
                 }
                 for (int sl = 0; sl < nsl; ++sl) umma_commit(&sh->empty[(c + sl) % kSlots]);
@@ -351,11 +363,11 @@ __device__ inline bool tc_gemm_blocks(TcShared* sh, uint8_t* ring, const CUtenso
         const int r = 32 * q + lane;
         for (int j = 0; j < nblk; ++j) {
             const uint32_t gi = base + j;
-            const int buf = gi & 1;
+            const int buf = buf_of(gi);
             if (threadIdx.x == 128) {
                 bool have = false;
                 if (!sh->failed) {
-                    have = mbar_wait(&sh->accf[buf], (gi >> 1) & 1, limit_ns);
+                    have = mbar_wait(&sh->accf[buf], use_of(gi) & 1, limit_ns);
                     if (!have) sh->failed = 1;
                 }
                 sh->ep_ok = have ? 1 : 0;
@@ -371,6 +383,12 @@ __device__ inline bool tc_gemm_blocks(TcShared* sh, uint8_t* ring, const CUtenso
                 const int c0 = 32 * ch;
                 uint32_t v[32];
                 tmem_ld32(sh->tmem_base + ((uint32_t)(32 * q) << 16) + (uint32_t)(kBN * buf + c0), v);
+                if (!dbl) {
+                    uint32_t w[32];
+                    tmem_ld32(sh->tmem_base + ((uint32_t)(32 * q) << 16) + (uint32_t)(kBN + c0), w);
+#pragma unroll
+                    for (int jj = 0; jj < 32; ++jj) v[jj] = __float_as_uint(__uint_as_float(v[jj]) + __uint_as_float(w[jj]));
+                }
                 if (gr < m) {
                     // All 32 reads first (independent, in flight together), then
                     // the 32 writes: one memory round trip per chunk, not 32.

@@ -82,6 +82,13 @@ struct ttg_solver {
     // (L_ijᵀ at off[i + j·nb], ld bs[j]).
     DevBuf<double> inv64, linv64, lt64;
     DevBuf<float> inv32, linv32, lt32;
+    // Folded sweeps (FP32 factor): W_i = L_ii⁻¹·L_i,i-1 (forward) and
+    // L_ii⁻ᵀ·L_i+1,iᵀ (backward), compact at woff_f / woff_b (ld bs[i]).
+    DevBuf<float> wf32, wb32;
+    DevBuf<int64_t> d_woff_f, d_woff_b;
+    DevBuf<WdDesc> d_wdesc_f, d_wdesc_b;
+    int64_t wsize_f = 0, wsize_b = 0;
+    int n_wdesc_f = 0, n_wdesc_b = 0;
     int64_t dsize = 0;  // elements of the compact diagonal
     DevBuf<int64_t> d_doff;
     DevBuf<int> d_strip_pre, d_step_fwd, d_step_bwd;
@@ -161,12 +168,37 @@ static ttg_status solver_tables(ttg_solver* S, const int* bs, const int64_t* off
     }
     S->items_fwd = fwd[nb];
     S->items_bwd = bwd[nb];
+    // W products of the folded sweeps: forward W_i (i >= 1) = linv_i · L(i, i-1);
+    // backward W_i (i <= nb-2) = inv_i · L(i+1, i)ᵀ (the transposed tile at
+    // off[(i+1) + i·nb], ld bs[i]).
+    std::vector<int64_t> woff_f(nb, 0), woff_b(nb, 0);
+    std::vector<WdDesc> wdf, wdb;
+    int64_t wf = 0, wb = 0;
+    for (int i = 0; i < nb; ++i) {
+        if (i >= 1 && bs[i] > 0 && bs[i - 1] > 0) {
+            woff_f[i] = wf;
+            wdf.push_back({doff[i], off[i + (size_t)(i - 1) * nb], wf, bs[i], bs[i - 1], bs[i]});
+            wf += (int64_t)bs[i] * bs[i - 1];
+        }
+        if (i + 1 < nb && bs[i] > 0 && bs[i + 1] > 0) {
+            woff_b[i] = wb;
+            wdb.push_back({doff[i], off[(i + 1) + (size_t)i * nb], wb, bs[i], bs[i + 1], bs[i]});
+            wb += (int64_t)bs[i] * bs[i + 1];
+        }
+    }
+    S->wsize_f = wf;
+    S->wsize_b = wb;
+    S->n_wdesc_f = (int)wdf.size();
+    S->n_wdesc_b = (int)wdb.size();
     S->n_tdesc_off = (int)to.size();
     S->n_tdesc_diag = (int)td.size();
     ttg_status st;
     if ((st = S->d_doff.ensure(nb)) != TTG_OK || (st = S->d_strip_pre.ensure(nb + 1)) != TTG_OK ||
         (st = S->d_step_fwd.ensure(nb + 1)) != TTG_OK || (st = S->d_step_bwd.ensure(nb + 1)) != TTG_OK ||
-        (st = S->d_sweep_ctr.ensure(2 * (size_t)(2 + nb + S->n_strips))) != TTG_OK || (st = S->d_err.ensure(1)) != TTG_OK ||
+        (st = S->d_sweep_ctr.ensure(2 * (size_t)(2 + 2 * nb + S->n_strips))) != TTG_OK || (st = S->d_err.ensure(1)) != TTG_OK ||
+        (st = S->d_woff_f.ensure(nb)) != TTG_OK || (st = S->d_woff_b.ensure(nb)) != TTG_OK ||
+        (st = S->d_wdesc_f.ensure(std::max<size_t>(1, wdf.size()))) != TTG_OK ||
+        (st = S->d_wdesc_b.ensure(std::max<size_t>(1, wdb.size()))) != TTG_OK ||
         (st = S->d_tdesc_off.ensure(std::max<size_t>(1, to.size()))) != TTG_OK ||
         (st = S->d_tdesc_diag.ensure(td.size())) != TTG_OK || (st = S->d_tsub_off.ensure(so.size())) != TTG_OK ||
         (st = S->d_tsub_diag.ensure(sd.size())) != TTG_OK)
@@ -175,6 +207,10 @@ static ttg_status solver_tables(ttg_solver* S, const int* bs, const int64_t* off
     TTG_CUDA_CHECK(cudaMemcpy(S->d_strip_pre.p, sp.data(), sizeof(int) * (nb + 1), cudaMemcpyHostToDevice));
     TTG_CUDA_CHECK(cudaMemcpy(S->d_step_fwd.p, fwd.data(), sizeof(int) * (nb + 1), cudaMemcpyHostToDevice));
     TTG_CUDA_CHECK(cudaMemcpy(S->d_step_bwd.p, bwd.data(), sizeof(int) * (nb + 1), cudaMemcpyHostToDevice));
+    TTG_CUDA_CHECK(cudaMemcpy(S->d_woff_f.p, woff_f.data(), sizeof(int64_t) * nb, cudaMemcpyHostToDevice));
+    TTG_CUDA_CHECK(cudaMemcpy(S->d_woff_b.p, woff_b.data(), sizeof(int64_t) * nb, cudaMemcpyHostToDevice));
+    if (!wdf.empty()) TTG_CUDA_CHECK(cudaMemcpy(S->d_wdesc_f.p, wdf.data(), sizeof(WdDesc) * wdf.size(), cudaMemcpyHostToDevice));
+    if (!wdb.empty()) TTG_CUDA_CHECK(cudaMemcpy(S->d_wdesc_b.p, wdb.data(), sizeof(WdDesc) * wdb.size(), cudaMemcpyHostToDevice));
     if (!to.empty())
         TTG_CUDA_CHECK(cudaMemcpy(S->d_tdesc_off.p, to.data(), sizeof(TransposeDesc) * to.size(), cudaMemcpyHostToDevice));
     TTG_CUDA_CHECK(cudaMemcpy(S->d_tdesc_diag.p, td.data(), sizeof(TransposeDesc) * td.size(), cudaMemcpyHostToDevice));
@@ -233,7 +269,7 @@ void ttg_solver_destroy(ttg_solver* S) {
     for (auto* b : {&S->A64, &S->inv64, &S->linv64, &S->lt64, &S->B, &S->X, &S->R, &S->D, &S->W, &S->T1, &S->T2, &S->P, &S->Vd, &S->part, &S->colv,
                     &S->coefA, &S->coefB})
         b->release();
-    for (auto* b : {&S->A32, &S->A32lo, &S->Pf, &S->inv32, &S->linv32, &S->lt32, &S->f1, &S->f2, &S->f3, &S->Vf}) b->release();
+    for (auto* b : {&S->A32, &S->A32lo, &S->Pf, &S->wf32, &S->wb32, &S->inv32, &S->linv32, &S->lt32, &S->f1, &S->f2, &S->f3, &S->Vf}) b->release();
     S->d_off.release();
     S->d_bs.release();
     S->d_displ.release();
@@ -299,6 +335,20 @@ static ttg_status prepare_operands(ttg_solver* S, const TM* L, DevBuf<TM>& inv, 
         ttg_note_launch();
         transpose_tiles<TM><<<S->ctx->sms * 8, 256, 0, s>>>(S->d_tdesc_off.p, S->d_tsub_off.p, S->n_tdesc_off, L, lt.p);
     }
+    if constexpr (sizeof(TM) == 4) {
+        // Folded sweeps: the W products (FP32, 16 parts of 128×128 blocks each).
+        if ((st = S->wf32.ensure(std::max<int64_t>(1, S->wsize_f))) != TTG_OK ||
+            (st = S->wb32.ensure(std::max<int64_t>(1, S->wsize_b))) != TTG_OK)
+            return st;
+        if (S->n_wdesc_f > 0) {
+            ttg_note_launch();
+            wd_gemm_kernel<float><<<dim3(S->n_wdesc_f, 16), kThreads, smem, s>>>(S->d_wdesc_f.p, linv.p, L, S->wf32.p);
+        }
+        if (S->n_wdesc_b > 0) {
+            ttg_note_launch();
+            wd_gemm_kernel<float><<<dim3(S->n_wdesc_b, 16), kThreads, smem, s>>>(S->d_wdesc_b.p, inv.p, lt.p, S->wb32.p);
+        }
+    }
     TTG_CUDA_CHECK(cudaGetLastError());
     return TTG_OK;
 }
@@ -323,7 +373,7 @@ const char* sweep_trace_path() {
 template <class T, class TM>
 ttg_status sweeps(ttg_solver* S, const TM* L, const TM* LT, const TM* Linv, const TM* invT, T* R, T* Y, T* X, int nrhs, int grid,
                   cudaStream_t s) {
-    const size_t region = 2 + S->nb + S->n_strips;
+    const size_t region = 2 + 2 * S->nb + S->n_strips;
     TTG_CUDA_CHECK(cudaMemsetAsync(S->d_sweep_ctr.p, 0, sizeof(int) * 2 * region, s));
     SweepArgs a;
     a.off = S->d_off.p;
@@ -337,6 +387,14 @@ ttg_status sweeps(ttg_solver* S, const TM* L, const TM* LT, const TM* Linv, cons
     a.err = S->d_err.p;
     a.timeout_ns = (long long)(std::max(1.0, S->ctx->timeout_s) * 1e9);
     a.trace = nullptr;
+    // FP32 vectors with an FP32 factor sweep in the folded form.  The fold
+    // moves the cancellation of Vin_i against the previous row's update after
+    // the multiplication by L_ii⁻¹, which amplifies rounding by κ(L_ii): the
+    // double-float sweeps of the FP64 Krylov variant (used for ill-conditioned
+    // matrices) stay unfolded (α = 1e-8, N = 32768: 57 iterations unfolded,
+    // 150 folded).
+    constexpr bool fold = sizeof(TM) == 4 && sizeof(T) == 4;
+    a.fold = fold ? 1 : 0;
     const size_t n_trace = 4 * ((size_t)S->items_fwd + S->items_bwd);
     if (sweep_trace_path()) {
         ttg_status st = S->d_trace.ensure(n_trace);
@@ -348,16 +406,20 @@ ttg_status sweeps(ttg_solver* S, const TM* L, const TM* LT, const TM* Linv, cons
         a.claim = ctr;
         a.ready = ctr + 2;
         a.applied = ctr + 2 + S->nb;
+        a.zready = ctr + 2 + S->nb + S->n_strips;
+        a.woff = dir ? S->d_woff_b.p : S->d_woff_f.p;
         a.backward = dir;
         a.step_start = dir ? S->d_step_bwd.p : S->d_step_fwd.p;
         if (sweep_trace_path()) a.trace = S->d_trace.p + (dir ? 4 * (size_t)S->items_fwd : 0);
+        const TM* W = nullptr;
+        if constexpr (fold) W = dir ? S->wb32.p : S->wf32.p;
         if (dir == 0) {
             ttg_note_launch();
-            sweep_kernel<T, TM><<<grid, 256, smem, s>>>(a, L, Linv, R, Y);
+            sweep_kernel<T, TM><<<grid, 256, smem, s>>>(a, L, Linv, W, R, Y);
         }
         else {
             ttg_note_launch();
-            sweep_kernel<T, TM><<<grid, 256, smem, s>>>(a, LT, invT, Y, X);
+            sweep_kernel<T, TM><<<grid, 256, smem, s>>>(a, LT, invT, W, Y, X);
         }
         TTG_CUDA_CHECK(cudaGetLastError());
     }
