@@ -98,7 +98,10 @@ def test_split_bf16_factor_is_fp32_accurate(ctx, b, nb):
         p.close()
     assert errs[2] < 1e-5, errs
     assert errs[2] < errs[0] / 30, errs
-    assert errs[2] < 10 * errs[1], errs
+    # Measured 1.0×, 1.1×, 1.6× the FP32-update error for tiles 128, 256, 512;
+    # adding the small slice products onto the hi·hi accumulator (rather
+    # than into their own) costs enough accuracy to show here.
+    assert errs[2] < 2 * errs[1], errs
 
 
 def test_split_bf16_refines_an_ill_conditioned_system(ctx):
@@ -110,5 +113,20 @@ def test_split_bf16_refines_an_ill_conditioned_system(ctx):
     st, rep, X = p.solve_host(B, tol=BWD, max_outer=10, restart=30)
     assert st == t.TTG_OK, rep.as_dict()
     assert rep.remedy == 4
+    assert rep.bwd_err <= BWD and bwd_err(A, X, B) <= 2 * BWD
+    p.close()
+
+
+def test_split_bf16_preconditions_an_ill_conditioned_system(ctx):
+    """alpha = 1e-8 (cond ~ 1e9): FP64 Krylov GMRES-IR preconditioned by the
+    split-BF16 factor converges in few iterations (10 measured at N = 2048) —
+    a guard on the factor's accuracy, which sets the preconditioner quality."""
+    p = t.CholPlan(ctx, 256, 8, kind=2, matrix=1, alpha=1e-8, seed=2, precision=t.PREC_MIXED, mixed_kind=2)
+    A = p.input_A()
+    B = orc.normals(0, p.N * 4, 11, 1).reshape(p.N, 4, order="F")
+    st, rep, X = p.solve_host(B, tol=BWD, max_outer=12, restart=30, gmres_prec=64)
+    assert st == t.TTG_OK, rep.as_dict()
+    assert rep.remedy == 4
+    assert rep.inner <= 14, rep.as_dict()
     assert rep.bwd_err <= BWD and bwd_err(A, X, B) <= 2 * BWD
     p.close()
