@@ -379,8 +379,8 @@ def run_ours(args, world, rank, local):
                 "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
                              "frac": achieved / bf16_peak,
                              # ncu capture of one N=8192 factorisation (profiles/exec_kernel_mixed_cholesky_n8192_full.md):
-                             # 1.353 GB of DRAM traffic, scaled by the tile-update count (N^3) to this N.
-                             "traffic": 1.353e9 * (N / 8192.0) ** 3,
+                             # 1.413 GB of DRAM traffic, scaled by the tile-update count (N^3) to this N.
+                             "traffic": 1.413e9 * (N / 8192.0) ** 3,
                              "traffic_note": "bytes per launch, from an N=8192 ncu capture scaled by (N/8192)^3",
                              "kernel": "exec_kernel_mixed (launches of one factorisation, all remedy attempts); "
                                        "achieved = N^3/3 / their duration",
