@@ -41,6 +41,7 @@ struct System {
     bool factored = false;   // the tiles already hold the factor: solve only
     int ir_steps = 0;        // mixed: refinement rounds
     int nrhs = 1;
+    int potrf_parts = 0;     // blocks per diagonal POTRF (0: the executor's team rule)
     // Device arrays of the system.
     double* A64 = nullptr;   // FP64 input tiles (packed lower, full diagonal tiles)
     double* W64 = nullptr;   // FP64: factor tiles
