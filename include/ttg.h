@@ -72,8 +72,12 @@ enum {
     TTG_OP_GEADD = 6,     /* c[m×n] <- alpha a + beta c  (tile accumulation)          */
     TTG_OP_TRSM_RLNN = 7, /* c[m×n] <- alpha c · a⁻¹, a[n×n] lower non-unit (cblas_dtrsm R,L,N,N):
                              the backward step of a block solve with row-vector RHS */
-    TTG_OP_CONVERT = 8    /* c[m×n] <- alpha a + beta c with a and c of either precision:
+    TTG_OP_CONVERT = 8,   /* c[m×n] <- alpha a + beta c with a and c of either precision:
                              flags bit 0 = a is float, bit 1 = c is float (prec F64) */
+    TTG_OP_SPIN = 9       /* the block spins for alpha seconds (0 <= alpha <= 1): the
+                             task body of the scheduler micro-benchmarks
+                             (miniapp/mini_benchmarks/shared/ttor_wait.cpp, ttor_deps.cpp,
+                             spin_for_seconds in mini_benchmarks/common.hpp:21-28) */
 };
 
 /* Arithmetic of one task. */

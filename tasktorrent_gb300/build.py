@@ -26,7 +26,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp
 
 CU_SOURCES = ["ttg_exec.cu", "ttg_gen.cu", "ttg_mixed.cu", "ttg_solve.cu", "ttg_noalloc.cu", "ttg_batch.cu", "ttg_serve.cu"]
 CPP_SOURCES = ["apps.cpp"]
-MINIAPPS = ["2d_cholesky.cpp", "2d_gemm.cpp"]
+MINIAPPS = ["2d_cholesky.cpp", "2d_gemm.cpp", "ttor_wait.cpp", "ttor_deps.cpp"]
 
 
 def _run(cmd):

@@ -109,12 +109,15 @@ __device__ inline int wait_slot(const ExecParams& p, int* slot) {
 // Called by all lanes of warp 0.  Returns a claimed task id and its part
 // (*part, the same on all lanes), or -1 to exit.
 //
-// A level queue holds one slot per ready task.  The task at the head stays
-// there until its parts are handed out: a block takes a part with an atomic
-// increment of the task's part counter, and the block that takes the last
-// part (or finds none left) advances the head by compare-and-swap.  The
-// contended compare-and-swap thus runs once per task, not once per part.
-// A bound queue holds one slot per part.
+// Queues hold one slot per part of a ready task.  A level queue is a
+// counting semaphore over its slots: q_tail[lvl·32] reserves slots for the
+// producers, q_tail[lvl·32 + 1] counts the slots written and not yet claimed
+// ("available", raised after the writes), q_head[lvl·32] hands out slots.  A
+// claimer reserves with an atomic decrement of the available count (undone
+// when it was empty) and then takes the next slot with an atomic increment
+// of the head: two fetch-and-adds, no retried compare-and-swap, so claims do
+// not serialise on the head.  The part index comes from the task's part
+// counter.  A bound queue (one worker) is read in order.
 __device__ inline int claim_task(const ExecParams& p, int* part) {
     const int lane = threadIdx.x & 31;
     const int w = blockIdx.x;
@@ -146,40 +149,38 @@ __device__ inline int claim_task(const ExecParams& p, int* part) {
                 return task;
             }
         }
-        int hs[kLevelGroups], ts[kLevelGroups];
+        int av[kLevelGroups];
 #pragma unroll
         for (int g = 0; g < kLevelGroups; ++g) {
             const int l = g * 32 + lane;
-            hs[g] = ts[g] = 0;
-            if (l < p.n_levels) {
-                hs[g] = ld_volatile(p.q_head + l * 32);
-                ts[g] = ld_volatile(p.q_tail + l * 32);
-            }
+            av[g] = l < p.n_levels ? ld_volatile(p.q_tail + l * 32 + 1) : 0;
         }
         unsigned mask = 0;
-        int grp = 0, h = 0;
+        int grp = 0;
 #pragma unroll
         for (int g = kLevelGroups - 1; g >= 0; --g) {
-            const unsigned m = __ballot_sync(0xffffffffu, g * 32 + lane < p.n_levels && hs[g] < ts[g]);
+            const unsigned m = __ballot_sync(0xffffffffu, g * 32 + lane < p.n_levels && av[g] > 0);
             if (m) {
                 mask = m;
                 grp = g;
-                h = hs[g];
             }
         }
         if (mask) {
             const int lvl = grp * 32 + __ffs(mask) - 1;
             int got = -1, pt = 0;
             if (lane == (lvl & 31)) {
-                // Slot h is reserved (h < tail); its producer may still be writing it.
-                const int t = wait_slot(p, p.qbuf + p.q_off[lvl] + h);
-                if (t < 0) {
-                    got = -2;
+                if (atomicSub(p.q_tail + lvl * 32 + 1, 1) > 0) {
+                    // Reserved: slot k exists; its producer may still be writing it.
+                    const int k = atomicAdd(p.q_head + lvl * 32, 1);
+                    const int t = wait_slot(p, p.qbuf + p.q_off[lvl] + k);
+                    if (t < 0) {
+                        got = -2;
+                    } else {
+                        pt = atomicAdd(p.part_next + t, 1);
+                        got = t;
+                    }
                 } else {
-                    pt = atomicAdd(p.part_next + t, 1);
-                    const int P = p.parts[t];
-                    if (pt < P) got = t;
-                    if (pt >= P - 1) atomicCAS(p.q_head + lvl * 32, h, h + 1);
+                    atomicAdd(p.q_tail + lvl * 32 + 1, 1);  // it was empty: undo
                 }
             }
             got = __shfl_sync(0xffffffffu, got, lvl & 31);
@@ -189,7 +190,7 @@ __device__ inline int claim_task(const ExecParams& p, int* part) {
                 __threadfence();
                 return got;
             }
-            continue;  // the head task had no part left; rescan at once
+            continue;  // lost the race for the last slots; rescan at once
         }
         int d = 0, e = 0;
         if (lane == 0) {
@@ -220,8 +221,7 @@ __device__ __forceinline__ void push_ready(const ExecParams& p, int s) {
     // counter at one pushes), so a queue never outgrows the number of tasks
     // assigned to it; the bound checks below only guard against a corrupted
     // graph.
-    // In a bound queue a task of P parts takes P consecutive slots, one per
-    // part; in a level queue it takes one slot.
+    // A task of P parts takes P consecutive slots, one per part.
     if (b >= 0) {
         const int w = b % p.n_workers;
         const int slot = atomicAdd(p.bq_tail + w, P);
@@ -231,11 +231,12 @@ __device__ __forceinline__ void push_ready(const ExecParams& p, int s) {
             set_error(p, TTG_EOVERCOUNT, s, 0);
         }
     } else {
-        // One slot per task: its parts are handed out at the head.
         const int lvl = p.level[s];
-        const int slot = atomicAdd(p.q_tail + lvl * 32, 1);
-        if (p.q_off[lvl] + slot + 1 <= p.q_off[lvl + 1]) {
-            st_volatile(p.qbuf + p.q_off[lvl] + slot, s);
+        const int slot = atomicAdd(p.q_tail + lvl * 32, P);
+        if (p.q_off[lvl] + slot + P <= p.q_off[lvl + 1]) {
+            for (int q = 0; q < P; ++q) st_volatile(p.qbuf + p.q_off[lvl] + slot + q, s);
+            __threadfence();
+            atomicAdd(p.q_tail + lvl * 32 + 1, P);  // available once written
         } else {
             set_error(p, TTG_EOVERCOUNT, s, 0);
         }

@@ -11,6 +11,22 @@ namespace ttg {
 // Shared memory (doubles) the plain tile kernels need.
 constexpr int kPlainSmemDoubles = kF64SmemDoubles > kSmallSmem ? kF64SmemDoubles : kSmallSmem;
 
+// TTG_OP_SPIN: the block is busy for `seconds` of the global timer (thread 0
+// spins, the others wait at the barrier).  The host accepts 0 <= seconds <= 1.
+__device__ inline void spin_block(double seconds) {
+    if (threadIdx.x == 0) {
+        long long t0;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+        const long long ns = (long long)(seconds * 1e9);
+        for (;;) {
+            long long t;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+            if (t - t0 >= ns) break;
+        }
+    }
+    __syncthreads();
+}
+
 // Returns 0.  POTRF (FP64 only) is run by the caller.
 template <class T>
 __device__ int run_op_plain(const ttg_op& op, int part, int parts, T* smem) {
@@ -50,6 +66,9 @@ __device__ int run_op_plain(const ttg_op& op, int part, int parts, T* smem) {
             return 0;
         case TTG_OP_CONVERT:
             convert_tile(op.m, op.n, op.alpha, op.a, op.lda, op.beta, op.c, op.ldc, op.flags, part, parts);
+            return 0;
+        case TTG_OP_SPIN:
+            spin_block(op.alpha);
             return 0;
         default:
             return 0;

@@ -347,6 +347,8 @@ static double task_cost_us(const ttg_op& op) {
             flops = m * n;
             rate = 5.0e4;
             break;
+        case TTG_OP_SPIN:
+            return 2.0 + op.alpha * 1e6;
         default:
             break;
     }
@@ -437,7 +439,8 @@ extern "C" ttg_status ttg_graph_upload(ttg_ctx* c, const ttg_graph_desc* gd) {
     for (int t = 0; t < n; ++t) {
         if (gd->init_count[t] < 0 || gd->succ_ptr[t] > gd->succ_ptr[t + 1]) return TTG_EINVAL;
         const int k = gd->ops[t].kind;
-        if (k < TTG_OP_NOP || k > TTG_OP_CONVERT) return TTG_EINVAL;
+        if (k < TTG_OP_NOP || k > TTG_OP_SPIN) return TTG_EINVAL;
+        if (k == TTG_OP_SPIN && !(gd->ops[t].alpha >= 0.0 && gd->ops[t].alpha <= 1.0)) return TTG_EINVAL;
         if (gd->ops[t].prec != TTG_PREC_F64 && gd->ops[t].prec != TTG_PREC_MIXED) return TTG_EINVAL;
     }
     if (n > 0 && gd->succ_ptr[0] != 0) return TTG_EINVAL;
@@ -500,7 +503,7 @@ extern "C" ttg_status ttg_graph_upload(ttg_ctx* c, const ttg_graph_desc* gd) {
     for (int t = 0; t < n; ++t) {
         if (!runnable[t]) continue;
         if (bind[t] >= 0) bqcount[bind[t] % W] += parts[t];  // one slot per part
-        else qcount[level[t]] += 1;                           // one slot per task
+        else qcount[level[t]] += parts[t];
     }
     std::vector<int> q_off(kMaxLevels + 1, 0), bq_off(W + 1, 0);
     for (int l = 0; l < kMaxLevels; ++l) q_off[l + 1] = q_off[l] + qcount[l];
@@ -516,9 +519,11 @@ extern "C" ttg_status ttg_graph_upload(ttg_ctx* c, const ttg_graph_desc* gd) {
             for (int q = 0; q < parts[t]; ++q) bqinit[bq_off[w] + btail0[w]++] = t;
         } else {
             const int l = level[t];
-            qinit[q_off[l] + tail0[l * 32]++] = t;
+            for (int q = 0; q < parts[t]; ++q) qinit[q_off[l] + tail0[l * 32]++] = t;
         }
     }
+    // Available slots of each level at launch: all the initial ones.
+    for (int l = 0; l < kMaxLevels; ++l) tail0[l * 32 + 1] = tail0[l * 32];
 
     DevGraph& g = c->g;
     g.n_tasks = n;

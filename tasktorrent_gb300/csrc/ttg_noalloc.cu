@@ -252,8 +252,7 @@ extern "C" ttg_status ttg_run_graph_noalloc(int device, const ttg_graph_desc* gd
     int n_levels = 1;
     levels_static(n, gd->priority, &n_levels);
 
-    // Queue layout: level queues (one slot per task) then bound queues (one
-    // slot per part).
+    // Queue layout: level queues then bound queues, one slot per part.
     long q_total = 0;
     for (int l = 0; l < ttg::kMaxLevels; ++l) h_qfill[l] = 0;
     for (int w = 0; w < W; ++w) h_bqfill[w] = 0;
@@ -263,7 +262,7 @@ extern "C" ttg_status ttg_run_graph_noalloc(int device, const ttg_graph_desc* gd
         h_bind[t] = (gd->bind && gd->bind[t] >= 0) ? gd->bind[t] : -1;
         h_count[t] = gd->init_count[t];
         if (!h_runnable[t]) continue;
-        const int slots = h_bind[t] >= 0 ? h_parts[t] : 1;
+        const int slots = h_parts[t];
         if (h_bind[t] >= 0) h_bqfill[h_bind[t] % W] += slots;
         else h_qfill[h_level[t]] += slots;
         q_total += slots;
@@ -284,9 +283,10 @@ extern "C" ttg_status ttg_run_graph_noalloc(int device, const ttg_graph_desc* gd
             for (int q = 0; q < h_parts[t]; ++q) h_qbuf[q_levels + h_bqoff[w] + h_bqtail[w]++] = t;
         } else {
             const int l = h_level[t];
-            h_qbuf[h_qoff[l] + h_qtail[l * 32]++] = t;
+            for (int q = 0; q < h_parts[t]; ++q) h_qbuf[h_qoff[l] + h_qtail[l * 32]++] = t;
         }
     }
+    for (int l = 0; l < ttg::kMaxLevels; ++l) h_qtail[l * 32 + 1] = h_qtail[l * 32];  // available at launch
     std::memset(&h_status, 0, sizeof(h_status));
     h_status.start = ~0ULL;
 

@@ -41,6 +41,16 @@ inline ttg_op make_op(int kind) {
     return op;
 }
 
+// spin_for_seconds(t): the task keeps its block busy for t seconds — the body
+// of the reference's scheduler micro-benchmarks (mini_benchmarks/common.hpp:21-28
+// spins a host thread).  0 <= t <= 1.
+inline void spin_for_seconds(double seconds) {
+    if (!(seconds >= 0.0 && seconds <= 1.0)) throw std::invalid_argument("ttor::gpu::spin_for_seconds: 0 <= seconds <= 1");
+    ttg_op op = make_op(TTG_OP_SPIN);
+    op.alpha = seconds;
+    record(op);
+}
+
 // LAPACKE_dpotrf(LAPACK_COL_MAJOR, 'L', n, A, lda): in-place lower Cholesky.
 // Returns 0; a failing pivot is reported by the executor (TTG_ENOTPD with the
 // column in ttg_report::info) after join().
