@@ -576,20 +576,6 @@ __global__ void invert_diag_tiles(TileLayout lay, const int64_t* doff, const TM*
     trsm_rltn_tile<TM>(b, b, TM(1), Ljj, b, T, b, reinterpret_cast<TM*>(smem_inv), p, parts);
 }
 
-// Dense N×N column-major symmetric matrix from packed lower tiles (both
-// triangles), converted to TD.  rowblk[r] is the block row of row r.
-template <class TS, class TD>
-__global__ void dense_from_tiles(TileLayout lay, const int* __restrict__ rowblk, const TS* tiles, TD* A) {
-    const int N = lay.N;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)N * N; e += (int64_t)gridDim.x * blockDim.x) {
-        const int r = (int)(e % N), c = (int)(e / N);
-        const int gi = r >= c ? r : c, gj = r >= c ? c : r;  // lower-triangle element (gi >= gj)
-        const int bi = rowblk[gi], bj = rowblk[gj];
-        const int li = gi - lay.displ[bi], lj = gj - lay.displ[bj];
-        A[e] = (TD)tiles[lay.off[bi + (size_t)bj * lay.nb] + li + (int64_t)lj * lay.bs[bi]];
-    }
-}
-
 // Y = A X (mode 0) or Y = B - A X (mode 2) for dense column-major A (N×N),
 // X, B, Y N × nrhs.  Grid (row blocks of 128, K splits); partial sums of the
 // K splits go to P[split] and are added by reduce_partials in a fixed order.
@@ -730,19 +716,24 @@ __global__ void __launch_bounds__(256, 2) dense_matmul_f32_partial(int N, const 
 }
 
 // Y = A X partials in double-float arithmetic: A = Ah + Al (two FP32
-// copies, Al = fl32(A - Ah)), X FP64 (split per staged chunk); the same grid
-// and partial layout as dense_matmul_partial<double>.
-__global__ void dense_matmul_df_partial(int N, const float* __restrict__ Ah, const float* __restrict__ Al,
-                                        const double* __restrict__ X, int nrhs, double* P, int splits) {
+// copies, Al = fl32(A - Ah)), X FP64 (split per staged chunk).  Grid (row
+// blocks of 256, K splits); thread t takes rows 256·bx + (t & 127) and that
+// + 128 for the right-hand sides 8·(t >> 7) .. +7, so each staged x pair
+// (read as float4) serves two rows.  Partial sums of split y go to
+// P[y·N·nrhs + ...] and are added by reduce_partials in a fixed order.
+__global__ void __launch_bounds__(256) dense_matmul_df_partial(int N, const float* __restrict__ Ah, const float* __restrict__ Al,
+                                                               const double* __restrict__ X, int nrhs, double* P, int splits) {
+    constexpr int H = kMaxRhs / 2;
     __shared__ __align__(16) float sXh[128 * kMaxRhs], sXl[128 * kMaxRhs];
     const int rb = blockIdx.x, sp = blockIdx.y;
-    const int r = rb * 128 + (threadIdx.x & 127);
-    const int half = threadIdx.x >> 7;  // two threads per row: rhs halves
+    const int half = threadIdx.x >> 7;
+    const int ra = rb * 256 + (threadIdx.x & 127), rbw = ra + 128;
+    const bool oka = ra < N, okb = rbw < N;
     const int kper = (N + splits - 1) / splits;
-    const int k0 = sp * kper, k1 = min(N, k0 + kper);
-    float sh[kMaxRhs / 2], sl[kMaxRhs / 2];
+    const int k0 = min(N, sp * kper), k1 = min(N, k0 + kper);
+    float ha[H], la[H], hb[H], lb[H];
 #pragma unroll
-    for (int q = 0; q < kMaxRhs / 2; ++q) sh[q] = sl[q] = 0.0f;
+    for (int q = 0; q < H; ++q) ha[q] = la[q] = hb[q] = lb[q] = 0.0f;
     for (int c0 = k0; c0 < k1; c0 += 128) {
         const int kc = min(128, k1 - c0);
         __syncthreads();
@@ -754,23 +745,37 @@ __global__ void dense_matmul_df_partial(int N, const float* __restrict__ Ah, con
             sXl[c * kMaxRhs + q] = lo;
         }
         __syncthreads();
-        if (r < N) {
-            for (int c = 0; c < kc; ++c) {
-                const float ah = Ah[r + (size_t)(c0 + c) * N], al = Al[r + (size_t)(c0 + c) * N];
-                const float* xh = sXh + c * kMaxRhs + half * (kMaxRhs / 2);
-                const float* xl = sXl + c * kMaxRhs + half * (kMaxRhs / 2);
+#pragma unroll 2
+        for (int c = 0; c < kc; ++c) {
+            const size_t col = (size_t)(c0 + c) * N;
+            const float aah = oka ? Ah[ra + col] : 0.0f, aal = oka ? Al[ra + col] : 0.0f;
+            const float abh = okb ? Ah[rbw + col] : 0.0f, abl = okb ? Al[rbw + col] : 0.0f;
+            const float4* xh4 = reinterpret_cast<const float4*>(sXh + c * kMaxRhs + half * H);
+            const float4* xl4 = reinterpret_cast<const float4*>(sXl + c * kMaxRhs + half * H);
 #pragma unroll
-                for (int q = 0; q < kMaxRhs / 2; ++q) df_fma(ah, al, xh[q], xl[q], sh[q], sl[q]);
+            for (int v = 0; v < H / 4; ++v) {
+                const float4 xh = xh4[v], xl = xl4[v];
+                const float xhs[4] = {xh.x, xh.y, xh.z, xh.w}, xls[4] = {xl.x, xl.y, xl.z, xl.w};
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int q = 4 * v + j;
+                    df_fma(aah, aal, xhs[j], xls[j], ha[q], la[q]);
+                    df_fma(abh, abl, xhs[j], xls[j], hb[q], lb[q]);
+                }
             }
+        }
 #pragma unroll
-            for (int q = 0; q < kMaxRhs / 2; ++q) df_renorm(sh[q], sl[q]);
+        for (int q = 0; q < H; ++q) {
+            df_renorm(ha[q], la[q]);
+            df_renorm(hb[q], lb[q]);
         }
     }
-    if (r < N) {
 #pragma unroll
-        for (int q = 0; q < kMaxRhs / 2; ++q) {
-            const int qq = half * (kMaxRhs / 2) + q;
-            if (qq < nrhs) P[(size_t)sp * N * nrhs + r + (size_t)qq * N] = (double)sh[q] + (double)sl[q];
+    for (int q = 0; q < H; ++q) {
+        const int qq = half * H + q;
+        if (qq < nrhs) {
+            if (oka) P[(size_t)sp * N * nrhs + ra + (size_t)qq * N] = (double)ha[q] + (double)la[q];
+            if (okb) P[(size_t)sp * N * nrhs + rbw + (size_t)qq * N] = (double)hb[q] + (double)lb[q];
         }
     }
 }
@@ -835,13 +840,102 @@ __global__ void column_axpby(int N, int nrhs, const double* a, const TX* X, cons
     }
 }
 
-// ‖A‖∞ of the symmetric matrix (max absolute row sum) from the dense copy.
-template <class T>
-__global__ void row_abs_sums(int N, const T* A, double* rowsum) {
+// ‖A‖∞: rowsum[r] = Σ_y part[y·N + r], added in order (the same value on
+// every run).
+__global__ void row_abs_final(int N, int splits, const double* __restrict__ part, double* rowsum) {
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < N; r += gridDim.x * blockDim.x) {
         double s = 0.0;
-        for (int c = 0; c < N; ++c) s += fabs((double)A[r + (size_t)c * N]);
+        for (int y = 0; y < splits; ++y) s += part[(size_t)y * N + r];
         rowsum[r] = s;
+    }
+}
+
+// Dense N×N copies of the symmetric matrix held as packed lower tiles: FP64
+// (A64), and when set its FP32 rounding (A32) and the FP32 rounding of the
+// remainder (A32lo = fl32(A - A32), the low half of the double-float form),
+// with the row sums of |A| by 64-column block: Q[j·N + r] = Σ_{c in block j}
+// |A(r, c)|, each written once.  Work unit: a 64×64 sub-block of the lower
+// triangle, read once with coalesced column segments (16 loads in flight per
+// thread), written in place and, through a shared-memory transpose, at the
+// mirrored position.  Block 64×4 threads; sub-block sb = R(R+1)/2 + C, R >= C.
+constexpr int kDenseSb = 64;
+__global__ void __launch_bounds__(256) dense_sym_from_tiles(TileLayout lay, const int* __restrict__ rowblk,
+                                                            const double* __restrict__ tiles, double* __restrict__ A64,
+                                                            float* __restrict__ A32, float* __restrict__ A32lo, double* __restrict__ Q) {
+    constexpr int E = kDenseSb, K = E / 4;
+    __shared__ double T[E][E + 1];   // T[a][b] = A(r0 + b, c0 + a)
+    __shared__ double red[2][4][E];  // per-thread partial row sums: in place, mirrored
+    const int N = lay.N;
+    const int nsb = (N + E - 1) / E;
+    const int64_t total = (int64_t)nsb * (nsb + 1) / 2;
+    const int tx = threadIdx.x & (E - 1), ty = threadIdx.x / E;
+    auto lower = [&](int gi, int gj) {  // element (gi, gj), gi >= gj, of the tiles
+        const int bi = rowblk[gi], bj = rowblk[gj];
+        return tiles[lay.off[bi + (size_t)bj * lay.nb] + (gi - lay.displ[bi]) + (int64_t)(gj - lay.displ[bj]) * lay.bs[bi]];
+    };
+    auto put = [&](size_t e, double v) {
+        A64[e] = v;
+        if (A32) {
+            const float h = __double2float_rn(v);
+            A32[e] = h;
+            if (A32lo) A32lo[e] = __double2float_rn(v - (double)h);
+        }
+    };
+    for (int64_t sb = blockIdx.x; sb < total; sb += gridDim.x) {
+        int R = (int)((sqrt(8.0 * (double)sb + 1.0) - 1.0) * 0.5);
+        while ((int64_t)R * (R + 1) / 2 > sb) --R;
+        while ((int64_t)(R + 1) * (R + 2) / 2 <= sb) ++R;
+        const int C = (int)(sb - (int64_t)R * (R + 1) / 2);
+        const int r0 = E * R, c0 = E * C;
+        // A sub-block inside one tile (the usual case) reads it with one base
+        // offset and the tile's leading dimension.
+        const int bi = rowblk[r0], bj = rowblk[c0];
+        const bool one_tile = bi == rowblk[min(r0 + E - 1, N - 1)] && bj == rowblk[min(c0 + E - 1, N - 1)];
+        const int ld = lay.bs[bi];
+        const double* base = tiles + lay.off[bi + (size_t)bj * lay.nb] + (r0 - lay.displ[bi]) + (int64_t)(c0 - lay.displ[bj]) * ld;
+        const int r = r0 + tx;
+        double v[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int yy = ty + 4 * k, c = c0 + yy;
+            v[k] = 0.0;
+            if (r < N && c < N) {
+                if (one_tile) v[k] = r >= c ? base[tx + (int64_t)yy * ld] : base[yy + (int64_t)tx * ld];
+                else v[k] = r >= c ? lower(r, c) : lower(c, r);
+            }
+        }
+        double pin = 0.0;
+#pragma unroll
+        for (int k = 0; k < K; ++k) pin += fabs(v[k]);
+        __syncthreads();  // the previous sub-block's reads of T and red are done
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int yy = ty + 4 * k, c = c0 + yy;
+            if (r < N && c < N) put(r + (size_t)c * N, v[k]);
+            T[yy][tx] = v[k];
+        }
+        red[0][ty][tx] = pin;
+        if (R != C) {  // a diagonal sub-block covered both triangles
+            __syncthreads();
+            double pm = 0.0;
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const int yy = ty + 4 * k;
+                const int rr = c0 + tx, cc = r0 + yy;  // mirrored element (c0 + tx, r0 + yy) = T[tx][yy]
+                const double w = T[tx][yy];
+                pm += fabs(w);
+                if (rr < N && cc < N) put(rr + (size_t)cc * N, w);
+            }
+            red[1][ty][tx] = pm;
+        }
+        __syncthreads();
+        if (Q) {
+            const int m = threadIdx.x / E;  // 0: rows r0.. (column block C), 1: rows c0.. (column block R)
+            if (m == 0 && r0 + tx < N)
+                Q[(size_t)C * N + r0 + tx] = ((red[0][0][tx] + red[0][1][tx]) + red[0][2][tx]) + red[0][3][tx];
+            else if (m == 1 && R != C && c0 + tx < N)
+                Q[(size_t)R * N + c0 + tx] = ((red[1][0][tx] + red[1][1][tx]) + red[1][2][tx]) + red[1][3][tx];
+        }
     }
 }
 
