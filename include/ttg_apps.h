@@ -62,7 +62,8 @@ ttg_status ttg_chol_plan_set_matrix(ttg_chol_plan* plan, const double* h_A, void
 
 /* Restore the working tiles from the pristine input (device copy). */
 ttg_status ttg_chol_plan_restore(ttg_chol_plan* plan, void* stream);
-/* Run the captured task graph once on the working tiles (no restore). */
+/* Run the captured task graph once: an FP64 plan on the working tiles (no
+ * restore), a mixed plan on the pristine input (converted to FP32). */
 ttg_status ttg_chol_plan_factor(ttg_chol_plan* plan, void* stream, ttg_report* rep);
 
 /* End-to-end: host matrix in (pinned or pageable), factor, host factor out.
@@ -85,7 +86,9 @@ ttg_status ttg_chol_plan_get_factor(ttg_chol_plan* plan, double* h_L);
 /* The input as a dense N×N column-major symmetric host array. */
 ttg_status ttg_chol_plan_get_input(ttg_chol_plan* plan, double* h_A);
 
-/* Device pointers of the working tiles (lower, packed) and their offsets. */
+/* Device pointers of the working tiles (lower, packed) and their offsets.
+ * An FP64 plan factors these tiles in place; a mixed plan factors its input
+ * (ttg_chol_plan_set_matrix / _generate) and uses them as FP64 scratch. */
 double* ttg_chol_plan_tiles(ttg_chol_plan* plan, const int64_t** h_off);
 
 /* DAG record of the last run in the oracle's CSV format. */

@@ -423,8 +423,9 @@ static ttg_status chol_factor_from(ttg_chol_plan* P, void* stream, ttg_report* r
     // tensor-core updates (FP32-level accuracy), then FP32 updates, then FP32
     // updates on A + 16·2^-24·diag(A), and last BF16 updates on A +
     // 8·2^-8·diag(A).  A shifted factor only preconditions: refinement always
-    // solves the unshifted system.  Retries start from the restored input (a
-    // failed run overwrote it).
+    // solves the unshifted system.  Every attempt converts the plan's input
+    // (pristine) afresh; the FP64 working tiles are only the diagonal POTRF's
+    // scratch, so they need no restore.
     const bool tc = ttg_mixed_has_tc(P->mixed);
     const bool first_x3 = P->args.mixed_kind == 2;
     struct Attempt {
@@ -443,11 +444,7 @@ static ttg_status chol_factor_from(ttg_chol_plan* P, void* stream, ttg_report* r
     ttg_status s = TTG_OK;
     float total_ms = 0.f;
     for (size_t a = std::min(first_attempt, plan.size() - 1); a < plan.size(); ++a) {
-        if (a > first_attempt) {
-            s = ttg_chol_plan_restore(P, stream);
-            if (s != TTG_OK) return s;
-        }
-        s = ttg_mixed_prepare(P->mixed, stream, plan[a].shift, plan[a].upd);
+        s = ttg_mixed_prepare(P->mixed, stream, plan[a].shift, plan[a].upd, P->pristine);
         if (s != TTG_OK) return s;
         s = plan[a].tp->replay(stream);
         const ttg_report r = plan[a].tp->report();
@@ -469,12 +466,15 @@ extern "C" ttg_status ttg_chol_factor_host(ttg_chol_plan* P, const double* h_A, 
     if (!P || !h_A) return TTG_EINVAL;
     TTG_CUDA_CHECK(cudaSetDevice(P->ctx->device));
     cudaStream_t s = (cudaStream_t)stream;
-    ttg_status st = dense_to_tiles(P, h_A, P->tiles, s);
+    // The FP64 path factors the working tiles in place; the mixed path
+    // factors the plan's input.
+    ttg_status st = dense_to_tiles(P, h_A, P->mixed ? P->pristine : P->tiles, s);
     if (st != TTG_OK) return st;
+    if (P->mixed && P->solver) ttg_solver_input_changed(P->solver);
     st = ttg_chol_plan_factor(P, stream, rep);
     if (st != TTG_OK) return st;
     if (h_L) {
-        st = tiles_to_dense(P, P->tiles, h_L, s);
+        st = tiles_to_dense(P, P->mixed ? ttg_mixed_factor_tiles(P->mixed) : P->tiles, h_L, s);
         if (st != TTG_OK) return st;
         TTG_CUDA_CHECK(cudaStreamSynchronize(s));
         for (int j = 0; j < P->N; ++j) std::fill(h_L + (size_t)j * P->N, h_L + (size_t)j * P->N + j, 0.0);
@@ -497,11 +497,11 @@ extern "C" ttg_status ttg_chol_factor_host_tiles(ttg_chol_plan* P, const double*
     if (!P || !h_in) return TTG_EINVAL;
     TTG_CUDA_CHECK(cudaSetDevice(P->ctx->device));
     cudaStream_t s = (cudaStream_t)stream;
-    // The input becomes the plan's input (a mixed factorisation may restart
-    // from it), then the working tiles are restored from it and factored.
+    // The input becomes the plan's input (the mixed factorisation converts it
+    // directly), then the FP64 working tiles are restored from it and factored.
     TTG_CUDA_CHECK(cudaMemcpyAsync(P->pristine, h_in, sizeof(double) * P->elems, cudaMemcpyHostToDevice, s));
     if (P->solver) ttg_solver_input_changed(P->solver);
-    ttg_status st = ttg_chol_plan_restore(P, stream);
+    ttg_status st = P->mixed ? TTG_OK : ttg_chol_plan_restore(P, stream);
     if (st != TTG_OK) return st;
     st = ttg_chol_plan_factor(P, stream, rep);
     if (st != TTG_OK) return st;
@@ -570,7 +570,9 @@ extern "C" ttg_status ttg_chol_plan_solve(ttg_chol_plan* P, const double* d_B, d
 extern "C" ttg_status ttg_chol_posv(ttg_chol_plan* P, const double* d_B, double* d_X, const ttg_solve_opts* o,
                                    ttg_solve_report* rep, void* stream) {
     if (!P || !o) return TTG_EINVAL;
-    ttg_status st = ttg_chol_plan_restore(P, stream);
+    // The FP64 path factors the working tiles in place: restore them from the
+    // input.  The mixed path converts the input itself.
+    ttg_status st = P->mixed ? TTG_OK : ttg_chol_plan_restore(P, stream);
     if (st != TTG_OK) return st;
     ttg_report fr{};
     st = ttg_chol_plan_factor(P, stream, &fr);

@@ -780,10 +780,39 @@ __global__ void __launch_bounds__(256) dense_matmul_df_partial(int N, const floa
     }
 }
 
+// h = fl32(v) and l = fl32(v - h) (round to nearest even), bit for bit those
+// of the FP64 formula, from integer operations on v's bits for 2^-60 <= |v|
+// < 2^101: on this GPU FP64 arithmetic and conversions from FP64 run at the
+// FP64 rate, 1/64 of the FP32 one.  The remainder v - h is the low 29
+// mantissa bits (rounded down) or their complement to the next unit of h
+// (rounded up), an integer times 2^(e-52), which the FP32 conversion rounds
+// to nearest and an exact power-of-two scale places.  Other values (zero,
+// tiny, huge, non-finite) take the FP64 formula.
+__device__ __forceinline__ void split_f64_f32(double v, float& h, float& l) {
+    const unsigned hiw = (unsigned)__double2hiint(v), low = (unsigned)__double2loint(v);
+    const unsigned sign = hiw >> 31;
+    const int ex = (int)((hiw >> 20) & 0x7FFu) - 1023;
+    if (ex < -60 || ex > 100) {
+        h = __double2float_rn(v);
+        l = __double2float_rn(v - (double)h);
+        return;
+    }
+    const unsigned top = ((hiw & 0xFFFFFu) << 3) | (low >> 29);  // 23 mantissa bits of h before rounding
+    const unsigned rem = low & 0x1FFFFFFFu;                       // the 29 bits below them
+    const unsigned up = (rem > (1u << 28) || (rem == (1u << 28) && (top & 1u))) ? 1u : 0u;
+    h = __uint_as_float(((sign << 31) | ((unsigned)(ex + 127) << 23) | top) + up);  // a carry moves to the exponent
+    const unsigned rm = up ? (1u << 29) - rem : rem;
+    const float lv = __fmul_rn(__uint2float_rn(rm), __uint_as_float((unsigned)(ex + 1023 - 948) << 23));  // rm · 2^(e-52)
+    l = rm == 0 ? 0.0f : ((sign ^ up) ? -lv : lv);
+}
+
 // Al = fl32(A - Ah): the low FP32 half of the dense copy.
-__global__ void split_low_half(int64_t n, const double* __restrict__ A, const float* __restrict__ Ah, float* __restrict__ Al) {
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
-        Al[e] = __double2float_rn(A[e] - (double)Ah[e]);
+__global__ void split_low_half(int64_t n, const double* __restrict__ A, float* __restrict__ Al) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+        float h, l;
+        split_f64_f32(A[e], h, l);
+        Al[e] = l;
+    }
 }
 
 template <class T>
@@ -876,9 +905,10 @@ __global__ void __launch_bounds__(256) dense_sym_from_tiles(TileLayout lay, cons
     auto put = [&](size_t e, double v) {
         A64[e] = v;
         if (A32) {
-            const float h = __double2float_rn(v);
+            float h, l;
+            split_f64_f32(v, h, l);
             A32[e] = h;
-            if (A32lo) A32lo[e] = __double2float_rn(v - (double)h);
+            if (A32lo) A32lo[e] = l;
         }
     };
     for (int64_t sb = blockIdx.x; sb < total; sb += gridDim.x) {

@@ -603,11 +603,12 @@ ttg_op ttg_mixed_update_op(ttg_mixed_state* m, int k, int i, int j, int upd) {
     return op;
 }
 
-ttg_status ttg_mixed_prepare(ttg_mixed_state* m, void* stream, double shift, int upd) {
+ttg_status ttg_mixed_prepare(ttg_mixed_state* m, void* stream, double shift, int upd, const double* src) {
     const bool tc = upd != TTG_UPD_FP32;
     cudaStream_t s = (cudaStream_t)stream;
+    if (!src) return TTG_EINVAL;
     ttg_note_launch();
-    convert_f64_to_f32<<<m->ctx->sms * 8, 256, 0, s>>>(m->tiles64, m->w32, m->elems);
+    convert_f64_to_f32<<<m->ctx->sms * 8, 256, 0, s>>>(src, m->w32, m->elems);
     TTG_CUDA_CHECK(cudaGetLastError());
     if (shift > 0) {
         for (int j = 0; j < m->nb; ++j) {
@@ -620,7 +621,7 @@ ttg_status ttg_mixed_prepare(ttg_mixed_state* m, void* stream, double shift, int
     MixedCtx* mc = (MixedCtx*)m->ctx->mixed;
     if (m->kind == 0 && tc) {
         ttg_note_launch();
-        block_row_scales<<<m->nb, 256, 0, s>>>(m->tiles64, m->diag_off, m->b, m->nb, m->rowscale);
+        block_row_scales<<<m->nb, 256, 0, s>>>(src, m->diag_off, m->b, m->nb, m->rowscale);
         TTG_CUDA_CHECK(cudaGetLastError());
         mc->globals = m->globals;
     } else {

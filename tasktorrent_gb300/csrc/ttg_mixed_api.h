@@ -29,10 +29,11 @@ bool ttg_mixed_has_tc(const ttg_mixed_state* m);
 ttg_op ttg_mixed_potrf_op(ttg_mixed_state* m, int j, int upd);
 ttg_op ttg_mixed_trsm_op(ttg_mixed_state* m, int i, int j, int upd);
 ttg_op ttg_mixed_update_op(ttg_mixed_state* m, int k, int i, int j, int upd);
-// Convert the FP64 input tiles (tiles64) to the FP32 working tiles, adding
-// shift·|a_ii| to every diagonal entry (shift 0: none), for a run with
-// update arithmetic upd.
-ttg_status ttg_mixed_prepare(ttg_mixed_state* m, void* stream, double shift, int upd);
+// Convert the FP64 input tiles src (the plan's input, same layout as
+// tiles64, which the factorisation only uses as FP64 scratch) to the FP32
+// working tiles, adding shift·|a_ii| to every diagonal entry (shift 0: none),
+// for a run with update arithmetic upd.
+ttg_status ttg_mixed_prepare(ttg_mixed_state* m, void* stream, double shift, int upd, const double* src);
 // The low-precision factor as FP64 tiles (converted into tiles64).
 const double* ttg_mixed_factor_tiles(ttg_mixed_state* m);
 // The FP32 factor tiles (same layout as tiles64).

@@ -481,7 +481,7 @@ ttg_status matmul_df(ttg_solver* S, const double* X, double* Y, int nrhs, cudaSt
     if (!S->lo_valid) {
         if ((st = S->A32lo.ensure(NN)) != TTG_OK) return st;
         ttg_note_launch();
-        split_low_half<<<S->ctx->sms * 8, 256, 0, s>>>((int64_t)NN, S->A64.p, S->A32.p, S->A32lo.p);
+        split_low_half<<<S->ctx->sms * 8, 256, 0, s>>>((int64_t)NN, S->A64.p, S->A32lo.p);
         TTG_CUDA_CHECK(cudaGetLastError());
         S->lo_valid = true;
     }
