@@ -124,7 +124,7 @@ typedef struct ttg_solve_opts {
     int32_t max_outer;  /* refinement steps (0 = 10)                                   */
     int32_t restart;    /* GMRES iterations per step (0 = 20, at most 60)              */
     int32_t gmres_prec; /* 0 auto (FP32 Krylov work, FP64 once FP32 stalls), 32, 64    */
-    double inner_tol;   /* relative GMRES tolerance per step (0 = 1e-6)                */
+    double inner_tol;   /* relative GMRES tolerance per step (0 = 1e-5)                */
 } ttg_solve_opts;
 
 typedef struct ttg_solve_report {
