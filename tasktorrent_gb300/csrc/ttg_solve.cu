@@ -746,13 +746,17 @@ ttg_status ttg_solver_solve(ttg_solver* S, const double* pristine, const double*
         // from an FP64 residual.
         constexpr double kDfTrust = 1e-11;     // predicted backward error below which FP64 is used at once
         constexpr double kDfFloor = 1e-11;     // smallest double-float value that steers a correction
+        constexpr double kDfSafe = 5e-13;      // smallest outcome (value × last cycle's gain) it may steer to
         constexpr double kContraction = 1e-2;  // assumed gain of one cycle, for choosing the next residual
         double expect = INFINITY;              // predicted backward error of the current X
         for (int outer = 0;; ++outer) {
             bool df = S->lo_valid && prec == 32 && expect >= kDfTrust;
             if ((st = backward_errors(S, nrhs, s, be, rn, df)) != TTG_OK) return st;
             double worst = *std::max_element(be.begin(), be.end());
-            if (df && (worst < kDfFloor || worst <= 2 * tol)) {
+            // A cycle that gains as much as the last one would land near the
+            // double-float floor: steer it in FP64.
+            const bool lands_low = outer > 0 && worst * std::min(1.0, worst / prev) < kDfSafe;
+            if (df && (worst < kDfFloor || worst <= 2 * tol || lands_low)) {
                 if (solve_verbose()) fprintf(stderr, "[ttg solve] outer %d double-float estimate %.3e\n", outer, worst);
                 df = false;
                 if ((st = backward_errors(S, nrhs, s, be, rn)) != TTG_OK) return st;
