@@ -135,3 +135,41 @@ def test_device_pointer_solve_matches_host_path(ctx, nrhs):
     assert bwd_err(A, Xd, B) <= 2 * BWD
     assert np.linalg.norm(Xd - Xh) <= 1e-10 * np.linalg.norm(Xh)
     p.close()
+
+
+@pytest.mark.parametrize("mk", [1, 2])
+def test_mixed_factor_reads_the_input(ctx, mk):
+    """A mixed factorisation converts the plan's input itself (no restore of
+    the FP64 working tiles, which are the diagonal POTRF's scratch): two
+    factorisations in a row, without a restore, give the same factor bits,
+    and a matrix set afterwards is the one factored."""
+    p = t.CholPlan(ctx, 128, 6, kind=2, matrix=1, alpha=1.0, seed=4, precision=t.PREC_MIXED, mixed_kind=mk)
+    st, _ = p.factor(restore=False)
+    assert st == t.TTG_OK
+    L1 = p.factor_L()
+    st, _ = p.factor(restore=False)
+    assert st == t.TTG_OK
+    assert np.array_equal(p.factor_L(), L1)
+    A2 = p.input_A() + 2.0 * np.eye(p.N)
+    p.set_matrix(A2)
+    st, _ = p.factor(restore=False)
+    assert st == t.TTG_OK
+    L2 = p.factor_L()
+    assert np.linalg.norm(L2 @ L2.T - A2) / np.linalg.norm(A2) < 1e-5
+    p.close()
+
+
+@pytest.mark.parametrize("tol", [1e-9, 1e-11])
+def test_reported_backward_error_is_fp64_at_a_loose_tolerance(ctx, tol):
+    """Early refinement residuals may be double-float estimates; the one that
+    decides convergence, and the reported backward error, are FP64: the report
+    matches the backward error recomputed on the host."""
+    p = t.CholPlan(ctx, 256, 8, kind=2, matrix=1, alpha=1e-4, seed=2, precision=t.PREC_MIXED, mixed_kind=2)
+    A = p.input_A()
+    B = rhs(p.N, 16, seed=7)
+    st, rep, X = p.solve_host(B, tol=tol, max_outer=12)
+    assert st == t.TTG_OK, rep.as_dict()
+    host = bwd_err(A, X, B)
+    assert rep.bwd_err <= tol and host <= 2 * tol
+    assert abs(rep.bwd_err - host) <= 1e-3 * host + 1e-17, (rep.bwd_err, host)
+    p.close()
