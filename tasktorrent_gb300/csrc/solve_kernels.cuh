@@ -745,11 +745,21 @@ __global__ void __launch_bounds__(256) dense_matmul_df_partial(int N, const floa
             sXl[c * kMaxRhs + q] = lo;
         }
         __syncthreads();
+        // Column c + 1 of A is loaded while column c is used (the loads are
+        // otherwise the main stall).
+        auto load = [&](int c, float& ah_, float& al_, float& bh_, float& bl_) {
+            const size_t col = (size_t)(c0 + c) * N;
+            ah_ = oka ? Ah[ra + col] : 0.0f;
+            al_ = oka ? Al[ra + col] : 0.0f;
+            bh_ = okb ? Ah[rbw + col] : 0.0f;
+            bl_ = okb ? Al[rbw + col] : 0.0f;
+        };
+        float nah = 0.0f, nal = 0.0f, nbh = 0.0f, nbl = 0.0f;
+        if (kc > 0) load(0, nah, nal, nbh, nbl);
 #pragma unroll 2
         for (int c = 0; c < kc; ++c) {
-            const size_t col = (size_t)(c0 + c) * N;
-            const float aah = oka ? Ah[ra + col] : 0.0f, aal = oka ? Al[ra + col] : 0.0f;
-            const float abh = okb ? Ah[rbw + col] : 0.0f, abl = okb ? Al[rbw + col] : 0.0f;
+            const float aah = nah, aal = nal, abh = nbh, abl = nbl;
+            if (c + 1 < kc) load(c + 1, nah, nal, nbh, nbl);
             const float4* xh4 = reinterpret_cast<const float4*>(sXh + c * kMaxRhs + half * H);
             const float4* xl4 = reinterpret_cast<const float4*>(sXl + c * kMaxRhs + half * H);
 #pragma unroll
