@@ -154,6 +154,10 @@ ttg_status ttg_chol_solve_host(ttg_chol_plan* plan, const double* h_B, double* h
  * keep the resident input), h_B in, h_X out (N×nrhs column-major). */
 ttg_status ttg_chol_posv_host(ttg_chol_plan* plan, const double* h_tiles, const double* h_B, double* h_X,
                               const ttg_solve_opts* opts, ttg_solve_report* rep, void* stream);
+/* The FP32 high/low split of FP64 values that the mixed solver's dense
+ * copies use (hi = fl32(v), lo = fl32(v - hi), bit for bit), computed on the
+ * host by the same source as the device kernels: n values of v -> hi, lo. */
+ttg_status ttg_split_f64_f32(const double* v, int64_t n, float* hi, float* lo);
 
 /* Arguments of 2d_gemm (2d_gemm.cpp:243-253) at one rank. */
 typedef struct ttg_gemm_args {

@@ -180,6 +180,7 @@ SIGNATURES = {
     "ttg_chol_plan_solve": (_STATUS, [_P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveReport), _P]),
     "ttg_chol_posv": (_STATUS, [_P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveReport), _P]),
     "ttg_chol_posv_host": (_STATUS, [_P, _P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveReport), _P]),
+    "ttg_split_f64_f32": (_STATUS, [_P, ctypes.c_int64, _P, _P]),
     "ttg_chol_solve_host": (_STATUS, [_P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveReport), _P]),
     "ttg_gemm_plan_create": (_STATUS, [_P, ctypes.POINTER(GemmArgs), ctypes.POINTER(_P)]),
     "ttg_gemm_plan_destroy": (_STATUS, [_P]),

@@ -7,6 +7,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "tile_f64.cuh"
 
@@ -798,21 +799,37 @@ __global__ void __launch_bounds__(256) dense_matmul_df_partial(int N, const floa
 // (rounded up), an integer times 2^(e-52), which the FP32 conversion rounds
 // to nearest and an exact power-of-two scale places.  Other values (zero,
 // tiny, huge, non-finite) take the FP64 formula.
-__device__ __forceinline__ void split_f64_f32(double v, float& h, float& l) {
+// Also compiled for the host (ttg_split_f64_f32), where the bit casts are
+// copies and the FP32 operations round to nearest as on the device.
+__host__ __device__ __forceinline__ void split_f64_f32(double v, float& h, float& l) {
+#ifdef __CUDA_ARCH__
     const unsigned hiw = (unsigned)__double2hiint(v), low = (unsigned)__double2loint(v);
+    auto as_float = [](unsigned u) { return __uint_as_float(u); };
+#else
+    unsigned long long bits;
+    memcpy(&bits, &v, sizeof bits);
+    const unsigned hiw = (unsigned)(bits >> 32), low = (unsigned)bits;
+    auto as_float = [](unsigned u) {
+        float f;
+        memcpy(&f, &u, sizeof f);
+        return f;
+    };
+#endif
     const unsigned sign = hiw >> 31;
     const int ex = (int)((hiw >> 20) & 0x7FFu) - 1023;
     if (ex < -60 || ex > 100) {
-        h = __double2float_rn(v);
-        l = __double2float_rn(v - (double)h);
+        h = (float)v;
+        l = (float)(v - (double)h);
         return;
     }
     const unsigned top = ((hiw & 0xFFFFFu) << 3) | (low >> 29);  // 23 mantissa bits of h before rounding
     const unsigned rem = low & 0x1FFFFFFFu;                       // the 29 bits below them
     const unsigned up = (rem > (1u << 28) || (rem == (1u << 28) && (top & 1u))) ? 1u : 0u;
-    h = __uint_as_float(((sign << 31) | ((unsigned)(ex + 127) << 23) | top) + up);  // a carry moves to the exponent
+    h = as_float(((sign << 31) | ((unsigned)(ex + 127) << 23) | top) + up);  // a carry moves to the exponent
     const unsigned rm = up ? (1u << 29) - rem : rem;
-    const float lv = __fmul_rn(__uint2float_rn(rm), __uint_as_float((unsigned)(ex + 1023 - 948) << 23));  // rm · 2^(e-52)
+    // rm · 2^(e-52): rm has at most 29 bits, so the conversion rounds to
+    // nearest once and the power-of-two scale is exact.
+    const float lv = (float)rm * as_float((unsigned)(ex + 1023 - 948) << 23);
     l = rm == 0 ? 0.0f : ((sign ^ up) ? -lv : lv);
 }
 

@@ -287,6 +287,12 @@ void ttg_solver_destroy(ttg_solver* S) {
     delete S;
 }
 
+extern "C" ttg_status ttg_split_f64_f32(const double* v, int64_t n, float* hi, float* lo) {
+    if (n < 0 || (n > 0 && (!v || !hi || !lo))) return TTG_EINVAL;
+    for (int64_t i = 0; i < n; ++i) split_f64_f32(v[i], hi[i], lo[i]);
+    return TTG_OK;
+}
+
 void ttg_solver_input_changed(ttg_solver* S) {
     if (S) S->dense_valid = S->lo_valid = false;
 }
