@@ -173,3 +173,28 @@ def test_reported_backward_error_is_fp64_at_a_loose_tolerance(ctx, tol):
     assert rep.bwd_err <= tol and host <= 2 * tol
     assert abs(rep.bwd_err - host) <= 1e-3 * host + 1e-17, (rep.bwd_err, host)
     p.close()
+
+
+@pytest.mark.parametrize("mk", [1, 2])
+def test_host_tiles_replace_the_input(ctx, mk):
+    """ttg_chol_posv_host with new host tiles: the plan factors and solves the
+    new matrix (its dense copies are rebuilt), and later calls without tiles
+    keep it as the resident input."""
+    kw = dict(kind=2, matrix=1, alpha=1e-4, precision=t.PREC_MIXED, mixed_kind=mk)
+    p = t.CholPlan(ctx, 128, 6, seed=2, **kw)
+    q = t.CholPlan(ctx, 128, 6, seed=5, **kw)
+    A1, A2 = p.input_A(), q.input_A()
+    assert not np.array_equal(A1, A2)
+    tiles2 = np.empty(q.tile_elems(), dtype=np.float64)
+    q.copy_tiles(1, tiles2)
+    B = rhs(p.N, 4, seed=11)
+    st, rep, X1 = p.solve_host(B)
+    assert st == t.TTG_OK and bwd_err(A1, X1, B) <= 2 * BWD
+    st, rep, X2 = p.solve_host(B, tiles=tiles2)
+    assert st == t.TTG_OK, rep.as_dict()
+    assert bwd_err(A2, X2, B) <= 2 * BWD and rep.bwd_err <= BWD
+    st, rep, X3 = p.solve_host(B)
+    assert st == t.TTG_OK and bwd_err(A2, X3, B) <= 2 * BWD
+    assert np.array_equal(X3, X2)
+    p.close()
+    q.close()
