@@ -519,18 +519,22 @@ __global__ void wd_gemm_kernel(const WdDesc* __restrict__ d, const TM* A, const 
 
 // Transposes of tiles: dst[doff_t + c + r·rows_t] = src[soff_t + r + c·rows_t]
 // for the tiles of a descriptor list (rows × cols each, column-major source
-// with ld rows, column-major destination with ld cols).  Block = 32×8
-// threads over 32×32 sub-tiles; sub_pre[t] = sub-tiles before tile t.
+// with ld rows, column-major destination with ld cols).  Block = 64×4
+// threads over 64×64 sub-tiles (16 loads in flight per thread, one
+// descriptor search per sub-tile); sub_pre[t] = sub-tiles before tile t.
 struct TransposeDesc {
     int64_t src, dst;
     int rows, cols;
 };
+constexpr int kTrEdge = 64;
 
 template <class TM>
-__global__ void transpose_tiles(const TransposeDesc* __restrict__ d, const int64_t* __restrict__ sub_pre, int n_desc,
-                                const TM* __restrict__ src, TM* __restrict__ dst) {
-    __shared__ TM t[32][33];
+__global__ void __launch_bounds__(256) transpose_tiles(const TransposeDesc* __restrict__ d, const int64_t* __restrict__ sub_pre,
+                                                       int n_desc, const TM* __restrict__ src, TM* __restrict__ dst) {
+    constexpr int E = kTrEdge, K = E / 4;
+    __shared__ TM t[E][E + 1];
     const int64_t total = sub_pre[n_desc];
+    const int tx = threadIdx.x & (E - 1), ty = threadIdx.x / E;
     for (int64_t b = blockIdx.x; b < total; b += gridDim.x) {
         int lo = 0, hi = n_desc;
         while (hi - lo > 1) {
@@ -540,18 +544,23 @@ __global__ void transpose_tiles(const TransposeDesc* __restrict__ d, const int64
         }
         const TransposeDesc td = d[lo];
         const int64_t sb = b - sub_pre[lo];
-        const int nbr = (td.rows + 31) / 32;
+        const int nbr = (td.rows + E - 1) / E;
         const int br = (int)(sb % nbr), bc = (int)(sb / nbr);
-        const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-        __syncthreads();
-        for (int yy = ty; yy < 32; yy += 8) {
-            const int r = br * 32 + tx, c = bc * 32 + yy;
-            if (r < td.rows && c < td.cols) t[yy][tx] = src[td.src + r + (int64_t)c * td.rows];
+        const int r = br * E + tx;
+        TM v[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int c = bc * E + ty + 4 * k;
+            v[k] = (r < td.rows && c < td.cols) ? src[td.src + r + (int64_t)c * td.rows] : TM(0);
         }
+        __syncthreads();  // the previous sub-tile's reads of t are done
+#pragma unroll
+        for (int k = 0; k < K; ++k) t[ty + 4 * k][tx] = v[k];
         __syncthreads();
-        for (int yy = ty; yy < 32; yy += 8) {
-            const int c = bc * 32 + tx, r = br * 32 + yy;  // destination (c, r) in a cols × rows tile
-            if (r < td.rows && c < td.cols) dst[td.dst + c + (int64_t)r * td.cols] = t[tx][yy];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int c = bc * E + tx, rr = br * E + ty + 4 * k;  // destination (c, rr) in a cols × rows tile
+            if (rr < td.rows && c < td.cols) dst[td.dst + c + (int64_t)rr * td.cols] = t[tx][ty + 4 * k];
         }
     }
 }

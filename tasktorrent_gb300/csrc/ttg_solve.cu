@@ -161,10 +161,10 @@ static ttg_status solver_tables(ttg_solver* S, const int* bs, const int64_t* off
         for (int i = j + 1; i < nb; ++i) {
             const int64_t o = off[i + (size_t)j * nb];
             to.push_back({o, o, bs[i], bs[j]});
-            so.push_back(so.back() + (int64_t)((bs[i] + 31) / 32) * ((bs[j] + 31) / 32));
+            so.push_back(so.back() + (int64_t)((bs[i] + kTrEdge - 1) / kTrEdge) * ((bs[j] + kTrEdge - 1) / kTrEdge));
         }
         td.push_back({doff[j], doff[j], bs[j], bs[j]});
-        sd.push_back(sd.back() + (int64_t)((bs[j] + 31) / 32) * ((bs[j] + 31) / 32));
+        sd.push_back(sd.back() + (int64_t)((bs[j] + kTrEdge - 1) / kTrEdge) * ((bs[j] + kTrEdge - 1) / kTrEdge));
     }
     S->items_fwd = fwd[nb];
     S->items_bwd = bwd[nb];
