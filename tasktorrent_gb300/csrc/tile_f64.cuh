@@ -292,19 +292,24 @@ __device__ __forceinline__ void geadd_f64(int m, int n, double alpha, const doub
 //
 // The tile is cut into P×P blocks of 32×32 (P = ceil(n/32)), and the
 // factorisation into items over the lower blocks:
-//   D(j)       factor the diagonal block (j,j) and invert it,
-//   R(j, i)    panel block (i,j) <- A_ij · L_jj⁻ᵀ            (i > j),
-//   T(p, i, j) trailing update A_ij -= L_ip · L_jpᵀ           (i >= j > p).
-// One state byte per block counts what it has received: block (i,j) holds
-// state p after the updates of panels 0..p-1, and j+1 once it is final (D or
-// R done).  Every item waits only for the blocks it reads and writes — D(j)
-// for state(j,j) = j; R(j,i) for state(j,j) = j+1 and state(i,j) = j;
-// T(p,i,j) for state(i,p) = state(j,p) = p+1 and state(i,j) = p — so the next
-// panel starts as soon as its own blocks are ready (look-ahead) and the
-// updates of every block are applied in panel order (deterministic result).
+//   F(j)       for j >= 1 first the panel block (j,j-1) <- A_j,j-1 · L_j-1,j-1⁻ᵀ
+//              (published at once) and the last update of the diagonal block,
+//              A_jj -= L_j,j-1 · L_j,j-1ᵀ; then factor (j,j) and invert it,
+//   R(j, i)    panel block (i,j) <- A_ij · L_jj⁻ᵀ            (i >= j+2),
+//   T(p, i, j) trailing update A_ij -= L_ip · L_jpᵀ           (i >= j > p, not i = j = p+1).
+// F(j) holds the whole critical chain of a panel (one handoff per panel
+// instead of three); its arithmetic is that of the separate D, R and T steps,
+// in the same order.  One state byte per block counts what it has received:
+// block (i,j) holds state p after the updates of panels 0..p-1, and j+1 once
+// it is final.  Every item waits only for the blocks it reads and writes —
+// F(j) for state(j-1,j-1) = j, state(j,j-1) = state(j,j) = j-1; R(j,i) for
+// state(j,j) = j+1 and state(i,j) = j; T(p,i,j) for state(i,p) = state(j,p)
+// = p+1 and state(i,j) = p — so the next panel starts as soon as its own
+// blocks are ready (look-ahead) and the updates of every block are applied
+// in panel order (deterministic result).
 //
 // Blocks of the team claim items from one counter in a fixed order, segment
-// by segment: seg(j) = D(j), R(j,·), T(j-1,·,j+1), T(j,·,j+1), then the rest
+// by segment: seg(j) = F(j), T(j-1,·,j), R(j,·), T(j-1,·,j+1), then the rest
 // of panel j-1's trailing update T(j-1,·,>=j+2).  The next panel's critical
 // items come before the bulk of the previous trailing update, and everything
 // an item waits for is claimed before it by a block that is running, so the
@@ -336,7 +341,7 @@ __device__ __forceinline__ long long team_clock() {
     return t;
 }
 
-// One item of the order above: kind 0 D(p), 1 R(p, bi), 2 T(p, bi, bj); kind
+// One item of the order above: kind 0 F(p), 1 R(p, bi), 2 T(p, bi, bj); kind
 // -1 past the last item.
 struct TeamItem {
     int kind, p, bi, bj;
@@ -344,7 +349,7 @@ struct TeamItem {
 
 __host__ __device__ inline int team_segment_items(int P, int j) {
     const int m = P - 1 - j;
-    return 1 + 2 * m + (j >= 1 ? m + m * (m - 1) / 2 : 0);
+    return 1 + (m > 1 ? m - 1 : 0) + (j >= 1 ? 2 * m + m * (m - 1) / 2 : 0);
 }
 
 __host__ __device__ inline int team_total_items(int P) {
@@ -362,22 +367,23 @@ __host__ __device__ inline TeamItem team_item(int P, int idx) {
             continue;
         }
         int k = idx;
-        if (k < 1) return {0, j, j, j};
+        if (k < 1) return {0, j, j, j};  // F(j)
         k -= 1;
-        if (k < m) return {1, j, j + 1 + k, j};
-        k -= m;
         if (j >= 1) {
-            if (k < m) return {2, j - 1, j + 1 + k, j + 1};
+            if (k < m) return {2, j - 1, j + 1 + k, j};  // panel j-1, column j
             k -= m;
         }
-        if (k < m) return {2, j, j + 1 + k, j + 1};
+        const int nr = m > 1 ? m - 1 : 0;
+        if (k < nr) return {1, j, j + 2 + k, j};  // R(j, i), i >= j+2
+        k -= nr;
+        if (k < m) return {2, j - 1, j + 1 + k, j + 1};  // panel j-1, column j+1 (j >= 1 here)
         k -= m;
         int bj = j + 2;
         while (k >= P - bj) {
             k -= P - bj;
             ++bj;
         }
-        return {2, j - 1, bj + k, bj};
+        return {2, j - 1, bj + k, bj};  // rest of panel j-1
     }
     return {-1, 0, 0, 0};
 }
@@ -544,6 +550,23 @@ __device__ __forceinline__ size_t team_xoff(int n, int lda, int k) {
     return (size_t)(k % h) + (size_t)(n - h + k / h) * lda;
 }
 
+// W1 (32 rows × nb, ld 33) <- W1 · Xᵀ for the lower triangular X = L_pp⁻¹
+// (ld 33): thread (row r, group g) forms columns g, g+8, g+16, g+24.
+__device__ inline void team_apply_inverse(double* W1, const double* X, int nb) {
+    const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
+    double acc[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int j = g + 8 * k;
+        double a = 0.0;
+        for (int c = 0; c <= j && c < nb; ++c) a = fma(W1[r * 33 + c], X[j * 33 + c], a);
+        acc[k] = a;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 4; ++k) W1[r * 33 + g + 8 * k] = acc[k];
+}
+
 // Team lower Cholesky of the FP64 tile A[n×n] (lda); requires team_fits(n).
 // With an FP32 source (W32 != nullptr, the mixed path) A is FP64 scratch:
 // the first item that touches a block reads it from W32 (ldw), and every
@@ -574,6 +597,25 @@ __device__ inline int potrf_l_f64_team(int n, double* A, int lda, double* smem, 
         s_xpanel = -1;
     }
     auto rows_of = [&](int b) { return min(kPanel, n - kPanel * b); };
+    // X = L_qq⁻¹ for the panel-block products of panel q: the kept copy (mixed
+    // path) or recomputed from L_qq, the same bits whichever block does it.
+    auto panel_inverse = [&](int q, int nq) {
+        if (s_xpanel == q) return;
+        if (keep_x) {
+            for (int e = threadIdx.x; e < 32 * 32; e += kThreads) {
+                const int r = e & 31, c = e >> 5;
+                X[r * 33 + c] = ldcg(A + team_xoff(n, lda, q * 1024 + e));
+            }
+        } else {
+            team_load_block(S, A, lda, nullptr, 0, false, kPanel * q, kPanel * q, nq, nq, true);
+            __syncthreads();
+            if (threadIdx.x < nq) inv[threadIdx.x] = 1.0 / S[threadIdx.x * 33 + threadIdx.x];
+            __syncthreads();
+            team_diag_inverse(S, inv, nq, X);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) s_xpanel = q;
+    };
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -587,11 +629,46 @@ __device__ inline int potrf_l_f64_team(int n, double* A, int lda, double* smem, 
         const TeamItem itm = team_item(P, idx);
         const int p = itm.p, bi = itm.bi, bj = itm.bj;
         if (itm.kind == 0) {
-            // D(p): factor and invert the diagonal block.
+            // F(p): for p >= 1 the panel block (p, p-1) and the last update of
+            // the diagonal block (the arithmetic of R(p-1, p) and T(p-1, p, p)),
+            // then the factor and inverse of the diagonal block (D(p)).
             const int nb = rows_of(p);
-            const int w = team_wait_states(tc, team_state(tc, p, p), p, nullptr, 0, nullptr, 0);
+            const int w = p >= 1 ? team_wait_states(tc, team_state(tc, p - 1, p - 1), p, team_state(tc, p, p - 1), p - 1,
+                                                    team_state(tc, p, p), p - 1)
+                                 : team_wait_states(tc, nullptr, 0, nullptr, 0, nullptr, 0);
             if (w) return w;
-            team_load_block(S, A, lda, W32, ldw, W32 && p == 0, kPanel * p, kPanel * p, nb, nb, true);
+            if (p >= 1) {
+                const int q = p - 1, nq = rows_of(q);
+                panel_inverse(q, nq);
+                team_load_block(W1, A, lda, W32, ldw, W32 && q == 0, kPanel * p, kPanel * q, nb, nq, false);
+                __syncthreads();
+                team_apply_inverse(W1, X, nq);
+                __syncthreads();
+                team_store_block(W1, A, lda, W32, ldw, kPanel * p, kPanel * q, nb, nq, false);
+                team_publish(team_state(tc, p, q), p);
+                // S = lower(A_pp) - L_pq · L_pqᵀ, A_pp from the FP32 source on
+                // its first touch (q == 0), in the T item's order.
+                {
+                    const bool wide = W32 && q == 0;
+                    const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
+                    const int gi = kPanel * p + r;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const int j = g + 8 * k, gj = kPanel * p + j;
+                        double v = 0.0;
+                        if (r < nb && j < nb && r >= j) {
+                            const double cv = wide ? (double)__ldcg(W32 + gi + (size_t)gj * ldw) : ldcg(A + gi + (size_t)gj * lda);
+                            double acc = 0.0;
+#pragma unroll 8
+                            for (int c = 0; c < kPanel; ++c) acc = fma(W1[r * 33 + c], W1[j * 33 + c], acc);
+                            v = cv - acc;
+                        }
+                        S[r * 33 + j] = v;
+                    }
+                }
+            } else {
+                team_load_block(S, A, lda, W32, ldw, W32 != nullptr, 0, 0, nb, nb, true);
+            }
             for (int e = threadIdx.x; e < 32 * 32; e += kThreads) {
                 const int j = e >> 5, c = e & 31;
                 X[j * 33 + c] = (j == c && j < nb) ? 1.0 : 0.0;
@@ -621,38 +698,10 @@ __device__ inline int potrf_l_f64_team(int n, double* A, int lda, double* smem, 
             const int nb = rows_of(p), rb = rows_of(bi);
             const int w = team_wait_states(tc, team_state(tc, p, p), p + 1, team_state(tc, bi, p), p, nullptr, 0);
             if (w) return w;
-            if (s_xpanel != p) {
-                if (keep_x) {
-                    for (int e = threadIdx.x; e < 32 * 32; e += kThreads) {
-                        const int r = e & 31, c = e >> 5;
-                        X[r * 33 + c] = ldcg(A + team_xoff(n, lda, p * 1024 + e));
-                    }
-                } else {
-                    team_load_block(S, A, lda, nullptr, 0, false, kPanel * p, kPanel * p, nb, nb, true);
-                    __syncthreads();
-                    if (threadIdx.x < nb) inv[threadIdx.x] = 1.0 / S[threadIdx.x * 33 + threadIdx.x];
-                    __syncthreads();
-                    team_diag_inverse(S, inv, nb, X);
-                }
-                __syncthreads();
-                if (threadIdx.x == 0) s_xpanel = p;
-            }
+            panel_inverse(p, nb);
             team_load_block(W1, A, lda, W32, ldw, W32 && p == 0, kPanel * bi, kPanel * p, rb, nb, false);
             __syncthreads();
-            {
-                const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
-                double acc[4];
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const int j = g + 8 * k;
-                    double a = 0.0;
-                    for (int c = 0; c <= j && c < nb; ++c) a = fma(W1[r * 33 + c], X[j * 33 + c], a);
-                    acc[k] = a;
-                }
-                __syncthreads();
-#pragma unroll
-                for (int k = 0; k < 4; ++k) W1[r * 33 + g + 8 * k] = acc[k];
-            }
+            team_apply_inverse(W1, X, nb);
             __syncthreads();
             team_store_block(W1, A, lda, W32, ldw, kPanel * bi, kPanel * p, rb, nb, false);
             team_publish(team_state(tc, bi, p), p + 1);
