@@ -57,6 +57,14 @@ const char* ttg_last_cuda_error(void);
  * kernels again).  Differences bracket a region of work. */
 int64_t ttg_kernel_launches(void);
 
+/* Item idx of the team POTRF dataflow of a P×P-block diagonal tile (the
+ * order the team's blocks claim items in): *kind 0 = F(p) (panel block
+ * (p,p-1), last update and factor of the diagonal block p), 1 = R(p, bi)
+ * (panel block (bi,p)), 2 = T(p, bi, bj) (update of block (bi,bj) by panel
+ * p), -1 past the last item.  Host computation of the device's table, for
+ * checking the order (every item once, every wait on an earlier claim). */
+ttg_status ttg_team_item(int32_t P, int32_t idx, int32_t* kind, int32_t* p, int32_t* bi, int32_t* bj);
+
 /* ------------------------------------------------------------------ tasks */
 
 /* Tile operation of one task.  The reference task bodies call BLAS/LAPACK on

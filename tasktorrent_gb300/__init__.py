@@ -118,6 +118,7 @@ SIGNATURES = {
     "ttg_strerror": (ctypes.c_char_p, [ctypes.c_int]),
     "ttg_last_cuda_error": (ctypes.c_char_p, []),
     "ttg_kernel_launches": (ctypes.c_int64, []),
+    "ttg_team_item": (_STATUS, [ctypes.c_int32, ctypes.c_int32, _P, _P, _P, _P]),
     "ttg_create": (_STATUS, [ctypes.POINTER(_P), ctypes.POINTER(Opts)]),
     "ttg_destroy": (_STATUS, [_P]),
     "ttg_graph_upload": (_STATUS, [_P, ctypes.POINTER(GraphDesc)]),

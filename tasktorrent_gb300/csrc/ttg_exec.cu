@@ -98,6 +98,16 @@ static std::atomic<long long> g_launches{0};
 void ttg_note_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 extern "C" int64_t ttg_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
 
+extern "C" ttg_status ttg_team_item(int32_t P, int32_t idx, int32_t* kind, int32_t* p, int32_t* bi, int32_t* bj) {
+    if (P < 1 || idx < 0 || !kind || !p || !bi || !bj) return TTG_EINVAL;
+    const ttg::TeamItem t = ttg::team_item(P, idx);
+    *kind = t.kind;
+    *p = t.p;
+    *bi = t.bi;
+    *bj = t.bj;
+    return TTG_OK;
+}
+
 extern "C" const char* ttg_strerror(ttg_status s) {
     switch (s) {
         case TTG_OK: return "ok";
