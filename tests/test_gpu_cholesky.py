@@ -84,6 +84,22 @@ def test_host_path_equals_resident_path(ctx):
     p.close()
 
 
+@pytest.mark.parametrize("mk", [1, 2])
+def test_host_path_equals_resident_path_mixed(ctx, mk):
+    """A mixed plan's host path factors the host matrix (written as the plan's
+    input) and returns the mixed factor: the resident path's bits."""
+    p = t.CholPlan(ctx, 64, 6, matrix=1, alpha=1.0, seed=0, precision=t.PREC_MIXED, mixed_kind=mk)
+    st, _ = p.factor()
+    assert st == t.TTG_OK
+    L1 = p.factor_L()
+    A = p.input_A()
+    st, rep, L2 = p.factor_host(A)
+    assert st == t.TTG_OK
+    assert np.array_equal(L1, L2)
+    assert np.linalg.norm(L2 @ L2.T - A) / np.linalg.norm(A) < 1e-5
+    p.close()
+
+
 def test_repeated_factorisations_are_identical(ctx):
     p = t.CholPlan(ctx, 96, 7, kind=2, matrix=1, alpha=1e-4, seed=2)
     outs = []
