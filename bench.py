@@ -10,7 +10,8 @@ right-hand sides, through ttg_chol_posv: the mixed-precision tiled Cholesky
 terms per operand, six products, for FP32-level updates (--mixed-kind 2) —
 FP32 TRSM, FP64 diagonal POTRF;
 one persistent-kernel launch of the task graph captured from the Taskflow<K>
-drop-in) followed by GMRES-based iterative refinement with FP64 residuals.
+drop-in) followed by GMRES-based iterative refinement (FP64 residuals decide
+convergence; double-float ones steer the early steps).
 Inputs (4.4 GB of FP64 lower tiles) are resident in HBM and larger than L2.
 `value` is N³/3 / time to solution (effective Cholesky TFLOP/s); solves/s is
 reported beside it.  `e2e` runs the same step through the C ABI with pinned

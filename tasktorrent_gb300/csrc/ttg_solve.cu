@@ -6,8 +6,10 @@
 //   inverted diagonal tiles), then one FP64 residual for the backward error.
 // Mixed plan (low-precision factor L̃, FP32): GMRES-IR —
 //   x0 = M⁻¹ b with M = L̃L̃ᵀ (FP32 sweeps);
-//   repeat: r = b − A x in FP64 (dense FP64 copy of A);
-//           stop when ‖r‖∞ / (‖A‖∞ ‖x‖∞) ≤ tol for every column;
+//   repeat: r = b − A x — in FP64 (dense FP64 copy of A), or, for a residual
+//           that only steers an early FP32 cycle, in double-float from the
+//           FP32 high and low copies;
+//           stop when the FP64 ‖r‖∞ / (‖A‖∞ ‖x‖∞) ≤ tol for every column;
 //           solve A d = r by GMRES left-preconditioned with M (the Krylov
 //           basis, the matrix-vector products and M⁻¹ in FP32, or in FP64
 //           when FP32 stops making progress; orthogonalisation sums in FP64);

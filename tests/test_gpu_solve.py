@@ -1,5 +1,5 @@
 """Solves with a Cholesky plan's factor: FP64 direct, and the mixed path
-(low-precision factor + GMRES-IR with FP64 residuals) to backward error
+(low-precision factor + GMRES-IR, convergence on FP64 residuals) to backward error
 ≤ 1e-14; forward errors against the FP64 oracle solution."""
 import numpy as np
 import pytest
