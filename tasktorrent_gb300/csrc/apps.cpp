@@ -81,6 +81,21 @@ struct ttg_chol_plan {
     size_t host_b_elems = 0;
     long factor_gen = 0;   // incremented by every successful factorisation
     long solver_gen = -1;  // factorisation the solver's inverted tiles belong to
+    // Frees whatever was allocated, so every early return of
+    // ttg_chol_plan_create (through the owning unique_ptr) releases the
+    // device tiles as ttg_chol_plan_destroy does.
+    ~ttg_chol_plan() {
+        if (ctx) cudaSetDevice(ctx->device);
+        tp.reset();
+        tp32.reset();
+        tpx3.reset();
+        for (double* t : tmp) cudaFree(t);
+        if (tiles) cudaFree(tiles);
+        if (pristine) cudaFree(pristine);
+        if (mixed) ttg_mixed_state_destroy(mixed);
+        if (solver) ttg_solver_destroy(solver);
+        if (d_b) cudaFree(d_b);
+    }
 };
 
 static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry, int upd, std::unique_ptr<Threadpool_shared>& tp_out) {
@@ -258,10 +273,19 @@ extern "C" ttg_status ttg_chol_plan_create(ttg_ctx* ctx, const ttg_chol_args* ar
     if (args->block_size <= 0 || args->num_blocks <= 0 || args->n_threads <= 0) return TTG_EINVAL;
     if (args->precision != TTG_PREC_F64 && args->precision != TTG_PREC_MIXED) return TTG_EINVAL;
     if (args->precision == TTG_PREC_MIXED && args->accumulate) return TTG_EINVAL;
+    if (args->precision == TTG_PREC_MIXED && (args->mixed_kind < 0 || args->mixed_kind > 2)) return TTG_EINVAL;
     std::unique_ptr<ttg_chol_plan> P(new ttg_chol_plan());
     P->ctx = ctx;
     P->args = *args;
     if (!cholesky_block_sizes(args->block_size, args->num_blocks, args->upper_block_size, P->bs)) return TTG_EINVAL;
+    if (args->precision == TTG_PREC_MIXED && args->mixed_kind != 1) {
+        // Tensor-core updates (mixed_kind 0 and 2) need uniform tiles whose
+        // size is a multiple of 128 (the MMA's M); checked before any
+        // allocation.  FP32 updates (mixed_kind 1) take any tiles.
+        for (int b : P->bs)
+            if (b != P->bs[0]) return TTG_EINVAL;
+        if (P->bs[0] % 128 != 0) return TTG_EINVAL;
+    }
     P->nb = args->num_blocks;
     P->displ.assign(P->nb + 1, 0);
     for (int i = 0; i < P->nb; ++i) P->displ[i + 1] = P->displ[i] + P->bs[i];
@@ -272,7 +296,6 @@ extern "C" ttg_status ttg_chol_plan_create(ttg_ctx* ctx, const ttg_chol_args* ar
     TTG_CUDA_CHECK(cudaMalloc((void**)&P->tiles, sizeof(double) * std::max<int64_t>(1, P->elems)));
     TTG_CUDA_CHECK(cudaMalloc((void**)&P->pristine, sizeof(double) * std::max<int64_t>(1, P->elems)));
     if (args->precision == TTG_PREC_MIXED) {
-        if (args->mixed_kind < 0 || args->mixed_kind > 2) return TTG_EINVAL;
         ttg_status s = ttg_mixed_state_create(ctx, P->N, P->nb, P->bs.data(), P->off.data(), P->tiles,
                                               args->mixed_kind == 1 ? 1 : 0, &P->mixed);
         if (s != TTG_OK) return s;
@@ -283,15 +306,8 @@ extern "C" ttg_status ttg_chol_plan_create(ttg_ctx* ctx, const ttg_chol_args* ar
     ttg_status s = chol_build_graph(P.get(), false, first, P->tp);
     if (s == TTG_OK && tc) s = chol_build_graph(P.get(), false, TTG_UPD_FP32, P->tp32);
     if (s == TTG_OK && tc && first == TTG_UPD_BF16) s = chol_build_graph(P.get(), false, TTG_UPD_BF16X3, P->tpx3);
-    if (s != TTG_OK) {
-        ttg_chol_plan_destroy(P.release());
-        return s;
-    }
-    s = ttg_chol_plan_generate(P.get(), nullptr);
-    if (s != TTG_OK) {
-        ttg_chol_plan_destroy(P.release());
-        return s;
-    }
+    if (s == TTG_OK) s = ttg_chol_plan_generate(P.get(), nullptr);
+    if (s != TTG_OK) return s;  // P's destructor frees what was allocated
     *out = P.release();
     return TTG_OK;
 }
@@ -313,18 +329,7 @@ extern "C" ttg_status ttg_chol_dag_dump(const ttg_chol_args* args, const char* p
 }
 
 extern "C" ttg_status ttg_chol_plan_destroy(ttg_chol_plan* P) {
-    if (!P) return TTG_OK;
-    cudaSetDevice(P->ctx->device);
-    P->tp.reset();
-    P->tp32.reset();
-    P->tpx3.reset();
-    for (double* t : P->tmp) cudaFree(t);
-    if (P->tiles) cudaFree(P->tiles);
-    if (P->pristine) cudaFree(P->pristine);
-    if (P->mixed) ttg_mixed_state_destroy(P->mixed);
-    if (P->solver) ttg_solver_destroy(P->solver);
-    if (P->d_b) cudaFree(P->d_b);
-    delete P;
+    delete P;  // the destructor frees the device buffers
     return TTG_OK;
 }
 
@@ -680,6 +685,14 @@ struct ttg_gemm_plan {
     int N = 0, b = 0, nb = 0;
     double *A = nullptr, *B = nullptr, *C = nullptr;  // tiles, b×b each, tile (i,j) at (i + j·nb)·b²
     std::unique_ptr<Threadpool_shared> tp;
+    // Frees whatever was allocated (early returns of ttg_gemm_plan_create too).
+    ~ttg_gemm_plan() {
+        if (ctx) cudaSetDevice(ctx->device);
+        tp.reset();
+        if (A) cudaFree(A);
+        if (B) cudaFree(B);
+        if (C) cudaFree(C);
+    }
 };
 
 static ttg_status gemm_build_graph(ttg_gemm_plan* Pp, bool dry) {
@@ -774,22 +787,13 @@ extern "C" ttg_status ttg_gemm_plan_create(ttg_ctx* ctx, const ttg_gemm_args* a,
         if (s != TTG_OK) return s;
     }
     ttg_status st = gemm_build_graph(P.get(), false);
-    if (st != TTG_OK) {
-        ttg_gemm_plan_destroy(P.release());
-        return st;
-    }
+    if (st != TTG_OK) return st;  // P's destructor frees the tiles
     *out = P.release();
     return TTG_OK;
 }
 
 extern "C" ttg_status ttg_gemm_plan_destroy(ttg_gemm_plan* P) {
-    if (!P) return TTG_OK;
-    cudaSetDevice(P->ctx->device);
-    P->tp.reset();
-    if (P->A) cudaFree(P->A);
-    if (P->B) cudaFree(P->B);
-    if (P->C) cudaFree(P->C);
-    delete P;
+    delete P;  // the destructor frees the device tiles
     return TTG_OK;
 }
 

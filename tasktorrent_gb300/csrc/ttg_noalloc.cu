@@ -170,8 +170,8 @@ ttg_status setup_device(int device, DeviceSetup& d) {
 }
 
 // Priority levels without heap use: rank of each runnable task's priority
-// among the distinct values (descending) if there are at most 32 of them,
-// else 32 equal-count groups of the sorted values.
+// among the distinct values (descending) if there are at most kMaxLevels
+// (128) of them, else kMaxLevels equal-count groups of the sorted values.
 void levels_static(int n, const double* prio, int* n_levels) {
     for (int t = 0; t < n; ++t) h_level[t] = 0;
     *n_levels = 1;
@@ -182,9 +182,16 @@ void levels_static(int n, const double* prio, int* n_levels) {
     if (m == 0) return;
     auto desc = [](double a, double b) { return a > b; };
     std::sort(h_sorted, h_sorted + m, desc);
-    for (int l = 0; l < ttg::kMaxLevels; ++l)
-        h_cut[l] = h_sorted[std::min(m - 1, (int)((long)(l + 1) * m / ttg::kMaxLevels) - 1)];
-    const int distinct = (int)(std::unique(h_sorted, h_sorted + m) - h_sorted);
+    int distinct = 1;
+    for (int i = 1; i < m; ++i) distinct += h_sorted[i] != h_sorted[i - 1];
+    if (distinct > ttg::kMaxLevels) {
+        // Group cuts from the sorted values: here m >= distinct > kMaxLevels,
+        // so every index (l+1)·m/kMaxLevels − 1 lies in [0, m).
+        for (int l = 0; l < ttg::kMaxLevels; ++l)
+            h_cut[l] = h_sorted[std::max(0, std::min(m - 1, (int)((long)(l + 1) * m / ttg::kMaxLevels) - 1))];
+    } else {
+        std::unique(h_sorted, h_sorted + m);
+    }
     for (int t = 0; t < n; ++t) {
         if (!h_runnable[t]) continue;
         int l = 0;
@@ -212,6 +219,9 @@ extern "C" ttg_status ttg_run_graph_noalloc(int device, const ttg_graph_desc* gd
     for (int t = 0; t < n; ++t) {
         if (gd->init_count[t] < 0 || gd->succ_ptr[t] > gd->succ_ptr[t + 1]) return TTG_EINVAL;
         if (gd->ops[t].kind < TTG_OP_NOP || gd->ops[t].kind > TTG_OP_GEADD) return TTG_EINVAL;
+        // The FP64 tile kernels only: a mixed-precision op's tiles are FP32
+        // or BF16 and would be read as doubles.
+        if (gd->ops[t].kind != TTG_OP_NOP && gd->ops[t].prec != TTG_PREC_F64) return TTG_EINVAL;
     }
     for (int64_t e = 0; e < n_edges; ++e)
         if (gd->succ_idx[e] < 0 || gd->succ_idx[e] >= n) return TTG_EINVAL;
@@ -290,76 +300,85 @@ extern "C" ttg_status ttg_run_graph_noalloc(int device, const ttg_graph_desc* gd
     std::memset(&h_status, 0, sizeof(h_status));
     h_status.start = ~0ULL;
 
-    // Fill the scratch: every array the kernel reads is rewritten here.
+    // Fill the scratch, launch and read the status back.  Every array the
+    // kernel reads is rewritten here.
     unsigned char* S = d.scratch;
     cudaStream_t s = (cudaStream_t)stream;
-    if (n > 0) {
-        TTG_CUDA_CHECK(cudaMemcpyAsync(S + oOps, h_ops, sizeof(ttg_op) * n, cudaMemcpyHostToDevice, s));
-        TTG_CUDA_CHECK(cudaMemcpyAsync(S + oCount, h_count, 4 * n, cudaMemcpyHostToDevice, s));
-        TTG_CUDA_CHECK(cudaMemsetAsync(S + oRuns, 0, 4 * n, s));
-        TTG_CUDA_CHECK(cudaMemcpyAsync(S + oParts, h_parts, 4 * n, cudaMemcpyHostToDevice, s));
-        TTG_CUDA_CHECK(cudaMemsetAsync(S + oPartNext, 0, 4 * n, s));
-        TTG_CUDA_CHECK(cudaMemsetAsync(S + oPartDone, 0, 4 * n, s));
-        TTG_CUDA_CHECK(cudaMemcpyAsync(S + oBind, h_bind, 4 * n, cudaMemcpyHostToDevice, s));
-        TTG_CUDA_CHECK(cudaMemcpyAsync(S + oLevel, h_level, n, cudaMemcpyHostToDevice, s));
-        TTG_CUDA_CHECK(cudaMemcpyAsync(S + oRunnable, h_runnable, n, cudaMemcpyHostToDevice, s));
-        TTG_CUDA_CHECK(cudaMemcpyAsync(S + oSuccPtr, gd->succ_ptr, 8 * (n + 1), cudaMemcpyHostToDevice, s));
-    }
-    if (n_edges > 0) TTG_CUDA_CHECK(cudaMemcpyAsync(S + oSuccIdx, gd->succ_idx, 4 * n_edges, cudaMemcpyHostToDevice, s));
-    if (q_total > 0) TTG_CUDA_CHECK(cudaMemcpyAsync(S + oQbuf, h_qbuf, 4 * q_total, cudaMemcpyHostToDevice, s));
-    TTG_CUDA_CHECK(cudaMemcpyAsync(S + oQoff, h_qoff, 4 * (ttg::kMaxLevels + 1), cudaMemcpyHostToDevice, s));
-    TTG_CUDA_CHECK(cudaMemsetAsync(S + oQhead, 0, 4 * ttg::kMaxLevels * 32, s));
-    TTG_CUDA_CHECK(cudaMemcpyAsync(S + oQtail, h_qtail, 4 * ttg::kMaxLevels * 32, cudaMemcpyHostToDevice, s));
-    TTG_CUDA_CHECK(cudaMemcpyAsync(S + oBqoff, h_bqoff, 4 * (W + 1), cudaMemcpyHostToDevice, s));
-    TTG_CUDA_CHECK(cudaMemsetAsync(S + oBqhead, 0, 4 * W, s));
-    TTG_CUDA_CHECK(cudaMemcpyAsync(S + oBqtail, h_bqtail, 4 * W, cudaMemcpyHostToDevice, s));
-    TTG_CUDA_CHECK(cudaMemcpyAsync(S + oStatus, &h_status, sizeof(h_status), cudaMemcpyHostToDevice, s));
-
     RunStatus* dst = (RunStatus*)(S + oStatus);
-    if (n_runnable > 0) {
-        ttg::ExecParams p;
-        p.ops = (const ttg_op*)(S + oOps);
-        p.n_tasks = n;
-        p.n_runnable = n_runnable;
-        p.count = (int*)(S + oCount);
-        p.runs = (int*)(S + oRuns);
-        p.parts = (const int*)(S + oParts);
-        p.part_next = (int*)(S + oPartNext);
-        p.part_done = (int*)(S + oPartDone);
-        p.succ_ptr = (const int64_t*)(S + oSuccPtr);
-        p.succ_idx = (const int32_t*)(S + oSuccIdx);
-        p.level = (const uint8_t*)(S + oLevel);
-        p.bind = (const int32_t*)(S + oBind);
-        p.n_levels = n_levels;
-        p.n_workers = W;
-        p.qbuf = (int*)(S + oQbuf);
-        p.q_off = (const int*)(S + oQoff);
-        p.q_head = (int*)(S + oQhead);
-        p.q_tail = (int*)(S + oQtail);
-        p.bq_buf = (int*)(S + oQbuf) + q_levels;
-        p.bq_off = (const int*)(S + oBqoff);
-        p.bq_head = (int*)(S + oBqhead);
-        p.bq_tail = (int*)(S + oBqtail);
-        p.has_bound = h_bqoff[W] > 0;
-        p.done = &dst->done;
-        p.err = &dst->err;
-        p.err_task = &dst->err_task;
-        p.err_info = &dst->err_info;
-        p.trace = nullptr;
-        p.timeout_ns = (long long)((timeout_s > 0 ? timeout_s : 10.0) * 1e9);
-        p.team_ctr = nullptr;  // POTRF tasks run on one block here
-        p.team_slot = nullptr;
-        void* args[] = {(void*)&p, (void*)&dst};
-        TTG_CUDA_CHECK(cudaLaunchCooperativeKernel((const void*)exec_kernel_noalloc, dim3(W), dim3(ttg::kThreads), args,
-                                                   ttg::kF64SmemDoubles * sizeof(double), s));
-    }
-    if (n > 0) {
-        summarize_noalloc<<<std::max(1, std::min(64, (n + 255) / 256)), 256, 0, s>>>(
-            (const int*)(S + oRuns), (const int*)(S + oCount), (const uint8_t*)(S + oRunnable), n, dst);
-        TTG_CUDA_CHECK(cudaGetLastError());
-    }
-    TTG_CUDA_CHECK(cudaMemcpyAsync(&h_status, dst, sizeof(h_status), cudaMemcpyDeviceToHost, s));
-    TTG_CUDA_CHECK(cudaStreamSynchronize(s));
+    auto enqueue = [&]() -> ttg_status {
+        if (n > 0) {
+            TTG_CUDA_CHECK(cudaMemcpyAsync(S + oOps, h_ops, sizeof(ttg_op) * n, cudaMemcpyHostToDevice, s));
+            TTG_CUDA_CHECK(cudaMemcpyAsync(S + oCount, h_count, 4 * n, cudaMemcpyHostToDevice, s));
+            TTG_CUDA_CHECK(cudaMemsetAsync(S + oRuns, 0, 4 * n, s));
+            TTG_CUDA_CHECK(cudaMemcpyAsync(S + oParts, h_parts, 4 * n, cudaMemcpyHostToDevice, s));
+            TTG_CUDA_CHECK(cudaMemsetAsync(S + oPartNext, 0, 4 * n, s));
+            TTG_CUDA_CHECK(cudaMemsetAsync(S + oPartDone, 0, 4 * n, s));
+            TTG_CUDA_CHECK(cudaMemcpyAsync(S + oBind, h_bind, 4 * n, cudaMemcpyHostToDevice, s));
+            TTG_CUDA_CHECK(cudaMemcpyAsync(S + oLevel, h_level, n, cudaMemcpyHostToDevice, s));
+            TTG_CUDA_CHECK(cudaMemcpyAsync(S + oRunnable, h_runnable, n, cudaMemcpyHostToDevice, s));
+            TTG_CUDA_CHECK(cudaMemcpyAsync(S + oSuccPtr, gd->succ_ptr, 8 * (n + 1), cudaMemcpyHostToDevice, s));
+        }
+        if (n_edges > 0) TTG_CUDA_CHECK(cudaMemcpyAsync(S + oSuccIdx, gd->succ_idx, 4 * n_edges, cudaMemcpyHostToDevice, s));
+        if (q_total > 0) TTG_CUDA_CHECK(cudaMemcpyAsync(S + oQbuf, h_qbuf, 4 * q_total, cudaMemcpyHostToDevice, s));
+        TTG_CUDA_CHECK(cudaMemcpyAsync(S + oQoff, h_qoff, 4 * (ttg::kMaxLevels + 1), cudaMemcpyHostToDevice, s));
+        TTG_CUDA_CHECK(cudaMemsetAsync(S + oQhead, 0, 4 * ttg::kMaxLevels * 32, s));
+        TTG_CUDA_CHECK(cudaMemcpyAsync(S + oQtail, h_qtail, 4 * ttg::kMaxLevels * 32, cudaMemcpyHostToDevice, s));
+        TTG_CUDA_CHECK(cudaMemcpyAsync(S + oBqoff, h_bqoff, 4 * (W + 1), cudaMemcpyHostToDevice, s));
+        TTG_CUDA_CHECK(cudaMemsetAsync(S + oBqhead, 0, 4 * W, s));
+        TTG_CUDA_CHECK(cudaMemcpyAsync(S + oBqtail, h_bqtail, 4 * W, cudaMemcpyHostToDevice, s));
+        TTG_CUDA_CHECK(cudaMemcpyAsync(S + oStatus, &h_status, sizeof(h_status), cudaMemcpyHostToDevice, s));
+
+        if (n_runnable > 0) {
+            ttg::ExecParams p;
+            p.ops = (const ttg_op*)(S + oOps);
+            p.n_tasks = n;
+            p.n_runnable = n_runnable;
+            p.count = (int*)(S + oCount);
+            p.runs = (int*)(S + oRuns);
+            p.parts = (const int*)(S + oParts);
+            p.part_next = (int*)(S + oPartNext);
+            p.part_done = (int*)(S + oPartDone);
+            p.succ_ptr = (const int64_t*)(S + oSuccPtr);
+            p.succ_idx = (const int32_t*)(S + oSuccIdx);
+            p.level = (const uint8_t*)(S + oLevel);
+            p.bind = (const int32_t*)(S + oBind);
+            p.n_levels = n_levels;
+            p.n_workers = W;
+            p.qbuf = (int*)(S + oQbuf);
+            p.q_off = (const int*)(S + oQoff);
+            p.q_head = (int*)(S + oQhead);
+            p.q_tail = (int*)(S + oQtail);
+            p.bq_buf = (int*)(S + oQbuf) + q_levels;
+            p.bq_off = (const int*)(S + oBqoff);
+            p.bq_head = (int*)(S + oBqhead);
+            p.bq_tail = (int*)(S + oBqtail);
+            p.has_bound = h_bqoff[W] > 0;
+            p.done = &dst->done;
+            p.err = &dst->err;
+            p.err_task = &dst->err_task;
+            p.err_info = &dst->err_info;
+            p.trace = nullptr;
+            p.timeout_ns = (long long)((timeout_s > 0 ? timeout_s : 10.0) * 1e9);
+            p.team_ctr = nullptr;  // POTRF tasks run on one block here
+            p.team_slot = nullptr;
+            void* args[] = {(void*)&p, (void*)&dst};
+            TTG_CUDA_CHECK(cudaLaunchCooperativeKernel((const void*)exec_kernel_noalloc, dim3(W), dim3(ttg::kThreads), args,
+                                                       ttg::kF64SmemDoubles * sizeof(double), s));
+        }
+        if (n > 0) {
+            summarize_noalloc<<<std::max(1, std::min(64, (n + 255) / 256)), 256, 0, s>>>(
+                (const int*)(S + oRuns), (const int*)(S + oCount), (const uint8_t*)(S + oRunnable), n, dst);
+            TTG_CUDA_CHECK(cudaGetLastError());
+        }
+        TTG_CUDA_CHECK(cudaMemcpyAsync(&h_status, dst, sizeof(h_status), cudaMemcpyDeviceToHost, s));
+        return TTG_OK;
+    };
+    const ttg_status enq = enqueue();
+    // Whatever was enqueued finishes before the lock is released, also when
+    // a step failed: the next call rewrites the shared scratch.
+    const cudaError_t se = cudaStreamSynchronize(s);
+    if (enq != TTG_OK) return enq;
+    TTG_CUDA_CHECK(se);
 
     const int err = h_status.err;
     ttg_status result = err;

@@ -84,11 +84,13 @@ def test_host_path_equals_resident_path(ctx):
     p.close()
 
 
-@pytest.mark.parametrize("mk", [1, 2])
-def test_host_path_equals_resident_path_mixed(ctx, mk):
+@pytest.mark.parametrize("mk,b", [(1, 64), (2, 128)])
+def test_host_path_equals_resident_path_mixed(ctx, mk, b):
     """A mixed plan's host path factors the host matrix (written as the plan's
-    input) and returns the mixed factor: the resident path's bits."""
-    p = t.CholPlan(ctx, 64, 6, matrix=1, alpha=1.0, seed=0, precision=t.PREC_MIXED, mixed_kind=mk)
+    input) and returns the mixed factor: the resident path's bits.  FP32
+    updates (mixed_kind 1) take any tile; split-BF16 tensor-core updates
+    (mixed_kind 2) need tiles that are a multiple of 128."""
+    p = t.CholPlan(ctx, b, 6, matrix=1, alpha=1.0, seed=0, precision=t.PREC_MIXED, mixed_kind=mk)
     st, _ = p.factor()
     assert st == t.TTG_OK
     L1 = p.factor_L()
@@ -134,3 +136,36 @@ def test_not_positive_definite_is_reported(ctx):
     st, rep = p.factor()
     assert st == t.TTG_ENOTPD and rep.info >= 1
     p.close()
+
+
+@pytest.mark.parametrize("mk,b,upper", [(2, 64, -1), (0, 96, -1), (2, 128, 200), (3, 128, -1)])
+def test_rejected_mixed_plan_allocates_nothing(ctx, mk, b, upper):
+    """Tensor-core updates need uniform tiles that are a multiple of 128, and
+    mixed_kind is 0, 1 or 2: other requests return TTG_EINVAL and leave the
+    device's free memory where it was."""
+    import torch
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info(0)
+    for _ in range(3):
+        with pytest.raises(t.TTGError) as e:
+            t.CholPlan(ctx, b, 6, matrix=1, alpha=1.0, seed=0, precision=t.PREC_MIXED, mixed_kind=mk, upper_block_size=upper)
+        assert e.value.status == t.TTG_EINVAL
+    free1, _ = torch.cuda.mem_get_info(0)
+    assert free1 == free0
+
+
+def test_plans_release_their_memory(ctx):
+    """Creating and destroying FP64, mixed and GEMM plans returns the device
+    memory they took."""
+    import torch
+    for _ in range(2):  # the first round sets up lazily created context buffers
+        torch.cuda.synchronize()
+        free0, _ = torch.cuda.mem_get_info(0)
+        p = t.CholPlan(ctx, 128, 8, matrix=1, alpha=1.0, seed=0)
+        q = t.CholPlan(ctx, 128, 8, matrix=1, alpha=1.0, seed=0, precision=t.PREC_MIXED, mixed_kind=2)
+        g = t.GemmPlan(ctx, 512, 128)
+        p.close()
+        q.close()
+        g.close()
+        free1, _ = torch.cuda.mem_get_info(0)
+    assert free1 == free0

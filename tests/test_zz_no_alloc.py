@@ -75,17 +75,34 @@ def to_dense(tiles, off, b, nb):
     return np.tril(L)
 
 
-def graph_desc(ops, indeg, ptr, idx):
+def graph_desc(ops, indeg, ptr, idx, prio=None):
     n = len(ops)
     keep = [(t.Op * n)(*ops), np.ascontiguousarray(indeg, np.int32), np.ascontiguousarray(ptr, np.int64),
-            np.ascontiguousarray(idx if len(idx) else [0], np.int32)]
-    g = t.GraphDesc(n, keep[0], keep[1].ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), None, None,
+            np.ascontiguousarray(idx if len(idx) else [0], np.int32),
+            None if prio is None else np.ascontiguousarray(prio, np.float64)]
+    g = t.GraphDesc(n, keep[0], keep[1].ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                    None if prio is None else keep[4].ctypes.data_as(ctypes.POINTER(ctypes.c_double)), None,
                     keep[2].ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
                     keep[3].ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
     return g, keep
 
 
-def test_noalloc_matches_regular_entry_point(ctx):
+def kind2_priorities(b, nb):
+    """Priorities of the tasks of cholesky_graph in 2d_cholesky's --kind 2
+    form: potrf 9(nb-j)-1, trsm 9(nb-j)-2, gemm 9nb-9j-2 (fewer distinct
+    values than the executor's 128 levels)."""
+    pr = []
+    for j in range(nb):
+        pr.append(9 * (nb - j) - 1)
+        pr += [9 * (nb - j) - 2] * (nb - 1 - j)
+    for j in range(nb):
+        for i in range(j, nb):
+            pr += [9 * nb - 9 * j - 2] * j
+    return np.array(pr, np.float64)
+
+
+@pytest.mark.parametrize("with_priorities", [False, True])
+def test_noalloc_matches_regular_entry_point(ctx, with_priorities):
     import torch
     b, nb = 64, 6
     N = b * nb
@@ -111,7 +128,9 @@ def test_noalloc_matches_regular_entry_point(ctx):
 
     # No-alloc entry point, two calls in a row on the same input.
     ops, indeg, ptr, idx, off = cholesky_graph(na_dev.data_ptr(), b, nb)
-    g, keep = graph_desc(ops, indeg, ptr, idx)
+    prio = kind2_priorities(b, nb) if with_priorities else None
+    assert prio is None or len(prio) == len(ops)
+    g, keep = graph_desc(ops, indeg, ptr, idx, prio)
     for call in range(2):
         na_dev.copy_(torch.from_numpy(packed))
         torch.cuda.synchronize()
@@ -128,5 +147,14 @@ def test_noalloc_rejects_graphs_beyond_its_limits():
     n = 16385  # TTG_NOALLOC_MAX_TASKS + 1
     ops = [t.Op(kind=t.OP_NOP) for _ in range(n)]
     g, keep = graph_desc(ops, np.zeros(n, np.int32), np.zeros(n + 1, np.int64), np.zeros(0, np.int32))
+    rep = t.Report()
+    assert t.lib().ttg_run_graph_noalloc(0, ctypes.byref(g), 0, 5.0, None, ctypes.byref(rep)) == t.TTG_EINVAL
+
+
+def test_noalloc_rejects_mixed_precision_ops():
+    """Only FP64 tile operations: a mixed-precision op is refused before
+    anything reaches the device."""
+    op = t.Op(kind=t.OP_POTRF_L, prec=t.PREC_MIXED, m=64, n=64, ldc=64, c=0)
+    g, keep = graph_desc([op], np.zeros(1, np.int32), np.zeros(2, np.int64), np.zeros(0, np.int32))
     rep = t.Report()
     assert t.lib().ttg_run_graph_noalloc(0, ctypes.byref(g), 0, 5.0, None, ctypes.byref(rep)) == t.TTG_EINVAL
