@@ -52,6 +52,14 @@ typedef struct orc_chol_args {
     uint32_t seed;
     int record_dag;
     const char* dag_prefix; /* <prefix>.tasks.csv / <prefix>.edges.csv */
+    /* Bounded CPU samples of a large factorisation: run only the tasks of
+     * the first panel_limit panel steps (potrf j, trsm (i,j) with j < limit,
+     * gemm (k,i,j) with k < limit; every predecessor of such a task is one
+     * too).  0 = the whole graph. */
+    int panel_limit;
+    /* matrix 2: the input as packed lower tiles (tile (i,j), i >= j, column
+     * of tiles after column of tiles, each column-major with ld = bs[i]). */
+    const double* in_tiles;
 } orc_chol_args;
 
 typedef struct orc_chol_out {
@@ -59,6 +67,7 @@ typedef struct orc_chol_out {
     double* A;     /* optional N×N column-major input (symmetric) */
     double time_s; /* seeding to join */
     double potrf_s, trsm_s, gemm_s, accu_s;
+    double flops;  /* of the tasks run: potrf b^3/3, trsm m b^2, syrk b^2 k, gemm 2 m n k */
     long n_tasks_run;
     long n_edges;
     long errors;
@@ -226,19 +235,37 @@ int cholesky_run(const orc_chol_args* a, orc_chol_out* out) {
         Ad.resize((size_t)N * N);
         gen_gram(N, a->alpha, a->seed, Ad.data());
     }
+    if (a->matrix == 2 && !a->in_tiles) return -1;
     auto val = [&](int i, int j) -> double {
         if (a->matrix == 1) return Ad[i + (size_t)j * N];
         return 1.0 / (double)((i - j) * (i - j) + 1);
     };
     std::vector<std::vector<double>> blocks((size_t)nb * nb);
-    for (int ii = 0; ii < nb; ++ii)
-        for (int jj = 0; jj <= ii; ++jj) {
+    size_t packed = 0;  // matrix 2: offset of tile (ii, jj) in the packed input
+    for (int jj = 0; jj < nb; ++jj)
+        for (int ii = jj; ii < nb; ++ii) {
             auto& t = blocks[ii + (size_t)jj * nb];
             t.resize((size_t)bs[ii] * bs[jj]);
+            if (a->matrix == 2) {
+                std::copy(a->in_tiles + packed, a->in_tiles + packed + t.size(), t.begin());
+                packed += t.size();
+                continue;
+            }
             for (int j = 0; j < bs[jj]; ++j)
                 for (int i = 0; i < bs[ii]; ++i) t[i + (size_t)j * bs[ii]] = val(displ[ii] + i, displ[jj] + j);
         }
-    if (out->A)
+    if (out->A && a->matrix == 2) {
+        for (int jj = 0; jj < nb; ++jj)
+            for (int ii = jj; ii < nb; ++ii) {
+                const auto& t = blocks[ii + (size_t)jj * nb];
+                for (int j = 0; j < bs[jj]; ++j)
+                    for (int i = 0; i < bs[ii]; ++i) {
+                        const double v = t[i + (size_t)j * bs[ii]];
+                        out->A[displ[ii] + i + (size_t)(displ[jj] + j) * N] = v;
+                        out->A[displ[jj] + j + (size_t)(displ[ii] + i) * N] = v;
+                    }
+            }
+    } else if (out->A)
         for (int j = 0; j < N; ++j)
             for (int i = 0; i < N; ++i) out->A[i + (size_t)j * N] = val(i, j);
     Ad.clear();
@@ -279,6 +306,11 @@ int cholesky_run(const orc_chol_args* a, orc_chol_out* out) {
         return (kij[1] == kij[2] ? 1 : 2) + (kij[0] == 0 ? 0 : 1);
     };
 
+    // Tasks of the first `limit` panel steps only (bounded samples).
+    const int limit = a->panel_limit > 0 ? std::min(a->panel_limit, nb) : nb;
+    std::atomic<long long> flops_x3(0);  // 3 × flops, exact integers
+    std::atomic<long> ran(0);            // task bodies run
+
     Recorder rec;
     rec.on = a->record_dag != 0;
     std::atomic<long long> t_potrf(0), t_trsm(0), t_gemm(0), t_accu(0);
@@ -297,15 +329,29 @@ int cholesky_run(const orc_chol_args* a, orc_chol_out* out) {
     Flow<K2> trsm(&tp, 0);
     Flow<K3> gemm(&tp, 0);
     Flow<K3> accu(&tp, 0);
-    auto promise_potrf = [&](int j) { rec.promise(potrf_name(j), potrf_indeg(j)); potrf.fulfill_promise(j); };
-    auto promise_trsm = [&](K2 ij) { rec.promise(trsm_name(ij), trsm_indeg(ij)); trsm.fulfill_promise(ij); };
-    auto promise_gemm = [&](K3 kij) { rec.promise(gemm_name(kij), gemm_indeg(kij)); gemm.fulfill_promise(kij); };
+    auto promise_potrf = [&](int j) {
+        if (j >= limit) return;
+        rec.promise(potrf_name(j), potrf_indeg(j));
+        potrf.fulfill_promise(j);
+    };
+    auto promise_trsm = [&](K2 ij) {
+        if (ij[1] >= limit) return;
+        rec.promise(trsm_name(ij), trsm_indeg(ij));
+        trsm.fulfill_promise(ij);
+    };
+    auto promise_gemm = [&](K3 kij) {
+        if (kij[0] >= limit) return;
+        rec.promise(gemm_name(kij), gemm_indeg(kij));
+        gemm.fulfill_promise(kij);
+    };
     auto promise_accu = [&](K3 kij) { rec.promise(accu_name(kij), 1); accu.fulfill_promise(kij); };
 
     potrf.set_task([&](int j) {
              rec.begin(potrf_name(j));
              auto s = clk::now();
              const int r = dpotrf_l(bs[j], blocks[j + (size_t)j * nb].data(), lda(j));
+             flops_x3 += (long long)bs[j] * bs[j] * bs[j];
+             ++ran;
              if (r != 0) {
                  int z = 0;
                  info.compare_exchange_strong(z, displ[j] + r);
@@ -326,6 +372,8 @@ int cholesky_run(const orc_chol_args* a, orc_chol_out* out) {
             auto s = clk::now();
             const int i = ij[0], j = ij[1];
             dtrsm_rltn(bs[i], bs[j], 1.0, blocks[j + (size_t)j * nb].data(), lda(j), blocks[i + (size_t)j * nb].data(), lda(i));
+            flops_x3 += 3LL * bs[i] * bs[j] * bs[j];
+            ++ran;
             t_trsm += us(s);
         })
         .set_fulfill([&](K2 ij) {
@@ -356,6 +404,8 @@ int cholesky_run(const orc_chol_args* a, orc_chol_out* out) {
             else
                 dgemm(NoTrans, Trans, bs[i], bs[j], bs[k], -1.0, blocks[i + (size_t)k * nb].data(), lda(i),
                       blocks[j + (size_t)k * nb].data(), lda(j), beta, C, lda(i));
+            flops_x3 += (i == j ? 3LL : 6LL) * bs[i] * bs[j] * bs[k];
+            ++ran;
             t_gemm += us(s);
             if (accumulate) {
                 std::lock_guard<std::mutex> g(acc[i + (size_t)j * nb].m);
@@ -389,6 +439,7 @@ int cholesky_run(const orc_chol_args* a, orc_chol_out* out) {
             auto& C = blocks[i + (size_t)j * nb];
             for (size_t e = 0; e < C.size(); ++e) C[e] += part[e];
             t_accu += us(s);
+            ++ran;
         })
         .set_fulfill([&](K3 kij) {
             if (kij[1] == kij[2]) promise_potrf(kij[1]);
@@ -409,11 +460,12 @@ int cholesky_run(const orc_chol_args* a, orc_chol_out* out) {
     out->trsm_s = t_trsm.load() * 1e-6;
     out->gemm_s = t_gemm.load() * 1e-6;
     out->accu_s = t_accu.load() * 1e-6;
+    out->flops = (double)flops_x3.load() / 3.0;
     out->info = info.load();
     out->errors = 0;
     for (auto& kv : rec.tasks)
         if (kv.second[1] > kv.second[0] || kv.second[2] != 1) out->errors++;
-    out->n_tasks_run = rec.runs();
+    out->n_tasks_run = rec.on ? rec.runs() : ran.load();
     out->n_edges = (long)rec.edges.size();
     snprintf(out->blas, sizeof(out->blas), "%s", blas().name.c_str());
     if (out->L) {

@@ -19,13 +19,14 @@ class CholArgs(ctypes.Structure):
     _fields_ = [("n_threads", ctypes.c_int), ("block_size", ctypes.c_int), ("num_blocks", ctypes.c_int),
                 ("prio_kind", ctypes.c_int), ("accumulate", ctypes.c_int), ("upper_block_size", ctypes.c_int),
                 ("matrix", ctypes.c_int), ("alpha", ctypes.c_double), ("seed", ctypes.c_uint32),
-                ("record_dag", ctypes.c_int), ("dag_prefix", ctypes.c_char_p)]
+                ("record_dag", ctypes.c_int), ("dag_prefix", ctypes.c_char_p), ("panel_limit", ctypes.c_int),
+                ("in_tiles", ctypes.c_void_p)]
 
 
 class CholOut(ctypes.Structure):
     _fields_ = [("L", ctypes.c_void_p), ("A", ctypes.c_void_p), ("time_s", ctypes.c_double), ("potrf_s", ctypes.c_double),
                 ("trsm_s", ctypes.c_double), ("gemm_s", ctypes.c_double), ("accu_s", ctypes.c_double),
-                ("n_tasks_run", ctypes.c_long), ("n_edges", ctypes.c_long), ("errors", ctypes.c_long), ("info", ctypes.c_int),
+                ("flops", ctypes.c_double), ("n_tasks_run", ctypes.c_long), ("n_edges", ctypes.c_long), ("errors", ctypes.c_long), ("info", ctypes.c_int),
                 ("blas", ctypes.c_char * 256)]
 
 
@@ -97,19 +98,32 @@ def blas_name():
 
 
 def cholesky(N=None, block_size=32, num_blocks=8, n_threads=4, kind=0, accumulate=False, upper_block_size=-1, matrix=1,
-             alpha=1.0, seed=0, want_L=True, want_A=False, dag_prefix=None):
-    """One run of the oracle's Cholesky task graph.  Returns a dict."""
+             alpha=1.0, seed=0, want_L=True, want_A=False, dag_prefix=None, panel_limit=0, tiles=None):
+    """One run of the oracle's Cholesky task graph.  Returns a dict.
+
+    tiles: the input as packed lower tiles (float64, the device layout of
+    ttg_tile_layout); sets matrix = 2.  panel_limit > 0 runs only the tasks
+    of the first panel_limit panel steps (a bounded sample; `flops` counts
+    the tasks that ran)."""
     sizes = block_sizes(block_size, num_blocks, upper_block_size)
     n = int(sizes.sum())
     L = np.zeros((n, n), order="F") if want_L else None
     A = np.zeros((n, n), order="F") if want_A else None
+    tp = None
+    if tiles is not None:
+        matrix = 2
+        tiles = np.ascontiguousarray(tiles, dtype=np.float64)
+        need = sum(int(sizes[i]) * int(sizes[j]) for j in range(num_blocks) for i in range(j, num_blocks))
+        if tiles.size < need:
+            raise ValueError("tiles: %d elements, the layout needs %d" % (tiles.size, need))
+        tp = tiles.ctypes.data
     a = CholArgs(n_threads, block_size, num_blocks, kind, 1 if accumulate else 0, upper_block_size, matrix, alpha, seed,
-                 1 if dag_prefix else 0, dag_prefix.encode() if dag_prefix else None)
+                 1 if dag_prefix else 0, dag_prefix.encode() if dag_prefix else None, panel_limit, tp)
     o = CholOut(L.ctypes.data if L is not None else None, A.ctypes.data if A is not None else None)
     r = lib().orc_cholesky(ctypes.byref(a), ctypes.byref(o))
     if r != 0:
         raise RuntimeError("orc_cholesky failed")
-    return {"L": L, "A": A, "time_s": o.time_s, "tasks": o.n_tasks_run, "edges": o.n_edges, "errors": o.errors,
+    return {"L": L, "A": A, "time_s": o.time_s, "flops": o.flops, "tasks": o.n_tasks_run, "edges": o.n_edges, "errors": o.errors,
             "info": o.info, "blas": o.blas.decode(), "N": n,
             "kind_s": {"potrf": o.potrf_s, "trsm": o.trsm_s, "gemm": o.gemm_s, "accu": o.accu_s}}
 

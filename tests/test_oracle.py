@@ -156,3 +156,44 @@ def test_restated_runtime_equals_reference_runtime(tmp_path, args):
     else:
         # The accumulate flow adds partial products in arrival order.
         assert np.linalg.norm(r["L"] - Lref) <= 1e-14 * np.linalg.norm(Lref)
+
+
+def _pack_lower_tiles(A, sizes):
+    """Packed lower tiles of A in the device layout: tile (i,j), i >= j, column
+    of tiles after column of tiles, each column-major."""
+    displ = np.concatenate([[0], np.cumsum(sizes)])
+    parts = []
+    for j in range(len(sizes)):
+        for i in range(j, len(sizes)):
+            parts.append(A[displ[i]:displ[i + 1], displ[j]:displ[j + 1]].reshape(-1, order="F"))
+    return np.concatenate(parts)
+
+
+def test_packed_tile_input_equals_generated_input():
+    """matrix 2 (packed tiles given) factors the same input to the same bits."""
+    b, nb = 32, 6
+    r1 = orc.cholesky(block_size=b, num_blocks=nb, n_threads=4, kind=2, matrix=1, alpha=1e-4, seed=2, want_A=True)
+    tiles = _pack_lower_tiles(r1["A"], orc.block_sizes(b, nb))
+    r2 = orc.cholesky(block_size=b, num_blocks=nb, n_threads=4, kind=2, tiles=tiles, want_A=True)
+    assert np.array_equal(r1["A"], r2["A"])
+    assert np.array_equal(r1["L"], r2["L"])
+    N = b * nb
+    assert r1["flops"] == pytest.approx(N ** 3 / 3.0, rel=1e-12)
+
+
+@pytest.mark.parametrize("limit", [1, 2, 3])
+def test_panel_limited_sample(limit):
+    """panel_limit P runs the tasks of the first P panel steps: their count and
+    flops follow the task formulas, and the first P tile columns are final."""
+    b, nb = 16, 6
+    full = orc.cholesky(block_size=b, num_blocks=nb, n_threads=4, kind=2, matrix=1, alpha=1.0, seed=0)
+    part = orc.cholesky(block_size=b, num_blocks=nb, n_threads=4, kind=2, matrix=1, alpha=1.0, seed=0, panel_limit=limit)
+    tasks = sum(1 + (nb - 1 - j) for j in range(limit)) + sum((nb - k - 1) * (nb - k) // 2 for k in range(limit))
+    assert part["tasks"] == tasks and part["errors"] == 0 and part["info"] == 0
+    flops = sum(b ** 3 / 3 + (nb - 1 - j) * b ** 3 for j in range(limit))
+    for k in range(limit):
+        m = nb - k - 1  # trailing tile rows
+        flops += m * b ** 3 + m * (m - 1) // 2 * 2 * b ** 3  # SYRKs + GEMMs of panel step k
+    assert part["flops"] == pytest.approx(flops, rel=1e-12)
+    c = limit * b
+    assert np.array_equal(part["L"][:, :c], full["L"][:, :c])
