@@ -120,42 +120,118 @@ def allmax(world, v):
     return float(t.item())
 
 
-def cpu_sample(steps, warmup, N=16384, b=512):
-    """The reference's algorithm on the host cores: the oracle port (restated
-    Taskflow/Threadpool_shared + OpenBLAS, one BLAS thread per task) on all
-    cores, FP64 Cholesky of N×N with tile b.  Returns (TFLOP/s, cores, blas)."""
+def _tasks(nb):
+    return nb + nb * (nb - 1) // 2 + (nb - 1) * nb * (nb + 1) // 6
+
+
+def workload_config(args):
+    """The workload both arms report (the same dict: same matrix, tiles,
+    right-hand sides and conditioning)."""
+    nb = args.n // args.block
+    N = nb * args.block
+    elems = nb * (nb + 1) // 2 * args.block ** 2
+    return {"workload": "tiled Cholesky + solve of A X = B to backward error <= %g, A = G*G^T/N + alpha*I" % args.tol,
+            "gpu_variant": "mixed precision: BF16 tensor-core updates (%s), FP32 TRSM, FP64 diagonal POTRF, GMRES-IR" % (
+                {0: "plain BF16 first", 1: "FP32 updates", 2: "split into three BF16 terms"}[args.mixed_kind]),
+            "mixed_kind": args.mixed_kind, "matrix_size": N, "block_size": args.block, "nrhs": args.nrhs,
+            "alpha": args.alpha, "seed": args.seed, "priority_kind": args.kind, "tasks": _tasks(nb),
+            "l2": "inputs larger than L2 (%.1f GB of FP64 tiles)" % (elems * 8 / 1e9)}
+
+
+def cpu_factor_sample(tiles, args, steps, warmup):
+    """The reference's algorithm on the host cores: the oracle port (the
+    Taskflow/Threadpool_shared graph of 2d_cholesky at one rank, OpenBLAS with
+    one BLAS thread per task, one worker per host core), FP64, on the given
+    packed lower tiles of the workload's matrix.  A bounded sample: only the
+    tasks of the first `args.cpu_panels` panel steps run (their exact flops
+    are counted), timed from seeding to join like 2d_cholesky.cpp:612-619.
+    Returns (TFLOP/s median, cores, blas, sample seconds median, sample
+    flops, fraction of N^3/3)."""
     from oracle import oracle as orc
     orc.lib(use_blas=True)
     cores = os.cpu_count() or 1
-    times = []
+    nb = args.n // args.block
+    N = nb * args.block
+    rates, times = [], []
     for i in range(warmup + steps):
-        r = orc.cholesky(block_size=b, num_blocks=N // b, n_threads=cores, kind=2, matrix=0, want_L=False)
-        if r["info"] != 0:
-            raise RuntimeError("oracle factorisation failed")
+        r = orc.cholesky(block_size=args.block, num_blocks=nb, n_threads=cores, kind=args.kind, want_L=False, tiles=tiles,
+                         panel_limit=args.cpu_panels)
+        if r["info"] != 0 or r["errors"] != 0:
+            raise RuntimeError("oracle factorisation sample failed (info %d)" % r["info"])
         if i >= warmup:
+            rates.append(r["flops"] / r["time_s"] / 1e12)
             times.append(r["time_s"])
-    t = statistics.median(times)
-    return N ** 3 / 3.0 / t / 1e12, cores, r["blas"], t
+    return (statistics.median(rates), cores, r["blas"], statistics.median(times), r["flops"],
+            r["flops"] / (N ** 3 / 3.0))
+
+
+def _cpu_sample_text(args, cores, blas, frac, tail):
+    nb = args.n // args.block
+    return ("FP64 tiled Cholesky of the same matrix (N=%d, tile %d, alpha=%g, seed %d): the tasks of the first %d of %d "
+            "panel steps (%.1f%% of N^3/3, where the task graph is widest), oracle port of 2d_cholesky at one rank "
+            "(Taskflow/Threadpool_shared restated, OpenBLAS %s one thread per task), %d worker threads; the triangular "
+            "solves (2*N^2*nrhs flops, <0.2%% of N^3/3) are not timed; %s" % (
+                args.n, args.block, args.alpha, args.seed, args.cpu_panels, nb, 100 * frac, os.path.basename(blas),
+                cores, tail))
+
+
+def gram_tiles_host(args):
+    """The workload's matrix as packed lower FP64 tiles in host memory.  Up to
+    N = 4096 the host restatement of the generator makes it (G*G^T as an
+    exact FP64 product of the integer G); above, the device generator does (G*G^T
+    at N=32768 takes minutes on the host cores) and a few entries are checked
+    against the host restatement's exact integer formula."""
+    import ctypes
+    import numpy as np
+    from oracle import oracle as orc
+    nb = args.n // args.block
+    N = nb * args.block
+    b = args.block
+    if N <= 4096:
+        G = orc.qnormals(0, N * N, args.seed, 0).astype(np.float64).reshape(N, N, order="F")
+        A = G @ G.T / (256.0 * N) + args.alpha * np.eye(N)
+        return np.concatenate([A[i * b:(i + 1) * b, j * b:(j + 1) * b].reshape(-1, order="F")
+                               for j in range(nb) for i in range(j, nb)])
+    import torch
+    import tasktorrent_gb300 as t
+    ctx = t.Context(device=0, timeout_s=60.0)
+    bs = np.full(nb, args.block, np.int32)
+    elems = nb * (nb + 1) // 2 * args.block ** 2
+    d = torch.empty(elems, dtype=torch.float64, device="cuda")
+    t.check(t.lib().ttg_gen_gram_tiles(ctx.h, nb * args.block, bs.ctypes.data, nb, args.alpha, args.seed,
+                                       ctypes.c_void_p(d.data_ptr()), None), "gram tiles")
+    torch.cuda.synchronize()
+    h = d.cpu().numpy()
+    del d
+    ctx.close()
+    torch.cuda.empty_cache()
+    # Spot check: entry (i, j) of A from the host generator's definition.
+    rng = np.random.default_rng(0)
+    for _ in range(4):
+        i, j = sorted(rng.integers(0, N, 2).tolist(), reverse=True)
+        ti, tj = i // b, j // b
+        o = sum((nb - c) * b * b for c in range(tj)) + (ti - tj) * b * b + (i - ti * b) + (j - tj * b) * b
+        v = orc.gram_entry(N, i, j, args.alpha, args.seed)
+        if h[o] != v:
+            raise RuntimeError("device input differs from the host generator at (%d, %d)" % (i, j))
+    return h
 
 
 def run_reference(args, world, rank):
     if rank != 0:
         return
-    v, cores, blas, t = cpu_sample(args.steps, args.warmup, args.cpu_n, args.cpu_b)
-    sample = "FP64 tiled Cholesky N=%d tile %d (%d tasks), oracle port of 2d_cholesky at one rank, %d threads, %s" % (
-        args.cpu_n, args.cpu_b, _tasks(args.cpu_n // args.cpu_b), cores, os.path.basename(blas))
+    tiles = gram_tiles_host(args)
+    v, cores, blas, t, flops, frac = cpu_factor_sample(tiles, args, args.steps, args.warmup)
+    sample = _cpu_sample_text(args, cores, blas, frac, "median of %d steps after %d warm-up" % (args.steps, args.warmup))
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "tiled Cholesky FP64 (bounded CPU sample)", "matrix_size": args.cpu_n,
-                       "block_size": args.cpu_b},
-            "cpu_baseline": {"value": v, "unit": "TFLOP/s", "cores": cores, "kind": "port", "sample": sample},
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic: the same seeded matrix as the GPU arm",
+            "config": workload_config(args),
+            "cpu_baseline": {"value": v, "unit": "TFLOP/s", "cores": cores, "kind": "port", "sample": sample,
+                             "sample_flops": flops, "kind_note": "the reference's runtime cannot be built on the "
+                             "measuring host (its sources are not shipped there); the oracle restates it"},
             "e2e": {"value": v, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
-
-
-def _tasks(nb):
-    return nb + nb * (nb - 1) // 2 + (nb - 1) * nb * (nb + 1) // 6
 
 
 def run_batched(ctx, args):
@@ -216,6 +292,71 @@ def run_serving(args, local):
     return out
 
 
+def run_small_configs(ctx, args, world):
+    """The two smaller workloads, device and host side by side: tiled Cholesky
+    N=2048 tile 128 (A = G*G^T/N + I, seed 0; FP64) and the 2D block GEMM DAG
+    N=8192 block 512 (A, B iid U[-1,1], seed 1; FP64).  Device: executor
+    kernel time, median of 5 after 1 warm-up.  Host: the oracle port on all
+    cores (OpenBLAS, one thread per task), median of 5 after 1 warm-up."""
+    import numpy as np
+    import tasktorrent_gb300 as t
+    from oracle import oracle as orc
+    out = {}
+    # Cholesky N=2048 tile 128.
+    p = t.CholPlan(ctx, 128, 16, n_threads=16, kind=args.kind, matrix=1, alpha=1.0, seed=0)
+    ms = []
+    for i in range(6):
+        st, rep = p.factor()
+        if st != t.TTG_OK:
+            raise RuntimeError("N=2048 factorisation failed: %s" % t.strerror(st))
+        if i:
+            ms.append(rep.elapsed_ms)
+    L = p.factor_L()
+    A = p.input_A()
+    p.close()
+    err = float(np.linalg.norm(L @ L.T - A) / np.linalg.norm(A))
+    flops = 2048.0 ** 3 / 3
+    out["cholesky_n2048_b128"] = {"gpu_ms": statistics.median(ms), "gpu_tflops": flops / statistics.median(ms) / 1e9,
+                                  "rel_err_LLt": err, "tasks": 816}
+    # 2D block GEMM N=8192 block 512.
+    g = t.GemmPlan(ctx, 8192, 512, n_threads=16, inputs=1, seed=1)
+    ms = []
+    for i in range(6):
+        st, rep = g.run()
+        if st != t.TTG_OK:
+            raise RuntimeError("N=8192 block GEMM failed: %s" % t.strerror(st))
+        if i:
+            ms.append(rep.elapsed_ms)
+    host = world == 1 and not args.no_cpu_baseline
+    C = g.C() if host else None
+    g.close()
+    gflops = 2 * 8192.0 ** 3
+    out["gemm_n8192_b512"] = {"gpu_ms": statistics.median(ms), "gpu_tflops": gflops / statistics.median(ms) / 1e9,
+                              "tasks": 4608}
+    if host:
+        orc.lib(use_blas=True)
+        cores = os.cpu_count() or 1
+        ts = []
+        for i in range(6):
+            r = orc.cholesky(block_size=128, num_blocks=16, n_threads=cores, kind=args.kind, matrix=1, alpha=1.0, seed=0,
+                             want_L=(i == 5))
+            if i:
+                ts.append(r["time_s"])
+        out["cholesky_n2048_b128"].update(
+            {"cpu_ms": statistics.median(ts) * 1e3, "cpu_tflops": flops / statistics.median(ts) / 1e12, "cpu_cores": cores,
+             "rel_diff_vs_oracle": float(np.linalg.norm(L - r["L"]) / np.linalg.norm(r["L"]))})
+        ts = []
+        for i in range(6):
+            r = orc.gemm(8192, 512, n_threads=cores, inputs=1, seed=1, want_C=(i == 5))
+            if i:
+                ts.append(r["time_s"])
+        out["gemm_n8192_b512"].update(
+            {"cpu_ms": statistics.median(ts) * 1e3, "cpu_tflops": gflops / statistics.median(ts) / 1e12, "cpu_cores": cores,
+             "rel_diff_vs_oracle": float(np.linalg.norm(C - r["C"]) / np.linalg.norm(r["C"]))})
+        out["cpu_note"] = "oracle port (%s, one BLAS thread per task), median of 5 after 1 warm-up" % os.path.basename(r["blas"])
+    return out
+
+
 def run_ours(args, world, rank, local):
     import ctypes
     import numpy as np
@@ -232,7 +373,7 @@ def run_ours(args, world, rank, local):
     # Right-hand sides: iid N(0,1) from seed, on the device.
     B = torch.empty(nrhs, N, dtype=torch.float64, device="cuda")  # column-major N×nrhs
     X = torch.empty_like(B)
-    t.check(lib.ttg_gen_normal(ctx.h, N * nrhs, args.seed + 100 + rank, 1, ctypes.c_void_p(B.data_ptr()), None), "rhs")
+    t.check(lib.ttg_gen_normal(ctx.h, N * nrhs, args.seed + 100, 1, ctypes.c_void_p(B.data_ptr()), None), "rhs")
     torch.cuda.synchronize()
 
     def opts():
@@ -257,7 +398,7 @@ def run_ours(args, world, rank, local):
     # Headline: mixed precision (BF16 tensor-core updates, split into three
     # BF16 terms by default) + GMRES-IR at alpha.
     plan = t.CholPlan(ctx, args.block, nb, n_threads=16, kind=args.kind, matrix=1, alpha=args.alpha,
-                      seed=args.seed + rank, precision=t.PREC_MIXED, mixed_kind=args.mixed_kind)
+                      seed=args.seed, precision=t.PREC_MIXED, mixed_kind=args.mixed_kind)
     n_tasks, capture_s = plan.tasks()
     for _ in range(args.warmup):
         posv(plan)
@@ -298,6 +439,7 @@ def run_ours(args, world, rank, local):
         # At least five timed calls: the host copy shares the host's memory
         # system with other work, and single calls have seen stalls.
         e2e_steps = max(args.steps, 5)
+        phases = {k: [] for k in ("h2d_ms", "compute_ms", "factor_ms", "solve_ms", "d2h_ms", "total_ms")}
         for _ in range(e2e_steps):
             s0 = time.perf_counter()
             st = lib.ttg_chol_posv_host(plan.h, ctypes.c_void_p(hin.data_ptr()), ctypes.c_void_p(hB.data_ptr()),
@@ -305,10 +447,17 @@ def run_ours(args, world, rank, local):
             ts.append(time.perf_counter() - s0)
             if st != t.TTG_OK:
                 raise RuntimeError("e2e failed: %s" % t.strerror(st))
+            for k in phases:
+                phases[k].append(getattr(rep, k))
         e2e_s = allmax(world, statistics.mean(ts))
         e2e = {"value": world * flops / e2e_s / 1e12, "unit": "TFLOP/s", "solves_per_s": world * nrhs / e2e_s,
                "h2d_bytes_per_step": elems * 8 + N * nrhs * 8, "d2h_bytes_per_step": N * nrhs * 8,
-               "steps": e2e_steps, "ms_per_step": e2e_s * 1e3}
+               "steps": e2e_steps, "ms_per_step": e2e_s * 1e3,
+               "phases_ms": {k: statistics.mean(v) for k, v in phases.items()},
+               "phases_note": "per call, mean: h2d (tiles + B, events), compute (factor + solve + refinement, events), "
+                              "factor (executor kernels), solve (host clock), d2h (X, events), total (host clock)"}
+        if world == 1 and not args.no_cpu_baseline:
+            host_tiles = hin.numpy().copy()
         del hin, hB, hX
     plan.close()
 
@@ -357,12 +506,17 @@ def run_ours(args, world, rank, local):
     if not args.quick and not args.no_serving:
         extra["serving"] = run_serving(args, local)
 
+    if not args.quick and not args.no_configs:
+        extra["configs"] = run_small_configs(ctx, args, world)
+
     cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
-        v, cores, blas, tcpu = cpu_sample(2, 1, args.cpu_n, args.cpu_b)
+    if world == 1 and not args.no_cpu_baseline:
+        if args.no_e2e:
+            host_tiles = gram_tiles_host(args)
+        v, cores, blas, tcpu, sflops, frac = cpu_factor_sample(host_tiles, args, 2, 1)
+        del host_tiles
         cpu = {"value": v, "unit": "TFLOP/s", "cores": cores, "kind": "port",
-               "sample": "FP64 tiled Cholesky factorisation N=%d tile %d, oracle port of 2d_cholesky at one rank, %d threads, "
-                         "%s, median of 2 after 1 warm-up" % (args.cpu_n, args.cpu_b, cores, os.path.basename(blas))}
+               "sample": _cpu_sample_text(args, cores, blas, frac, "median of 2 after 1 warm-up"), "sample_flops": sflops}
 
     if rank == 0:
         last = reps[-1]
@@ -370,14 +524,7 @@ def run_ours(args, world, rank, local):
                 "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "bf16",
                 "data": "synthetic: A = G*G^T/N + alpha*I, G quantised N(0,1) (Philox-4x32-10, seed %d); B iid N(0,1)" % args.seed,
-                "config": {"workload": "tiled Cholesky + solve, mixed precision (BF16 tensor-core updates, %s; FP32 TRSM, FP64 "
-                                       "diagonal POTRF) + GMRES-IR to backward error <= %g" % (
-                                           {0: "plain BF16 first", 1: "FP32 updates", 2: "split into three BF16 terms"}[args.mixed_kind],
-                                           args.tol),
-                           "mixed_kind": args.mixed_kind,
-                           "matrix_size": N, "block_size": args.block, "nrhs": nrhs, "alpha": args.alpha, "tasks": n_tasks,
-                           "l2": "inputs larger than L2 (%.1f GB of FP64 tiles)" % (elems * 8 / 1e9), "capture_s": capture_s,
-                           "wall_s_timed": wall},
+                "config": workload_config(args), "tasks": n_tasks, "capture_s": capture_s, "wall_s_timed": wall,
                 "solves_per_s": world * nrhs / (step_ms * 1e-3),
                 "bwd_err": last.bwd_err, "refinement": {"outer": last.outer, "inner": last.inner, "gmres_prec": last.gmres_prec,
                                                           "remedy": last.remedy, "factor_ms": last.factor_ms},
@@ -409,8 +556,10 @@ def main():
     ap.add_argument("--kind", type=int, default=2)
     ap.add_argument("--mixed-kind", dest="mixed_kind", type=int, default=2,
                     help="0: BF16 updates (remedies on loss of definiteness); 2: split BF16; 1: FP32")
-    ap.add_argument("--cpu-n", dest="cpu_n", type=int, default=16384)
-    ap.add_argument("--cpu-b", dest="cpu_b", type=int, default=512)
+    ap.add_argument("--cpu-panels", dest="cpu_panels", type=int, default=2,
+                    help="panel steps of the factorisation in the CPU samples")
+    ap.add_argument("--no-configs", dest="no_configs", action="store_true",
+                    help="skip the N=2048 Cholesky and N=8192 block-GEMM comparisons")
     ap.add_argument("--no-e2e", dest="no_e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", dest="no_cpu_baseline", action="store_true")
     ap.add_argument("--nrhs", type=int, default=16)

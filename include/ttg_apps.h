@@ -139,6 +139,12 @@ typedef struct ttg_solve_report {
     int32_t remedy;     /* mixed factor: 0 BF16 updates; after a loss of definiteness
                            4 split-BF16 updates, 2 FP32 updates, 3 FP32 updates on
                            A + 16·2^-24·diag(A), 1 BF16 updates on A + 8·2^-8·diag(A) */
+    double h2d_ms;      /* ttg_chol_posv_host / ttg_chol_solve_host: host-to-device copies
+                           of the tiles and B (device events; 0 elsewhere)             */
+    double d2h_ms;      /* ... the device-to-host copy of X                             */
+    double compute_ms;  /* ... from the end of the input copies to the start of the
+                           output copy: factorisation, solve, refinement (events)      */
+    double total_ms;    /* ... whole call, host clock                                   */
 } ttg_solve_report;
 
 /* d_B, d_X: device N×nrhs column-major (ld N). */

@@ -48,6 +48,18 @@ void orc_qnormals(uint64_t first, int count, uint32_t seed, uint32_t stream, int
     for (int i = 0; i < count; ++i) out[i] = ttg_qnormal_at(first + i, seed, stream);
 }
 
+/* One entry of A = G·Gᵀ/N + αI (the definition gen_gram computes for the
+ * whole matrix): an exact integer dot product of rows i and j of G. */
+double orc_gram_entry(int N, int i, int j, double alpha, uint32_t seed) {
+    int64_t s = 0;
+    for (int k = 0; k < N; ++k)
+        s += (int64_t)ttg_qnormal_at(i + (uint64_t)k * N, seed, TTG_STREAM_G) *
+             ttg_qnormal_at(j + (uint64_t)k * N, seed, TTG_STREAM_G);
+    double v = (double)s / (256.0 * (double)N);
+    if (i == j) v = v + alpha;
+    return v;
+}
+
 void orc_philox(const uint32_t* ctr, const uint32_t* key, uint32_t* out) {
     ttg_u32x4 c;
     for (int i = 0; i < 4; ++i) c.v[i] = ctr[i];

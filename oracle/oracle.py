@@ -89,6 +89,8 @@ def lib(use_blas=False):
         for f in ("orc_normals", "orc_uniforms", "orc_qnormals"):
             getattr(L, f).argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p]
         L.orc_philox.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_gram_entry.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_uint32]
+        L.orc_gram_entry.restype = ctypes.c_double
         _lib = L
     return _lib
 
@@ -143,6 +145,11 @@ def gram(N, alpha, seed):
     A = np.zeros((N, N), order="F")
     lib().orc_gen_gram(N, alpha, seed, A.ctypes.data)
     return A
+
+
+def gram_entry(N, i, j, alpha, seed):
+    """Entry (i, j) of A = G·Gᵀ/N + αI, computed on its own."""
+    return lib().orc_gram_entry(N, i, j, alpha, seed)
 
 
 def gemm_inputs(N, inputs, seed):

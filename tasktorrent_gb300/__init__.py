@@ -73,7 +73,9 @@ class SolveOpts(ctypes.Structure):
 class SolveReport(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int32), ("outer", ctypes.c_int32), ("inner", ctypes.c_int32),
                 ("gmres_prec", ctypes.c_int32), ("bwd_err", ctypes.c_double), ("anorm_inf", ctypes.c_double),
-                ("factor_ms", ctypes.c_double), ("solve_ms", ctypes.c_double), ("remedy", ctypes.c_int32)]
+                ("factor_ms", ctypes.c_double), ("solve_ms", ctypes.c_double), ("remedy", ctypes.c_int32),
+                ("h2d_ms", ctypes.c_double), ("d2h_ms", ctypes.c_double), ("compute_ms", ctypes.c_double),
+                ("total_ms", ctypes.c_double)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -79,6 +79,7 @@ struct ttg_chol_plan {
     ttg_solver* solver = nullptr;
     double* d_b = nullptr;         // device B and X of ttg_chol_posv_host
     size_t host_b_elems = 0;
+    cudaEvent_t host_ev[4] = {};   // phase events of the host-buffer entry points
     long factor_gen = 0;   // incremented by every successful factorisation
     long solver_gen = -1;  // factorisation the solver's inverted tiles belong to
     // Frees whatever was allocated, so every early return of
@@ -95,6 +96,8 @@ struct ttg_chol_plan {
         if (mixed) ttg_mixed_state_destroy(mixed);
         if (solver) ttg_solver_destroy(solver);
         if (d_b) cudaFree(d_b);
+        for (cudaEvent_t e : host_ev)
+            if (e) cudaEventDestroy(e);
     }
 };
 
@@ -600,39 +603,72 @@ static ttg_status ensure_host_b(ttg_chol_plan* P, size_t blk) {
     return TTG_OK;
 }
 
+static ttg_status ensure_host_events(ttg_chol_plan* P) {
+    for (cudaEvent_t& e : P->host_ev)
+        if (!e) TTG_CUDA_CHECK(cudaEventCreate(&e));
+    return TTG_OK;
+}
+
+// Phase times of a host-buffer call (events 0..3 recorded around the copies).
+static void host_phases(ttg_chol_plan* P, ttg_solve_report* rep, std::chrono::steady_clock::time_point t0) {
+    if (!rep) return;
+    float a = 0.f, b = 0.f, c = 0.f;
+    cudaEventElapsedTime(&a, P->host_ev[0], P->host_ev[1]);
+    cudaEventElapsedTime(&c, P->host_ev[1], P->host_ev[2]);
+    cudaEventElapsedTime(&b, P->host_ev[2], P->host_ev[3]);
+    rep->h2d_ms = a;
+    rep->d2h_ms = b;
+    rep->compute_ms = c;
+    rep->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
 extern "C" ttg_status ttg_chol_solve_host(ttg_chol_plan* P, const double* h_B, double* h_X, const ttg_solve_opts* o,
                                          ttg_solve_report* rep, void* stream) {
     if (!P || !o || !h_B || !h_X || o->nrhs < 1 || o->nrhs > 16) return TTG_EINVAL;
+    const auto t0 = std::chrono::steady_clock::now();
     TTG_CUDA_CHECK(cudaSetDevice(P->ctx->device));
     cudaStream_t s = (cudaStream_t)stream;
     const size_t blk = (size_t)P->N * o->nrhs;
     ttg_status st = ensure_host_b(P, blk);
+    if (st == TTG_OK) st = ensure_host_events(P);
     if (st != TTG_OK) return st;
+    TTG_CUDA_CHECK(cudaEventRecord(P->host_ev[0], s));
     TTG_CUDA_CHECK(cudaMemcpyAsync(P->d_b, h_B, sizeof(double) * blk, cudaMemcpyHostToDevice, s));
+    TTG_CUDA_CHECK(cudaEventRecord(P->host_ev[1], s));
     st = ttg_chol_plan_solve(P, P->d_b, P->d_b + blk, o, rep, stream);
     if (st != TTG_OK && st != TTG_ENOCONV) return st;
+    TTG_CUDA_CHECK(cudaEventRecord(P->host_ev[2], s));
     TTG_CUDA_CHECK(cudaMemcpyAsync(h_X, P->d_b + blk, sizeof(double) * blk, cudaMemcpyDeviceToHost, s));
+    TTG_CUDA_CHECK(cudaEventRecord(P->host_ev[3], s));
     TTG_CUDA_CHECK(cudaStreamSynchronize(s));
+    host_phases(P, rep, t0);
     return st;
 }
 
 extern "C" ttg_status ttg_chol_posv_host(ttg_chol_plan* P, const double* h_tiles, const double* h_B, double* h_X,
                                         const ttg_solve_opts* o, ttg_solve_report* rep, void* stream) {
     if (!P || !o || !h_B || !h_X || o->nrhs < 1 || o->nrhs > 16) return TTG_EINVAL;
+    const auto t0 = std::chrono::steady_clock::now();
     TTG_CUDA_CHECK(cudaSetDevice(P->ctx->device));
     cudaStream_t s = (cudaStream_t)stream;
     const size_t blk = (size_t)P->N * o->nrhs;
     ttg_status sb = ensure_host_b(P, blk);
+    if (sb == TTG_OK) sb = ensure_host_events(P);
     if (sb != TTG_OK) return sb;
+    TTG_CUDA_CHECK(cudaEventRecord(P->host_ev[0], s));
     if (h_tiles) {
         TTG_CUDA_CHECK(cudaMemcpyAsync(P->pristine, h_tiles, sizeof(double) * P->elems, cudaMemcpyHostToDevice, s));
         if (P->solver) ttg_solver_input_changed(P->solver);
     }
     TTG_CUDA_CHECK(cudaMemcpyAsync(P->d_b, h_B, sizeof(double) * blk, cudaMemcpyHostToDevice, s));
+    TTG_CUDA_CHECK(cudaEventRecord(P->host_ev[1], s));
     ttg_status st = ttg_chol_posv(P, P->d_b, P->d_b + blk, o, rep, stream);
     if (st != TTG_OK && st != TTG_ENOCONV) return st;
+    TTG_CUDA_CHECK(cudaEventRecord(P->host_ev[2], s));
     TTG_CUDA_CHECK(cudaMemcpyAsync(h_X, P->d_b + blk, sizeof(double) * blk, cudaMemcpyDeviceToHost, s));
+    TTG_CUDA_CHECK(cudaEventRecord(P->host_ev[3], s));
     TTG_CUDA_CHECK(cudaStreamSynchronize(s));
+    host_phases(P, rep, t0);
     return st;
 }
 

@@ -197,3 +197,11 @@ def test_panel_limited_sample(limit):
     assert part["flops"] == pytest.approx(flops, rel=1e-12)
     c = limit * b
     assert np.array_equal(part["L"][:, :c], full["L"][:, :c])
+
+
+def test_gram_entry_equals_whole_matrix():
+    """One entry computed alone (the bench's spot check of a large input)
+    equals the same entry of the whole generated matrix."""
+    A = orc.gram(96, 1e-4, 2)
+    for i, j in [(0, 0), (95, 0), (50, 17), (95, 95), (33, 32)]:
+        assert orc.gram_entry(96, i, j, 1e-4, 2) == A[i, j]
