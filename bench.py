@@ -149,6 +149,8 @@ def cpu_factor_sample(tiles, args, steps, warmup):
     flops, fraction of N^3/3)."""
     from oracle import oracle as orc
     orc.lib(use_blas=True)
+    if orc.blas_name() == "loops":
+        raise RuntimeError("the CPU sample needs the host OpenBLAS (oracle loaded without it)")
     cores = os.cpu_count() or 1
     nb = args.n // args.block
     N = nb * args.block
@@ -184,6 +186,7 @@ def gram_tiles_host(args):
     import ctypes
     import numpy as np
     from oracle import oracle as orc
+    orc.lib(use_blas=True)  # the first load decides: the CPU samples use OpenBLAS
     nb = args.n // args.block
     N = nb * args.block
     b = args.block

@@ -125,6 +125,10 @@ typedef struct ttg_solve_opts {
     int32_t restart;    /* GMRES iterations per step (0 = 20, at most 60)              */
     int32_t gmres_prec; /* 0 auto (FP32 Krylov work, FP64 once FP32 stalls), 32, 64    */
     double inner_tol;   /* relative GMRES tolerance per step (0 = 1e-5)                */
+    int32_t residual;   /* products with A in the refinement: 0 auto (sliced for N >= 256),
+                           1 FP64 FMA (and double-float steering of early FP32 steps),
+                           2 sliced: FP64-accurate on the BF16 tensor cores
+                           (ttg_sliced_matmul), also for the FP64 Krylov operator    */
 } ttg_solve_opts;
 
 typedef struct ttg_solve_report {
@@ -164,6 +168,20 @@ ttg_status ttg_chol_posv_host(ttg_chol_plan* plan, const double* h_tiles, const 
  * copies use (hi = fl32(v), lo = fl32(v - hi), bit for bit), computed on the
  * host by the same source as the device kernels: n values of v -> hi, lo. */
 ttg_status ttg_split_f64_f32(const double* v, int64_t n, float* hi, float* lo);
+
+/* Y = Aᵀ·X (mode 0) or Y = B − Aᵀ·X (mode 2) with FP64 accuracy on the BF16
+ * tensor cores; for the symmetric matrices of the solver Aᵀ·X = A·X.  d_A:
+ * dense N×N column-major FP64; d_X, d_B, d_Y: N×nrhs column-major (ld N),
+ * nrhs 1..16; all device pointers.  Each column of A is scaled by its largest
+ * magnitude and cut into eight signed base-256 digits (BF16 integers), each
+ * column of X likewise; the digit products are summed exactly (integer
+ * partial sums below 2^24 in the FP32 accumulator, int64 across K), and only
+ * the final combination of the eight digit groups and the scaling round in
+ * FP64 (Ozaki, Ogita, Oishi, Rump, Numer. Algorithms 59, 2012).  Allocates
+ * its workspace (16·N² bytes of digits) for the call.  Replaces the
+ * cblas_dgemv/dgemm products of the solve check, 2d_cholesky.cpp:646-689. */
+ttg_status ttg_sliced_matmul(ttg_ctx* ctx, int32_t N, const double* d_A, int32_t nrhs, const double* d_X, const double* d_B,
+                             double* d_Y, int32_t mode, void* stream);
 
 /* Arguments of 2d_gemm (2d_gemm.cpp:243-253) at one rank. */
 typedef struct ttg_gemm_args {

@@ -67,7 +67,8 @@ class GemmArgs(ctypes.Structure):
 
 class SolveOpts(ctypes.Structure):
     _fields_ = [("nrhs", ctypes.c_int32), ("tol", ctypes.c_double), ("max_outer", ctypes.c_int32),
-                ("restart", ctypes.c_int32), ("gmres_prec", ctypes.c_int32), ("inner_tol", ctypes.c_double)]
+                ("restart", ctypes.c_int32), ("gmres_prec", ctypes.c_int32), ("inner_tol", ctypes.c_double),
+                ("residual", ctypes.c_int32)]
 
 
 class SolveReport(ctypes.Structure):
@@ -184,6 +185,7 @@ SIGNATURES = {
     "ttg_chol_posv": (_STATUS, [_P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveReport), _P]),
     "ttg_chol_posv_host": (_STATUS, [_P, _P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveReport), _P]),
     "ttg_split_f64_f32": (_STATUS, [_P, ctypes.c_int64, _P, _P]),
+    "ttg_sliced_matmul": (_STATUS, [_P, _I32, _P, _I32, _P, _P, _P, _I32, _P]),
     "ttg_chol_solve_host": (_STATUS, [_P, _P, _P, ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveReport), _P]),
     "ttg_gemm_plan_create": (_STATUS, [_P, ctypes.POINTER(GemmArgs), ctypes.POINTER(_P)]),
     "ttg_gemm_plan_destroy": (_STATUS, [_P]),
@@ -397,14 +399,16 @@ class CholPlan:
     def dump_dag(self, prefix):
         check(lib().ttg_chol_plan_dump_dag(self.h, prefix.encode()), "dump_dag")
 
-    def solve_host(self, B, tiles=None, tol=1e-14, max_outer=10, restart=20, gmres_prec=0, inner_tol=0.0, factor=True):
+    def solve_host(self, B, tiles=None, tol=1e-14, max_outer=10, restart=20, gmres_prec=0, inner_tol=0.0, factor=True,
+                   residual=0):
         """Factor (unless factor=False) and solve A X = B with host arrays
-        (B: N×nrhs).  Returns (status, SolveReport, X)."""
+        (B: N×nrhs).  residual: 0 auto, 1 FP64 FMA, 2 sliced tensor-core
+        products.  Returns (status, SolveReport, X)."""
         B = np.asfortranarray(B, dtype=np.float64)
         if B.ndim == 1:
             B = B.reshape(-1, 1, order="F")
         X = np.zeros_like(B, order="F")
-        o = SolveOpts(B.shape[1], tol, max_outer, restart, gmres_prec, inner_tol)
+        o = SolveOpts(B.shape[1], tol, max_outer, restart, gmres_prec, inner_tol, residual)
         rep = SolveReport()
         if factor:
             st = lib().ttg_chol_posv_host(self.h, _ptr(tiles) if tiles is not None else None, _ptr(B), _ptr(X),

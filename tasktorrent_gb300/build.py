@@ -24,7 +24,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "--expt-relaxed-constexpr"]
 
-CU_SOURCES = ["ttg_exec.cu", "ttg_gen.cu", "ttg_mixed.cu", "ttg_solve.cu", "ttg_noalloc.cu", "ttg_batch.cu", "ttg_serve.cu"]
+CU_SOURCES = ["ttg_exec.cu", "ttg_gen.cu", "ttg_mixed.cu", "ttg_solve.cu", "ttg_sliced.cu", "ttg_noalloc.cu", "ttg_batch.cu",
+              "ttg_serve.cu"]
 CPP_SOURCES = ["apps.cpp"]
 MINIAPPS = ["2d_cholesky.cpp", "2d_gemm.cpp", "ttor_wait.cpp", "ttor_deps.cpp"]
 

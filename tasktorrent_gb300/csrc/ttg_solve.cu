@@ -30,6 +30,7 @@
 #include "../../include/ttg_apps.h"
 #include "solve_kernels.cuh"
 #include "ttg_internal.h"
+#include "ttg_sliced_api.h"
 #include "ttg_solve_api.h"
 
 using namespace ttg;
@@ -78,6 +79,11 @@ struct ttg_solver {
     DevBuf<float> A32lo;  // fl32(A - A32): the double-float matvec of FP64 Krylov work
     bool dense_valid = false;
     bool lo_valid = false;
+    // Digits of A for the FP64-accurate tensor-core products (built from A64
+    // when first needed after an input change).
+    ttg_sliced* sl = nullptr;
+    bool sl_valid = false;
+    bool use_sliced = false;  // this solve's products with A are sliced
     double anorm_inf = 0.0;
     // Operands of the sweeps for the current factor: L_ii⁻ᵀ and L_ii⁻¹
     // (compact diagonal tiles at doff) and the transposed off-diagonal tiles
@@ -286,6 +292,7 @@ void ttg_solver_destroy(ttg_solver* S) {
     S->d_tdesc_diag.release();
     S->d_tsub_off.release();
     S->d_tsub_diag.release();
+    if (S->sl) ttg_sliced_destroy(S->sl);
     delete S;
 }
 
@@ -296,7 +303,17 @@ extern "C" ttg_status ttg_split_f64_f32(const double* v, int64_t n, float* hi, f
 }
 
 void ttg_solver_input_changed(ttg_solver* S) {
-    if (S) S->dense_valid = S->lo_valid = false;
+    if (S) S->dense_valid = S->lo_valid = S->sl_valid = false;
+}
+
+// Digits of the dense copy for the sliced products (after ensure_dense).
+static ttg_status ensure_sliced(ttg_solver* S, cudaStream_t s) {
+    if (S->sl_valid) return TTG_OK;
+    ttg_status st;
+    if (!S->sl && (st = ttg_sliced_create(S->ctx, S->N, &S->sl)) != TTG_OK) return st;
+    if ((st = ttg_sliced_set_matrix(S->sl, S->A64.p, s)) != TTG_OK) return st;
+    S->sl_valid = true;
+    return TTG_OK;
 }
 
 // Dense copies of A (FP64, and FP32 for the mixed path) and ‖A‖∞.
@@ -534,8 +551,9 @@ ttg_status axpby(ttg_solver* S, const std::vector<double>& a, const TX* X, const
 // Backward errors ‖R_q‖∞ / (‖A‖∞ ‖X_q‖∞) of the current X (R = B − A X).
 ttg_status backward_errors(ttg_solver* S, int nrhs, cudaStream_t s, std::vector<double>& be, std::vector<double>& rnorm,
                            bool df = false) {
-    ttg_status st = df ? matmul_df(S, S->X.p, S->R.p, nrhs, s, S->B.p, 2)
-                       : matmul<double>(S, S->A64.p, S->X.p, S->B.p, S->R.p, S->P.p, nrhs, 2, s);
+    ttg_status st = df              ? matmul_df(S, S->X.p, S->R.p, nrhs, s, S->B.p, 2)
+                    : S->use_sliced ? ttg_sliced_matmul_run(S->sl, S->X.p, nrhs, S->B.p, S->R.p, 2, s)
+                                    : matmul<double>(S, S->A64.p, S->X.p, S->B.p, S->R.p, S->P.p, nrhs, 2, s);
     if (st != TTG_OK) return st;
     std::vector<double> xn(nrhs);
     rnorm.assign(nrhs, 0.0);
@@ -600,7 +618,11 @@ ttg_status gmres_cycle(ttg_solver* S, const float* L32, int nrhs, int m, double 
         // w = M⁻¹ (A v_k); FP64 Krylov vectors take A v_k in double-float
         // arithmetic (FP32 instruction rate, ~2^-46 accurate).
         if constexpr (sizeof(TG) == 8) {
-            if ((st = matmul_df(S, (const double*)vk, (double*)t1, nrhs, s)) != TTG_OK) return st;
+            if (S->use_sliced) {
+                if ((st = ttg_sliced_matmul_run(S->sl, (const double*)vk, nrhs, nullptr, (double*)t1, 0, s)) != TTG_OK) return st;
+            } else if ((st = matmul_df(S, (const double*)vk, (double*)t1, nrhs, s)) != TTG_OK) {
+                return st;
+            }
         } else {
             if ((st = matmul<TG>(S, A, vk, nullptr, t1, t3, nrhs, 0, s)) != TTG_OK) return st;
         }
@@ -710,6 +732,11 @@ ttg_status ttg_solver_solve(ttg_solver* S, const double* pristine, const double*
     clk.mark("buffers");
     if ((st = ensure_dense(S, pristine, s)) != TTG_OK) return st;
     clk.mark("dense copies of A");
+    S->use_sliced = o->residual == 2 || (o->residual == 0 && S->N >= 256);
+    if (S->use_sliced) {
+        if ((st = ensure_sliced(S, s)) != TTG_OK || (st = ttg_sliced_reset_err(S->sl, s)) != TTG_OK) return st;
+        clk.mark("digits of A");
+    }
     TTG_CUDA_CHECK(cudaMemcpyAsync(S->B.p, d_B, sizeof(double) * blk, cudaMemcpyDeviceToDevice, s));
     const double tol = o->tol > 0 ? o->tol : 1e-14;
     const int max_outer = o->max_outer > 0 ? o->max_outer : 10;
@@ -758,7 +785,7 @@ ttg_status ttg_solver_solve(ttg_solver* S, const double* pristine, const double*
         constexpr double kContraction = 1e-2;  // assumed gain of one cycle, for choosing the next residual
         double expect = INFINITY;              // predicted backward error of the current X
         for (int outer = 0;; ++outer) {
-            bool df = S->lo_valid && prec == 32 && expect >= kDfTrust;
+            bool df = !S->use_sliced && S->lo_valid && prec == 32 && expect >= kDfTrust;
             if ((st = backward_errors(S, nrhs, s, be, rn, df)) != TTG_OK) return st;
             double worst = *std::max_element(be.begin(), be.end());
             // A cycle that gains as much as the last one would land near the
@@ -770,7 +797,7 @@ ttg_status ttg_solver_solve(ttg_solver* S, const double* pristine, const double*
                 if ((st = backward_errors(S, nrhs, s, be, rn)) != TTG_OK) return st;
                 worst = *std::max_element(be.begin(), be.end());
             }
-            clk.mark(df ? "double-float residual" : "FP64 residual");
+            clk.mark(df ? "double-float residual" : S->use_sliced ? "sliced FP64 residual" : "FP64 residual");
             if (solve_verbose()) fprintf(stderr, "[ttg solve] outer %d backward error %.3e%s\n", outer, worst, df ? " (double-float)" : "");
             if (worst <= tol) break;
             expect = worst * kContraction;
@@ -807,10 +834,11 @@ ttg_status ttg_solver_solve(ttg_solver* S, const double* pristine, const double*
     r.bwd_err = be.empty() ? 0.0 : *std::max_element(be.begin(), be.end());
     r.anorm_inf = S->anorm_inf;
     TTG_CUDA_CHECK(cudaMemcpyAsync(d_X, S->X.p, sizeof(double) * blk, cudaMemcpyDeviceToDevice, s));
-    int h_err = 0;
-    TTG_CUDA_CHECK(cudaMemcpyAsync(&h_err, S->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    int h_err[2] = {0, 0};
+    TTG_CUDA_CHECK(cudaMemcpyAsync(&h_err[0], S->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (S->use_sliced) TTG_CUDA_CHECK(cudaMemcpyAsync(&h_err[1], ttg_sliced_err(S->sl), sizeof(int), cudaMemcpyDeviceToHost, s));
     TTG_CUDA_CHECK(cudaStreamSynchronize(s));
-    if (h_err) r.status = TTG_ETIMEOUT;  // a sweep gave up waiting: X is not valid
+    if (h_err[0] || h_err[1]) r.status = TTG_ETIMEOUT;  // a sweep or a product gave up waiting: X is not valid
     if (rep) *rep = r;
     return r.status;
 }
