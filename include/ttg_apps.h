@@ -129,6 +129,8 @@ typedef struct ttg_solve_opts {
                            1 FP64 FMA (and double-float steering of early FP32 steps),
                            2 sliced: FP64-accurate on the BF16 tensor cores
                            (ttg_sliced_matmul), also for the FP64 Krylov operator    */
+    int32_t refine;     /* mixed plans: 0 auto — classic steps x += M⁻¹ r while each
+                           gains 10×, then GMRES; 1 GMRES from the first step        */
 } ttg_solve_opts;
 
 typedef struct ttg_solve_report {

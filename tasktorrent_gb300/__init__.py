@@ -68,7 +68,7 @@ class GemmArgs(ctypes.Structure):
 class SolveOpts(ctypes.Structure):
     _fields_ = [("nrhs", ctypes.c_int32), ("tol", ctypes.c_double), ("max_outer", ctypes.c_int32),
                 ("restart", ctypes.c_int32), ("gmres_prec", ctypes.c_int32), ("inner_tol", ctypes.c_double),
-                ("residual", ctypes.c_int32)]
+                ("residual", ctypes.c_int32), ("refine", ctypes.c_int32)]
 
 
 class SolveReport(ctypes.Structure):
@@ -400,15 +400,16 @@ class CholPlan:
         check(lib().ttg_chol_plan_dump_dag(self.h, prefix.encode()), "dump_dag")
 
     def solve_host(self, B, tiles=None, tol=1e-14, max_outer=10, restart=20, gmres_prec=0, inner_tol=0.0, factor=True,
-                   residual=0):
+                   residual=0, refine=0):
         """Factor (unless factor=False) and solve A X = B with host arrays
         (B: N×nrhs).  residual: 0 auto, 1 FP64 FMA, 2 sliced tensor-core
-        products.  Returns (status, SolveReport, X)."""
+        products; refine: 0 classic steps then GMRES, 1 GMRES only.
+        Returns (status, SolveReport, X)."""
         B = np.asfortranarray(B, dtype=np.float64)
         if B.ndim == 1:
             B = B.reshape(-1, 1, order="F")
         X = np.zeros_like(B, order="F")
-        o = SolveOpts(B.shape[1], tol, max_outer, restart, gmres_prec, inner_tol, residual)
+        o = SolveOpts(B.shape[1], tol, max_outer, restart, gmres_prec, inner_tol, residual, refine)
         rep = SolveReport()
         if factor:
             st = lib().ttg_chol_posv_host(self.h, _ptr(tiles) if tiles is not None else None, _ptr(B), _ptr(X),

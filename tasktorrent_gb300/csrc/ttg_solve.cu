@@ -16,6 +16,8 @@
 //           x += d in FP64.
 // All RHS columns run in lockstep; each column has its own Krylov space and
 // Hessenberg matrix (solved on the host; they are tiny).
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -29,6 +31,7 @@
 #include "../../include/ttg.h"
 #include "../../include/ttg_apps.h"
 #include "solve_kernels.cuh"
+#include "sweep_tma.cuh"
 #include "ttg_internal.h"
 #include "ttg_sliced_api.h"
 #include "ttg_solve_api.h"
@@ -116,7 +119,37 @@ struct ttg_solver {
     DevBuf<float> Vf;   // Krylov basis, FP32 variant
     DevBuf<double> part, colv, coefA, coefB;
     int sweep_grid64 = 0, sweep_grid32 = 0, sweep_grid_mix = 0;
+    // FP32 sweeps with TMA-staged strips (uniform tiles, edge a multiple of
+    // 128 and at most 512): the operand maps of both directions, rebuilt
+    // when an operand pointer changes.
+    int tma_b = 0;  // 0: this layout takes the generic sweep kernel
+    SweepMaps tma_maps[2];
+    const void* tma_keys[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
 };
+
+// 2D FP32 tensor map of an array of b-row column-major tiles: (row, column)
+// with the b rows inner; box 64 rows × kTmaCols columns.
+static ttg_status encode_strip_map(CUtensorMap* map, const float* base, int64_t elems, int b) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || !fn || q != cudaDriverEntryPointSuccess) {
+        ttg_set_last_cuda_error(e, "cudaGetDriverEntryPointByVersion(cuTensorMapEncodeTiled)", __FILE__, __LINE__);
+        return TTG_ECUDA;
+    }
+    auto enc = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    cuuint64_t dims[2] = {(cuuint64_t)b, (cuuint64_t)std::max<int64_t>(1, elems / b)};
+    cuuint64_t strides[1] = {(cuuint64_t)b * 4};
+    cuuint32_t box[2] = {(cuuint32_t)kStrip, (cuuint32_t)kTmaCols};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                     CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        ttg_set_last_cuda_error(cudaErrorInvalidValue, "cuTensorMapEncodeTiled (sweep strips)", __FILE__, __LINE__);
+        return TTG_EINVAL;
+    }
+    return TTG_OK;
+}
 
 template <class T, class TM>
 static ttg_status sweep_grid(ttg_solver* S, int* grid) {
@@ -134,6 +167,7 @@ static ttg_status solver_init(ttg_solver* S) {
     if ((st = sweep_grid<double, double>(S, &S->sweep_grid64)) != TTG_OK) return st;
     if ((st = sweep_grid<float, float>(S, &S->sweep_grid32)) != TTG_OK) return st;
     if ((st = sweep_grid<double, float>(S, &S->sweep_grid_mix)) != TTG_OK) return st;
+    TTG_CUDA_CHECK(cudaFuncSetAttribute(sweep_kernel_f32_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, kTmaSmem));
     const int smem = kF64SmemDoubles * (int)sizeof(double);
     TTG_CUDA_CHECK(cudaFuncSetAttribute(invert_diag_tiles<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     TTG_CUDA_CHECK(cudaFuncSetAttribute(invert_diag_tiles<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
@@ -176,6 +210,11 @@ static ttg_status solver_tables(ttg_solver* S, const int* bs, const int64_t* off
     }
     S->items_fwd = fwd[nb];
     S->items_bwd = bwd[nb];
+    {
+        bool uni = bs[0] % 128 == 0 && bs[0] <= kTmaMaxK;
+        for (int i = 1; i < nb; ++i) uni = uni && bs[i] == bs[0];
+        S->tma_b = uni ? bs[0] : 0;
+    }
     // W products of the folded sweeps: forward W_i (i >= 1) = linv_i · L(i, i-1);
     // backward W_i (i <= nb-2) = inv_i · L(i+1, i)ᵀ (the transposed tile at
     // off[(i+1) + i·nb], ld bs[i]).
@@ -426,6 +465,28 @@ ttg_status sweeps(ttg_solver* S, const TM* L, const TM* LT, const TM* Linv, cons
         if (st != TTG_OK) return st;
     }
     const int smem = sweep_smem_bytes<T, TM>();
+    constexpr bool f32 = sizeof(T) == 4 && sizeof(TM) == 4;
+    const bool tma = f32 && S->tma_b > 0;
+    if constexpr (f32) {
+        if (tma) {
+            // Operand maps of the two directions (forward: L, L_ii⁻¹, W_f;
+            // backward: Lᵀ tiles, L_ii⁻ᵀ, W_b), rebuilt when a pointer changes.
+            const void* keys[2][3] = {{L, Linv, S->wf32.p}, {LT, invT, S->wb32.p}};
+            const int64_t n3[3] = {S->elems, S->dsize, 0};
+            for (int dir = 0; dir < 2; ++dir) {
+                if (std::equal(keys[dir], keys[dir] + 3, S->tma_keys[dir])) continue;
+                SweepMaps& m = S->tma_maps[dir];
+                m.b = S->tma_b;
+                ttg_status st;
+                if ((st = encode_strip_map(&m.mu, (const float*)keys[dir][0], n3[0], m.b)) != TTG_OK ||
+                    (st = encode_strip_map(&m.md, (const float*)keys[dir][1], n3[1], m.b)) != TTG_OK ||
+                    (st = encode_strip_map(&m.wd, (const float*)keys[dir][2], std::max<int64_t>(dir ? S->wsize_b : S->wsize_f, m.b),
+                                           m.b)) != TTG_OK)
+                    return st;
+                std::copy(keys[dir], keys[dir] + 3, S->tma_keys[dir]);
+            }
+        }
+    }
     for (int dir = 0; dir < 2; ++dir) {
         int* ctr = S->d_sweep_ctr.p + dir * region;
         a.claim = ctr;
@@ -438,6 +499,15 @@ ttg_status sweeps(ttg_solver* S, const TM* L, const TM* LT, const TM* Linv, cons
         if (sweep_trace_path()) a.trace = S->d_trace.p + (dir ? 4 * (size_t)S->items_fwd : 0);
         const TM* W = nullptr;
         if constexpr (fold) W = dir ? S->wb32.p : S->wf32.p;
+        if constexpr (f32) {
+            if (tma) {
+                ttg_note_launch();
+                if (dir == 0) sweep_kernel_f32_tma<<<S->ctx->sms, 256, kTmaSmem, s>>>(a, S->tma_maps[0], (float*)R, (float*)Y);
+                else sweep_kernel_f32_tma<<<S->ctx->sms, 256, kTmaSmem, s>>>(a, S->tma_maps[1], (float*)Y, (float*)X);
+                TTG_CUDA_CHECK(cudaGetLastError());
+                continue;
+            }
+        }
         if (dir == 0) {
             ttg_note_launch();
             sweep_kernel<T, TM><<<grid, 256, smem, s>>>(a, L, Linv, W, R, Y);
@@ -765,6 +835,7 @@ ttg_status ttg_solver_solve(ttg_solver* S, const double* pristine, const double*
         clk.mark("x0 = M^-1 b (FP32 sweeps)");
         int prec = o->gmres_prec == 64 ? 64 : 32;
         double prev = INFINITY;
+        bool richardson = o->refine == 0 && prec == 32, after_richardson = false;
         // Relative GMRES tolerance per cycle: FP32 cycles gain ~1e-3 whatever
         // it is (their arithmetic bounds them), and 1e-5 ends them one
         // iteration earlier than 1e-6 at equal refinement steps (N = 32768,
@@ -807,8 +878,32 @@ ttg_status ttg_solver_solve(ttg_solver* S, const double* pristine, const double*
                 r.status = TTG_ENOCONV;
                 break;
             }
-            // Switch to FP64 Krylov work when FP32 stops gaining (auto mode).
-            if (o->gmres_prec == 0 && prec == 32 && outer > 0 && worst > 0.1 * prev) prec = 64;
+            // Classic refinement first (auto mode): x += M⁻¹ r, one pair of
+            // FP32 sweeps per step, while each step gains at least 10×; a
+            // step that gains less hands over to GMRES for the rest.
+            if (richardson && outer > 0 && worst > 0.1 * prev) {
+                richardson = false;
+                after_richardson = true;
+                if (solve_verbose()) fprintf(stderr, "[ttg solve] outer %d: refinement step gained %.3g, GMRES from here\n", outer,
+                                             prev / worst);
+            }
+            if (richardson) {
+                std::vector<double> inv(nrhs), ones(nrhs, 1.0);
+                for (int q = 0; q < nrhs; ++q) inv[q] = rn[q] > 0 ? 1.0 / rn[q] : 0.0;
+                if ((st = axpby<double, float>(S, inv, S->R.p, nullptr, S->f1.p, nrhs, s)) != TTG_OK) return st;
+                if ((st = sweeps<float, float>(S, L32, S->lt32.p, S->linv32.p, S->inv32.p, S->f1.p, S->f2.p, S->f3.p, nrhs,
+                                               S->sweep_grid32, s)) != TTG_OK)
+                    return st;
+                if ((st = axpby<float, double>(S, rn, S->f3.p, &ones, S->X.p, nrhs, s)) != TTG_OK) return st;
+                clk.mark("refinement step (FP32 sweeps)");
+                r.outer = outer + 1;
+                prev = worst;
+                continue;
+            }
+            // Switch to FP64 Krylov work when FP32 stops gaining (auto mode;
+            // not on the first GMRES cycle after classic steps stalled).
+            if (o->gmres_prec == 0 && prec == 32 && outer > 0 && worst > 0.1 * prev && !after_richardson) prec = 64;
+            after_richardson = false;
             prev = worst;
             if (df && prec == 64) {  // an FP64 Krylov cycle is steered by an FP64 residual
                 if ((st = backward_errors(S, nrhs, s, be, rn)) != TTG_OK) return st;

@@ -198,3 +198,24 @@ def test_host_tiles_replace_the_input(ctx, mk):
     assert np.array_equal(X3, X2)
     p.close()
     q.close()
+
+
+@pytest.mark.parametrize("alpha", [1.0, 1e-4, 1e-8])
+def test_classic_steps_then_gmres(ctx, alpha):
+    """refine 0 (classic steps x += M⁻¹r while each gains 10×, then GMRES) and
+    refine 1 (GMRES from the start) both reach the FP64 backward error; a
+    well-conditioned matrix needs no GMRES iteration at all."""
+    p = t.CholPlan(ctx, 128, 6, matrix=1, alpha=alpha, seed=2, precision=t.PREC_MIXED, mixed_kind=2)
+    A = p.input_A()
+    B = np.random.default_rng(4).standard_normal((p.N, 8))
+    reps = {}
+    for refine in (0, 1):
+        st, rep, X = p.solve_host(B, tol=BWD, max_outer=30, restart=30, refine=refine)
+        assert st == t.TTG_OK, (refine, rep.as_dict())
+        R = B - A @ X
+        bwd = np.max(np.abs(R).max(axis=0) / (np.abs(A).sum(axis=1).max() * np.abs(X).max(axis=0)))
+        assert bwd <= BWD and rep.bwd_err <= BWD
+        reps[refine] = rep
+    if alpha == 1.0:
+        assert reps[0].inner == 0, reps[0].as_dict()
+    p.close()
