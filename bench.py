@@ -533,10 +533,12 @@ def run_ours(args, world, rank, local):
                                                           "remedy": last.remedy, "factor_ms": last.factor_ms},
                 "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
                              "frac": achieved / bf16_peak,
-                             # ncu capture of one N=8192 factorisation (profiles/exec_kernel_mixed_cholesky_n8192_full.md):
-                             # 1.413 GB of DRAM traffic, scaled by the tile-update count (N^3) to this N.
-                             "traffic": 1.413e9 * (N / 8192.0) ** 3,
-                             "traffic_note": "bytes per launch, from an N=8192 ncu capture scaled by (N/8192)^3",
+                             # ncu capture of one N=16384 factorisation of this kernel: 15.28 GB of
+                             # DRAM traffic, 13.63 GB of it growing with the update-task count
+                             # (C tiles and operand slices) and 1.65 GB with N^2 (input conversion).
+                             "traffic": 13.63e9 * ((nb - 1) * nb * (nb + 1) / 6) / 5456.0 + 1.65e9 * (N / 16384.0) ** 2,
+                             "traffic_note": "DRAM bytes per factorisation launch: an N=16384 ncu capture (15.28 GB) "
+                                             "scaled by the update-task count and N^2",
                              "kernel": "exec_kernel_mixed (launches of one factorisation, all remedy attempts); "
                                        "achieved = N^3/3 / their duration",
                              "peak_source": "measured: MEASURED_PEAKS.json bf16_tflops (burst)"},
