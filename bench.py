@@ -457,8 +457,9 @@ def run_ours(args, world, rank, local):
                "h2d_bytes_per_step": elems * 8 + N * nrhs * 8, "d2h_bytes_per_step": N * nrhs * 8,
                "steps": e2e_steps, "ms_per_step": e2e_s * 1e3,
                "phases_ms": {k: statistics.mean(v) for k, v in phases.items()},
-               "phases_note": "per call, mean: h2d (tiles + B, events), compute (factor + solve + refinement, events), "
-                              "factor (executor kernels), solve (host clock), d2h (X, events), total (host clock)"}
+               "phases_note": "per call, mean: h2d (the input tiles streaming in on a copy stream while the "
+                              "factorisation runs, events), compute (factor + solve + refinement, events), factor (executor "
+                              "kernels), solve (host clock), d2h (X, events), total (host clock)"}
         if world == 1 and not args.no_cpu_baseline:
             host_tiles = hin.numpy().copy()
         del hin, hB, hX

@@ -81,7 +81,9 @@ enum {
     TTG_OP_TRSM_RLNN = 7, /* c[m×n] <- alpha c · a⁻¹, a[n×n] lower non-unit (cblas_dtrsm R,L,N,N):
                              the backward step of a block solve with row-vector RHS */
     TTG_OP_CONVERT = 8,   /* c[m×n] <- alpha a + beta c with a and c of either precision:
-                             flags bit 0 = a is float, bit 1 = c is float (prec F64) */
+                             flags bit 0 = a is float, bit 1 = c is float; bit 2 (mixed-precision
+                             plans' input tasks) = first wait until word 1 + k of the uint32
+                             array aux equals its word 0 (the tile column has arrived) */
     TTG_OP_SPIN = 9       /* the block spins for alpha seconds (0 <= alpha <= 1): the
                              task body of the scheduler micro-benchmarks
                              (miniapp/mini_benchmarks/shared/ttor_wait.cpp, ttor_deps.cpp,

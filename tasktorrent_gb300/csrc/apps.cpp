@@ -12,6 +12,7 @@
 // The flows, indegrees, keys and names must equal the reference's for the
 // graph to be the same graph; the task bodies call the ttor::gpu spellings of
 // the same BLAS/LAPACK routines on device tiles.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -80,6 +81,13 @@ struct ttg_chol_plan {
     double* d_b = nullptr;         // device B and X of ttg_chol_posv_host
     size_t host_b_elems = 0;
     cudaEvent_t host_ev[4] = {};   // phase events of the host-buffer entry points
+    // Mixed plans: the first attempt's graph converts its input column by
+    // column (input tasks gated on arrival), so a host input can stream in
+    // while the factorisation runs.
+    bool input_tasks = false;
+    bool streaming = false;        // this factorisation's input is still arriving
+    cudaStream_t copy_s = nullptr; // host input copies
+    cudaEvent_t copy_ev[3] = {};   // start on the caller's stream, diagonal tiles in, all in
     long factor_gen = 0;   // incremented by every successful factorisation
     long solver_gen = -1;  // factorisation the solver's inverted tiles belong to
     // Frees whatever was allocated, so every early return of
@@ -98,6 +106,9 @@ struct ttg_chol_plan {
         if (d_b) cudaFree(d_b);
         for (cudaEvent_t e : host_ev)
             if (e) cudaEventDestroy(e);
+        for (cudaEvent_t e : copy_ev)
+            if (e) cudaEventDestroy(e);
+        if (copy_s) cudaStreamDestroy(copy_s);
     }
 };
 
@@ -270,6 +281,44 @@ static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry, int upd, std::uni
     return TTG_OK;
 }
 
+// The first attempt's graph of a mixed plan converts its own input: one
+// input task per tile column j (FP64 plan input -> FP32 working tiles) that
+// the column's first tasks wait for — POTRF_0 and TRSM_i_0 for column 0,
+// GEMM_0_i_j for column j >= 1 (every later task of a tile depends on its
+// first).  The input task has the highest priority among its successors'.
+static ttg_status add_input_tasks(ttg_chol_plan* P) {
+    Threadpool_shared& tp = *P->tp;
+    const auto& nodes = tp.device_task_nodes();
+    const int nb = P->nb;
+    std::vector<std::vector<int>> succ(nb);
+    std::vector<double> prio(nb, -1e300);
+    std::vector<int> seen(tp.n_nodes(), 0);
+    for (size_t d = 0; d < nodes.size(); ++d) {
+        if (seen[nodes[d]]++) continue;  // the node's first device task only
+        const std::string nm = tp.node_name(nodes[d]);
+        int col = -1, a = 0, b = 0, c = 0;
+        if (sscanf(nm.c_str(), "POTRF_%d", &a) == 1 && nm[0] == 'P') col = a == 0 ? 0 : -1;
+        else if (sscanf(nm.c_str(), "TRSM_%d_%d", &a, &b) == 2) col = b == 0 ? 0 : -1;
+        else if (sscanf(nm.c_str(), "GEMM_%d_%d_%d", &a, &b, &c) == 3) col = a == 0 ? c : -1;
+        if (col < 0) continue;
+        succ[col].push_back((int)d);
+        prio[col] = std::max(prio[col], tp.device_priority((int)d));
+    }
+    std::vector<ttg_op> ops(nb);
+    for (int j = 0; j < nb; ++j) {
+        if (succ[j].empty()) return TTG_OK;  // not the expected graph: keep the separate conversion
+        ops[j] = ttg_mixed_input_op(P->mixed, j, P->pristine);
+    }
+    try {
+        tp.add_device_tasks(ops, prio, succ);
+    } catch (const std::exception& e) {
+        fprintf(stderr, "ttg_chol_plan: %s\n", e.what());
+        return TTG_ECUDA;
+    }
+    P->input_tasks = true;
+    return TTG_OK;
+}
+
 extern "C" ttg_status ttg_chol_plan_create(ttg_ctx* ctx, const ttg_chol_args* args, ttg_chol_plan** out) {
     if (!ctx || !args || !out) return TTG_EINVAL;
     *out = nullptr;
@@ -309,6 +358,7 @@ extern "C" ttg_status ttg_chol_plan_create(ttg_ctx* ctx, const ttg_chol_args* ar
     ttg_status s = chol_build_graph(P.get(), false, first, P->tp);
     if (s == TTG_OK && tc) s = chol_build_graph(P.get(), false, TTG_UPD_FP32, P->tp32);
     if (s == TTG_OK && tc && first == TTG_UPD_BF16) s = chol_build_graph(P.get(), false, TTG_UPD_BF16X3, P->tpx3);
+    if (s == TTG_OK && P->mixed) s = add_input_tasks(P.get());
     if (s == TTG_OK) s = ttg_chol_plan_generate(P.get(), nullptr);
     if (s != TTG_OK) return s;  // P's destructor frees what was allocated
     *out = P.release();
@@ -451,9 +501,21 @@ static ttg_status chol_factor_from(ttg_chol_plan* P, void* stream, ttg_report* r
     if (tc && !first_x3) plan.push_back({P->tp.get(), 8.0 * 0.00390625, TTG_UPD_BF16, 1});
     ttg_status s = TTG_OK;
     float total_ms = 0.f;
+    const bool streamed = P->streaming;
     for (size_t a = std::min(first_attempt, plan.size() - 1); a < plan.size(); ++a) {
-        s = ttg_mixed_prepare(P->mixed, stream, plan[a].shift, plan[a].upd, P->pristine);
+        // The plan's first graph converts its input in its input tasks; a
+        // streamed input (ttg_chol_posv_host) opened the gate already.
+        // The plan's first graph has input tasks: they convert a streamed
+        // input (ttg_chol_posv_host opened the gate); for a resident input the
+        // conversion kernel runs and they only pass.
+        const bool graph_inputs = P->input_tasks && plan[a].tp == P->tp.get();
+        const bool in_graph = graph_inputs && P->streaming;
+        if (P->streaming && (!graph_inputs || plan[a].shift != 0.0)) return TTG_ESTATE;
+        if (!in_graph && streamed) TTG_CUDA_CHECK(cudaStreamWaitEvent((cudaStream_t)stream, P->copy_ev[2], 0));  // all copies in
+        s = ttg_mixed_prepare(P->mixed, stream, plan[a].shift, plan[a].upd, P->pristine, in_graph);
         if (s != TTG_OK) return s;
+        if (graph_inputs && !in_graph) ttg_mixed_gate_begin(P->mixed, stream, true);
+        P->streaming = false;  // a retry waits for the whole input
         s = plan[a].tp->replay(stream);
         const ttg_report r = plan[a].tp->report();
         total_ms += r.elapsed_ms;
@@ -645,6 +707,67 @@ extern "C" ttg_status ttg_chol_solve_host(ttg_chol_plan* P, const double* h_B, d
     return st;
 }
 
+// Enqueue a 32-bit store of v at addr on stream s, ordered after the
+// stream's earlier work (copies included): cuStreamWriteValue32 of the
+// driver API, which needs no SM (the persistent executor holds them all).
+static ttg_status stream_write_u32(cudaStream_t s, uint32_t* addr, uint32_t v) {
+    typedef CUresult (*write_fn)(CUstream, CUdeviceptr, cuuint32_t, unsigned int);
+    static write_fn fn = nullptr;
+    if (!fn) {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuStreamWriteValue32", &f, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess || !f || q != cudaDriverEntryPointSuccess) {
+            ttg_set_last_cuda_error(e, "cudaGetDriverEntryPointByVersion(cuStreamWriteValue32)", __FILE__, __LINE__);
+            return TTG_ECUDA;
+        }
+        fn = (write_fn)f;
+    }
+    if (fn((CUstream)s, (CUdeviceptr)addr, v, 0) != CUDA_SUCCESS) {
+        ttg_set_last_cuda_error(cudaErrorInvalidValue, "cuStreamWriteValue32", __FILE__, __LINE__);
+        return TTG_ECUDA;
+    }
+    return TTG_OK;
+}
+
+// Stream the host input tiles of a mixed plan into the plan input while the
+// factorisation runs: on a copy stream, the diagonal tiles first (the block-
+// row scales are computed from them before the launch), then each tile
+// column's remaining tiles, each followed by its arrival word; the input
+// tasks of the graph wait for the words.  Returns with the caller's stream
+// ordered after the diagonal tiles.
+static ttg_status stream_input(ttg_chol_plan* P, const double* h_tiles, cudaStream_t s) {
+    if (!P->copy_s) TTG_CUDA_CHECK(cudaStreamCreateWithFlags(&P->copy_s, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : P->copy_ev)
+        if (!e) TTG_CUDA_CHECK(cudaEventCreate(&e));
+    const uint32_t gen = ttg_mixed_gate_begin(P->mixed, s, false);
+    uint32_t* gate = ttg_mixed_gate(P->mixed);
+    TTG_CUDA_CHECK(cudaEventRecord(P->copy_ev[0], s));  // after the caller's earlier work and the new generation
+    TTG_CUDA_CHECK(cudaStreamWaitEvent(P->copy_s, P->copy_ev[0], 0));
+    TTG_CUDA_CHECK(cudaEventRecord(P->host_ev[0], P->copy_s));
+    const int nb = P->nb;
+    for (int j = 0; j < nb; ++j) {
+        const int64_t o = P->off[j + (size_t)j * nb];
+        TTG_CUDA_CHECK(cudaMemcpyAsync(P->pristine + o, h_tiles + o, sizeof(double) * P->bs[j] * P->bs[j], cudaMemcpyHostToDevice,
+                                       P->copy_s));
+    }
+    TTG_CUDA_CHECK(cudaEventRecord(P->copy_ev[1], P->copy_s));
+    for (int j = 0; j < nb; ++j) {
+        const int64_t o = P->off[j + (size_t)j * nb] + (int64_t)P->bs[j] * P->bs[j];
+        int64_t rest = 0;
+        for (int i = j + 1; i < nb; ++i) rest += (int64_t)P->bs[i] * P->bs[j];
+        if (rest > 0)
+            TTG_CUDA_CHECK(cudaMemcpyAsync(P->pristine + o, h_tiles + o, sizeof(double) * rest, cudaMemcpyHostToDevice, P->copy_s));
+        ttg_status st = stream_write_u32(P->copy_s, gate + 1 + j, gen);
+        if (st != TTG_OK) return st;
+    }
+    TTG_CUDA_CHECK(cudaEventRecord(P->copy_ev[2], P->copy_s));
+    TTG_CUDA_CHECK(cudaStreamWaitEvent(s, P->copy_ev[1], 0));
+    if (P->solver) ttg_solver_input_changed(P->solver);
+    P->streaming = true;
+    return TTG_OK;
+}
+
 extern "C" ttg_status ttg_chol_posv_host(ttg_chol_plan* P, const double* h_tiles, const double* h_B, double* h_X,
                                         const ttg_solve_opts* o, ttg_solve_report* rep, void* stream) {
     if (!P || !o || !h_B || !h_X || o->nrhs < 1 || o->nrhs > 16) return TTG_EINVAL;
@@ -655,6 +778,47 @@ extern "C" ttg_status ttg_chol_posv_host(ttg_chol_plan* P, const double* h_tiles
     ttg_status sb = ensure_host_b(P, blk);
     if (sb == TTG_OK) sb = ensure_host_events(P);
     if (sb != TTG_OK) return sb;
+    if (h_tiles && P->mixed && P->input_tasks) {
+        // The input streams in while the factorisation runs.
+        ttg_status st = stream_input(P, h_tiles, s);
+        if (st != TTG_OK) {
+            P->streaming = false;
+            cudaStreamSynchronize(P->copy_s);
+            return st;
+        }
+        TTG_CUDA_CHECK(cudaMemcpyAsync(P->d_b, h_B, sizeof(double) * blk, cudaMemcpyHostToDevice, s));
+        TTG_CUDA_CHECK(cudaEventRecord(P->host_ev[1], s));
+        ttg_report fr{};
+        st = ttg_chol_plan_factor(P, stream, &fr);
+        P->streaming = false;
+        // Whatever the outcome, the copies end before the input is used again.
+        cudaError_t ce = cudaStreamWaitEvent(s, P->copy_ev[2], 0);
+        if (st != TTG_OK) {
+            cudaStreamSynchronize(P->copy_s);
+            return st;
+        }
+        TTG_CUDA_CHECK(ce);
+        ttg_solve_report r{};
+        st = ttg_chol_plan_solve(P, P->d_b, P->d_b + blk, o, &r, stream);
+        r.factor_ms = fr.elapsed_ms;
+        if (rep) *rep = r;
+        if (st != TTG_OK && st != TTG_ENOCONV) return st;
+        TTG_CUDA_CHECK(cudaEventRecord(P->host_ev[2], s));
+        TTG_CUDA_CHECK(cudaMemcpyAsync(h_X, P->d_b + blk, sizeof(double) * blk, cudaMemcpyDeviceToHost, s));
+        TTG_CUDA_CHECK(cudaEventRecord(P->host_ev[3], s));
+        TTG_CUDA_CHECK(cudaStreamSynchronize(s));
+        if (rep) {
+            float a = 0.f, b = 0.f, c = 0.f;
+            cudaEventElapsedTime(&a, P->host_ev[0], P->copy_ev[2]);  // the whole input copy (overlapped)
+            cudaEventElapsedTime(&c, P->host_ev[1], P->host_ev[2]);
+            cudaEventElapsedTime(&b, P->host_ev[2], P->host_ev[3]);
+            rep->h2d_ms = a;
+            rep->compute_ms = c;
+            rep->d2h_ms = b;
+            rep->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        }
+        return st;
+    }
     TTG_CUDA_CHECK(cudaEventRecord(P->host_ev[0], s));
     if (h_tiles) {
         TTG_CUDA_CHECK(cudaMemcpyAsync(P->pristine, h_tiles, sizeof(double) * P->elems, cudaMemcpyHostToDevice, s));
@@ -681,7 +845,7 @@ extern "C" ttg_status ttg_chol_plan_dump_dag(ttg_chol_plan* P, const char* prefi
 extern "C" ttg_status ttg_chol_plan_kind_times(ttg_chol_plan* P, double* potrf_ms, double* trsm_ms, double* gemm_ms, double* accu_ms) {
     if (!P) return TTG_EINVAL;
     const int nd = (int)P->kind_of_dev.size();
-    std::vector<int64_t> s(nd), e(nd);
+    std::vector<int64_t> s(P->tp->n_uploaded_tasks()), e(P->tp->n_uploaded_tasks());
     ttg_status st = ttg_trace(P->ctx, s.data(), e.data(), nullptr);
     if (st != TTG_OK) return st;
     double t[4] = {0, 0, 0, 0};
@@ -697,18 +861,18 @@ extern "C" ttg_status ttg_chol_plan_kind_times(ttg_chol_plan* P, double* potrf_m
 extern "C" ttg_status ttg_chol_plan_trace_dump(ttg_chol_plan* P, const char* path) {
     if (!P || !path) return TTG_EINVAL;
     const auto& nodes = P->tp->device_task_nodes();
-    const int nd = (int)nodes.size();
-    std::vector<int64_t> s(nd), e(nd), busy(nd);
-    std::vector<int32_t> w(nd);
+    const int nd = (int)nodes.size(), nu = P->tp->n_uploaded_tasks();
+    std::vector<int64_t> s(nu), e(nu), busy(nu);
+    std::vector<int32_t> w(nu);
     ttg_status st = ttg_trace(P->ctx, s.data(), e.data(), w.data());
     if (st == TTG_OK) st = ttg_trace_busy(P->ctx, busy.data());
     if (st != TTG_OK) return st;
     FILE* f = fopen(path, "w");
     if (!f) return TTG_EINVAL;
     fprintf(f, "name,start_ns,end_ns,worker,busy_ns\n");
-    for (int d = 0; d < nd; ++d)
-        fprintf(f, "%s,%lld,%lld,%d,%lld\n", P->tp->node_name(nodes[d]).c_str(), (long long)s[d], (long long)e[d], w[d],
-                (long long)busy[d]);
+    for (int d = 0; d < nu; ++d)
+        fprintf(f, "%s,%lld,%lld,%d,%lld\n", d < nd ? P->tp->node_name(nodes[d]).c_str() : ("INPUT_" + std::to_string(d - nd)).c_str(),
+                (long long)s[d], (long long)e[d], w[d], (long long)busy[d]);
     fclose(f);
     return TTG_OK;
 }

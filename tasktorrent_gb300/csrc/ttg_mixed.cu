@@ -28,6 +28,11 @@ namespace ttg {
 
 // Mixed-op variants carried in ttg_op::flags.
 enum { kMixedF32 = 1, kMixedBF16 = 2, kMixedBF16x3 = 3 };
+// TTG_OP_CONVERT flags: a is float, c is float, and (mixed graphs) wait for
+// the task's input column to arrive first (gate words in aux, column in k).
+enum { kConvertAFloat = 1, kConvertCFloat = 2, kConvertGated = 4 };
+// Gate word 0 with this bit: the input is converted already (the tasks do nothing).
+constexpr uint32_t kGateConverted = 0x80000000u;
 
 // Device tables of the BF16 path: panel copies (one b×b K-major slot per lower
 // tile), the scale of each slot, and the power-of-two scale of each block row.
@@ -231,6 +236,36 @@ __device__ void publish_bf16_resident(const float* smem, int n, int r0, int rows
     __syncthreads();
 }
 
+// An input task's share of its tile column: FP64 -> FP32 (round to nearest,
+// as convert_f64_to_f32) over a contiguous chunk, 16 values per thread in
+// flight (16-byte loads; the column starts on a tile boundary and holds an
+// even number of values).
+__device__ inline void convert_input_chunk(const double* __restrict__ src, float* __restrict__ dst, int len, int part, int parts) {
+    const long per = ((long)len / parts + 2047) / 2048 * 2048;
+    const long e0 = min((long)len, part * per), e1 = min((long)len, e0 + per);
+    if (((uintptr_t)src & 15) || ((uintptr_t)dst & 7)) {  // odd tile edges: one value at a time
+        for (long e = e0 + threadIdx.x; e < e1; e += kThreads) dst[e] = (float)__ldcg(src + e);
+        __syncthreads();
+        return;
+    }
+    constexpr int U = 8;  // double2 loads per thread per round
+    for (long base = e0 + 2L * threadIdx.x; base < e1; base += 2L * kThreads * U) {
+        double2 v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const long e = base + 2L * kThreads * u;
+            v[u] = e + 1 < e1 ? __ldcg((const double2*)(src + e)) : make_double2(e < e1 ? __ldcg(src + e) : 0.0, 0.0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const long e = base + 2L * kThreads * u;
+            if (e + 1 < e1) *(float2*)(dst + e) = make_float2((float)v[u].x, (float)v[u].y);
+            else if (e < e1) dst[e] = (float)v[u].x;
+        }
+    }
+    __syncthreads();
+}
+
 __device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem, int* team, int* fin, tc::TcShared* tsh,
                              uint8_t* ring, const CUtensorMap* tmap, int* err, long long limit_ns) {
     if (op.prec == TTG_PREC_F64) {
@@ -325,6 +360,37 @@ __device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem,
                 return 0;
             }
             return run_op_plain<float>(op, part, parts, fsm);
+        case TTG_OP_CONVERT:
+            if (op.flags & kConvertGated) {
+                // An input task: wait (bounded) until its tile column is in
+                // device memory (gate word 1 + k equals the run's generation).
+                __shared__ int s_late;
+                if (threadIdx.x == 0) {
+                    const volatile uint32_t* gate = (const volatile uint32_t*)op.aux;
+                    const long long t0 = globaltimer();
+                    int late = 0;
+                    if (gate[0] & kGateConverted) late = -1;  // nothing to do
+                    for (unsigned it = 0; late == 0 && gate[1 + op.k] != gate[0]; ++it) {
+                        if ((it & 63) == 63 && globaltimer() - t0 > limit_ns) {
+                            late = 1;
+                            break;
+                        }
+                        __nanosleep(128);
+                    }
+                    __threadfence();
+                    s_late = late;
+                }
+                __syncthreads();
+                if (s_late > 0 && threadIdx.x == 0) atomicCAS(err, 0, TTG_ETIMEOUT);
+                if (s_late) return 0;
+            }
+            if (op.flags & kConvertGated) {
+                convert_input_chunk((const double*)op.a, (float*)op.c, op.m, part, parts);
+                return 0;
+            }
+            convert_tile(op.m, op.n, op.alpha, op.a, op.lda, op.beta, op.c, op.ldc, op.flags & (kConvertAFloat | kConvertCFloat),
+                         part, parts);
+            return 0;
         default:
             return run_op_plain<float>(op, part, parts, fsm);
     }
@@ -437,6 +503,8 @@ ttg_status ttg_launch_mixed(ttg_ctx* c, const ExecParams& p, cudaStream_t s) {
 
 struct ttg_mixed_state {
     ttg_ctx* ctx = nullptr;
+    uint32_t* gate = nullptr;  // [1 + nb]: run generation, then the generation of each arrived tile column
+    uint32_t gen = 0;
     int N = 0, nb = 0, kind = 1, b = 0;
     std::vector<int> bs;
     std::vector<int64_t> off;
@@ -508,6 +576,8 @@ ttg_status ttg_mixed_state_create(ttg_ctx* ctx, int N, int nb, const int* bs, co
     };
     cudaError_t e = cudaMalloc((void**)&m->w32, sizeof(float) * std::max<int64_t>(1, m->elems));
     if (e != cudaSuccess) return fail(e, "cudaMalloc w32");
+    if ((e = cudaMalloc((void**)&m->gate, sizeof(uint32_t) * (nb + 1))) != cudaSuccess) return fail(e, "cudaMalloc gate");
+    if ((e = cudaMemset(m->gate, 0, sizeof(uint32_t) * (nb + 1))) != cudaSuccess) return fail(e, "memset gate");
     if (kind == 0) {
         const int n_slots = nb * (nb + 1) / 2;
         // Three slices of slots: the BF16 copies (slice 0) and, for split
@@ -536,6 +606,7 @@ ttg_status ttg_mixed_state_create(ttg_ctx* ctx, int N, int nb, const int* bs, co
 void ttg_mixed_state_destroy(ttg_mixed_state* m) {
     if (!m) return;
     if (m->w32) cudaFree(m->w32);
+    if (m->gate) cudaFree(m->gate);
     if (m->b16) cudaFree(m->b16);
     if (m->slot_scale) cudaFree(m->slot_scale);
     if (m->rowscale) cudaFree(m->rowscale);
@@ -603,13 +674,15 @@ ttg_op ttg_mixed_update_op(ttg_mixed_state* m, int k, int i, int j, int upd) {
     return op;
 }
 
-ttg_status ttg_mixed_prepare(ttg_mixed_state* m, void* stream, double shift, int upd, const double* src) {
+ttg_status ttg_mixed_prepare(ttg_mixed_state* m, void* stream, double shift, int upd, const double* src, bool in_graph) {
     const bool tc = upd != TTG_UPD_FP32;
     cudaStream_t s = (cudaStream_t)stream;
-    if (!src) return TTG_EINVAL;
-    ttg_note_launch();
-    convert_f64_to_f32<<<m->ctx->sms * 8, 256, 0, s>>>(src, m->w32, m->elems);
-    TTG_CUDA_CHECK(cudaGetLastError());
+    if (!src || (in_graph && shift > 0)) return TTG_EINVAL;
+    if (!in_graph) {
+        ttg_note_launch();
+        convert_f64_to_f32<<<m->ctx->sms * 8, 256, 0, s>>>(src, m->w32, m->elems);
+        TTG_CUDA_CHECK(cudaGetLastError());
+    }
     if (shift > 0) {
         for (int j = 0; j < m->nb; ++j) {
             const int64_t o = m->off[j + (size_t)j * m->nb];
@@ -628,6 +701,43 @@ ttg_status ttg_mixed_prepare(ttg_mixed_state* m, void* stream, double shift, int
         mc->globals.has_tc = 0;
     }
     return TTG_OK;
+}
+
+ttg_op ttg_mixed_input_op(ttg_mixed_state* m, int j, const double* src) {
+    // The column's tiles (j..nb-1, j) are contiguous: convert them as one
+    // vector of `len` values, split into parts of at most 256K values.
+    const int64_t o = m->off[j + (size_t)j * m->nb];
+    int64_t len = 0;
+    for (int i = j; i < m->nb; ++i) len += (int64_t)m->bs[i] * m->bs[j];
+    ttg_op op{};
+    op.kind = TTG_OP_CONVERT;
+    op.prec = TTG_PREC_MIXED;
+    op.m = (int)len;
+    op.n = 1;
+    op.k = j;  // the gate word of the column
+    op.a = src + o;
+    op.lda = (int)std::max<int64_t>(1, len);
+    op.c = m->w32 + o;
+    op.ldc = op.lda;
+    op.alpha = 1.0;
+    op.beta = 0.0;
+    op.flags = kConvertCFloat | kConvertGated;
+    op.aux = m->gate;
+    op.parts = (int)std::min<int64_t>(64, std::max<int64_t>(1, (len + 262143) / 262144));
+    return op;
+}
+
+uint32_t* ttg_mixed_gate(ttg_mixed_state* m) { return m->gate; }
+
+__global__ void gate_fill(uint32_t* gate, int n, uint32_t gen) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) gate[i] = gen;
+}
+
+uint32_t ttg_mixed_gate_begin(ttg_mixed_state* m, void* stream, bool converted) {
+    if (++m->gen >= kGateConverted) m->gen = 1;  // 0 is the value of a fresh gate
+    ttg_note_launch();
+    gate_fill<<<1, 32, 0, (cudaStream_t)stream>>>(m->gate, 1, converted ? (m->gen | kGateConverted) : m->gen);
+    return m->gen;
 }
 
 const double* ttg_mixed_factor_tiles(ttg_mixed_state* m) {

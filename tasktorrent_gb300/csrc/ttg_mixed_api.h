@@ -33,7 +33,23 @@ ttg_op ttg_mixed_update_op(ttg_mixed_state* m, int k, int i, int j, int upd);
 // tiles64, which the factorisation only uses as FP64 scratch) to the FP32
 // working tiles, adding shift·|a_ii| to every diagonal entry (shift 0: none),
 // for a run with update arithmetic upd.
-ttg_status ttg_mixed_prepare(ttg_mixed_state* m, void* stream, double shift, int upd, const double* src);
+// in_graph: the run's graph converts the input itself (input tasks of
+// ttg_mixed_input_op, no shift); only the block-row scales are computed here.
+ttg_status ttg_mixed_prepare(ttg_mixed_state* m, void* stream, double shift, int upd, const double* src, bool in_graph = false);
+
+// Input tasks of a graph that converts its own input, one per tile column j:
+// FP64 src tiles of the column (contiguous in the packed layout) -> FP32
+// working tiles, after column j has arrived.  Arrival is signalled through
+// the gate words (ttg_mixed_gate): word 0 holds the run's generation, word
+// 1 + j the generation whose column j is in device memory; an input task
+// waits (bounded) until they are equal.
+ttg_op ttg_mixed_input_op(ttg_mixed_state* m, int j, const double* src);
+uint32_t* ttg_mixed_gate(ttg_mixed_state* m);
+// Open a run: a new generation in gate word 0 (enqueued on stream).
+// converted: the input was converted by ttg_mixed_prepare, the input tasks
+// only pass (word 0 carries a flag bit); else each waits for its column
+// word to receive the generation.  Returns the generation.
+uint32_t ttg_mixed_gate_begin(ttg_mixed_state* m, void* stream, bool converted);
 // The low-precision factor as FP64 tiles (converted into tiles64).
 const double* ttg_mixed_factor_tiles(ttg_mixed_state* m);
 // The FP32 factor tiles (same layout as tiles64).

@@ -207,6 +207,40 @@ class Threadpool_shared {
     int n_device_tasks() const { return (int)dev_node_.size(); }
     // Node (captured task) of each device task, and the task names.
     const std::vector<int>& device_task_nodes() const { return dev_node_; }
+    // Extension: device-only tasks appended to the uploaded graph (tasks the
+    // captured program does not have, e.g. the input conversion of a
+    // mixed-precision plan).  ops[e] runs with priority prio[e] and promises
+    // the device tasks succ[e] (whose counters each grow by one); the graph is
+    // uploaded again.  Call after capture_only().
+    void add_device_tasks(const std::vector<ttg_op>& ops, const std::vector<double>& prio, const std::vector<std::vector<int>>& succ) {
+        if (!uploaded_) throw std::logic_error("Threadpool_shared::add_device_tasks() before the graph was captured");
+        const int nd = (int)g_ops_.size();
+        std::vector<int64_t> ptr(g_ptr_);
+        std::vector<int32_t> idx(g_idx_);
+        for (size_t e = 0; e < ops.size(); ++e) {
+            g_ops_.push_back(ops[e]);
+            g_init_.push_back(0);
+            g_prio_.push_back(prio[e]);
+            g_bind_.push_back(-1);
+            for (int d : succ[e]) {
+                if (d < 0 || d >= nd) throw std::out_of_range("Threadpool_shared::add_device_tasks(): successor");
+                idx.push_back(d);
+                ++g_init_[d];
+            }
+            ptr.push_back((int64_t)idx.size());
+        }
+        g_ptr_ = std::move(ptr);
+        g_idx_ = std::move(idx);
+        extra_tasks_ += (int)ops.size();
+        upload();
+    }
+    // Priority of uploaded device task d.
+    double device_priority(int d) const { return g_prio_.at(d); }
+    // Device tasks appended by add_device_tasks (they follow the captured ones).
+    int n_extra_device_tasks() const { return extra_tasks_; }
+    // All tasks of the uploaded graph (the size of the context's per-task
+    // records: ttg_task_record, ttg_trace).
+    int n_uploaded_tasks() const { return (int)dev_node_.size() + extra_tasks_; }
     std::string node_name(int node) const { return cap_.nodes[node].name ? cap_.nodes[node].name() : "_"; }
     int n_nodes() const { return (int)cap_.nodes.size(); }
 
@@ -215,7 +249,7 @@ class Threadpool_shared {
     // <prefix>.edges.csv lists "src,dst" per promise ("ROOT" = main thread).
     void dump_dag(const std::string& prefix) const {
         std::vector<std::vector<std::string>> rows;
-        std::vector<int32_t> runs(dev_node_.size(), 0);
+        std::vector<int32_t> runs(n_uploaded_tasks(), 0);
         std::vector<int> node_runs(cap_.nodes.size(), 0);
         if (uploaded_) {
             ttg_task_record(ctx_, runs.data(), nullptr);
@@ -457,8 +491,8 @@ class Threadpool_shared {
     // Device trace -> Logger events named "<basename><worker>>run><task>".
     void fill_logger(timer t0, timer t1) {
         const int nd = (int)dev_node_.size();
-        std::vector<int64_t> s(nd), e(nd);
-        std::vector<int32_t> w(nd);
+        std::vector<int64_t> s(n_uploaded_tasks()), e(n_uploaded_tasks());
+        std::vector<int32_t> w(n_uploaded_tasks());
         if (ttg_trace(ctx_, s.data(), e.data(), w.data()) != TTG_OK) return;
         (void)t1;
         for (int d = 0; d < nd; ++d) {
@@ -493,6 +527,7 @@ class Threadpool_shared {
     std::vector<int32_t> g_init_, g_bind_, g_idx_;
     std::vector<double> g_prio_;
     bool cp_prio_ = false;
+    int extra_tasks_ = 0;
     std::vector<int64_t> g_ptr_;
     uint64_t graph_gen_ = 0;
 };

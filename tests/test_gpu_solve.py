@@ -219,3 +219,26 @@ def test_classic_steps_then_gmres(ctx, alpha):
     if alpha == 1.0:
         assert reps[0].inner == 0, reps[0].as_dict()
     p.close()
+
+
+@pytest.mark.parametrize("pinned", [False, True])
+def test_streamed_host_input_equals_resident_input(ctx, pinned):
+    """A mixed plan's host input streams in while the factorisation runs (the
+    graph's input tasks wait for each tile column); the solution has the
+    bits of the same solve on the resident input, pinned or pageable."""
+    import torch
+    p = t.CholPlan(ctx, 128, 8, matrix=1, alpha=1e-4, seed=5, precision=t.PREC_MIXED, mixed_kind=2)
+    q = t.CholPlan(ctx, 128, 8, matrix=1, alpha=1e-2, seed=9, precision=t.PREC_MIXED, mixed_kind=2)
+    host = torch.empty(q.tile_elems(), dtype=torch.float64, pin_memory=pinned)
+    q.copy_tiles(1, host.data_ptr())
+    B = rhs(p.N, 4, seed=13)
+    for _ in range(2):  # twice: the second run's gate generation differs
+        st, rep, X1 = p.solve_host(B, tiles=host.numpy())
+        assert st == t.TTG_OK, rep.as_dict()
+        assert rep.h2d_ms > 0 and rep.total_ms >= rep.compute_ms
+        st, rep2, X2 = p.solve_host(B)  # the same input, now resident
+        assert st == t.TTG_OK
+        assert np.array_equal(X1, X2)
+        assert rep.bwd_err == rep2.bwd_err and rep.bwd_err <= BWD
+    p.close()
+    q.close()
