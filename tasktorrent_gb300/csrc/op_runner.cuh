@@ -42,7 +42,7 @@ __device__ int run_op_plain(const ttg_op& op, int part, int parts, T* smem) {
             trsm_rows_small<T, false>(op.m, op.n, alpha, (const T*)op.a, op.lda, (T*)op.c, op.ldc, smem, part, parts);
             return 0;
         case TTG_OP_SYRK_LN:
-            gemm_tile<T, false, true>(op.n, op.n, op.k, alpha, (const T*)op.a, op.lda, (const T*)op.a, op.lda, beta, (T*)op.c,
+            gemm_tile_auto<T, false, true>(op.n, op.n, op.k, alpha, (const T*)op.a, op.lda, (const T*)op.a, op.lda, beta, (T*)op.c,
                                       op.ldc, smem, part, parts);
             return 0;
         case TTG_OP_GEMM_NT:
@@ -50,7 +50,7 @@ __device__ int run_op_plain(const ttg_op& op, int part, int parts, T* smem) {
                 gemm_small_m<T, false>(op.m, op.n, op.k, alpha, (const T*)op.a, op.lda, (const T*)op.b, op.ldb, beta, (T*)op.c,
                                        op.ldc, smem, part, parts);
             else
-                gemm_tile<T, false, false>(op.m, op.n, op.k, alpha, (const T*)op.a, op.lda, (const T*)op.b, op.ldb, beta,
+                gemm_tile_auto<T, false, false>(op.m, op.n, op.k, alpha, (const T*)op.a, op.lda, (const T*)op.b, op.ldb, beta,
                                            (T*)op.c, op.ldc, smem, part, parts);
             return 0;
         case TTG_OP_GEMM_NN:
@@ -58,7 +58,7 @@ __device__ int run_op_plain(const ttg_op& op, int part, int parts, T* smem) {
                 gemm_small_m<T, true>(op.m, op.n, op.k, alpha, (const T*)op.a, op.lda, (const T*)op.b, op.ldb, beta, (T*)op.c,
                                       op.ldc, smem, part, parts);
             else
-                gemm_tile<T, true, false>(op.m, op.n, op.k, alpha, (const T*)op.a, op.lda, (const T*)op.b, op.ldb, beta,
+                gemm_tile_auto<T, true, false>(op.m, op.n, op.k, alpha, (const T*)op.a, op.lda, (const T*)op.b, op.ldb, beta,
                                           (T*)op.c, op.ldc, smem, part, parts);
             return 0;
         case TTG_OP_GEADD:

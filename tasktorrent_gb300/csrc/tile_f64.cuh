@@ -32,17 +32,20 @@ __device__ __forceinline__ float ldcg(const float* p) { return __ldcg(p); }
 // C[m×n] = alpha·A·op(B) + beta·C on the block.  A is m×k (lda).  op(B)(kk,j)
 // is B[j + kk·ldb] (B_NN = false: B is n×k, "NT") or B[kk + j·ldb] (B_NN =
 // true: B is k×n, "NN").  LOWER restricts the update to i >= j (SYRK, m == n).
-// beta == 0 never reads C, as in BLAS.  The 128×128 output blocks (the lower
+// beta == 0 never reads C, as in BLAS.  The BS×BS output blocks (the lower
 // ones only for LOWER) are numbered column by column; part `part` of `parts`
-// computes blocks part, part + parts, ...
+// computes blocks part, part + parts, ...  BS = 128 (8×8 per thread) or 64
+// (4×4 per thread: small tiles split into four times as many parts).
 // T is double (the FP64 path) or float (the FP32 updates of the mixed path).
-template <class T, bool B_NN, bool LOWER>
+template <class T, bool B_NN, bool LOWER, int BS = 128>
 __device__ void gemm_tile(int m, int n, int k, T alpha, const T* __restrict__ A, int lda, const T* __restrict__ B, int ldb,
                           T beta, T* C, int ldc, T* smem, int part = 0, int parts = 1) {
-    T(*As)[kBM] = reinterpret_cast<T(*)[kBM]>(smem);
-    T(*Bs)[kBNP] = reinterpret_cast<T(*)[kBNP]>(smem + kBK * kBM);
+    static_assert(BS == 128 || BS == 64, "output block edge");
+    constexpr int R = BS / 16;  // outputs per thread and dimension
+    T(*As)[BS] = reinterpret_cast<T(*)[BS]>(smem);
+    T(*Bs)[BS + 1] = reinterpret_cast<T(*)[BS + 1]>(smem + kBK * BS);
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-    const int nbm = (m + kBM - 1) / kBM, nbn = (n + kBN - 1) / kBN;
+    const int nbm = (m + BS - 1) / BS, nbn = (n + BS - 1) / BS;
     const int nblk = LOWER ? nbm * (nbm + 1) / 2 : nbm * nbn;
     for (int bidx = part; bidx < nblk; bidx += parts) {
         int bi, bj;
@@ -58,27 +61,27 @@ __device__ void gemm_tile(int m, int n, int k, T alpha, const T* __restrict__ A,
             bi = bidx % nbm;
             bj = bidx / nbm;
         }
-        const int m0 = bi * kBM, n0 = bj * kBN;
+        const int m0 = bi * BS, n0 = bj * BS;
         {
-            T acc[8][8];
+            T acc[R][R];
 #pragma unroll
-            for (int r = 0; r < 8; ++r)
+            for (int r = 0; r < R; ++r)
 #pragma unroll
-                for (int c = 0; c < 8; ++c) acc[r][c] = T(0);
+                for (int c = 0; c < R; ++c) acc[r][c] = T(0);
             for (int k0 = 0; k0 < k; k0 += kBK) {
 #pragma unroll
-                for (int r = 0; r < (kBK * kBM) / kThreads; ++r) {
+                for (int r = 0; r < (kBK * BS) / kThreads; ++r) {
                     const int idx = tid + kThreads * r;
-                    const int i = idx & (kBM - 1), kk = idx / kBM;
+                    const int i = idx & (BS - 1), kk = idx / BS;
                     const int gi = m0 + i, gk = k0 + kk;
                     As[kk][i] = (gi < m && gk < k) ? ldcg(A + gi + (size_t)gk * lda) : T(0);
                 }
 #pragma unroll
-                for (int r = 0; r < (kBK * kBN) / kThreads; ++r) {
+                for (int r = 0; r < (kBK * BS) / kThreads; ++r) {
                     const int idx = tid + kThreads * r;
                     int j, kk;
                     if (B_NN) { kk = idx & (kBK - 1); j = idx / kBK; }
-                    else { j = idx & (kBN - 1); kk = idx / kBN; }
+                    else { j = idx & (BS - 1); kk = idx / BS; }
                     const int gj = n0 + j, gk = k0 + kk;
                     T v = T(0);
                     if (gj < n && gk < k) v = B_NN ? ldcg(B + gk + (size_t)gj * ldb) : ldcg(B + gj + (size_t)gk * ldb);
@@ -87,33 +90,33 @@ __device__ void gemm_tile(int m, int n, int k, T alpha, const T* __restrict__ A,
                 __syncthreads();
 #pragma unroll
                 for (int kk = 0; kk < kBK; ++kk) {
-                    T a[8], b[8];
+                    T a[R], b[R];
 #pragma unroll
-                    for (int r = 0; r < 8; ++r) a[r] = As[kk][tx + 16 * r];
+                    for (int r = 0; r < R; ++r) a[r] = As[kk][tx + 16 * r];
 #pragma unroll
-                    for (int c = 0; c < 8; ++c) b[c] = Bs[kk][ty + 16 * c];
+                    for (int c = 0; c < R; ++c) b[c] = Bs[kk][ty + 16 * c];
 #pragma unroll
-                    for (int r = 0; r < 8; ++r)
+                    for (int r = 0; r < R; ++r)
 #pragma unroll
-                        for (int c = 0; c < 8; ++c) acc[r][c] = fma(a[r], b[c], acc[r][c]);
+                        for (int c = 0; c < R; ++c) acc[r][c] = fma(a[r], b[c], acc[r][c]);
                 }
                 __syncthreads();
             }
-            // Per column: the eight reads of C first (in flight together),
-            // then the eight writes — with a short k the epilogue is
-            // otherwise a chain of 64 memory round trips.
+            // Per column: the R reads of C first (in flight together), then
+            // the R writes — with a short k the epilogue is otherwise a chain
+            // of R² memory round trips.
 #pragma unroll
-            for (int c = 0; c < 8; ++c) {
+            for (int c = 0; c < R; ++c) {
                 const int gj = n0 + ty + 16 * c;
-                T cv[8];
+                T cv[R];
 #pragma unroll
-                for (int r = 0; r < 8; ++r) {
+                for (int r = 0; r < R; ++r) {
                     const int gi = m0 + tx + 16 * r;
                     const bool ok = gi < m && gj < n && (!LOWER || gi >= gj);
                     cv[r] = (ok && beta != T(0)) ? ldcg(C + gi + (size_t)gj * ldc) : T(0);
                 }
 #pragma unroll
-                for (int r = 0; r < 8; ++r) {
+                for (int r = 0; r < R; ++r) {
                     const int gi = m0 + tx + 16 * r;
                     if (gi < m && gj < n && (!LOWER || gi >= gj)) {
                         T v = alpha * acc[r][c];
@@ -124,6 +127,20 @@ __device__ void gemm_tile(int m, int n, int k, T alpha, const T* __restrict__ A,
             }
         }
     }
+}
+
+// Output block edge of a tile update: 64 for tiles up to 256 (more parts, so
+// that small tiles spread over more SMs: at this GPU's FP64 rate a 128×128×128
+// update takes ~0.5 ms on one block), else 128.
+__host__ __device__ constexpr int gemm_block_edge(int m, int n) { return (m <= 256 && n <= 256) ? 64 : 128; }
+
+template <class T, bool B_NN, bool LOWER>
+__device__ __forceinline__ void gemm_tile_auto(int m, int n, int k, T alpha, const T* A, int lda, const T* B, int ldb, T beta, T* C,
+                                               int ldc, T* smem, int part = 0, int parts = 1) {
+    if (gemm_block_edge(m, n) == 64)
+        gemm_tile<T, B_NN, LOWER, 64>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, smem, part, parts);
+    else
+        gemm_tile<T, B_NN, LOWER, 128>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, smem, part, parts);
 }
 
 template <bool B_NN, bool LOWER>

@@ -87,15 +87,15 @@ __device__ int run_op_f64_noalloc(const ttg_op& op, int part, int parts, double*
             trsm_rltn_f64(op.m, op.n, op.alpha, (const double*)op.a, op.lda, (double*)op.c, op.ldc, smem, part, parts);
             return 0;
         case TTG_OP_SYRK_LN:
-            gemm_f64<false, true>(op.n, op.n, op.k, op.alpha, (const double*)op.a, op.lda, (const double*)op.a, op.lda,
+            gemm_tile_auto<double, false, true>(op.n, op.n, op.k, op.alpha, (const double*)op.a, op.lda, (const double*)op.a, op.lda,
                                   op.beta, (double*)op.c, op.ldc, smem, part, parts);
             return 0;
         case TTG_OP_GEMM_NT:
-            gemm_f64<false, false>(op.m, op.n, op.k, op.alpha, (const double*)op.a, op.lda, (const double*)op.b, op.ldb,
+            gemm_tile_auto<double, false, false>(op.m, op.n, op.k, op.alpha, (const double*)op.a, op.lda, (const double*)op.b, op.ldb,
                                    op.beta, (double*)op.c, op.ldc, smem, part, parts);
             return 0;
         case TTG_OP_GEMM_NN:
-            gemm_f64<true, false>(op.m, op.n, op.k, op.alpha, (const double*)op.a, op.lda, (const double*)op.b, op.ldb,
+            gemm_tile_auto<double, true, false>(op.m, op.n, op.k, op.alpha, (const double*)op.a, op.lda, (const double*)op.b, op.ldb,
                                   op.beta, (double*)op.c, op.ldc, smem, part, parts);
             return 0;
         case TTG_OP_GEADD:
