@@ -110,6 +110,14 @@ ttg_status ttg_chol_plan_kind_times(ttg_chol_plan* plan, double* potrf_ms, doubl
  * the task's part durations added up.  The timeline view of the reference's Logger output
  * (tasktorrent/src/util.hpp Logger, written by 2d_cholesky with -log). */
 ttg_status ttg_chol_plan_trace_dump(ttg_chol_plan* plan, const char* path);
+/* The last factorisation in the reference's trace formats, as 2d_cholesky
+ * writes them with --log and --depslog (2d_cholesky.cpp:630-644; read by
+ * tools/ttor_logging.py:11-25): log_path gets the Logger CSV, one line
+ * "<thread>>run><task>,<start s>,<end s>" per task (util.cpp Logger output;
+ * the thread is the executor block, "Wk_Chol_0_<block>"), deps_path the
+ * DepsLogger CSV, one line "<task>,<successor>" per dependency.  Either path
+ * may be NULL.  The log needs a context created with opts.trace. */
+ttg_status ttg_chol_plan_write_log(ttg_chol_plan* plan, const char* log_path, const char* deps_path);
 
 /* ------------------------------------------------------------------ solve */
 

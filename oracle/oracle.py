@@ -42,11 +42,12 @@ class GemmOut(ctypes.Structure):
 
 
 def build():
-    """Build liboracle.so (and oracle/_ref when the reference tree is present)."""
+    """Build liboracle.so, and oracle/_ref when the reference tree is present
+    (the Makefile's REF, or TTG_REFERENCE_DIR when set)."""
     subprocess.run(["make", "-s", "liboracle.so"], cwd=HERE, check=True)
-    ref = os.environ.get("TTG_REFERENCE_DIR", "/root/reference")
-    if os.path.isdir(os.path.join(ref, "tasktorrent", "src")):
-        subprocess.run(["make", "-s", "ref", "REF=" + ref], cwd=HERE, check=True)
+    ref = os.environ.get("TTG_REFERENCE_DIR")
+    cmd = ["make", "-s", "ref-if-present"] + (["REF=" + ref] if ref else [])
+    subprocess.run(cmd, cwd=HERE, check=True)
 
 
 def find_openblas():

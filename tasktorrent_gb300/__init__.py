@@ -178,6 +178,7 @@ SIGNATURES = {
     "ttg_chol_plan_dump_dag": (_STATUS, [_P, ctypes.c_char_p]),
     "ttg_chol_plan_kind_times": (_STATUS, [_P, _P, _P, _P, _P]),
     "ttg_chol_plan_trace_dump": (_STATUS, [_P, ctypes.c_char_p]),
+    "ttg_chol_plan_write_log": (_STATUS, [_P, ctypes.c_char_p, ctypes.c_char_p]),
     "ttg_chol_plan_remedy": (ctypes.c_int32, [_P]),
     "ttg_chol_dag_dump": (_STATUS, [ctypes.POINTER(CholArgs), ctypes.c_char_p]),
     "ttg_gemm_dag_dump": (_STATUS, [ctypes.POINTER(GemmArgs), ctypes.c_char_p]),

@@ -20,6 +20,7 @@
 #include <chrono>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
 #include <map>
 #include <memory>
 #include <random>
@@ -839,6 +840,20 @@ extern "C" ttg_status ttg_chol_posv_host(ttg_chol_plan* P, const double* h_tiles
 extern "C" ttg_status ttg_chol_plan_dump_dag(ttg_chol_plan* P, const char* prefix) {
     if (!P || !prefix) return TTG_EINVAL;
     P->tp->dump_dag(prefix);
+    return TTG_OK;
+}
+
+extern "C" ttg_status ttg_chol_plan_write_log(ttg_chol_plan* P, const char* log_path, const char* deps_path) {
+    if (!P) return TTG_EINVAL;
+    if (log_path) {
+        std::ofstream f(log_path);
+        if (!f || !P->tp->write_log(f)) return TTG_EINVAL;
+    }
+    if (deps_path) {
+        std::ofstream f(deps_path);
+        if (!f) return TTG_EINVAL;
+        P->tp->write_deps(f);
+    }
     return TTG_OK;
 }
 

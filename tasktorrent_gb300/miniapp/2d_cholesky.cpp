@@ -125,9 +125,12 @@ int main(int argc, const char** argv) {
     printf("GFLOP/s (N^3/3): %.3f\n", (double)N * N * N / 3.0 / total_time * 1e-9);
 
     if (log || depslog) {
+        // The reference's file names (2d_cholesky.cpp:630-644) at one rank.
         const std::string base = "ttor_dist_" + std::to_string(block_size) + "_" + std::to_string(num_blocks) + "_1_" +
                                  std::to_string(n_threads) + "_" + std::to_string(ca.kind);
-        ttg_chol_plan_dump_dag(plan, (base + ".dag").c_str());
+        const std::string logname = base + ".log.0", depsname = "deps_" + base + ".dot.0";
+        s = ttg_chol_plan_write_log(plan, log ? logname.c_str() : nullptr, depslog ? depsname.c_str() : nullptr);
+        if (s != TTG_OK) return fail("write_log", s);
     }
 
     int rc = 0;

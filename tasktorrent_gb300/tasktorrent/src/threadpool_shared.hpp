@@ -476,6 +476,7 @@ class Threadpool_shared {
         timer t0 = wctime();
         ttg_status s = ttg_run(context(), stream, &report_);
         timer t1 = wctime();
+        last_run_t0_ = t0;
         if (verb_ > 0)
             printf("[%s] device run: %lld tasks, %.3f ms, status %s\n", basename_.c_str(), (long long)report_.tasks_run,
                    report_.elapsed_ms, ttg_strerror(s));
@@ -488,6 +489,29 @@ class Threadpool_shared {
         return s;
     }
 
+public:
+    // Extension: the last device run's timeline in the Logger's CSV format
+    // ("<basename><worker>>run><task>,<start>,<end>", times in seconds), as
+    // 2d_cholesky writes with --log (needs a context created with trace).
+    bool write_log(std::ostream& os) {
+        Logger lg(std::max(1, (int)dev_node_.size()));
+        Logger* keep = logger_;
+        logger_ = &lg;
+        fill_logger(last_run_t0_, last_run_t0_);
+        logger_ = keep;
+        if (lg.n_events() == 0) return false;
+        os << lg;
+        return true;
+    }
+    // Extension: the captured dependencies in the DepsLogger's CSV format
+    // ("<task>,<successor>" per promise made by a task), as 2d_cholesky writes
+    // with --depslog.
+    void write_deps(std::ostream& os) const {
+        for (size_t i = 0; i < cap_.nodes.size(); ++i)
+            for (int s : cap_.nodes[i].succ) os << node_name((int)i) << "," << node_name(s) << "\n";
+    }
+
+private:
     // Device trace -> Logger events named "<basename><worker>>run><task>".
     void fill_logger(timer t0, timer t1) {
         const int nd = (int)dev_node_.size();
@@ -516,6 +540,7 @@ class Threadpool_shared {
     ttg_ctx* ctx_ = nullptr;
     bool own_ctx_ = false;
     ttg_report report_{};
+    timer last_run_t0_ = wctime();
     double capture_s_ = 0.0;
     std::mutex mtx_;
     detail::Capture cap_;

@@ -2,7 +2,7 @@
 runtime (ttor::Taskflow + ttor::Threadpool_shared compiled from the reference
 sources into oracle/_ref by oracle/Makefile).
 
-Run in a container that has the reference tree (default /root/reference):
+Run in a container that has the reference tree (oracle/Makefile's REF, or --ref):
 
     python tests/golden/make_golden.py [--ref /path/to/reference]
 
@@ -36,9 +36,9 @@ def gz(src, dst):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=None, help="reference tree (default: oracle/Makefile's REF)")
     a = ap.parse_args()
-    subprocess.run(["make", "-s", "ref", "REF=" + a.ref], cwd=ORACLE, check=True)
+    subprocess.run(["make", "-s", "ref"] + (["REF=" + a.ref] if a.ref else []), cwd=ORACLE, check=True)
     ref_dag = os.path.join(ORACLE, "_ref", "ref_dag")
     env = dict(os.environ)
     env.pop("TTG_ORACLE_BLAS", None)  # plain loops: bit-reproducible on any host
