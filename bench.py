@@ -575,12 +575,22 @@ def main():
     ap.add_argument("--no-serving", dest="no_serving", action="store_true")
     ap.add_argument("--batch-n", dest="batch_n", type=int, default=10000)
     ap.add_argument("--serve-n", dest="serve_n", type=int, default=600)
+    ap.add_argument("--serving-only", dest="serving_only", action="store_true",
+                    help="run only the serving stream and print its section")
     ap.add_argument("--serve-rates", dest="serve_rates", type=lambda s: [float(x) for x in s.split(",")],
                     default=[100.0, 1000.0, 10000.0])
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
     world, rank, local = dist_init()
+    if args.serving_only:
+        # The serving stream alone (e.g. --serve-n 10000): one JSON object.
+        import torch
+        torch.cuda.set_device(local)
+        out = run_serving(args, local)
+        if rank == 0:
+            print(json.dumps({"serving": out}))
+        return
     if args.impl == "reference":
         run_reference(args, world, rank)
     else:
