@@ -132,7 +132,8 @@ def workload_config(args):
     elems = nb * (nb + 1) // 2 * args.block ** 2
     return {"workload": "tiled Cholesky + solve of A X = B to backward error <= %g, A = G*G^T/N + alpha*I" % args.tol,
             "gpu_variant": "mixed precision: BF16 tensor-core updates (%s), FP32 TRSM, FP64 diagonal POTRF, GMRES-IR" % (
-                {0: "plain BF16 first", 1: "FP32 updates", 2: "split into three BF16 terms"}[args.mixed_kind]),
+                {0: "plain BF16 first", 1: "FP32 updates", 2: "split into three BF16 terms",
+                 3: "split into two FP16 terms"}[args.mixed_kind]),
             "mixed_kind": args.mixed_kind, "matrix_size": N, "block_size": args.block, "nrhs": args.nrhs,
             "alpha": args.alpha, "seed": args.seed, "priority_kind": args.kind, "tasks": _tasks(nb),
             "l2": "inputs larger than L2 (%.1f GB of FP64 tiles)" % (elems * 8 / 1e9)}
@@ -493,9 +494,9 @@ def run_ours(args, world, rank, local):
         p64.close()
         # The three conditionings of the workload (one step each).
         # mixed_kind 0: plain BF16 first (remedies on loss of definiteness);
-        # 2: split BF16 (FP32-level updates on the tensor cores).
+        # 2: split BF16 (FP32-level updates on the tensor cores); 3: split FP16.
         per_alpha = []
-        for mk in (0, 2):
+        for mk in (0, 2, 3):
             for a in (1.0, 1e-4, 1e-8):
                 pa = t.CholPlan(ctx, args.block, nb, n_threads=16, kind=args.kind, matrix=1, alpha=a, seed=args.seed + rank,
                                 precision=t.PREC_MIXED, mixed_kind=mk)
@@ -561,7 +562,7 @@ def main():
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--kind", type=int, default=2)
     ap.add_argument("--mixed-kind", dest="mixed_kind", type=int, default=2,
-                    help="0: BF16 updates (remedies on loss of definiteness); 2: split BF16; 1: FP32")
+                    help="0: BF16 updates (remedies on loss of definiteness); 2: split BF16; 3: split FP16; 1: FP32")
     ap.add_argument("--cpu-panels", dest="cpu_panels", type=int, default=2,
                     help="panel steps of the factorisation in the CPU samples")
     ap.add_argument("--no-configs", dest="no_configs", action="store_true",

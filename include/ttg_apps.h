@@ -41,7 +41,10 @@ typedef struct ttg_chol_args {
     int32_t precision;        /* TTG_PREC_F64 or TTG_PREC_MIXED                     */
     int32_t mixed_kind;       /* mixed path: 0 = BF16 tensor-core updates, 1 = FP32
                                  updates, 2 = split-BF16 tensor-core updates (three
-                                 BF16 slices per operand, FP32-level accuracy)      */
+                                 BF16 slices per operand, six products, FP32-level
+                                 accuracy), 3 = split-FP16 tensor-core updates (two
+                                 FP16 slices, three products, ~2^-22 accuracy); 0, 2
+                                 and 3 need uniform tiles, a multiple of 128        */
 } ttg_chol_args;
 
 typedef struct ttg_chol_plan ttg_chol_plan;
@@ -150,9 +153,10 @@ typedef struct ttg_solve_report {
     double anorm_inf;   /* ‖A‖∞                                                        */
     double factor_ms;   /* factorisation (device events; 0 for ttg_chol_plan_solve)     */
     double solve_ms;    /* solve and refinement (host clock)                           */
-    int32_t remedy;     /* mixed factor: 0 BF16 updates; after a loss of definiteness
-                           4 split-BF16 updates, 2 FP32 updates, 3 FP32 updates on
-                           A + 16·2^-24·diag(A), 1 BF16 updates on A + 8·2^-8·diag(A) */
+    int32_t remedy;     /* mixed factor: 0 BF16 updates, 5 split-FP16 updates; after a
+                           loss of definiteness 4 split-BF16 updates, 2 FP32 updates,
+                           3 FP32 updates on A + 16·2^-24·diag(A), 1 BF16 updates on
+                           A + 8·2^-8·diag(A)                                          */
     double h2d_ms;      /* ttg_chol_posv_host / ttg_chol_solve_host: host-to-device copies
                            of the tiles and B (device events; 0 elsewhere)             */
     double d2h_ms;      /* ... the device-to-host copy of X                             */

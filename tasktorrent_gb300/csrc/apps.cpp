@@ -73,7 +73,7 @@ struct ttg_chol_plan {
     double* pristine = nullptr;  // input copy
     std::unique_ptr<Threadpool_shared> tp;    // the plan's graph (FP64, or mixed with BF16 updates when available)
     std::unique_ptr<Threadpool_shared> tp32;  // mixed plans with tensor cores: the same graph with FP32 updates
-    std::unique_ptr<Threadpool_shared> tpx3;  // ... and with split-BF16 updates (mixed_kind 0)
+    std::unique_ptr<Threadpool_shared> tpx3;  // ... and with split-BF16 updates (mixed_kind 0 and 3)
     int remedy = 0;                           // last mixed factorisation: 0 none, 1 diagonal shift, 2 FP32 updates
     std::vector<int> kind_of_dev;  // per device task: 0 potrf, 1 trsm, 2 gemm, 3 accu, -1 other
     std::vector<double*> tmp;      // accumulate-flow temporaries (device)
@@ -326,13 +326,13 @@ extern "C" ttg_status ttg_chol_plan_create(ttg_ctx* ctx, const ttg_chol_args* ar
     if (args->block_size <= 0 || args->num_blocks <= 0 || args->n_threads <= 0) return TTG_EINVAL;
     if (args->precision != TTG_PREC_F64 && args->precision != TTG_PREC_MIXED) return TTG_EINVAL;
     if (args->precision == TTG_PREC_MIXED && args->accumulate) return TTG_EINVAL;
-    if (args->precision == TTG_PREC_MIXED && (args->mixed_kind < 0 || args->mixed_kind > 2)) return TTG_EINVAL;
+    if (args->precision == TTG_PREC_MIXED && (args->mixed_kind < 0 || args->mixed_kind > 3)) return TTG_EINVAL;
     std::unique_ptr<ttg_chol_plan> P(new ttg_chol_plan());
     P->ctx = ctx;
     P->args = *args;
     if (!cholesky_block_sizes(args->block_size, args->num_blocks, args->upper_block_size, P->bs)) return TTG_EINVAL;
     if (args->precision == TTG_PREC_MIXED && args->mixed_kind != 1) {
-        // Tensor-core updates (mixed_kind 0 and 2) need uniform tiles whose
+        // Tensor-core updates (mixed_kind 0, 2 and 3) need uniform tiles whose
         // size is a multiple of 128 (the MMA's M); checked before any
         // allocation.  FP32 updates (mixed_kind 1) take any tiles.
         for (int b : P->bs)
@@ -355,10 +355,11 @@ extern "C" ttg_status ttg_chol_plan_create(ttg_ctx* ctx, const ttg_chol_args* ar
     }
     // Graphs: the first attempt's update arithmetic, then the remedies'.
     const bool tc = P->mixed && ttg_mixed_has_tc(P->mixed);
-    const int first = !tc ? TTG_UPD_FP32 : (args->mixed_kind == 2 ? TTG_UPD_BF16X3 : TTG_UPD_BF16);
+    const int first = !tc ? TTG_UPD_FP32
+                          : (args->mixed_kind == 2 ? TTG_UPD_BF16X3 : (args->mixed_kind == 3 ? TTG_UPD_F16X2 : TTG_UPD_BF16));
     ttg_status s = chol_build_graph(P.get(), false, first, P->tp);
     if (s == TTG_OK && tc) s = chol_build_graph(P.get(), false, TTG_UPD_FP32, P->tp32);
-    if (s == TTG_OK && tc && first == TTG_UPD_BF16) s = chol_build_graph(P.get(), false, TTG_UPD_BF16X3, P->tpx3);
+    if (s == TTG_OK && tc && first != TTG_UPD_BF16X3) s = chol_build_graph(P.get(), false, TTG_UPD_BF16X3, P->tpx3);
     if (s == TTG_OK && P->mixed) s = add_input_tasks(P.get());
     if (s == TTG_OK) s = ttg_chol_plan_generate(P.get(), nullptr);
     if (s != TTG_OK) return s;  // P's destructor frees what was allocated
@@ -487,6 +488,7 @@ static ttg_status chol_factor_from(ttg_chol_plan* P, void* stream, ttg_report* r
     // scratch, so they need no restore.
     const bool tc = ttg_mixed_has_tc(P->mixed);
     const bool first_x3 = P->args.mixed_kind == 2;
+    const bool first_f16 = P->args.mixed_kind == 3;
     struct Attempt {
         Threadpool_shared* tp;
         double shift;
@@ -495,11 +497,12 @@ static ttg_status chol_factor_from(ttg_chol_plan* P, void* stream, ttg_report* r
     };
     std::vector<Attempt> plan;
     Threadpool_shared* tp32 = tc ? P->tp32.get() : P->tp.get();
-    if (tc && !first_x3) plan.push_back({P->tp.get(), 0.0, TTG_UPD_BF16, 0});
+    if (tc && first_f16) plan.push_back({P->tp.get(), 0.0, TTG_UPD_F16X2, 5});
+    else if (tc && !first_x3) plan.push_back({P->tp.get(), 0.0, TTG_UPD_BF16, 0});
     if (tc) plan.push_back({first_x3 ? P->tp.get() : P->tpx3.get(), 0.0, TTG_UPD_BF16X3, 4});
     plan.push_back({tp32, 0.0, TTG_UPD_FP32, 2});
     plan.push_back({tp32, 16.0 * 5.9604644775390625e-08, TTG_UPD_FP32, 3});
-    if (tc && !first_x3) plan.push_back({P->tp.get(), 8.0 * 0.00390625, TTG_UPD_BF16, 1});
+    if (tc && !first_x3 && !first_f16) plan.push_back({P->tp.get(), 8.0 * 0.00390625, TTG_UPD_BF16, 1});
     ttg_status s = TTG_OK;
     float total_ms = 0.f;
     const bool streamed = P->streaming;

@@ -123,6 +123,10 @@ __device__ __forceinline__ void tmem_dealloc(uint32_t taddr) {
 __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
+// The same with FP16 A and B (bits 7-9 and 10-12 = 0).
+__host__ __device__ constexpr uint32_t idesc_f16_f32(int M, int N) {
+    return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
 
 // Shared-memory descriptor of a K-major, 64B-swizzled operand whose rows are
 // 64 bytes and whose 8-row groups are 512 bytes apart: start address >> 4
@@ -211,6 +215,10 @@ __device__ inline void tc_teardown(TcShared* sh, long long limit_ns) {
 // first — mid·mid, hi·lo, lo·hi, hi·mid, mid·hi, hi·hi.
 __device__ __forceinline__ int split_pair_a(int p) { return p == 0 ? 1 : (p == 2 ? 2 : (p == 4 ? 1 : 0)); }
 __device__ __forceinline__ int split_pair_b(int p) { return p == 0 ? 1 : (p == 1 ? 2 : (p == 3 ? 1 : 0)); }
+// Split FP16 (slice 0 = hi, 1 = lo·2^11): hi·lo, lo·hi into the small
+// accumulator (scaled by 2^11), hi·hi last.
+__device__ __forceinline__ int f16_pair_a(int p) { return p == 1 ? 1 : 0; }
+__device__ __forceinline__ int f16_pair_b(int p) { return p == 0 ? 1 : 0; }
 
 // Number of 128×256 output blocks of an m×n tile (lower: blocks that meet
 // the lower triangle of a square tile), and the coordinates of block b.
@@ -263,12 +271,12 @@ __device__ inline bool tc_gemm_blocks(TcShared* sh, uint8_t* ring, const CUtenso
                                       int stride = 0) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ksteps = k / kBK;
-    const int nsl = split == 3 ? 3 : 1;  // slots (slices) per K step
-    const int npairs = split == 3 ? 6 : 1;
+    const int nsl = split;                 // slots (slices) per K step: 1, 2 (split FP16) or 3 (split BF16)
+    const int npairs = split == 3 ? 6 : (split == 2 ? 3 : 1);
     const int total = nsl * ksteps;      // slots per output block
     const uint32_t base = sh->nacc;
     const bool ok = !sh->failed;
-    const bool dbl = split != 3;  // double-buffered accumulators
+    const bool dbl = split == 1;  // double-buffered accumulators
     auto buf_of = [&](uint32_t gi) { return dbl ? (int)(gi & 1) : 0; };
     auto use_of = [&](uint32_t gi) { return dbl ? (gi >> 1) : gi; };
     if (warp == 2 || warp == 3) {
@@ -308,7 +316,7 @@ __device__ inline bool tc_gemm_blocks(TcShared* sh, uint8_t* ring, const CUtenso
         sh->produced = p;
     } else if (threadIdx.x == 32 && ok) {
         // MMA issuer.
-        const uint32_t idesc = idesc_bf16_f32(kBM, kBN);
+        const uint32_t idesc = split == 2 ? idesc_f16_f32(kBM, kBN) : idesc_bf16_f32(kBM, kBN);
         uint32_t c = sh->consumed;
         bool good = true;
         for (int j = 0; j < nblk && good; ++j) {
@@ -338,8 +346,8 @@ __device__ inline bool tc_gemm_blocks(TcShared* sh, uint8_t* ring, const CUtenso
                 if (!good) break;
                 tc_fence_after();
                 for (int pr = 0; pr < npairs; ++pr) {
-                    const uint32_t a0 = sbase[split == 3 ? split_pair_a(pr) : 0];
-                    const uint32_t bb = sbase[split == 3 ? split_pair_b(pr) : 0] + kSlotBytesA;
+                    const uint32_t a0 = sbase[split == 3 ? split_pair_a(pr) : (split == 2 ? f16_pair_a(pr) : 0)];
+                    const uint32_t bb = sbase[split == 3 ? split_pair_b(pr) : (split == 2 ? f16_pair_b(pr) : 0)] + kSlotBytesA;
                     // pair npairs-1 is hi·hi (the only one when not split)
                     const bool big = pr == npairs - 1;
                     const uint32_t d = big ? dacc : dsmall;
@@ -386,8 +394,9 @@ __device__ inline bool tc_gemm_blocks(TcShared* sh, uint8_t* ring, const CUtenso
                 if (!dbl) {
                     uint32_t w[32];
                     tmem_ld32(sh->tmem_base + ((uint32_t)(32 * q) << 16) + (uint32_t)(kBN + c0), w);
+                    const float ws = split == 2 ? 1.0f / 2048.0f : 1.0f;  // split FP16: lo carries 2^11
 #pragma unroll
-                    for (int jj = 0; jj < 32; ++jj) v[jj] = __float_as_uint(__uint_as_float(v[jj]) + __uint_as_float(w[jj]));
+                    for (int jj = 0; jj < 32; ++jj) v[jj] = __float_as_uint(fmaf(__uint_as_float(w[jj]), ws, __uint_as_float(v[jj])));
                 }
                 if (gr < m) {
                     // All 32 reads first (independent, in flight together), then

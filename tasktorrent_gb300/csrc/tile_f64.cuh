@@ -129,15 +129,18 @@ __device__ void gemm_tile(int m, int n, int k, T alpha, const T* __restrict__ A,
     }
 }
 
-// Output block edge of a tile update: 64 for tiles up to 256 (more parts, so
-// that small tiles spread over more SMs: at this GPU's FP64 rate a 128×128×128
-// update takes ~0.5 ms on one block), else 128.
-__host__ __device__ constexpr int gemm_block_edge(int m, int n) { return (m <= 256 && n <= 256) ? 64 : 128; }
+// Output block edge of an FP64 tile update: 64 for tiles up to 256 (more
+// parts, so that small tiles spread over more SMs: at this GPU's FP64 rate a
+// 128×128×128 update takes ~0.5 ms on one block), else 128.  FP32 updates
+// keep 128 (their 8×8 register blocks use the FMA pipe better).
+__host__ __device__ constexpr int gemm_block_edge(int m, int n, bool f64 = true) {
+    return (f64 && m <= 256 && n <= 256) ? 64 : 128;
+}
 
 template <class T, bool B_NN, bool LOWER>
 __device__ __forceinline__ void gemm_tile_auto(int m, int n, int k, T alpha, const T* A, int lda, const T* B, int ldb, T beta, T* C,
                                                int ldc, T* smem, int part = 0, int parts = 1) {
-    if (gemm_block_edge(m, n) == 64)
+    if (gemm_block_edge(m, n, sizeof(T) == 8) == 64)
         gemm_tile<T, B_NN, LOWER, 64>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, smem, part, parts);
     else
         gemm_tile<T, B_NN, LOWER, 128>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, smem, part, parts);

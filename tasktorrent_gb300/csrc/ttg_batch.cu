@@ -146,20 +146,33 @@ static void build_factor(Graph& g, const System& S, std::vector<int>& potrf, std
     potrf.assign(nb, -1);
     trsm.assign((size_t)nb * nb, -1);
     std::vector<int> gemm((size_t)nb * nb * nb, -1), cvt((size_t)nb * nb, -1);
+    // Thousands of systems keep every block busy: FP64 tile updates take one
+    // part per 128×128 output block and TRSMs one per 128 rows (the
+    // single-plan rule splits small FP64 tiles finer, to shorten one
+    // factorisation's chain).
+    auto c128 = [](int x) { return (x + 127) / 128; };
+    auto throughput = [&](ttg_op op) {
+        if (op.prec != TTG_PREC_F64) return op;
+        if (op.kind == TTG_OP_GEMM_NT) op.parts = std::min(16, c128(op.m) * c128(op.n));
+        else if (op.kind == TTG_OP_SYRK_LN) op.parts = std::min(16, c128(op.n) * (c128(op.n) + 1) / 2);
+        else if (op.kind == TTG_OP_TRSM_RLTN) op.parts = std::min(8, c128(op.m));
+        return op;
+    };
     for (int j = 0; j < nb; ++j) {
         ttg_op po = make_op(TTG_OP_POTRF_L, prec, S.bs(j), S.bs(j), 0, nullptr, 0, nullptr, 0, W(j, j), S.bs(j), 1.0, 0.0, 0,
                             mx ? (void*)(S.D64 + (size_t)j * S.tile * S.tile) : nullptr);
         po.parts = S.potrf_parts;
         potrf[j] = g.add(po);
         for (int i = j + 1; i < nb; ++i)
-            trsm[T(i, j)] = g.add(make_op(TTG_OP_TRSM_RLTN, prec, S.bs(i), S.bs(j), 0, W(j, j), S.bs(j), nullptr, 0, W(i, j),
-                                          S.bs(i), 1.0, 0.0, mx ? 1 : 0));
+            trsm[T(i, j)] = g.add(throughput(make_op(TTG_OP_TRSM_RLTN, prec, S.bs(i), S.bs(j), 0, W(j, j), S.bs(j), nullptr, 0,
+                                                     W(i, j), S.bs(i), 1.0, 0.0, mx ? 1 : 0)));
         for (int k = 0; k < j; ++k)
             for (int i = j; i < nb; ++i)
-                gemm[G(k, i, j)] = g.add(i == j ? make_op(TTG_OP_SYRK_LN, prec, S.bs(i), S.bs(i), S.bs(k), W(i, k), S.bs(i), nullptr,
-                                                          0, W(i, i), S.bs(i), -1.0, 1.0, mx ? 1 : 0)
-                                                : make_op(TTG_OP_GEMM_NT, prec, S.bs(i), S.bs(j), S.bs(k), W(i, k), S.bs(i), W(j, k),
-                                                          S.bs(j), W(i, j), S.bs(i), -1.0, 1.0, mx ? 1 : 0));
+                gemm[G(k, i, j)] = g.add(throughput(
+                    i == j ? make_op(TTG_OP_SYRK_LN, prec, S.bs(i), S.bs(i), S.bs(k), W(i, k), S.bs(i), nullptr, 0, W(i, i), S.bs(i),
+                                     -1.0, 1.0, mx ? 1 : 0)
+                           : make_op(TTG_OP_GEMM_NT, prec, S.bs(i), S.bs(j), S.bs(k), W(i, k), S.bs(i), W(j, k), S.bs(j), W(i, j),
+                                     S.bs(i), -1.0, 1.0, mx ? 1 : 0)));
     }
     if (mx)
         for (int j = 0; j < nb; ++j)

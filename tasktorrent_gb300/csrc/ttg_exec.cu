@@ -297,13 +297,13 @@ int ttg_task_parts(const ttg_op& op, bool team) {
     switch (op.kind) {
         case TTG_OP_GEMM_NT:
         case TTG_OP_GEMM_NN: {
-            const int e = gemm_block_edge(op.m, op.n);
+            const int e = gemm_block_edge(op.m, op.n, op.prec == TTG_PREC_F64);
             max_parts = std::max(1, cdiv(op.m, e) * cdiv(op.n, e));
             auto_parts = std::min(16, max_parts);
             break;
         }
         case TTG_OP_SYRK_LN: {
-            const int b = cdiv(op.n, gemm_block_edge(op.n, op.n));
+            const int b = cdiv(op.n, gemm_block_edge(op.n, op.n, op.prec == TTG_PREC_F64));
             max_parts = std::max(1, b * (b + 1) / 2);
             auto_parts = std::min(16, max_parts);
             break;
@@ -313,7 +313,7 @@ int ttg_task_parts(const ttg_op& op, bool team) {
             max_parts = std::max(1, cdiv(op.m, 16));
             // Rows per part: 128, or 32 for tiles up to 256 (more SMs on a
             // short critical chain).
-            auto_parts = std::min(8, std::max(1, cdiv(op.m, op.n <= 256 ? 32 : 128)));
+            auto_parts = std::min(8, std::max(1, cdiv(op.m, op.n <= 256 && op.prec == TTG_PREC_F64 ? 32 : 128)));
             // The mixed path's FP32 TRSM keeps each part's rows in shared
             // memory: at most 64 rows per part.
             if (op.prec == TTG_PREC_MIXED && op.kind == TTG_OP_TRSM_RLTN) auto_parts = std::min(max_parts, std::max(1, cdiv(op.m, 64)));

@@ -27,7 +27,9 @@
 namespace ttg {
 
 // Mixed-op variants carried in ttg_op::flags.
-enum { kMixedF32 = 1, kMixedBF16 = 2, kMixedBF16x3 = 3 };
+enum { kMixedF32 = 1, kMixedBF16 = 2, kMixedBF16x3 = 3, kMixedF16x2 = 4 };
+// Operand slices of a tensor-core update kind (tc_gemm_blocks' split).
+__host__ __device__ constexpr int mixed_split(int flags) { return flags == kMixedBF16x3 ? 3 : (flags == kMixedF16x2 ? 2 : 1); }
 // TTG_OP_CONVERT flags: a is float, c is float, and (mixed graphs) wait for
 // the task's input column to arrive first (gate words in aux, column in k).
 enum { kConvertAFloat = 1, kConvertCFloat = 2, kConvertGated = 4 };
@@ -70,6 +72,28 @@ __device__ inline void rows_to_bf16x3(const float* W, int ldw, int r0, int r1, i
         dst[o] = h;
         dst[slice + o] = mi;
         dst[2 * slice + o] = lo;
+    }
+}
+
+// Split FP16 slices of v (|v| <= 1): hi = fp16(v), lo = fp16((v − hi)·2^11);
+// v = hi + 2^-11·lo to ~2^-22 (the scale keeps lo out of FP16's subnormals).
+__device__ __forceinline__ void f16x2_split(float v, unsigned short& hi, unsigned short& lo) {
+    const __half h = __float2half_rn(v);
+    hi = __half_as_ushort(h);
+    lo = __half_as_ushort(__float2half_rn((v - __half2float(h)) * 2048.0f));
+}
+
+__device__ inline void rows_to_f16x2(const float* W, int ldw, int r0, int r1, int n, __nv_bfloat16* dst, size_t slice, int b,
+                                     float inv) {
+    unsigned short* d = reinterpret_cast<unsigned short*>(dst);
+    const long total = (long)(r1 - r0) * n;
+    for (long e = threadIdx.x; e < total; e += kThreads) {
+        const int r = r0 + (int)(e / n), c = (int)(e % n);
+        unsigned short h, l;
+        f16x2_split(__ldcg(W + r + (size_t)c * ldw) * inv, h, l);
+        const size_t o = (size_t)r * b + c;
+        d[o] = h;
+        d[slice + o] = l;
     }
 }
 
@@ -208,8 +232,10 @@ __device__ void trsm_rltn_f32_resident(int n, float alpha, const float* L, int l
 // three (hi, mid, lo; slice s at dst + s·slice).  Each slice goes through a
 // padded row-major buffer in the panel area, so the slot rows are written
 // with consecutive columns.
+// split: 1 plain BF16, 3 three BF16 slices, 2 split FP16 (mixed_split).
 __device__ void publish_bf16_resident(const float* smem, int n, int r0, int rows, __nv_bfloat16* dst, size_t slice, int b, float inv,
-                                      int nslices) {
+                                      int split) {
+    const int nslices = split;
     const float* Bs = smem;
     __nv_bfloat16* T = reinterpret_cast<__nv_bfloat16*>(const_cast<float*>(smem) + kTrsmRows * kTrsmMaxN);
     constexpr int kTs = kTrsmMaxN + 2;  // row stride (odd number of 4-byte words)
@@ -218,12 +244,19 @@ __device__ void publish_bf16_resident(const float* smem, int n, int r0, int rows
         for (int e = threadIdx.x; e < rows * n; e += kThreads) {
             const int r = e % rows, c = e / rows;
             const float v = Bs[c * kTrsmRows + r] * inv;
-            const __nv_bfloat16 h = __float2bfloat16_rn(v);
-            __nv_bfloat16 out = h;
-            if (sl > 0) {
-                const float r1v = v - __bfloat162float(h);
-                const __nv_bfloat16 mi = __float2bfloat16_rn(r1v);
-                out = sl == 1 ? mi : __float2bfloat16_rn(r1v - __bfloat162float(mi));
+            __nv_bfloat16 out;
+            if (split == 2) {
+                unsigned short h, l;
+                f16x2_split(v, h, l);
+                out = __ushort_as_bfloat16(sl == 0 ? h : l);
+            } else {
+                const __nv_bfloat16 h = __float2bfloat16_rn(v);
+                out = h;
+                if (sl > 0) {
+                    const float r1v = v - __bfloat162float(h);
+                    const __nv_bfloat16 mi = __float2bfloat16_rn(r1v);
+                    out = sl == 1 ? mi : __float2bfloat16_rn(r1v - __bfloat162float(mi));
+                }
             }
             T[r * kTs + c] = out;
         }
@@ -314,7 +347,7 @@ __device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem,
                         const size_t slice = (size_t)tb->n_slots * tb->b * tb->b;
                         if (r1 > r0)
                             publish_bf16_resident(fsm, op.n, r0, r1 - r0, tb->b16 + (size_t)op.ldb * tb->b * tb->b, slice, tb->b,
-                                                  1.0f / s, op.flags == kMixedBF16x3 ? 3 : 1);
+                                                  1.0f / s, mixed_split(op.flags));
                         if (threadIdx.x == 0 && part == 0) tb->slot_scale[op.ldb] = s;
                         tc::fence_proxy_async_global();
                     }
@@ -336,6 +369,9 @@ __device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem,
                 if (op.flags == kMixedBF16x3)
                     rows_to_bf16x3((const float*)op.c, op.ldc, r0, r1, op.n, tb->b16 + (size_t)op.ldb * tb->b * tb->b, slice, tb->b,
                                    1.0f / s);
+                else if (op.flags == kMixedF16x2)
+                    rows_to_f16x2((const float*)op.c, op.ldc, r0, r1, op.n, tb->b16 + (size_t)op.ldb * tb->b * tb->b, slice, tb->b,
+                                  1.0f / s);
                 else
                     rows_to_bf16((const float*)op.c, op.ldc, r0, r1, op.n, tb->b16 + (size_t)op.ldb * tb->b * tb->b, tb->b, 1.0f / s);
                 if (threadIdx.x == 0 && part == 0) tb->slot_scale[op.ldb] = s;
@@ -354,7 +390,7 @@ __device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem,
                 const float f = (float)op.alpha * __ldcg(tb->slot_scale + op.lda) * __ldcg(tb->slot_scale + op.ldb);
                 const int b0 = min(nblk, part * per), b1 = min(nblk, (part + 1) * per);
                 if (b1 > b0 && !tc::tc_gemm_blocks(tsh, ring, tmap, op.lda, op.ldb, b0, b1 - b0, op.k, f, (float*)op.c, op.ldc, op.m,
-                                                   op.n, lower, limit_ns, op.flags == kMixedBF16x3 ? 3 : 1, tb->n_slots) &&
+                                                   op.n, lower, limit_ns, mixed_split(op.flags), tb->n_slots) &&
                     threadIdx.x == 0)
                     atomicCAS(err, 0, TTG_ETIMEOUT);
                 return 0;
@@ -621,7 +657,9 @@ static ttg_op mixed_op(const ttg_mixed_state* m, int kind, int upd) {
     ttg_op op{};
     op.kind = kind;
     op.prec = TTG_PREC_MIXED;
-    op.flags = m->kind != 0 || upd == TTG_UPD_FP32 ? kMixedF32 : (upd == TTG_UPD_BF16X3 ? kMixedBF16x3 : kMixedBF16);
+    op.flags = m->kind != 0 || upd == TTG_UPD_FP32
+                   ? kMixedF32
+                   : (upd == TTG_UPD_BF16X3 ? kMixedBF16x3 : (upd == TTG_UPD_F16X2 ? kMixedF16x2 : kMixedBF16));
     op.alpha = 1.0;
     return op;
 }

@@ -16,7 +16,9 @@ struct ttg_mixed_state;
 // Trailing-update arithmetic of a mixed graph: FP32 on the CUDA cores, BF16
 // on the tensor cores, or split BF16 (three BF16 slices per operand, six
 // products, FP32-level accuracy) on the tensor cores.
-enum { TTG_UPD_FP32 = 0, TTG_UPD_BF16 = 1, TTG_UPD_BF16X3 = 2 };
+// Split FP16: two FP16 slices (hi, and the remainder scaled by 2^11), three
+// products, ~22-bit updates.
+enum { TTG_UPD_FP32 = 0, TTG_UPD_BF16 = 1, TTG_UPD_BF16X3 = 2, TTG_UPD_F16X2 = 3 };
 
 // kind: 0 = tensor-core updates available (BF16 and split BF16), 1 = FP32 updates only.
 ttg_status ttg_mixed_state_create(ttg_ctx* ctx, int N, int nb, const int* bs, const int64_t* off, double* tiles64, int kind,

@@ -138,10 +138,10 @@ def test_not_positive_definite_is_reported(ctx):
     p.close()
 
 
-@pytest.mark.parametrize("mk,b,upper", [(2, 64, -1), (0, 96, -1), (2, 128, 200), (3, 128, -1)])
+@pytest.mark.parametrize("mk,b,upper", [(2, 64, -1), (0, 96, -1), (2, 128, 200), (3, 64, -1), (4, 128, -1)])
 def test_rejected_mixed_plan_allocates_nothing(ctx, mk, b, upper):
     """Tensor-core updates need uniform tiles that are a multiple of 128, and
-    mixed_kind is 0, 1 or 2: other requests return TTG_EINVAL and leave the
+    mixed_kind is 0 to 3: other requests return TTG_EINVAL and leave the
     device's free memory where it was."""
     import torch
     torch.cuda.synchronize()

@@ -130,3 +130,38 @@ def test_split_bf16_preconditions_an_ill_conditioned_system(ctx):
     assert rep.inner <= 14, rep.as_dict()
     assert rep.bwd_err <= BWD and bwd_err(A, X, B) <= 2 * BWD
     p.close()
+
+
+@pytest.mark.parametrize("b,nb", [(128, 3), (256, 2), (512, 3)])
+def test_split_fp16_factor_accuracy(ctx, b, nb):
+    """Split-FP16 updates (two FP16 slices, the remainder scaled by 2^11;
+    three tensor-core products) give a factor near FP32 accuracy, far better
+    than plain BF16, from the same task graph."""
+    errs, dags = {}, {}
+    for mk in (0, 1, 3):
+        p = t.CholPlan(ctx, b, nb, kind=2, matrix=1, alpha=1.0, seed=4, precision=t.PREC_MIXED, mixed_kind=mk)
+        st, rep = p.factor()
+        assert st == t.TTG_OK, t.strerror(st)
+        assert rep.tasks_run == rep.tasks_total and rep.bad_runs == 0
+        A = p.input_A()
+        errs[mk] = rel(p.factor_L() @ p.factor_L().T, A)
+        p.close()
+    assert errs[3] < 1e-5, errs
+    assert errs[3] < errs[0] / 30, errs
+    assert errs[3] < 8 * errs[1], errs
+
+
+@pytest.mark.parametrize("alpha", [1e-4, 1e-8])
+def test_split_fp16_refines_to_fp64_backward_error(ctx, alpha):
+    """The split-FP16 factor keeps definiteness at alpha = 1e-4 (no remedy:
+    remedy 5) and the refinement reaches FP64 backward error; at 1e-8 the
+    refinement still converges (GMRES after the classic steps)."""
+    p = t.CholPlan(ctx, 128, 8, kind=2, matrix=1, alpha=alpha, seed=2, precision=t.PREC_MIXED, mixed_kind=3)
+    A = p.input_A()
+    B = orc.normals(0, p.N * 4, 9, 1).reshape(p.N, 4, order="F")
+    st, rep, X = p.solve_host(B, tol=BWD, max_outer=30, restart=30)
+    assert st == t.TTG_OK, rep.as_dict()
+    if alpha == 1e-4:
+        assert rep.remedy == 5
+    assert rep.bwd_err <= BWD and bwd_err(A, X, B) <= 2 * BWD
+    p.close()
