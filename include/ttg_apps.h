@@ -32,7 +32,10 @@ typedef struct ttg_chol_args {
                                  4 (extension): longest remaining path in
                                  estimated device time (ttg_critical_path_priority);
                                  5 (extension): look-ahead — POTRF, then TRSM and
-                                 the next panel column's updates, then the rest  */
+                                 the next panel column's updates, then the rest;
+                                 6 (extension): POTRF(j), TRSM(j+1,j) and the
+                                 updates of tiles (j,j), (j+1,j) above all other
+                                 tasks (by column), the rest as kind 2          */
     int32_t accumulate;       /* --accumulate                                      */
     int32_t upper_block_size; /* --upper_block_size (-1 = block_size)              */
     int32_t matrix;           /* 0: 1/((i-j)^2+1) (the miniapp's); 1: G·Gᵀ/N + αI    */
@@ -43,7 +46,9 @@ typedef struct ttg_chol_args {
                                  updates, 2 = split-BF16 tensor-core updates (three
                                  BF16 slices per operand, six products, FP32-level
                                  accuracy), 3 = split-FP16 tensor-core updates (two
-                                 FP16 slices, three products, ~2^-22 accuracy); 0, 2
+                                 FP16 slices, three products, ~2^-22 accuracy; in
+                                 ttg_chol_posv* a first refinement step that gains
+                                 < 10x replaces it by the split-BF16 factor); 0, 2
                                  and 3 need uniform tiles, a multiple of 128        */
 } ttg_chol_args;
 
@@ -156,7 +161,8 @@ typedef struct ttg_solve_report {
     int32_t remedy;     /* mixed factor: 0 BF16 updates, 5 split-FP16 updates; after a
                            loss of definiteness 4 split-BF16 updates, 2 FP32 updates,
                            3 FP32 updates on A + 16·2^-24·diag(A), 1 BF16 updates on
-                           A + 8·2^-8·diag(A)                                          */
+                           A + 8·2^-8·diag(A); 4 also after a split-FP16 factor whose
+                           first refinement step gained < 10x (ttg_chol_posv*)     */
     double h2d_ms;      /* ttg_chol_posv_host / ttg_chol_solve_host: host-to-device copies
                            of the tiles and B (device events; 0 elsewhere)             */
     double d2h_ms;      /* ... the device-to-host copy of X                             */

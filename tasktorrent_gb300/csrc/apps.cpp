@@ -122,6 +122,12 @@ static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry, int upd, std::uni
     // (extension): look-ahead — three levels, the POTRFs, then the TRSMs and
     // the updates of the next panel column (GEMM (k, i, k+1)), then the other
     // updates; within a level tasks run in the order they become ready.
+    // kind 6 (extension): the critical chain above everything else — POTRF(j),
+    // TRSM(j+1, j) and every update of the tiles (j, j) and (j+1, j) at
+    // 9nb + 9(nb-j), the other TRSMs and updates of column j at kind 2's
+    // 9(nb-j)-2 — so a chain task never queues behind the bulk of a column
+    // (kind 2 ranks the next diagonal tile's update below the current
+    // column's TRSMs).  2nb distinct values: 128 levels for 64 tile columns.
     const int pk = a.kind == 4 ? 3 : a.kind;
     const bool mixed = a.precision == TTG_PREC_MIXED;
     auto block = [P](int i, int j) { return P->tiles + P->off[i + (size_t)j * P->nb]; };
@@ -132,6 +138,7 @@ static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry, int upd, std::uni
         if (pk == 5) return 3.0;
         if (pk == 3) return (double)(9 * (nb - j) - 1) + 18 * nb * nb;
         if (pk == 2) return (double)(9 * (nb - j) - 1);
+        if (pk == 6) return (double)(9 * nb + 9 * (nb - j));
         if (pk == 1) return 3.0 * (double)(nb - j);
         return 3.0;
     };
@@ -139,6 +146,7 @@ static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry, int upd, std::uni
         if (pk == 5) return 2.0;
         if (pk == 3) return (double)((nb - ij[0]) + nb * (9.0 * nb - 9.0 * ij[1] - 2.0) + 9 * nb * nb);
         if (pk == 2) return (double)(9 * (nb - ij[1]) - 2);
+        if (pk == 6) return ij[0] == ij[1] + 1 ? (double)(9 * nb + 9 * (nb - ij[1])) : (double)(9 * (nb - ij[1]) - 2);
         if (pk == 1) return 2.0 * (double)(nb - ij[0]);
         return 2.0;
     };
@@ -149,6 +157,7 @@ static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry, int upd, std::uni
             return (double)(nb - kij[1]) + nb * (9.0 * nb - 3.0 * kij[2] - 6.0 * kij[0] - 2.0);
         }
         if (pk == 2) return (double)(9 * nb - 9 * kij[2] - 2);
+        if (pk == 6) return kij[1] <= kij[2] + 1 ? (double)(9 * nb + 9 * (nb - kij[2])) : (double)(9 * (nb - kij[2]) - 2);
         if (pk == 1) return (double)(nb - kij[1]);
         return 1.0;
     };
@@ -610,8 +619,8 @@ extern "C" ttg_status ttg_chol_plan_get_input(ttg_chol_plan* P, double* h_A) {
     return TTG_OK;
 }
 
-extern "C" ttg_status ttg_chol_plan_solve(ttg_chol_plan* P, const double* d_B, double* d_X, const ttg_solve_opts* o,
-                                          ttg_solve_report* rep, void* stream) {
+static ttg_status plan_solve(ttg_chol_plan* P, const double* d_B, double* d_X, const ttg_solve_opts* o, ttg_solve_report* rep,
+                             void* stream, bool* weak_first_step) {
     if (!P || !o || !d_B || !d_X) return TTG_EINVAL;
     if (P->factor_gen == 0) return TTG_ESTATE;
     TTG_CUDA_CHECK(cudaSetDevice(P->ctx->device));
@@ -634,10 +643,40 @@ extern "C" ttg_status ttg_chol_plan_solve(ttg_chol_plan* P, const double* d_B, d
         }
     }
     ttg_solve_report r{};
-    ttg_status st = ttg_solver_solve(P->solver, P->pristine, P->tiles, L32, d_B, d_X, o, &r, s);
+    ttg_status st = ttg_solver_solve(P->solver, P->pristine, P->tiles, L32, d_B, d_X, o, &r, s, weak_first_step);
     r.remedy = mixed ? P->remedy : 0;
     r.solve_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     if (rep) *rep = r;
+    return st;
+}
+
+extern "C" ttg_status ttg_chol_plan_solve(ttg_chol_plan* P, const double* d_B, double* d_X, const ttg_solve_opts* o,
+                                          ttg_solve_report* rep, void* stream) {
+    return plan_solve(P, d_B, d_X, o, rep, stream, nullptr);
+}
+
+// The solve that follows a factorisation.  FP16 keeps 11 significant bits
+// over a narrow exponent range, so on an ill-conditioned matrix (small
+// pivots, factor entries far below their block row's scale) the split-FP16
+// factor (remedy 5) preconditions poorly: when its first classic refinement
+// step gains less than 10×, the plan factors again with split-BF16 updates
+// (remedy 4) and solves from the start — cheaper than a long GMRES on the
+// weaker preconditioner.
+static ttg_status solve_after_factor(ttg_chol_plan* P, const double* d_B, double* d_X, const ttg_solve_opts* o, ttg_solve_report* r,
+                                     void* stream, float factor_ms) {
+    bool weak = false;
+    const bool check = P->mixed && P->remedy == 5 && o->refine == 0;
+    ttg_status st = plan_solve(P, d_B, d_X, o, r, stream, check ? &weak : nullptr);
+    if (st == TTG_OK && weak) {
+        const double first_ms = r->solve_ms;
+        ttg_report fr{};
+        st = chol_factor_from(P, stream, &fr, 1);  // the split-BF16 attempt
+        if (st != TTG_OK) return st;
+        factor_ms += fr.elapsed_ms;
+        st = plan_solve(P, d_B, d_X, o, r, stream, nullptr);
+        r->solve_ms += first_ms;
+    }
+    r->factor_ms = factor_ms;
     return st;
 }
 
@@ -651,10 +690,8 @@ extern "C" ttg_status ttg_chol_posv(ttg_chol_plan* P, const double* d_B, double*
     ttg_report fr{};
     st = ttg_chol_plan_factor(P, stream, &fr);
     if (st != TTG_OK) return st;
-    const float factor_ms = fr.elapsed_ms;
     ttg_solve_report r{};
-    st = ttg_chol_plan_solve(P, d_B, d_X, o, &r, stream);
-    r.factor_ms = factor_ms;
+    st = solve_after_factor(P, d_B, d_X, o, &r, stream, fr.elapsed_ms);
     if (rep) *rep = r;
     return st;
 }
@@ -803,8 +840,7 @@ extern "C" ttg_status ttg_chol_posv_host(ttg_chol_plan* P, const double* h_tiles
         }
         TTG_CUDA_CHECK(ce);
         ttg_solve_report r{};
-        st = ttg_chol_plan_solve(P, P->d_b, P->d_b + blk, o, &r, stream);
-        r.factor_ms = fr.elapsed_ms;
+        st = solve_after_factor(P, P->d_b, P->d_b + blk, o, &r, stream, fr.elapsed_ms);
         if (rep) *rep = r;
         if (st != TTG_OK && st != TTG_ENOCONV) return st;
         TTG_CUDA_CHECK(cudaEventRecord(P->host_ev[2], s));

@@ -297,7 +297,9 @@ int ttg_task_parts(const ttg_op& op, bool team) {
     switch (op.kind) {
         case TTG_OP_GEMM_NT:
         case TTG_OP_GEMM_NN: {
-            const int e = gemm_block_edge(op.m, op.n, op.prec == TTG_PREC_F64);
+            // Row-vector products (m <= 16 right-hand-side rows) split their
+            // columns by 128 whatever the precision.
+            const int e = op.m <= 16 ? 128 : gemm_block_edge(op.m, op.n, op.prec == TTG_PREC_F64);
             max_parts = std::max(1, cdiv(op.m, e) * cdiv(op.n, e));
             auto_parts = std::min(16, max_parts);
             break;
@@ -330,6 +332,19 @@ int ttg_task_parts(const ttg_op& op, bool team) {
     return std::max(1, auto_parts);
 }
 
+// Flops per µs per block of a tile update: FP64 DFMA, FP32 FFMA (mixed flags
+// 1), or the tensor cores with plain BF16 (2), split BF16 (3: six products)
+// and split FP16 (4: three products) operands.
+static double mixed_update_rate(const ttg_op& op, bool mixed) {
+    if (!mixed) return 7.5e3;
+    switch (op.flags) {
+        case 2: return 3.0e6;
+        case 3: return 5.0e5;
+        case 4: return 1.0e6;
+        default: return 2.0e5;
+    }
+}
+
 // Estimated duration (µs) of a task on this executor: its flops over the
 // per-block rate of its kernel times the blocks that share it, plus a fixed
 // cost for claiming and releasing it.
@@ -350,12 +365,12 @@ static double task_cost_us(const ttg_op& op) {
             break;
         case TTG_OP_SYRK_LN:
             flops = n * n * k;
-            rate = mixed ? (op.flags == 2 ? 3.0e6 : (op.flags == 3 ? 5.0e5 : 2.0e5)) : 7.5e3;
+            rate = mixed_update_rate(op, mixed);
             break;
         case TTG_OP_GEMM_NT:
         case TTG_OP_GEMM_NN:
             flops = 2.0 * m * n * k;
-            rate = mixed ? (op.flags == 2 ? 3.0e6 : (op.flags == 3 ? 5.0e5 : 2.0e5)) : 7.5e3;
+            rate = mixed_update_rate(op, mixed);
             break;
         case TTG_OP_GEADD:
             flops = m * n;
@@ -427,14 +442,16 @@ static void assign_levels(int n, const double* prio, const std::vector<uint8_t>&
         *n_levels = (int)distinct.size();
         return;
     }
-    // Equal-count split of the sorted (descending) runnable priorities.
-    std::vector<double> cut(kMaxLevels);
-    for (int l = 0; l < kMaxLevels; ++l) cut[l] = vals[std::min(vals.size() - 1, (size_t)((l + 1) * vals.size() / kMaxLevels) - 1)];
+    // Equal-width split of the range of the runnable priorities: tasks whose
+    // priorities differ by more than a 128th of the range never share a
+    // level, wherever they sit in the order (an equal-count split leaves the
+    // few tasks of a factorisation's last steps in one first-in-first-out
+    // level, and their chain waits behind its own updates).
+    const double hi = distinct.front(), width = (distinct.front() - distinct.back()) / kMaxLevels;
     for (int t = 0; t < n; ++t) {
         if (!runnable[t]) continue;
-        int l = 0;
-        while (l < kMaxLevels - 1 && prio[t] < cut[l]) ++l;
-        level[t] = (uint8_t)l;
+        const double q = (hi - prio[t]) / width;
+        level[t] = (uint8_t)(q >= kMaxLevels - 1 ? kMaxLevels - 1 : (q > 0 ? (int)q : 0));
     }
     *n_levels = kMaxLevels;
 }

@@ -783,8 +783,9 @@ struct PhaseClock {
 }  // namespace
 
 ttg_status ttg_solver_solve(ttg_solver* S, const double* pristine, const double* L64, const float* L32, const double* d_B,
-                            double* d_X, const ttg_solve_opts* o, ttg_solve_report* rep, cudaStream_t s) {
+                            double* d_X, const ttg_solve_opts* o, ttg_solve_report* rep, cudaStream_t s, bool* weak_first_step) {
     PhaseClock clk(s, solve_verbose());
+    if (weak_first_step) *weak_first_step = false;
     const int nrhs = o->nrhs;
     if (nrhs < 1 || nrhs > kMaxRhs || !d_B || !d_X) return TTG_EINVAL;
     TTG_CUDA_CHECK(cudaSetDevice(S->ctx->device));
@@ -882,6 +883,11 @@ ttg_status ttg_solver_solve(ttg_solver* S, const double* pristine, const double*
             // FP32 sweeps per step, while each step gains at least 10×; a
             // step that gains less hands over to GMRES for the rest.
             if (richardson && outer > 0 && worst > 0.1 * prev) {
+                if (weak_first_step && outer == 1) {
+                    if (solve_verbose()) fprintf(stderr, "[ttg solve] first refinement step gained %.3g: new factor\n", prev / worst);
+                    *weak_first_step = true;
+                    break;
+                }
                 richardson = false;
                 after_richardson = true;
                 if (solve_verbose()) fprintf(stderr, "[ttg solve] outer %d: refinement step gained %.3g, GMRES from here\n", outer,

@@ -15,6 +15,10 @@ void ttg_solver_destroy(ttg_solver* S);
 void ttg_solver_input_changed(ttg_solver* S);
 // A new factor is in L64 (FP64 plan) or L32 (mixed plan): invert its diagonal tiles.
 ttg_status ttg_solver_factor_done(ttg_solver* S, const double* L64, const float* L32, cudaStream_t s);
-// Solve with the current factor (see ttg_chol_plan_solve).
+// Solve with the current factor (see ttg_chol_plan_solve).  With
+// weak_first_step set, a mixed solve whose first classic refinement step
+// gains less than 10× stops there and sets *weak_first_step (the caller
+// replaces the factor by a more accurate one and solves again).
 ttg_status ttg_solver_solve(ttg_solver* S, const double* pristine, const double* L64, const float* L32, const double* d_B,
-                            double* d_X, const ttg_solve_opts* o, ttg_solve_report* rep, cudaStream_t s);
+                            double* d_X, const ttg_solve_opts* o, ttg_solve_report* rep, cudaStream_t s,
+                            bool* weak_first_step = nullptr);

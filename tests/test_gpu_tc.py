@@ -154,14 +154,14 @@ def test_split_fp16_factor_accuracy(ctx, b, nb):
 @pytest.mark.parametrize("alpha", [1e-4, 1e-8])
 def test_split_fp16_refines_to_fp64_backward_error(ctx, alpha):
     """The split-FP16 factor keeps definiteness at alpha = 1e-4 (no remedy:
-    remedy 5) and the refinement reaches FP64 backward error; at 1e-8 the
-    refinement still converges (GMRES after the classic steps)."""
+    remedy 5) and the refinement reaches FP64 backward error; at 1e-8 its
+    first refinement step gains less than 10x, so the plan factors again
+    with split-BF16 updates (remedy 4) and converges from there."""
     p = t.CholPlan(ctx, 128, 8, kind=2, matrix=1, alpha=alpha, seed=2, precision=t.PREC_MIXED, mixed_kind=3)
     A = p.input_A()
     B = orc.normals(0, p.N * 4, 9, 1).reshape(p.N, 4, order="F")
     st, rep, X = p.solve_host(B, tol=BWD, max_outer=30, restart=30)
     assert st == t.TTG_OK, rep.as_dict()
-    if alpha == 1e-4:
-        assert rep.remedy == 5
+    assert rep.remedy == (5 if alpha == 1e-4 else 4), rep.as_dict()
     assert rep.bwd_err <= BWD and bwd_err(A, X, B) <= 2 * BWD
     p.close()
