@@ -33,9 +33,9 @@ typedef struct ttg_chol_args {
                                  estimated device time (ttg_critical_path_priority);
                                  5 (extension): look-ahead — POTRF, then TRSM and
                                  the next panel column's updates, then the rest;
-                                 6 (extension): POTRF(j), TRSM(j+1,j) and the
-                                 updates of tiles (j,j), (j+1,j) above all other
-                                 tasks (by column), the rest as kind 2          */
+                                 6 (extension): the tasks of the tiles within
+                                 two of the diagonal above all others (by
+                                 column), the rest as kind 2                    */
     int32_t accumulate;       /* --accumulate                                      */
     int32_t upper_block_size; /* --upper_block_size (-1 = block_size)              */
     int32_t matrix;           /* 0: 1/((i-j)^2+1) (the miniapp's); 1: G·Gᵀ/N + αI    */

@@ -122,9 +122,10 @@ static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry, int upd, std::uni
     // (extension): look-ahead — three levels, the POTRFs, then the TRSMs and
     // the updates of the next panel column (GEMM (k, i, k+1)), then the other
     // updates; within a level tasks run in the order they become ready.
-    // kind 6 (extension): the critical chain above everything else — POTRF(j),
-    // TRSM(j+1, j) and every update of the tiles (j, j) and (j+1, j) at
-    // 9nb + 9(nb-j), the other TRSMs and updates of column j at kind 2's
+    // kind 6 (extension): the critical chain above everything else — the
+    // tasks of the tiles within two of the diagonal (POTRF(j), TRSM(j+1, j),
+    // TRSM(j+2, j) and every update of the tiles (j, j), (j+1, j), (j+2, j))
+    // at 9nb + 9(nb-j), the other TRSMs and updates of column j at kind 2's
     // 9(nb-j)-2 — so a chain task never queues behind the bulk of a column
     // (kind 2 ranks the next diagonal tile's update below the current
     // column's TRSMs).  2nb distinct values: 128 levels for 64 tile columns.
@@ -146,7 +147,7 @@ static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry, int upd, std::uni
         if (pk == 5) return 2.0;
         if (pk == 3) return (double)((nb - ij[0]) + nb * (9.0 * nb - 9.0 * ij[1] - 2.0) + 9 * nb * nb);
         if (pk == 2) return (double)(9 * (nb - ij[1]) - 2);
-        if (pk == 6) return ij[0] == ij[1] + 1 ? (double)(9 * nb + 9 * (nb - ij[1])) : (double)(9 * (nb - ij[1]) - 2);
+        if (pk == 6) return ij[0] <= ij[1] + 2 ? (double)(9 * nb + 9 * (nb - ij[1])) : (double)(9 * (nb - ij[1]) - 2);
         if (pk == 1) return 2.0 * (double)(nb - ij[0]);
         return 2.0;
     };
@@ -157,7 +158,7 @@ static ttg_status chol_build_graph(ttg_chol_plan* P, bool dry, int upd, std::uni
             return (double)(nb - kij[1]) + nb * (9.0 * nb - 3.0 * kij[2] - 6.0 * kij[0] - 2.0);
         }
         if (pk == 2) return (double)(9 * nb - 9 * kij[2] - 2);
-        if (pk == 6) return kij[1] <= kij[2] + 1 ? (double)(9 * nb + 9 * (nb - kij[2])) : (double)(9 * (nb - kij[2]) - 2);
+        if (pk == 6) return kij[1] <= kij[2] + 2 ? (double)(9 * nb + 9 * (nb - kij[2])) : (double)(9 * (nb - kij[2]) - 2);
         if (pk == 1) return (double)(nb - kij[1]);
         return 1.0;
     };

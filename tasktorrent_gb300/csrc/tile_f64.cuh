@@ -571,20 +571,60 @@ __device__ __forceinline__ size_t team_xoff(int n, int lda, int k) {
 }
 
 // W1 (32 rows × nb, ld 33) <- W1 · Xᵀ for the lower triangular X = L_pp⁻¹
-// (ld 33): thread (row r, group g) forms columns g, g+8, g+16, g+24.
+// (ld 33): thread (row r, group g) forms columns g, 15-g, 16+g and 31-g
+// (column j sums j+1 products: 66 per thread in every group).
+__device__ __forceinline__ int team_apply_col(int g, int k) { return k == 0 ? g : (k == 1 ? 15 - g : (k == 2 ? 16 + g : 31 - g)); }
 __device__ inline void team_apply_inverse(double* W1, const double* X, int nb) {
     const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
     double acc[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        const int j = g + 8 * k;
+        const int j = team_apply_col(g, k);
         double a = 0.0;
         for (int c = 0; c <= j && c < nb; ++c) a = fma(W1[r * 33 + c], X[j * 33 + c], a);
         acc[k] = a;
     }
     __syncthreads();
 #pragma unroll
-    for (int k = 0; k < 4; ++k) W1[r * 33 + g + 8 * k] = acc[k];
+    for (int k = 0; k < 4; ++k) W1[r * 33 + team_apply_col(g, k)] = acc[k];
+}
+
+// S = lower(C) − W1·W1ᵀ for the nb×nb diagonal block (C at (r0, r0) of A, or
+// of the FP32 source when wide): the 528 lower entries packed over the
+// block's threads (half the FP64 instructions of a full 32×32 product: on
+// this GPU a warp's FP64 FMA holds its sub-partition's FP64 pipe for 64
+// cycles whatever lanes are active), three independent sums per thread (32
+// products each, in column order).  The upper part of S is zero.
+__device__ inline void team_syrk_lower(double* S, const double* W1, const double* A, int lda, const float* W32, int ldw, bool wide,
+                                       int r0, int nb) {
+    int rr[3], jj[3];
+    bool on[3];
+    double cv[3], acc[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const int e = threadIdx.x + q * kThreads;
+        int r = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
+        while (r > 0 && r * (r + 1) / 2 > e) --r;
+        while ((r + 1) * (r + 2) / 2 <= e) ++r;
+        rr[q] = r;
+        jj[q] = e - r * (r + 1) / 2;
+        on[q] = e < 528 && r < nb;
+        const size_t o = (size_t)(r0 + r) + (size_t)(r0 + jj[q]) * (wide ? ldw : lda);
+        cv[q] = !on[q] ? 0.0 : (wide ? (double)__ldcg(W32 + o) : ldcg(A + o));
+        acc[q] = 0.0;
+    }
+#pragma unroll 8
+    for (int c = 0; c < kPanel; ++c) {
+#pragma unroll
+        for (int q = 0; q < 3; ++q)
+            if (on[q]) acc[q] = fma(W1[rr[q] * 33 + c], W1[jj[q] * 33 + c], acc[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < 3; ++q)
+        if (threadIdx.x + q * kThreads < 528) {
+            S[rr[q] * 33 + jj[q]] = on[q] ? cv[q] - acc[q] : 0.0;
+            if (jj[q] != rr[q]) S[jj[q] * 33 + rr[q]] = 0.0;
+        }
 }
 
 // Team lower Cholesky of the FP64 tile A[n×n] (lda); requires team_fits(n).
@@ -668,24 +708,7 @@ __device__ inline int potrf_l_f64_team(int n, double* A, int lda, double* smem, 
                 team_publish(team_state(tc, p, q), p);
                 // S = lower(A_pp) - L_pq · L_pqᵀ, A_pp from the FP32 source on
                 // its first touch (q == 0), in the T item's order.
-                {
-                    const bool wide = W32 && q == 0;
-                    const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
-                    const int gi = kPanel * p + r;
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        const int j = g + 8 * k, gj = kPanel * p + j;
-                        double v = 0.0;
-                        if (r < nb && j < nb && r >= j) {
-                            const double cv = wide ? (double)__ldcg(W32 + gi + (size_t)gj * ldw) : ldcg(A + gi + (size_t)gj * lda);
-                            double acc = 0.0;
-#pragma unroll 8
-                            for (int c = 0; c < kPanel; ++c) acc = fma(W1[r * 33 + c], W1[j * 33 + c], acc);
-                            v = cv - acc;
-                        }
-                        S[r * 33 + j] = v;
-                    }
-                }
+                team_syrk_lower(S, W1, A, lda, W32, ldw, W32 && q == 0, kPanel * p, nb);
             } else {
                 team_load_block(S, A, lda, W32, ldw, W32 != nullptr, 0, 0, nb, nb, true);
             }
