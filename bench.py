@@ -10,8 +10,10 @@ right-hand sides, through ttg_chol_posv: the mixed-precision tiled Cholesky
 terms per operand, six products, for FP32-level updates (--mixed-kind 2) —
 FP32 TRSM, FP64 diagonal POTRF;
 one persistent-kernel launch of the task graph captured from the Taskflow<K>
-drop-in) followed by GMRES-based iterative refinement (FP64 residuals decide
-convergence; double-float ones steer the early steps).
+drop-in) followed by iterative refinement (classic steps x += M⁻¹r while
+each gains 10×, then GMRES; every residual an FP64-accurate product on the
+tensor cores).  The same step with split-FP16 updates (--mixed-kind 3: two
+FP16 terms per operand, three products) is reported beside it.
 Inputs (4.4 GB of FP64 lower tiles) are resident in HBM and larger than L2.
 `value` is N³/3 / time to solution (effective Cholesky TFLOP/s); solves/s is
 reported beside it.  `e2e` runs the same step through the C ABI with pinned
@@ -506,6 +508,22 @@ def run_ours(args, world, rank, local):
                                   "inner": ra.inner, "gmres_prec": ra.gmres_prec, "remedy": ra.remedy, "bwd_err": ra.bwd_err})
                 pa.close()
         extra["mixed_per_alpha"] = per_alpha
+        # The same step with split-FP16 updates (two FP16 slices per operand,
+        # three products; the split-BF16 factor replaces it when its first
+        # refinement step gains less than 10x), timed like the headline.
+        alt = 3 if args.mixed_kind != 3 else 2
+        pf = t.CholPlan(ctx, args.block, nb, n_threads=16, kind=args.kind, matrix=1, alpha=args.alpha, seed=args.seed + rank,
+                        precision=t.PREC_MIXED, mixed_kind=alt)
+        for _ in range(args.warmup):
+            posv(pf)
+        fm, fr = [], None
+        for _ in range(args.steps):
+            msf, fr = posv(pf)
+            fm.append(msf)
+        pf.close()
+        extra["mixed_kind_%d" % alt] = {"ms_per_step": statistics.mean(fm), "tflops": flops / (statistics.mean(fm) * 1e-3) / 1e12,
+                                        "factor_ms": fr.factor_ms, "bwd_err": fr.bwd_err, "outer": fr.outer, "inner": fr.inner,
+                                        "remedy": fr.remedy, "steps": args.steps}
     if not args.quick and not args.no_batched:
         extra["batched"] = run_batched(ctx, args)
     if not args.quick and not args.no_serving:

@@ -266,17 +266,22 @@ __device__ __forceinline__ void tc_block_coords(int b, int m, int n, bool lower,
 // products), which keeps the update FP32-accurate.  accf[b] says buffer b is
 // complete, afree[b] that it has been read.  All threads call it; returns
 // false if a wait timed out.
-__device__ inline bool tc_gemm_blocks(TcShared* sh, uint8_t* ring, const CUtensorMap* map, int slotA, int slotB, int b0, int nblk,
-                                      int k, float f, float* C, int ldc, int m, int n, bool lower, long long limit_ns, int split = 1,
-                                      int stride = 0) {
+// One instantiation per split (its slot and product counts are constants),
+// each compiled out of line: its registers and schedule do not depend on the
+// rest of the executor kernel.
+template <int SPLIT>
+static __device__ __noinline__ bool tc_gemm_blocks_t(TcShared* sh, uint8_t* ring, const CUtensorMap* map, int slotA, int slotB, int b0,
+                                                     int nblk, int k, float f, float* C, int ldc, int m, int n, bool lower,
+                                                     long long limit_ns, int stride) {
+    constexpr int split = SPLIT;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ksteps = k / kBK;
-    const int nsl = split;                 // slots (slices) per K step: 1, 2 (split FP16) or 3 (split BF16)
-    const int npairs = split == 3 ? 6 : (split == 2 ? 3 : 1);
+    constexpr int nsl = split;  // slots (slices) per K step: 1, 2 (split FP16) or 3 (split BF16)
+    constexpr int npairs = split == 3 ? 6 : (split == 2 ? 3 : 1);
     const int total = nsl * ksteps;      // slots per output block
     const uint32_t base = sh->nacc;
     const bool ok = !sh->failed;
-    const bool dbl = split == 1;  // double-buffered accumulators
+    constexpr bool dbl = split == 1;  // double-buffered accumulators
     auto buf_of = [&](uint32_t gi) { return dbl ? (int)(gi & 1) : 0; };
     auto use_of = [&](uint32_t gi) { return dbl ? (gi >> 1) : gi; };
     if (warp == 2 || warp == 3) {
@@ -317,6 +322,7 @@ __device__ inline bool tc_gemm_blocks(TcShared* sh, uint8_t* ring, const CUtenso
     } else if (threadIdx.x == 32 && ok) {
         // MMA issuer.
         const uint32_t idesc = split == 2 ? idesc_f16_f32(kBM, kBN) : idesc_bf16_f32(kBM, kBN);
+        const uint32_t ring_u32 = smem_u32(ring);
         uint32_t c = sh->consumed;
         bool good = true;
         for (int j = 0; j < nblk && good; ++j) {
@@ -333,7 +339,6 @@ __device__ inline bool tc_gemm_blocks(TcShared* sh, uint8_t* ring, const CUtenso
             const uint32_t dsmall = sh->tmem_base + (uint32_t)kBN;  // split: the five smaller products
             for (int ks = 0; ks < ksteps && good; ++ks, c += nsl) {
                 // The K step's slots (one per slice) must all be loaded.
-                uint32_t sbase[3];
                 for (int sl = 0; sl < nsl; ++sl) {
                     const uint32_t cs = c + sl;
                     if (!mbar_wait(&sh->full[cs % kSlots], (cs / kSlots) & 1, limit_ns)) {
@@ -341,13 +346,18 @@ __device__ inline bool tc_gemm_blocks(TcShared* sh, uint8_t* ring, const CUtenso
                         good = false;
                         break;
                     }
-                    sbase[sl] = smem_u32(ring + (size_t)(cs % kSlots) * kSlotBytes);
                 }
                 if (!good) break;
                 tc_fence_after();
+                // The K step's slot addresses in registers (an indexed array of
+                // them would live in local memory).
+                const uint32_t s0 = ring_u32 + (uint32_t)(c % kSlots) * kSlotBytes;
+                const uint32_t s1 = ring_u32 + (uint32_t)((c + 1) % kSlots) * kSlotBytes;
+                const uint32_t s2 = ring_u32 + (uint32_t)((c + 2) % kSlots) * kSlotBytes;
+                auto slot = [&](int sl) { return sl == 0 ? s0 : (sl == 1 ? s1 : s2); };
                 for (int pr = 0; pr < npairs; ++pr) {
-                    const uint32_t a0 = sbase[split == 3 ? split_pair_a(pr) : (split == 2 ? f16_pair_a(pr) : 0)];
-                    const uint32_t bb = sbase[split == 3 ? split_pair_b(pr) : (split == 2 ? f16_pair_b(pr) : 0)] + kSlotBytesA;
+                    const uint32_t a0 = slot(split == 3 ? split_pair_a(pr) : (split == 2 ? f16_pair_a(pr) : 0));
+                    const uint32_t bb = slot(split == 3 ? split_pair_b(pr) : (split == 2 ? f16_pair_b(pr) : 0)) + kSlotBytesA;
                     // pair npairs-1 is hi·hi (the only one when not split)
                     const bool big = pr == npairs - 1;
                     const uint32_t d = big ? dacc : dsmall;
@@ -424,6 +434,14 @@ __device__ inline bool tc_gemm_blocks(TcShared* sh, uint8_t* ring, const CUtenso
     if (threadIdx.x == 0) sh->nacc = base + nblk;
     __syncthreads();
     return !sh->failed;
+}
+
+__device__ inline bool tc_gemm_blocks(TcShared* sh, uint8_t* ring, const CUtensorMap* map, int slotA, int slotB, int b0, int nblk, int k,
+                                      float f, float* C, int ldc, int m, int n, bool lower, long long limit_ns, int split = 1,
+                                      int stride = 0) {
+    if (split == 3) return tc_gemm_blocks_t<3>(sh, ring, map, slotA, slotB, b0, nblk, k, f, C, ldc, m, n, lower, limit_ns, stride);
+    if (split == 2) return tc_gemm_blocks_t<2>(sh, ring, map, slotA, slotB, b0, nblk, k, f, C, ldc, m, n, lower, limit_ns, stride);
+    return tc_gemm_blocks_t<1>(sh, ring, map, slotA, slotB, b0, nblk, k, f, C, ldc, m, n, lower, limit_ns, stride);
 }
 
 }  // namespace tc

@@ -17,60 +17,64 @@
 namespace ttg {
 
 constexpr int kSmallM = 16;
-constexpr int kSmallKC = 16;              // k rows staged per pass
+constexpr int kSmallKC = 16;              // (layout of the TRSM's shared memory below)
+constexpr int kSmallKA = 128;             // k rows of A staged per pass of gemm_small_cols
+constexpr int kSmallU = 16;               // loads of B in flight per thread
 constexpr int kSmallBPad = kThreads + 1;  // staged B row (conflict-free stores)
-// Shared memory (elements of T) used by the small-m kernels.
+// Shared memory (elements of T) used by the small-m kernels: the staged A of
+// gemm_small_cols, then the TRSM's panel of L and its inverse diagonal.
 constexpr int kSmallSmem = kSmallKC * kSmallBPad + kSmallKC * kSmallM + kPanel * (kPanel + 1) + kPanel;
+static_assert(kSmallKA * kSmallM <= kSmallKC * kSmallBPad + kSmallKC * kSmallM, "staged A below the TRSM panel");
 
 // C[m×n] (columns [j0, j1)) <- alpha·A·op(B) + beta·C, m <= kSmallM; A is m×k
 // (lda).  op(B)(kk, j) = B[j + kk·ldb] (NT) or B[kk + j·ldb] (NN).  Thread t
-// owns columns j0 + t, j0 + t + kThreads, ...; k is staged kSmallKC rows at a
-// time through shared memory (coalesced loads for both layouts).
-template <class T, bool B_NN>
-__device__ void gemm_small_cols(int m, int j0, int j1, int k, T alpha, const T* A, int lda, const T* B, int ldb, T beta, T* C,
-                                int ldc, T* smem) {
-    T* sB = smem;                          // [kSmallKC][kSmallBPad]
-    T* sA = smem + kSmallKC * kSmallBPad;  // [kSmallKC][kSmallM]
+// owns columns j0 + t, j0 + t + kThreads, ... and reads its column of op(B)
+// straight from L2, kSmallU values at a time (all loads issued before the
+// FMAs, so a thread keeps kSmallU loads in flight; NT reads are coalesced
+// across the warp, NN reads walk down a column); A is staged kSmallKA rows
+// of k at a time through shared memory.  The product is HBM/L2-latency
+// bound (m·n·k FMAs on n·k elements of B): the work is the m·n·k the
+// operation needs and the reads are as many as there are elements of B.
+// MQ: kSmallM, or 1 when m == 1 (one right-hand side: no predicated rows).
+template <class T, bool B_NN, int MQ>
+__device__ void gemm_small_cols_q(int m, int j0, int j1, int k, T alpha, const T* A, int lda, const T* B, int ldb, T beta, T* C,
+                                  int ldc, T* smem) {
+    T* sA = smem;  // [kSmallKA][MQ]: sA[kk·MQ + q] = A(q, k0 + kk)
     for (int c0 = j0; c0 < j1; c0 += kThreads) {
-        const int cols = min(kThreads, j1 - c0);
         const int j = c0 + threadIdx.x;
-        T acc[kSmallM];
+        const bool act = j < j1;
+        T acc[MQ];
 #pragma unroll
-        for (int q = 0; q < kSmallM; ++q) acc[q] = T(0);
-        for (int k0 = 0; k0 < k; k0 += kSmallKC) {
-            const int kc = min(kSmallKC, k - k0);
+        for (int q = 0; q < MQ; ++q) acc[q] = T(0);
+        for (int k0 = 0; k0 < k; k0 += kSmallKA) {
+            const int kc = min(kSmallKA, k - k0);
             __syncthreads();
-            for (int e = threadIdx.x; e < kSmallKC * cols; e += kThreads) {
-                int kk, jj;
-                if (B_NN) {
-                    kk = e % kSmallKC;
-                    jj = e / kSmallKC;
-                } else {
-                    jj = e % cols;
-                    kk = e / cols;
-                }
-                T v = T(0);
-                if (kk < kc) v = B_NN ? ldcg(B + (k0 + kk) + (size_t)(c0 + jj) * ldb) : ldcg(B + (c0 + jj) + (size_t)(k0 + kk) * ldb);
-                sB[kk * kSmallBPad + jj] = v;
-            }
-            for (int e = threadIdx.x; e < kSmallKC * kSmallM; e += kThreads) {
-                const int q = e % kSmallM, kk = e / kSmallM;
+            for (int e = threadIdx.x; e < kSmallKA * MQ; e += kThreads) {
+                const int q = e % MQ, kk = e / MQ;
                 sA[e] = (q < m && kk < kc) ? ldcg(A + q + (size_t)(k0 + kk) * lda) : T(0);
             }
             __syncthreads();
-            if (threadIdx.x < cols) {
+            if (act) {
+                for (int u0 = 0; u0 < kc; u0 += kSmallU) {
+                    T b[kSmallU];
 #pragma unroll
-                for (int kk = 0; kk < kSmallKC; ++kk) {
-                    const T b = sB[kk * kSmallBPad + threadIdx.x];
+                    for (int u = 0; u < kSmallU; ++u) {
+                        const int kk = k0 + u0 + u;
+                        b[u] = u0 + u < kc ? ldcg(B_NN ? B + kk + (size_t)j * ldb : B + j + (size_t)kk * ldb) : T(0);
+                    }
 #pragma unroll
-                    for (int q = 0; q < kSmallM; ++q)
-                        if (q < m) acc[q] = fma(sA[kk * kSmallM + q], b, acc[q]);
+                    for (int u = 0; u < kSmallU; ++u) {
+                        const T* a = sA + (u0 + u) * MQ;
+#pragma unroll
+                        for (int q = 0; q < MQ; ++q)
+                            if (q < m) acc[q] = fma(a[q], b[u], acc[q]);
+                    }
                 }
             }
         }
-        if (threadIdx.x < cols) {
+        if (act) {
 #pragma unroll
-            for (int q = 0; q < kSmallM; ++q) {
+            for (int q = 0; q < MQ; ++q) {
                 if (q >= m) break;
                 T* p = C + q + (size_t)j * ldc;
                 T v = alpha * acc[q];
@@ -80,6 +84,76 @@ __device__ void gemm_small_cols(int m, int j0, int j1, int k, T alpha, const T* 
         }
     }
     __syncthreads();
+}
+
+// The NN form with B read down its columns: warp w takes columns j0 + w,
+// j0 + w + 8, ..., its lanes split k (kSmallUN loads of 32 consecutive
+// elements in flight per lane, coalesced), and the warp's partial sums are
+// added by shuffles.  A (m×k) is staged whole when it fits, else read from
+// L2.
+template <class T, int MQ>
+__device__ void gemm_small_cols_nn_warp(int m, int j0, int j1, int k, T alpha, const T* A, int lda, const T* B, int ldb, T beta,
+                                        T* C, int ldc, T* smem) {
+    constexpr int kSmallUN = 4;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    T* sA = smem;  // [k][MQ] when staged
+    const bool staged = k * MQ <= kSmallKA * kSmallM;
+    if (staged) {
+        for (int e = threadIdx.x; e < k * MQ; e += kThreads) {
+            const int q = e % MQ, kk = e / MQ;
+            sA[e] = q < m ? ldcg(A + q + (size_t)kk * lda) : T(0);
+        }
+        __syncthreads();
+    }
+    for (int j = j0 + warp; j < j1; j += kThreads / 32) {
+        T acc[MQ];
+#pragma unroll
+        for (int q = 0; q < MQ; ++q) acc[q] = T(0);
+        const T* bj = B + (size_t)j * ldb;
+        for (int k0 = 0; k0 < k; k0 += 32 * kSmallUN) {
+            T b[kSmallUN];
+#pragma unroll
+            for (int u = 0; u < kSmallUN; ++u) {
+                const int kk = k0 + 32 * u + lane;
+                b[u] = kk < k ? ldcg(bj + kk) : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < kSmallUN; ++u) {
+                const int kk = k0 + 32 * u + lane;
+                if (kk < k) {
+#pragma unroll
+                    for (int q = 0; q < MQ; ++q)
+                        if (q < m) acc[q] = fma(staged ? sA[kk * MQ + q] : ldcg(A + q + (size_t)kk * lda), b[u], acc[q]);
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < MQ; ++q) {
+            if (q >= m) break;
+            T v = acc[q];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) {
+                T* p = C + q + (size_t)j * ldc;
+                T r = alpha * v;
+                if (beta != T(0)) r = fma(beta, ldcg(p), r);
+                *p = r;
+            }
+        }
+    }
+    __syncthreads();
+}
+
+template <class T, bool B_NN>
+__device__ inline void gemm_small_cols(int m, int j0, int j1, int k, T alpha, const T* A, int lda, const T* B, int ldb, T beta, T* C,
+                                       int ldc, T* smem) {
+    if (B_NN) {
+        if (m == 1) gemm_small_cols_nn_warp<T, 1>(m, j0, j1, k, alpha, A, lda, B, ldb, beta, C, ldc, smem);
+        else gemm_small_cols_nn_warp<T, kSmallM>(m, j0, j1, k, alpha, A, lda, B, ldb, beta, C, ldc, smem);
+        return;
+    }
+    if (m == 1) gemm_small_cols_q<T, false, 1>(m, j0, j1, k, alpha, A, lda, B, ldb, beta, C, ldc, smem);
+    else gemm_small_cols_q<T, false, kSmallM>(m, j0, j1, k, alpha, A, lda, B, ldb, beta, C, ldc, smem);
 }
 
 // The part `part` of `parts` of a small-m GEMM: a contiguous range of columns.
@@ -159,18 +233,38 @@ __device__ inline void trsm_rows_small(int m, int n, T alpha, const T* L, int ld
 }
 
 // C[m×n] <- alpha·A + beta·C with A and C of either precision (TTG_OP_CONVERT:
-// flags bit 0: A is float, bit 1: C is float); parts split the elements.
+// flags bit 0: A is float, bit 1: C is float); parts split the elements,
+// each thread keeps kConvU elements' reads in flight.
+constexpr int kConvU = 8;
 __device__ inline void convert_tile(int m, int n, double alpha, const void* A, int lda, double beta, void* C, int ldc, int flags,
                                     int part, int parts) {
     const bool af = flags & 1, cf = flags & 2;
-    for (long e = threadIdx.x + (long)part * kThreads; e < (long)m * n; e += (long)kThreads * parts) {
-        const int i = (int)(e % m), j = (int)(e / m);
-        const size_t ia = i + (size_t)j * lda, ic = i + (size_t)j * ldc;
-        const double a = af ? (double)__ldcg((const float*)A + ia) : __ldcg((const double*)A + ia);
-        double v = alpha * a;
-        if (beta != 0.0) v = fma(beta, cf ? (double)__ldcg((const float*)C + ic) : __ldcg((const double*)C + ic), v);
-        if (cf) ((float*)C)[ic] = (float)v;
-        else ((double*)C)[ic] = v;
+    const long total = (long)m * n, stride = (long)kThreads * parts;
+    for (long e0 = threadIdx.x + (long)part * kThreads; e0 < total; e0 += stride * kConvU) {
+        double a[kConvU], c[kConvU];
+#pragma unroll
+        for (int u = 0; u < kConvU; ++u) {
+            const long e = e0 + u * stride;
+            a[u] = c[u] = 0.0;
+            if (e < total) {
+                const int i = (int)(e % m), j = (int)(e / m);
+                const size_t ia = i + (size_t)j * lda, ic = i + (size_t)j * ldc;
+                a[u] = af ? (double)__ldcg((const float*)A + ia) : __ldcg((const double*)A + ia);
+                if (beta != 0.0) c[u] = cf ? (double)__ldcg((const float*)C + ic) : __ldcg((const double*)C + ic);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kConvU; ++u) {
+            const long e = e0 + u * stride;
+            if (e < total) {
+                const int i = (int)(e % m), j = (int)(e / m);
+                const size_t ic = i + (size_t)j * ldc;
+                double v = alpha * a[u];
+                if (beta != 0.0) v = fma(beta, c[u], v);
+                if (cf) ((float*)C)[ic] = (float)v;
+                else ((double*)C)[ic] = v;
+            }
+        }
     }
     __syncthreads();
 }

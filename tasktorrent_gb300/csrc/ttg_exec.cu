@@ -321,9 +321,14 @@ int ttg_task_parts(const ttg_op& op, bool team) {
             if (op.prec == TTG_PREC_MIXED && op.kind == TTG_OP_TRSM_RLTN) auto_parts = std::min(max_parts, std::max(1, cdiv(op.m, 64)));
             break;
         case TTG_OP_GEADD:
-        case TTG_OP_CONVERT:
             max_parts = std::max(1, cdiv((long)op.m * op.n, 256));
             auto_parts = std::min(8, std::max(1, cdiv((long)op.m * op.n, 65536)));
+            break;
+        case TTG_OP_CONVERT:
+            // Conversions of whole tiles (batched and serving inputs, refinement
+            // vectors): 8192 elements per part, up to 16 parts.
+            max_parts = std::max(1, cdiv((long)op.m * op.n, 256));
+            auto_parts = std::min(16, std::max(1, cdiv((long)op.m * op.n, 8192)));
             break;
         default:
             return 1;
