@@ -42,6 +42,9 @@ struct System {
     int ir_steps = 0;        // mixed: refinement rounds
     int nrhs = 1;
     int potrf_parts = 0;     // blocks per diagonal POTRF (0: the executor's team rule)
+    // Mixed systems with tensor-core updates (split BF16): the device tables
+    // of ttg_mixed_tc_header (null: FP32 updates on the CUDA cores).
+    void* tc_tables = nullptr;
     // Device arrays of the system.
     double* A64 = nullptr;   // FP64 input tiles (packed lower, full diagonal tiles)
     double* W64 = nullptr;   // FP64: factor tiles
@@ -57,6 +60,10 @@ struct System {
         nb = (N + tile - 1) / tile;
     }
     int bs(int i) const { return i < nb - 1 ? tile : N - (nb - 1) * tile; }
+    // Tensor-core panel slot of lower tile (i, j): column-major over the lower tiles.
+    int slot(int i, int j) const { return j * nb - j * (j - 1) / 2 + (i - j); }
+    // Tensor-core updates apply: tiles a multiple of 128 up to 512, and updates to do.
+    static bool tc_fits(int n, int t) { return t % 128 == 0 && t <= 512 && n > t; }
     int displ(int i) const { return i * tile; }
     // Packed lower tiles, column by column: tile (i, j), i >= j.  Tile
     // columns c < j are full width (c < nb - 1) with N − c·tile rows.

@@ -12,6 +12,7 @@
 #include "../../include/ttg_batch.h"
 #include "../../include/ttg_philox.h"
 #include "batch_graph.h"
+#include "ttg_mixed_api.h"
 #include "ttg_internal.h"
 
 namespace {
@@ -158,21 +159,35 @@ static void build_factor(Graph& g, const System& S, std::vector<int>& potrf, std
         else if (op.kind == TTG_OP_TRSM_RLTN) op.parts = std::min(8, c128(op.m));
         return op;
     };
+    // Tensor-core systems: split-BF16 updates (mixed flags 3) on the panel
+    // slots that each TRSM publishes (ldb = its slot, k = its block row);
+    // an update's lda/ldb are the slots of L_ik and L_jk.
+    const bool tc = mx && S.tc_tables;
+    constexpr int kTcSplitBF16 = 3;
     for (int j = 0; j < nb; ++j) {
         ttg_op po = make_op(TTG_OP_POTRF_L, prec, S.bs(j), S.bs(j), 0, nullptr, 0, nullptr, 0, W(j, j), S.bs(j), 1.0, 0.0, 0,
                             mx ? (void*)(S.D64 + (size_t)j * S.tile * S.tile) : nullptr);
         po.parts = S.potrf_parts;
         potrf[j] = g.add(po);
         for (int i = j + 1; i < nb; ++i)
-            trsm[T(i, j)] = g.add(throughput(make_op(TTG_OP_TRSM_RLTN, prec, S.bs(i), S.bs(j), 0, W(j, j), S.bs(j), nullptr, 0,
-                                                     W(i, j), S.bs(i), 1.0, 0.0, mx ? 1 : 0)));
+            trsm[T(i, j)] = g.add(tc ? make_op(TTG_OP_TRSM_RLTN, prec, S.bs(i), S.bs(j), i, W(j, j), S.bs(j), nullptr, S.slot(i, j),
+                                               W(i, j), S.bs(i), 1.0, 0.0, kTcSplitBF16, S.tc_tables)
+                                     : throughput(make_op(TTG_OP_TRSM_RLTN, prec, S.bs(i), S.bs(j), 0, W(j, j), S.bs(j), nullptr,
+                                                          0, W(i, j), S.bs(i), 1.0, 0.0, mx ? 1 : 0)));
         for (int k = 0; k < j; ++k)
-            for (int i = j; i < nb; ++i)
+            for (int i = j; i < nb; ++i) {
+                if (tc) {
+                    gemm[G(k, i, j)] =
+                        g.add(make_op(i == j ? TTG_OP_SYRK_LN : TTG_OP_GEMM_NT, prec, S.bs(i), S.bs(j), S.bs(k), nullptr, S.slot(i, k),
+                                      nullptr, S.slot(j, k), W(i, j), S.bs(i), -1.0, 1.0, kTcSplitBF16, S.tc_tables));
+                    continue;
+                }
                 gemm[G(k, i, j)] = g.add(throughput(
                     i == j ? make_op(TTG_OP_SYRK_LN, prec, S.bs(i), S.bs(i), S.bs(k), W(i, k), S.bs(i), nullptr, 0, W(i, i), S.bs(i),
                                      -1.0, 1.0, mx ? 1 : 0)
                            : make_op(TTG_OP_GEMM_NT, prec, S.bs(i), S.bs(j), S.bs(k), W(i, k), S.bs(i), W(j, k), S.bs(j), W(i, j),
                                      S.bs(i), -1.0, 1.0, mx ? 1 : 0)));
+            }
     }
     if (mx)
         for (int j = 0; j < nb; ++j)
@@ -339,6 +354,14 @@ struct ttg_batch {
     float* W32 = nullptr;   // mixed: FP32 working tiles
     double *B = nullptr, *X = nullptr, *R = nullptr;
     float* D32 = nullptr;
+    // Tensor-core data of the mixed systems whose tiles allow it (split-BF16
+    // updates): headers, panel slots, slot and block-row scales, and the
+    // list of diagonal tiles whose block-row scales each run computes.
+    uint8_t* tc_hdr = nullptr;
+    __nv_bfloat16* tc_slots = nullptr;
+    float* tc_scales = nullptr;
+    TcRowScaleItem* tc_rs = nullptr;
+    int n_tc = 0, n_rs = 0;
     Graph g;
     uint64_t gen = 0;  // context graph generation of our upload
     cudaGraphExec_t gexec = nullptr;
@@ -378,9 +401,11 @@ ttg_status batch_record(ttg_batch* b, cudaStream_t s) {
         cudaGraphExecDestroy(b->gexec);
         b->gexec = nullptr;
     }
-    if (b->mixed) ttg_mixed_no_tc(b->ctx);  // the launch parameters are recorded with the graph
+    if (b->mixed) ttg_mixed_set_tc(b->ctx, b->n_tc > 0);  // the launch parameters are recorded with the graph
     TTG_CUDA_CHECK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     ttg_status st = TTG_OK;
+    // Block-row scales of the tensor-core systems (from their FP64 inputs).
+    if (b->n_rs > 0) st = ttg_mixed_row_scales(b->tc_rs, b->n_rs, s);
     if (!b->mixed) {
         if (cudaMemcpyAsync(b->W64, b->A64, sizeof(double) * b->tile_elems, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
             cudaMemcpyAsync(b->X, b->B, sizeof(double) * b->vec_elems, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
@@ -445,6 +470,55 @@ extern "C" ttg_status ttg_batch_create(ttg_ctx* ctx, const ttg_batch_args* args,
         ttg_batch_destroy(b);
         return st;
     }
+    // Tensor-core systems (mixed, tiles a multiple of 128 up to 512, more
+    // than one tile row): headers, slots (128-byte aligned per system) and
+    // scales, written once here.
+    std::vector<size_t> slot_base(args->n_systems, 0), scale_base(args->n_systems, 0), hdr_index(args->n_systems, 0);
+    if (b->mixed) {
+        size_t slots = 0, scales = 0;
+        for (int s = 0; s < args->n_systems; ++s) {
+            const System& S = b->sys[s];
+            if (!System::tc_fits(S.N, S.tile)) continue;
+            hdr_index[s] = (size_t)b->n_tc++;
+            slot_base[s] = slots;
+            slots += (ttg_mixed_tc_slot_elems(S.tile, S.nb) + 63) / 64 * 64;
+            scale_base[s] = scales;
+            scales += (size_t)(S.nb * (S.nb + 1) / 2 + S.nb + 31) / 32 * 32;
+            b->n_rs += S.nb;
+        }
+        if (b->n_tc > 0) {
+            std::vector<uint8_t> hh(kTcHeaderBytes * (size_t)b->n_tc);
+            std::vector<TcRowScaleItem> rs;
+            rs.reserve(b->n_rs);
+            if ((st = dev_alloc(&b->tc_hdr, kTcHeaderBytes * (size_t)b->n_tc)) != TTG_OK || (st = dev_alloc(&b->tc_slots, slots)) != TTG_OK ||
+                (st = dev_alloc(&b->tc_scales, scales)) != TTG_OK || (st = dev_alloc(&b->tc_rs, (size_t)b->n_rs)) != TTG_OK) {
+                ttg_batch_destroy(b);
+                return st;
+            }
+            for (int s = 0; s < args->n_systems; ++s) {
+                System& S = b->sys[s];
+                if (!System::tc_fits(S.N, S.tile)) continue;
+                const size_t h = hdr_index[s];
+                float* slot_scale = b->tc_scales + scale_base[s];
+                float* rowscale = slot_scale + S.nb * (S.nb + 1) / 2;
+                st = ttg_mixed_tc_header(hh.data() + kTcHeaderBytes * h, b->tc_hdr + kTcHeaderBytes * h, b->tc_slots + slot_base[s],
+                                         slot_scale, rowscale, S.tile, S.nb, &S.tc_tables);
+                if (st != TTG_OK) {
+                    ttg_batch_destroy(b);
+                    return st;
+                }
+                for (int i = 0; i < S.nb; ++i)
+                    rs.push_back(TcRowScaleItem{b->A64 + tb[s] + S.off(i, i), S.bs(i), S.bs(i), rowscale + i});
+            }
+            cudaError_t e = cudaMemcpy(b->tc_hdr, hh.data(), hh.size(), cudaMemcpyHostToDevice);
+            if (e == cudaSuccess) e = cudaMemcpy(b->tc_rs, rs.data(), sizeof(TcRowScaleItem) * rs.size(), cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) {
+                ttg_set_last_cuda_error(e, "cudaMemcpy (tensor-core tables)", __FILE__, __LINE__);
+                ttg_batch_destroy(b);
+                return TTG_ECUDA;
+            }
+        }
+    }
     for (int s = 0; s < args->n_systems; ++s) {
         System& S = b->sys[s];
         S.A64 = b->A64 + tb[s];
@@ -482,7 +556,8 @@ extern "C" void ttg_batch_destroy(ttg_batch* b) {
     cudaSetDevice(b->ctx->device);
     if (b->gexec) cudaGraphExecDestroy(b->gexec);
     if (b->own) cudaStreamDestroy(b->own);
-    for (void* p : {(void*)b->A64, (void*)b->W64, (void*)b->W32, (void*)b->B, (void*)b->X, (void*)b->R, (void*)b->D32})
+    for (void* p : {(void*)b->A64, (void*)b->W64, (void*)b->W32, (void*)b->B, (void*)b->X, (void*)b->R, (void*)b->D32,
+                    (void*)b->tc_hdr, (void*)b->tc_slots, (void*)b->tc_scales, (void*)b->tc_rs})
         if (p) cudaFree(p);
     delete b;
 }

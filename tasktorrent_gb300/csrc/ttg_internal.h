@@ -118,8 +118,6 @@ ttg_status ttg_gen_gemm_tiles(ttg_ctx* c, int32_t N, int32_t b, int32_t inputs, 
 ttg_status ttg_mixed_init(ttg_ctx* c);
 void ttg_mixed_free(ttg_ctx* c);
 ttg_status ttg_launch_mixed(ttg_ctx* c, const ttg::ExecParams& p, cudaStream_t s);
-// Graphs without tensor-core tasks (no plan tensor map in the launch).
-void ttg_mixed_no_tc(ttg_ctx* c);
 int ttg_mixed_max_workers(const ttg_ctx* c);
 
 #define TTG_CUDA_CHECK(expr)                                                            \

@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstring>
 #include <vector>
 
 #include "../../include/ttg.h"
@@ -44,6 +45,9 @@ struct MixedTables {
     const float* rowscale;
     int b;
     int n_slots;
+    // Tensor map over b16 in device memory (a system of a batch or a serving
+    // request), or null: the kernel parameter's map (a Cholesky plan).
+    const CUtensorMap* map;
 };
 
 // Kernel parameters of the mixed executor (the tensor map must live in the
@@ -140,7 +144,7 @@ __device__ __forceinline__ bool trsm_resident_ok(int m, int n, const float* L, i
 
 // Rows [r0, r0 + rows) (r0 and rows multiples of 4, rows <= 64) solved in
 // shared memory; on return Bs holds the solved slice (also written to B).
-__device__ void trsm_rltn_f32_resident(int n, float alpha, const float* L, int ldl, float* B, int ldb, int r0, int rows,
+static __device__ __noinline__ void trsm_rltn_f32_resident(int n, float alpha, const float* L, int ldl, float* B, int ldb, int r0, int rows,
                                        float* smem) {
     float* Bs = smem;
     float* Ls = smem + kTrsmRows * kTrsmMaxN;
@@ -233,7 +237,7 @@ __device__ void trsm_rltn_f32_resident(int n, float alpha, const float* L, int l
 // padded row-major buffer in the panel area, so the slot rows are written
 // with consecutive columns.
 // split: 1 plain BF16, 3 three BF16 slices, 2 split FP16 (mixed_split).
-__device__ void publish_bf16_resident(const float* smem, int n, int r0, int rows, __nv_bfloat16* dst, size_t slice, int b, float inv,
+static __device__ __noinline__ void publish_bf16_resident(const float* smem, int n, int r0, int rows, __nv_bfloat16* dst, size_t slice, int b, float inv,
                                       int split) {
     const int nslices = split;
     const float* Bs = smem;
@@ -389,7 +393,8 @@ __device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem,
                 const int per = (nblk + parts - 1) / parts;
                 const float f = (float)op.alpha * __ldcg(tb->slot_scale + op.lda) * __ldcg(tb->slot_scale + op.ldb);
                 const int b0 = min(nblk, part * per), b1 = min(nblk, (part + 1) * per);
-                if (b1 > b0 && !tc::tc_gemm_blocks(tsh, ring, tmap, op.lda, op.ldb, b0, b1 - b0, op.k, f, (float*)op.c, op.ldc, op.m,
+                const CUtensorMap* mp = tb->map ? tb->map : tmap;
+                if (b1 > b0 && !tc::tc_gemm_blocks(tsh, ring, mp, op.lda, op.ldb, b0, b1 - b0, op.k, f, (float*)op.c, op.ldc, op.m,
                                                    op.n, lower, limit_ns, mixed_split(op.flags), tb->n_slots) &&
                     threadIdx.x == 0)
                     atomicCAS(err, 0, TTG_ETIMEOUT);
@@ -514,10 +519,6 @@ ttg_status ttg_mixed_init(ttg_ctx* c) {
     return TTG_OK;
 }
 
-void ttg_mixed_no_tc(ttg_ctx* c) {
-    if (c->mixed) ((MixedCtx*)c->mixed)->globals.has_tc = 0;
-}
-
 int ttg_mixed_max_workers(const ttg_ctx* c) { return c->mixed ? ((const MixedCtx*)c->mixed)->max_workers : 0; }
 
 void ttg_mixed_free(ttg_ctx* c) {
@@ -558,7 +559,9 @@ struct ttg_mixed_state {
 
 static int slot_of(const ttg_mixed_state* m, int i, int j) { return (int)(m->off[i + (size_t)j * m->nb] / ((int64_t)m->b * m->b)); }
 
-static ttg_status encode_tmap(ttg_mixed_state* m, int n_slots) {
+// Tensor map over n_slots b×b K-major slots of three slices (slice s of
+// slot t at z = t + s·n_slots): boxes of 32 columns × 128 rows, 64-byte swizzle.
+static ttg_status encode_slot_map(CUtensorMap* map, void* b16, int b, int n_slots) {
     void* fn = nullptr;
     cudaDriverEntryPointQueryResult q;
     cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
@@ -567,20 +570,87 @@ static ttg_status encode_tmap(ttg_mixed_state* m, int n_slots) {
         return TTG_ECUDA;
     }
     auto encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
-    const int b = m->b;
     cuuint64_t dims[3] = {(cuuint64_t)b, (cuuint64_t)b, (cuuint64_t)(3 * n_slots)};  // three slices
     cuuint64_t strides[2] = {(cuuint64_t)b * 2, (cuuint64_t)b * b * 2};
     cuuint32_t box[3] = {(cuuint32_t)tc::kBK, 128u, 1u};
     cuuint32_t estr[3] = {1, 1, 1};
-    CUresult r = encode(&m->globals.tmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, (void*)m->b16, dims, strides, box, estr,
-                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, b16, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
         ttg_set_last_cuda_error(cudaErrorInvalidValue, "cuTensorMapEncodeTiled", __FILE__, __LINE__);
         return TTG_EINVAL;
     }
-    m->globals.has_tc = 1;
     return TTG_OK;
+}
+
+static ttg_status encode_tmap(ttg_mixed_state* m, int n_slots) {
+    const ttg_status st = encode_slot_map(&m->globals.tmap, (void*)m->b16, m->b, n_slots);
+    if (st == TTG_OK) m->globals.has_tc = 1;
+    return st;
+}
+
+// ------------------------------------------------ per-system tensor-core data
+
+// Header of one system in device memory: its tensor map, then its tables.
+struct __align__(128) TcSysHeader {
+    CUtensorMap map;
+    MixedTables tables;
+};
+static_assert(sizeof(TcSysHeader) <= kTcHeaderBytes, "tensor-core system header");
+
+size_t ttg_mixed_tc_slot_elems(int b, int nb) { return (size_t)3 * (size_t)(nb * (nb + 1) / 2) * b * b; }
+
+ttg_status ttg_mixed_tc_header(void* host_hdr, void* dev_hdr, __nv_bfloat16* slots, float* slot_scale, const float* rowscale, int b,
+                               int nb, void** tables) {
+    if (!host_hdr || !dev_hdr || !slots || !slot_scale || !rowscale || b <= 0 || b % 128 != 0 || b > 512 || nb < 1 ||
+        ((uintptr_t)dev_hdr & 127) != 0 || ((uintptr_t)slots & 127) != 0)
+        return TTG_EINVAL;
+    TcSysHeader* h = reinterpret_cast<TcSysHeader*>(host_hdr);
+    memset(h, 0, sizeof(TcSysHeader));
+    const int n_slots = nb * (nb + 1) / 2;
+    const ttg_status st = encode_slot_map(&h->map, slots, b, n_slots);
+    if (st != TTG_OK) return st;
+    TcSysHeader* d = reinterpret_cast<TcSysHeader*>(dev_hdr);
+    h->tables = MixedTables{slots, slot_scale, rowscale, b, n_slots, &d->map};
+    if (tables) *tables = &d->tables;
+    return TTG_OK;
+}
+
+namespace ttg {
+// One block per item: 2^e >= sqrt(max |diag|) of the item's diagonal tile.
+__global__ void row_scales_list(const TcRowScaleItem* items, int n) {
+    __shared__ double red[128];
+    for (int it = blockIdx.x; it < n; it += gridDim.x) {
+        const TcRowScaleItem x = items[it];
+        double mx = 0.0;
+        for (int r = threadIdx.x; r < x.bs; r += blockDim.x) mx = fmax(mx, fabs(x.diag[r + (size_t)r * x.ld]));
+        red[threadIdx.x] = mx;
+        __syncthreads();
+        for (int s2 = blockDim.x / 2; s2 > 0; s2 >>= 1) {
+            if (threadIdx.x < s2) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s2]);
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            int e = 0;
+            frexp(sqrt(fmax(red[0], 1e-300)), &e);
+            *x.out = ldexpf(1.0f, e);
+        }
+        __syncthreads();
+    }
+}
+}  // namespace ttg
+
+ttg_status ttg_mixed_row_scales(const TcRowScaleItem* d_items, int n, void* stream) {
+    if (n <= 0) return TTG_OK;
+    if (!d_items) return TTG_EINVAL;
+    ttg_note_launch();
+    row_scales_list<<<std::min(n, 4096), 128, 0, (cudaStream_t)stream>>>(d_items, n);
+    TTG_CUDA_CHECK(cudaGetLastError());
+    return TTG_OK;
+}
+
+void ttg_mixed_set_tc(ttg_ctx* c, bool on) {
+    if (c->mixed) ((MixedCtx*)c->mixed)->globals.has_tc = on ? 1 : 0;
 }
 
 ttg_status ttg_mixed_state_create(ttg_ctx* ctx, int N, int nb, const int* bs, const int64_t* off, double* tiles64, int kind,
@@ -627,7 +697,7 @@ ttg_status ttg_mixed_state_create(ttg_ctx* ctx, int N, int nb, const int* bs, co
         std::vector<int64_t> doff(nb);
         for (int i = 0; i < nb; ++i) doff[i] = off[i + (size_t)i * nb];
         cudaMemcpy(m->diag_off, doff.data(), sizeof(int64_t) * nb, cudaMemcpyHostToDevice);
-        MixedTables t{m->b16, m->slot_scale, m->rowscale, m->b, n_slots};
+        MixedTables t{m->b16, m->slot_scale, m->rowscale, m->b, n_slots, nullptr};
         cudaMemcpy(m->tables, &t, sizeof(t), cudaMemcpyHostToDevice);
         ttg_status st = encode_tmap(m, n_slots);
         if (st != TTG_OK) {

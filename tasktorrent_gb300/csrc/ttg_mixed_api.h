@@ -7,6 +7,8 @@
 // tensor-core updates), and the FP64 tiles of the plan used as scratch for the
 // FP64 diagonal POTRF.
 #pragma once
+#include <cuda_bf16.h>
+#include <stddef.h>
 #include <stdint.h>
 
 #include "../../include/ttg.h"
@@ -56,3 +58,28 @@ uint32_t ttg_mixed_gate_begin(ttg_mixed_state* m, void* stream, bool converted);
 const double* ttg_mixed_factor_tiles(ttg_mixed_state* m);
 // The FP32 factor tiles (same layout as tiles64).
 const float* ttg_mixed_factor32(ttg_mixed_state* m);
+
+// Tensor-core updates for the systems of a batch or a serving lane (uniform
+// tiles b, a multiple of 128 up to 512, except a ragged last tile row): each
+// system has kTcHeaderBytes of header (its tensor map and tables, 128-byte
+// aligned) and ttg_mixed_tc_slot_elems BF16 values of panel slots (three
+// slices of one b×b slot per lower tile (i, j), slot j·nb − j(j−1)/2 + i − j),
+// n_slots slot scales and nb block-row scales, all in device memory the
+// caller owns.  The ops of such a system carry the device tables as aux
+// (TRSM: ldb = slot, k = block row; GEMM/SYRK: lda, ldb = slots).
+constexpr size_t kTcHeaderBytes = 256;
+size_t ttg_mixed_tc_slot_elems(int b, int nb);
+// Fill the host copy of a header (copied by the caller to dev_hdr); *tables
+// receives the device address of its tables.
+ttg_status ttg_mixed_tc_header(void* host_hdr, void* dev_hdr, __nv_bfloat16* slots, float* slot_scale, const float* rowscale, int b,
+                               int nb, void** tables);
+// Block-row scales (2^e >= sqrt(max |diag|) of each diagonal tile) of a list
+// of tiles, before a launch that publishes slots scaled by them.
+struct TcRowScaleItem {
+    const double* diag;  // the diagonal tile (FP64 input)
+    int bs, ld;
+    float* out;
+};
+ttg_status ttg_mixed_row_scales(const TcRowScaleItem* d_items, int n, void* stream);
+// Whether the mixed executor of ctx sets up the tensor cores (TMEM, barriers).
+void ttg_mixed_set_tc(ttg_ctx* ctx, bool on);

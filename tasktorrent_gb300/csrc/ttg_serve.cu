@@ -24,6 +24,7 @@
 #include "../../include/ttg_philox.h"
 #include "../../include/ttg_serve.h"
 #include "batch_graph.h"
+#include "ttg_mixed_api.h"
 #include "ttg_internal.h"
 
 using namespace ttg::batch;
@@ -118,6 +119,7 @@ struct ServeRequest {
     double* R = nullptr;
     float* D32 = nullptr;
     double* D64 = nullptr;  // mixed factorisation scratch
+    uint8_t* tc = nullptr;  // mixed, tensor-core updates: header, scales, panel slots
     size_t work_bytes = 0;
     int key = -1;  // resident factor it factors or uses
     std::vector<double> result;
@@ -148,6 +150,13 @@ struct Lane {
     unsigned long long* d_acc = nullptr;
     double* h_err = nullptr;     // pinned
     double* d_err = nullptr;
+    // Tensor-core systems of the launch: their headers (pinned staging) and
+    // the diagonal tiles whose block-row scales run before the executor.
+    uint8_t* h_hdr = nullptr;  // pinned, max_batch headers
+    std::vector<TcRowScaleItem> rs;
+    TcRowScaleItem* h_rs = nullptr;  // pinned
+    TcRowScaleItem* d_rs = nullptr;
+    int rs_cap = 0, n_hdr = 0;
 };
 
 struct ttg_serve {
@@ -170,6 +179,11 @@ size_t factor_bytes(const ttg_serve* s, int N, int tile) {
     return e * 8 + (s->a.precision == TTG_PREC_MIXED ? e * 4 : e * 8);
 }
 
+// Tensor-core data of a mixed factorisation: header, slot and block-row
+// scales (256-byte aligned), then the panel slots.
+size_t tc_scale_bytes(const System& S) { return ((size_t)(S.nb * (S.nb + 1) / 2 + S.nb) * 4 + 255) / 256 * 256; }
+size_t tc_bytes(const System& S) { return kTcHeaderBytes + tc_scale_bytes(S) + ttg_mixed_tc_slot_elems(S.tile, S.nb) * 2; }
+
 size_t work_bytes(const ttg_serve* s, int N, int tile, bool factor) {
     const size_t v = (size_t)N * s->a.nrhs;
     size_t b = v * 16;  // B, X
@@ -179,6 +193,7 @@ size_t work_bytes(const ttg_serve* s, int N, int tile, bool factor) {
             System S;
             S.set_size(N, tile);
             b += (size_t)S.nb * S.tile * S.tile * 8;  // diagonal POTRF scratch
+            if (System::tc_fits(S.N, S.tile)) b += tc_bytes(S);
         }
     }
     return b;
@@ -283,6 +298,23 @@ bool admit(ttg_serve* s, Lane& L, int i, ttg_status* err) {
     if (e == TTG_OK && mixed) {
         if ((e = pool_alloc(&q.R, v, st)) == TTG_OK) e = pool_alloc(&q.D32, v, st);
         if (e == TTG_OK && need_factor) e = pool_alloc(&q.D64, (size_t)S.nb * S.tile * S.tile, st);
+        // Split-BF16 updates on the tensor cores when the tiles allow it.
+        if (e == TTG_OK && need_factor && System::tc_fits(S.N, S.tile) && L.n_hdr < s->a.max_batch) {
+            e = pool_alloc(&q.tc, tc_bytes(S), st);
+            if (e == TTG_OK) {
+                float* slot_scale = (float*)(q.tc + kTcHeaderBytes);
+                float* rowscale = slot_scale + S.nb * (S.nb + 1) / 2;
+                __nv_bfloat16* slots = (__nv_bfloat16*)(q.tc + kTcHeaderBytes + tc_scale_bytes(S));
+                uint8_t* h = L.h_hdr + kTcHeaderBytes * (size_t)L.n_hdr;
+                e = ttg_mixed_tc_header(h, q.tc, slots, slot_scale, rowscale, S.tile, S.nb, &S.tc_tables);
+                if (e == TTG_OK)
+                    e = cudaMemcpyAsync(q.tc, h, kTcHeaderBytes, cudaMemcpyHostToDevice, st) == cudaSuccess ? TTG_OK : TTG_ECUDA;
+                if (e == TTG_OK) {
+                    ++L.n_hdr;
+                    for (int i = 0; i < S.nb; ++i) L.rs.push_back(TcRowScaleItem{r.A64 + S.off(i, i), S.bs(i), S.bs(i), rowscale + i});
+                }
+            }
+        }
     }
     if (e == TTG_OK) e = ttg_gen_rhs_rows_async(q.N, s->a.nrhs, q.seed_b, q.B, st);
     if (e == TTG_OK && !mixed)
@@ -312,6 +344,8 @@ bool admit(ttg_serve* s, Lane& L, int i, ttg_status* err) {
 ttg_status dispatch(ttg_serve* s, Lane& L, std::deque<int>& queue) {
     L.g.clear();
     L.reqs.clear();
+    L.rs.clear();
+    L.n_hdr = 0;
     ttg_status err = TTG_OK;
     double flops = 0.0;
     for (auto it = queue.begin(); it != queue.end() && (int)L.reqs.size() < s->a.max_batch;) {
@@ -334,6 +368,14 @@ ttg_status dispatch(ttg_serve* s, Lane& L, std::deque<int>& queue) {
     if (st != TTG_OK) return st;
     ttg_graph_desc d = L.g.desc();
     if ((st = ttg_graph_upload(L.ctx, &d)) != TTG_OK) return st;
+    // Block-row scales of the launch's tensor-core factorisations.
+    if ((int)L.rs.size() > L.rs_cap) return TTG_EINVAL;
+    if (!L.rs.empty()) {
+        std::copy(L.rs.begin(), L.rs.end(), L.h_rs);
+        TTG_CUDA_CHECK(cudaMemcpyAsync(L.d_rs, L.h_rs, sizeof(TcRowScaleItem) * L.rs.size(), cudaMemcpyHostToDevice, L.s));
+        if ((st = ttg_mixed_row_scales(L.d_rs, (int)L.rs.size(), L.s)) != TTG_OK) return st;
+    }
+    ttg_mixed_set_tc(L.ctx, L.n_hdr > 0);
     if ((st = ttg_launch(L.ctx, L.s)) != TTG_OK) return st;
     // Backward errors of the launch, then the completion event.
     const int n = (int)L.reqs.size();
@@ -385,6 +427,7 @@ ttg_status complete(ttg_serve* s, Lane& L, std::deque<int>& queue, double t) {
         pool_free(q.R, L.s);
         pool_free(q.D32, L.s);
         pool_free(q.D64, L.s);
+        pool_free(q.tc, L.s);
         s->used -= q.work_bytes;
         q.work_bytes = 0;
         Resident& r = s->res[q.key];
@@ -464,6 +507,11 @@ extern "C" ttg_status ttg_serve_create(int device, const ttg_serve_args* a, ttg_
             if (e == cudaSuccess) e = cudaMalloc((void**)&L.d_acc, sizeof(unsigned long long) * 33 * maxb);
             if (e == cudaSuccess) e = cudaMallocHost((void**)&L.h_err, sizeof(double) * maxb);
             if (e == cudaSuccess) e = cudaMalloc((void**)&L.d_err, sizeof(double) * maxb);
+            // Diagonal tiles of the launch's factorisations: nb <= n_max / 128 + 1.
+            L.rs_cap = maxb * (a->n_max / 128 + 2);
+            if (e == cudaSuccess) e = cudaMallocHost((void**)&L.h_hdr, kTcHeaderBytes * (size_t)maxb);
+            if (e == cudaSuccess) e = cudaMallocHost((void**)&L.h_rs, sizeof(TcRowScaleItem) * (size_t)L.rs_cap);
+            if (e == cudaSuccess) e = cudaMalloc((void**)&L.d_rs, sizeof(TcRowScaleItem) * (size_t)L.rs_cap);
         }
         if (st != TTG_OK || e != cudaSuccess) {
             if (e != cudaSuccess) ttg_set_last_cuda_error(e, "serve lane set-up", __FILE__, __LINE__);
@@ -492,7 +540,7 @@ extern "C" void ttg_serve_destroy(ttg_serve* s) {
             if (p) cudaFree(p);
     }
     for (ServeRequest& q : s->req)
-        for (void* p : {(void*)q.B, (void*)q.X, (void*)q.R, (void*)q.D32, (void*)q.D64})
+        for (void* p : {(void*)q.B, (void*)q.X, (void*)q.R, (void*)q.D32, (void*)q.D64, (void*)q.tc})
             if (p) cudaFree(p);
     for (Lane& L : s->lanes) {
         if (L.ctx) ttg_destroy(L.ctx);
@@ -500,6 +548,9 @@ extern "C" void ttg_serve_destroy(ttg_serve* s) {
         if (L.s) cudaStreamDestroy(L.s);
         if (L.h_items) cudaFreeHost(L.h_items);
         if (L.d_items) cudaFree(L.d_items);
+        if (L.h_hdr) cudaFreeHost(L.h_hdr);
+        if (L.h_rs) cudaFreeHost(L.h_rs);
+        if (L.d_rs) cudaFree(L.d_rs);
         if (L.d_acc) cudaFree(L.d_acc);
         if (L.h_err) cudaFreeHost(L.h_err);
         if (L.d_err) cudaFree(L.d_err);
