@@ -144,9 +144,65 @@ __device__ void gemm_small_cols_nn_warp(int m, int j0, int j1, int k, T alpha, c
     __syncthreads();
 }
 
+// The NN form with one right-hand side (m = 1), k <= kSmallKA·kSmallM: the
+// row of A staged whole; a warp takes kSmallCW columns at a time, its lanes
+// split k (kSmallUN loads of 32 consecutive elements per column in flight
+// per lane), shuffle reductions.  (Splitting k over thread groups for the NT
+// form, with a shared-memory reduction, measured 2.7× slower per task than
+// one thread per column.)
+constexpr int kSmallCW = 4;
+template <class T>
+__device__ void gemm_small_nn_m1(int j0, int j1, int k, T alpha, const T* A, int lda, const T* B, int ldb, T beta, T* C, int ldc,
+                                 T* smem) {
+    constexpr int kSmallUN = 4;
+    T* sA = smem;  // [k]
+    for (int e = threadIdx.x; e < k; e += kThreads) sA[e] = ldcg(A + (size_t)e * lda);
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int jb = j0 + kSmallCW * warp; jb < j1; jb += kSmallCW * (kThreads / 32)) {
+        T acc[kSmallCW];
+#pragma unroll
+        for (int c = 0; c < kSmallCW; ++c) acc[c] = T(0);
+        for (int k0 = 0; k0 < k; k0 += 32 * kSmallUN) {
+            T b[kSmallCW][kSmallUN];
+#pragma unroll
+            for (int c = 0; c < kSmallCW; ++c)
+#pragma unroll
+                for (int u = 0; u < kSmallUN; ++u) {
+                    const int kk = k0 + 32 * u + lane;
+                    b[c][u] = (jb + c < j1 && kk < k) ? ldcg(B + kk + (size_t)(jb + c) * ldb) : T(0);
+                }
+#pragma unroll
+            for (int c = 0; c < kSmallCW; ++c)
+#pragma unroll
+                for (int u = 0; u < kSmallUN; ++u) {
+                    const int kk = k0 + 32 * u + lane;
+                    if (kk < k) acc[c] = fma(sA[kk], b[c][u], acc[c]);
+                }
+        }
+#pragma unroll
+        for (int c = 0; c < kSmallCW; ++c) {
+            T v = acc[c];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0 && jb + c < j1) {
+                T* p = C + (size_t)(jb + c) * ldc;
+                T r = alpha * v;
+                if (beta != T(0)) r = fma(beta, ldcg(p), r);
+                *p = r;
+            }
+        }
+    }
+    __syncthreads();
+}
+
 template <class T, bool B_NN>
 __device__ inline void gemm_small_cols(int m, int j0, int j1, int k, T alpha, const T* A, int lda, const T* B, int ldb, T beta, T* C,
                                        int ldc, T* smem) {
+    if (B_NN && m == 1 && k <= kSmallKA * kSmallM) {
+        gemm_small_nn_m1<T>(j0, j1, k, alpha, A, lda, B, ldb, beta, C, ldc, smem);
+        return;
+    }
     if (B_NN) {
         if (m == 1) gemm_small_cols_nn_warp<T, 1>(m, j0, j1, k, alpha, A, lda, B, ldb, beta, C, ldc, smem);
         else gemm_small_cols_nn_warp<T, kSmallM>(m, j0, j1, k, alpha, A, lda, B, ldb, beta, C, ldc, smem);
