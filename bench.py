@@ -282,12 +282,14 @@ def run_serving(args, local):
     three rounds of FP64-residual refinement in the launch — a request above
     the tolerance solves again with twice the rounds) and plain FP64."""
     import tasktorrent_gb300 as t
-    out = {"requests_per_rate": args.serve_n, "n_range": [64, 8192], "alpha": 1e-4, "followup_frac": 0.3,
+    out = {"requests_per_rate": {"mixed": args.serve_n, "fp64": args.serve_n_fp64}, "n_range": [64, 8192], "alpha": 1e-4,
+           "followup_frac": 0.3,
            "hbm_budget_gb": 180.0, "lanes": 4, "mixed_ir_steps": 3}
     for name, prec in (("mixed", t.PREC_MIXED), ("fp64", t.PREC_F64)):
         rows = []
         for rate in args.serve_rates:
-            s = t.Serve(args.serve_n, rate=rate, n_min=64, n_max=8192, alpha=1e-4, seed=2, followup_frac=0.3, precision=prec,
+            n_req = args.serve_n if prec == t.PREC_MIXED else args.serve_n_fp64
+            s = t.Serve(n_req, rate=rate, n_min=64, n_max=8192, alpha=1e-4, seed=2, followup_frac=0.3, precision=prec,
                         ir_steps=3, lanes=4, max_batch=16, hbm_budget_gb=180.0, device=local)
             st, rep, _ = s.run()
             s.close()
@@ -595,7 +597,10 @@ def main():
     ap.add_argument("--no-batched", dest="no_batched", action="store_true")
     ap.add_argument("--no-serving", dest="no_serving", action="store_true")
     ap.add_argument("--batch-n", dest="batch_n", type=int, default=10000)
-    ap.add_argument("--serve-n", dest="serve_n", type=int, default=600)
+    ap.add_argument("--serve-n", dest="serve_n", type=int, default=10000,
+                    help="requests per arrival rate of the mixed serving stream")
+    ap.add_argument("--serve-n-fp64", dest="serve_n_fp64", type=int, default=2000,
+                    help="requests per arrival rate of the plain FP64 serving stream (saturates near 90 solves/s)")
     ap.add_argument("--serving-only", dest="serving_only", action="store_true",
                     help="run only the serving stream and print its section")
     ap.add_argument("--serve-rates", dest="serve_rates", type=lambda s: [float(x) for x in s.split(",")],

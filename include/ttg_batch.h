@@ -33,7 +33,9 @@ typedef struct ttg_batch_args {
     const int32_t* sizes;  /* N_i (host, n_systems entries, each 1..131072)               */
     int32_t tile;          /* tile size (>= 1); each system has ceil(N_i / tile) tiles,
                               the last one ragged                                          */
-    int32_t precision;     /* TTG_PREC_F64 or TTG_PREC_MIXED                             */
+    int32_t precision;     /* TTG_PREC_F64, or TTG_PREC_MIXED: FP32 factor with FP64
+                              diagonal POTRFs, split-BF16 tensor-core updates for systems
+                              with tile 128..512 and N > tile, FP32 ones otherwise       */
     int32_t nrhs;          /* right-hand sides per system, 1..16                          */
     int32_t ir_steps;      /* TTG_PREC_MIXED: refinement rounds inside the launch (>= 0) */
     uint32_t seed;         /* system i: A_i = G_i·G_iᵀ/N_i + alpha·I with the quantised

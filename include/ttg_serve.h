@@ -41,7 +41,9 @@ typedef struct ttg_serve_args {
                                right-hand sides from (seed + i, stream 1)                   */
     double followup_frac;   /* share of follow-up right-hand sides on an earlier factor     */
     int32_t precision;      /* TTG_PREC_F64: FP64 factor + solve; TTG_PREC_MIXED: FP32
-                               factor (FP64 diagonal POTRF) + FP64-residual refinement       */
+                               factor (FP64 diagonal POTRF; split-BF16 tensor-core updates
+                               when the tile is 128..512 and N > tile) + FP64-residual
+                               refinement                                                   */
     int32_t ir_steps;       /* mixed: refinement rounds of a first attempt                  */
     int32_t nrhs;           /* right-hand sides per request, 1..16                          */
     int32_t lanes;          /* executors sharing the GPU (>= 1)                              */
