@@ -286,6 +286,15 @@ class Threadpool_shared {
         std::sort(edges.begin(), edges.end());
         std::ofstream ef(prefix + ".edges.csv");
         for (auto& e : edges) ef << e.first << "," << e.second << "\n";
+        // <prefix>.prio.csv: name,priority of every task as captured (the
+        // value its Taskflow's priority function gave).
+        std::vector<std::pair<std::string, double>> prio;
+        for (size_t i = 0; i < cap_.nodes.size(); ++i) prio.push_back({node_name((int)i), cap_.nodes[i].priority});
+        std::sort(prio.begin(), prio.end());
+        prio.erase(std::unique(prio.begin(), prio.end(), [](const auto& a, const auto& b) { return a.first == b.first; }), prio.end());
+        std::ofstream pf(prefix + ".prio.csv");
+        pf << "name,priority\n";
+        for (auto& e : prio) pf << e.first << "," << e.second << "\n";
     }
 
     // ---- used by Taskflow<K> (not part of the reference interface) ----

@@ -69,6 +69,55 @@ def test_captured_cholesky_dag_equals_oracle(tmp_path, nb, nt, kind, acc, upper)
     assert orc.read_dag(pre_t) == orc.read_dag(pre_o)
 
 
+def read_prio(prefix):
+    out = {}
+    with open(prefix + ".prio.csv") as f:
+        next(f)
+        for line in f:
+            n, v = line.strip().split(",")
+            out[n] = float(v)
+    return out
+
+
+def task_coords(name):
+    parts = name.split("_")
+    return parts[0], [int(x) for x in parts[1:]]
+
+
+@pytest.mark.parametrize("kind", [2, 6])
+def test_captured_priorities_follow_the_kind(tmp_path, kind):
+    """--kind 2 is the reference's formula (2d_cholesky.cpp: potrf 9(nb-j)-1,
+    trsm and gemm 9(nb-j)-2 by the target column j); kind 6 (extension) puts
+    the tasks of the tiles within two of the diagonal above every other task,
+    by column, and leaves the rest as kind 2."""
+    nb = 12
+    pre = str(tmp_path / "p")
+    t.chol_dag_dump(pre, 4, nb, n_threads=4, kind=kind)
+    prio = read_prio(pre)
+    assert len(prio) == nb + nb * (nb - 1) // 2 + sum(j * (nb - j) for j in range(nb))
+    chain, bulk = [], []
+    for name, v in prio.items():
+        kd, c = task_coords(name)
+        if kd == "POTRF":
+            i = j = c[0]
+        elif kd == "TRSM":
+            i, j = c
+        else:  # GEMM_k_i_j
+            i, j = c[1], c[2]
+        k2 = 9 * (nb - j) - (1 if kd == "POTRF" else 2)
+        if kind == 2:
+            assert v == k2, name
+        elif i <= j + 2:
+            assert v == 9 * nb + 9 * (nb - j), name
+            chain.append(v)
+        else:
+            assert v == 9 * (nb - j) - 2, name
+            bulk.append(v)
+    if kind == 6:
+        assert min(chain) > max(bulk)
+        assert len(set(chain)) + len(set(bulk)) <= 2 * nb  # fits the executor's 128 levels up to 64 tile columns
+
+
 @pytest.mark.parametrize("N,b", [(8, 8), (24, 8), (40, 4)])
 def test_captured_gemm_dag_equals_oracle(tmp_path, N, b):
     pre_t, pre_o = str(tmp_path / "t"), str(tmp_path / "o")
