@@ -276,7 +276,9 @@ def run_batched(ctx, args):
 def run_serving(args, local):
     """cfg5: a Poisson stream of factor-and-solve requests (N log-uniform in
     [64, 8192], A = G·Gᵀ/N + 1e-4·I, 30% follow-up right-hand sides on a
-    resident factor) over four executor lanes sharing the GPU, admission by an
+    resident factor) over executor lanes sharing the GPU (four for mixed, the
+    best of 2, 4 and 8 measured; two for FP64, which saturates at ~92
+    solves/s on two lanes and ~67 on four), admission by an
     180 GB HBM budget; p50/p99 latency and solves/s per arrival rate, mixed
     (FP32 factor, split-BF16 tensor-core updates for tiles of 128 and 256, and
     three rounds of FP64-residual refinement in the launch — a request above
@@ -284,13 +286,14 @@ def run_serving(args, local):
     import tasktorrent_gb300 as t
     out = {"requests_per_rate": {"mixed": args.serve_n, "fp64": args.serve_n_fp64}, "n_range": [64, 8192], "alpha": 1e-4,
            "followup_frac": 0.3,
-           "hbm_budget_gb": 180.0, "lanes": 4, "mixed_ir_steps": 3}
+           "hbm_budget_gb": 180.0, "lanes": {"mixed": 4, "fp64": 2}, "mixed_ir_steps": 3}
     for name, prec in (("mixed", t.PREC_MIXED), ("fp64", t.PREC_F64)):
         rows = []
         for rate in args.serve_rates:
             n_req = args.serve_n if prec == t.PREC_MIXED else args.serve_n_fp64
             s = t.Serve(n_req, rate=rate, n_min=64, n_max=8192, alpha=1e-4, seed=2, followup_frac=0.3, precision=prec,
-                        ir_steps=3, lanes=4, max_batch=16, hbm_budget_gb=180.0, device=local)
+                        ir_steps=3, lanes=4 if prec == t.PREC_MIXED else 2, max_batch=16, hbm_budget_gb=180.0,
+                        device=local)
             st, rep, _ = s.run()
             s.close()
             if st != t.TTG_OK:
