@@ -51,6 +51,14 @@ typedef struct ttg_serve_args {
     double hbm_budget_gb;   /* resident factors + requests in flight                        */
     double tol;             /* backward-error target                                        */
     int32_t keep_results;   /* keep every solution for ttg_serve_get_x                      */
+    int32_t admission;      /* 0: a lane takes waiting requests when its launch ends (one
+                               launch per batch of requests); 1 (mixed): open lanes — each
+                               lane's executor keeps running and takes a request's tasks as
+                               soon as they are published, between other tasks; the lanes
+                               leave half the SMs to the input generators and backward
+                               errors (env TTG_SERVE_SPARE_SMS sets the count).  On the
+                               synthetic stream mode 0 is faster (the generators need the
+                               whole GPU between launches)                                  */
 } ttg_serve_args;
 
 typedef struct ttg_serve_report {

@@ -97,7 +97,7 @@ class ServeArgs(ctypes.Structure):
                 ("alpha", ctypes.c_double), ("seed", ctypes.c_uint32), ("followup_frac", ctypes.c_double),
                 ("precision", ctypes.c_int32), ("ir_steps", ctypes.c_int32), ("nrhs", ctypes.c_int32), ("lanes", ctypes.c_int32),
                 ("max_batch", ctypes.c_int32), ("hbm_budget_gb", ctypes.c_double), ("tol", ctypes.c_double),
-                ("keep_results", ctypes.c_int32)]
+                ("keep_results", ctypes.c_int32), ("admission", ctypes.c_int32)]
 
 
 class ServeReport(ctypes.Structure):
@@ -558,9 +558,9 @@ class Serve:
 
     def __init__(self, n_requests, rate, n_min=64, n_max=8192, alpha=1e-4, seed=2, followup_frac=0.3,
                  precision=PREC_MIXED, ir_steps=4, nrhs=1, lanes=2, max_batch=16, hbm_budget_gb=180.0, tol=1e-14,
-                 keep_results=False, device=0):
+                 keep_results=False, device=0, admission=0):
         self.args = ServeArgs(n_requests, rate, n_min, n_max, alpha, seed, followup_frac, precision, ir_steps, nrhs, lanes,
-                              max_batch, hbm_budget_gb, tol, 1 if keep_results else 0)
+                              max_batch, hbm_budget_gb, tol, 1 if keep_results else 0, admission)
         self.nrhs = nrhs
         h = _P()
         check(lib().ttg_serve_create(device, ctypes.byref(self.args), ctypes.byref(h)), "ttg_serve_create")

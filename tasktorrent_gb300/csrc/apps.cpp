@@ -749,28 +749,6 @@ extern "C" ttg_status ttg_chol_solve_host(ttg_chol_plan* P, const double* h_B, d
     return st;
 }
 
-// Enqueue a 32-bit store of v at addr on stream s, ordered after the
-// stream's earlier work (copies included): cuStreamWriteValue32 of the
-// driver API, which needs no SM (the persistent executor holds them all).
-static ttg_status stream_write_u32(cudaStream_t s, uint32_t* addr, uint32_t v) {
-    typedef CUresult (*write_fn)(CUstream, CUdeviceptr, cuuint32_t, unsigned int);
-    static write_fn fn = nullptr;
-    if (!fn) {
-        void* f = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        cudaError_t e = cudaGetDriverEntryPointByVersion("cuStreamWriteValue32", &f, 12000, cudaEnableDefault, &q);
-        if (e != cudaSuccess || !f || q != cudaDriverEntryPointSuccess) {
-            ttg_set_last_cuda_error(e, "cudaGetDriverEntryPointByVersion(cuStreamWriteValue32)", __FILE__, __LINE__);
-            return TTG_ECUDA;
-        }
-        fn = (write_fn)f;
-    }
-    if (fn((CUstream)s, (CUdeviceptr)addr, v, 0) != CUDA_SUCCESS) {
-        ttg_set_last_cuda_error(cudaErrorInvalidValue, "cuStreamWriteValue32", __FILE__, __LINE__);
-        return TTG_ECUDA;
-    }
-    return TTG_OK;
-}
 
 // Stream the host input tiles of a mixed plan into the plan input while the
 // factorisation runs: on a copy stream, the diagonal tiles first (the block-
@@ -800,7 +778,7 @@ static ttg_status stream_input(ttg_chol_plan* P, const double* h_tiles, cudaStre
         for (int i = j + 1; i < nb; ++i) rest += (int64_t)P->bs[i] * P->bs[j];
         if (rest > 0)
             TTG_CUDA_CHECK(cudaMemcpyAsync(P->pristine + o, h_tiles + o, sizeof(double) * rest, cudaMemcpyHostToDevice, P->copy_s));
-        ttg_status st = stream_write_u32(P->copy_s, gate + 1 + j, gen);
+        ttg_status st = ttg_stream_write_u32(P->copy_s, gate + 1 + j, gen);
         if (st != TTG_OK) return st;
     }
     TTG_CUDA_CHECK(cudaEventRecord(P->copy_ev[2], P->copy_s));

@@ -70,7 +70,20 @@ struct ExecParams {
     long long timeout_ns;
     int* team_ctr;          // kTeamStride words per team task, zero at launch; or null
     const int* team_slot;   // per task: its team counter block, -1 if none; or null
+    // Open graph (a serving lane that takes new work while it runs), or null:
+    // pub[0] tasks published, pub[1] roots published, pub[2] closed flag —
+    // written by the host's copy stream after the tasks' data; roots[] the
+    // published root tasks in order; admit[0] roots pushed so far, admit[1]
+    // a lock held by the worker that pushes them.  The launch ends when the
+    // graph is closed and every published task has run.
+    const int* pub;
+    const int* roots;
+    int* admit;
 };
+
+// Internal op kind of open graphs: a request's last task, which writes op.m
+// to the host-visible word op.c once every task it depends on has run.
+constexpr int kOpSignal = 99;
 
 __device__ __forceinline__ long long globaltimer() {
     long long t;
@@ -106,6 +119,40 @@ __device__ inline int wait_slot(const ExecParams& p, int* slot) {
     }
 }
 
+// The task tables are read through L2 only: an open graph appends entries
+// while the launch runs, after a block may have cached their line in L1.
+__device__ __forceinline__ int ld_tab(const int* a) { return __ldcg(a); }
+__device__ __forceinline__ int64_t ld_tab(const int64_t* a) { return (int64_t)__ldcg((const long long*)a); }
+__device__ __forceinline__ int ld_tab(const uint8_t* a) { return __ldcg((const unsigned char*)a); }
+__device__ __forceinline__ ttg_op ld_op(const ttg_op* a) {
+    static_assert(sizeof(ttg_op) % 8 == 0, "ttg_op words");
+    ttg_op o;
+    const unsigned long long* s = (const unsigned long long*)a;
+    unsigned long long* d = (unsigned long long*)&o;
+#pragma unroll
+    for (int i = 0; i < (int)(sizeof(ttg_op) / 8); ++i) d[i] = __ldcg(s + i);
+    return o;
+}
+
+__device__ inline void push_ready(const ExecParams& p, int s);
+
+// Open graphs (lane 0 of an idle worker): push the roots published since the
+// last admission onto their queues, under the admission lock.
+__device__ inline void admit_roots(const ExecParams& p) {
+    const int want = ld_volatile(p.pub + 1);
+    if (ld_volatile(p.admit) >= want) return;
+    if (atomicCAS(p.admit + 1, 0, 1) != 0) return;  // another worker is admitting
+    __threadfence();
+    const int have = ld_volatile(p.admit);
+    const int upto = ld_volatile(p.pub + 1);
+    __threadfence();  // the roots (and their tasks) were written before pub[1]
+    for (int r = have; r < upto; ++r) push_ready(p, ld_volatile(p.roots + r));
+    __threadfence();
+    st_volatile(p.admit, upto);
+    __threadfence();
+    atomicExch(p.admit + 1, 0);
+}
+
 // Called by all lanes of warp 0.  Returns a claimed task id and its part
 // (*part, the same on all lanes), or -1 to exit.
 //
@@ -121,7 +168,7 @@ __device__ inline int wait_slot(const ExecParams& p, int* slot) {
 __device__ inline int claim_task(const ExecParams& p, int* part) {
     const int lane = threadIdx.x & 31;
     const int w = blockIdx.x;
-    int last_done = -1;
+    int last_done = -1, last_target = -1;
     long long idle_since = 0;
     {
         int e = 0;
@@ -192,21 +239,35 @@ __device__ inline int claim_task(const ExecParams& p, int* part) {
             }
             continue;  // lost the race for the last slots; rescan at once
         }
-        int d = 0, e = 0;
+        int d = 0, e = 0, target = p.n_runnable, closed = 1;
         if (lane == 0) {
+            if (p.pub) {
+                // The closed flag first: once it is seen, pub[0] is final.
+                admit_roots(p);
+                closed = ld_volatile(p.pub + 2);
+                __threadfence();
+                target = ld_volatile(p.pub);
+                __threadfence();
+            }
             d = ld_volatile(p.done);
             e = ld_volatile(p.err);
         }
         d = __shfl_sync(0xffffffffu, d, 0);
         e = __shfl_sync(0xffffffffu, e, 0);
-        if (d >= p.n_runnable || e != 0) return -1;
+        target = __shfl_sync(0xffffffffu, target, 0);
+        closed = __shfl_sync(0xffffffffu, closed, 0);
+        if ((closed && d >= target) || e != 0) return -1;
         long long now = 0;
         if (lane == 0) now = globaltimer();
         now = __shfl_sync(0xffffffffu, now, 0);
-        if (d != last_done) {
+        // An open graph with every published task done waits for more work
+        // (or its closing) up to ten times the no-progress limit.
+        const bool waiting = d >= target;
+        if (d != last_done || target != last_target) {
             last_done = d;
+            last_target = target;
             idle_since = now;
-        } else if (now - idle_since > p.timeout_ns) {
+        } else if (now - idle_since > (waiting ? 10 * p.timeout_ns : p.timeout_ns)) {
             if (lane == 0) set_error(p, TTG_ETIMEOUT, -1, 0);
             return -1;
         }
@@ -215,8 +276,8 @@ __device__ inline int claim_task(const ExecParams& p, int* part) {
 }
 
 __device__ __forceinline__ void push_ready(const ExecParams& p, int s) {
-    const int b = p.bind[s];
-    const int P = p.parts[s];
+    const int b = ld_tab(p.bind + s);
+    const int P = ld_tab(p.parts + s);
     // Every task is pushed at most once (only the decrement that finds the
     // counter at one pushes), so a queue never outgrows the number of tasks
     // assigned to it; the bound checks below only guard against a corrupted
@@ -231,7 +292,7 @@ __device__ __forceinline__ void push_ready(const ExecParams& p, int s) {
             set_error(p, TTG_EOVERCOUNT, s, 0);
         }
     } else {
-        const int lvl = p.level[s];
+        const int lvl = ld_tab(p.level + s);
         const int slot = atomicAdd(p.q_tail + lvl * 32, P);
         if (p.q_off[lvl] + slot + P <= p.q_off[lvl + 1]) {
             for (int q = 0; q < P; ++q) st_volatile(p.qbuf + p.q_off[lvl] + slot + q, s);
@@ -247,9 +308,9 @@ __device__ __forceinline__ void push_ready(const ExecParams& p, int s) {
 __device__ inline void fulfil_successors(const ExecParams& p, int t) {
     const int lane = threadIdx.x & 31;
     __threadfence();  // release the tile writes of the whole block (after bar.sync)
-    const int64_t e0 = p.succ_ptr[t], e1 = p.succ_ptr[t + 1];
+    const int64_t e0 = ld_tab(p.succ_ptr + t), e1 = ld_tab(p.succ_ptr + t + 1);
     for (int64_t e = e0 + lane; e < e1; e += 32) {
-        const int s = p.succ_idx[e];
+        const int s = ld_tab(p.succ_idx + e);
         const int old = atomicSub(p.count + s, 1);
         if (old == 1) {
             __threadfence();
@@ -296,11 +357,11 @@ __device__ void executor_loop(const ExecParams& p, double* smem, RunOp run_op) {
         __syncthreads();
         const int t = s_task;
         if (t < 0) break;
-        const ttg_op op = p.ops[t];
-        const int nparts = p.parts[t];
+        const ttg_op op = ld_op(p.ops + t);
+        const int nparts = ld_tab(p.parts + t);
         int* team = nullptr;
         if (p.team_slot) {
-            const int slot = p.team_slot[t];
+            const int slot = ld_tab(p.team_slot + t);
             if (slot >= 0) team = p.team_ctr + (size_t)slot * kTeamStride;
         }
         const int info = run_op(op, s_part, nparts, smem, team, &s_fin);

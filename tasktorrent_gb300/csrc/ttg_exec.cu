@@ -4,6 +4,7 @@
 // launch/wait and the run report.  Device side: the persistent kernel that
 // runs the FP64 tile tasks (tile_f64.cuh) and the mixed-precision tile tasks
 // (tile_mixed.cuh) through the executor loop (exec.cuh).
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -676,7 +677,33 @@ static ExecParams ttg_make_params(ttg_ctx* c) {
     p.timeout_ns = (long long)(c->timeout_s * 1e9);
     p.team_ctr = g.team_ctr;
     p.team_slot = g.team_slot;
+    p.pub = nullptr;  // a closed graph
+    p.roots = nullptr;
+    p.admit = nullptr;
     return p;
+}
+
+// Enqueue a 32-bit store of v at addr on stream s, ordered after the
+// stream's earlier work (copies included): cuStreamWriteValue32 of the
+// driver API, which needs no SM (the persistent executor holds them all).
+ttg_status ttg_stream_write_u32(cudaStream_t s, uint32_t* addr, uint32_t v) {
+    typedef CUresult (*write_fn)(CUstream, CUdeviceptr, cuuint32_t, unsigned int);
+    static write_fn fn = nullptr;
+    if (!fn) {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuStreamWriteValue32", &f, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess || !f || q != cudaDriverEntryPointSuccess) {
+            ttg_set_last_cuda_error(e, "cudaGetDriverEntryPointByVersion(cuStreamWriteValue32)", __FILE__, __LINE__);
+            return TTG_ECUDA;
+        }
+        fn = (write_fn)f;
+    }
+    if (fn((CUstream)s, (CUdeviceptr)addr, v, 0) != CUDA_SUCCESS) {
+        ttg_set_last_cuda_error(cudaErrorInvalidValue, "cuStreamWriteValue32", __FILE__, __LINE__);
+        return TTG_ECUDA;
+    }
+    return TTG_OK;
 }
 
 extern "C" ttg_status ttg_launch(ttg_ctx* c, void* stream) {

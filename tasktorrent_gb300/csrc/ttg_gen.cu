@@ -312,6 +312,14 @@ ttg_status ttg_gen_gram_async(ttg_ctx* c, int n, int tile, double alpha, uint32_
     return TTG_OK;
 }
 
+ttg_status ttg_gen_preload() {
+    cudaFuncAttributes fa;
+    TTG_CUDA_CHECK(cudaFuncGetAttributes(&fa, gen_qgauss_kernel));
+    TTG_CUDA_CHECK(cudaFuncGetAttributes(&fa, gram_grid_kernel));
+    TTG_CUDA_CHECK(cudaFuncGetAttributes(&fa, rhs_rows_kernel));
+    return TTG_OK;
+}
+
 ttg_status ttg_gen_rhs_rows_async(int n, int nrhs, uint32_t seed, double* d_B, cudaStream_t s) {
     if (n <= 0 || nrhs < 1 || !d_B) return TTG_EINVAL;
     ttg_note_launch();

@@ -98,6 +98,9 @@ void ttg_graph_free(ttg_ctx* c);
 // Blocks that share one task.  team: a POTRF may be split over a team of
 // blocks (needs a team counter block at run time).
 int ttg_task_parts(const ttg_op& op, bool team = false);
+// A 32-bit store of v at addr (device memory) enqueued on stream s after its
+// earlier work, copies included (cuStreamWriteValue32: no SM needed).
+ttg_status ttg_stream_write_u32(cudaStream_t s, uint32_t* addr, uint32_t v);
 
 // Lower tiles of the miniapp matrix 1/((i-j)^2+1) (ttg_gen.cu).
 ttg_status ttg_gen_miniapp_tiles(ttg_ctx* c, const int32_t* h_bs, int32_t nb, double* d_tiles, void* stream);
@@ -109,6 +112,10 @@ ttg_status ttg_gen_gram_async(ttg_ctx* c, int n, int tile, double alpha, uint32_
 // Right-hand sides as an nrhs × n row block (ld nrhs), entry (r, q) of the
 // column-major N(0,1) array of (seed, stream 1); enqueued on s.
 ttg_status ttg_gen_rhs_rows_async(int n, int nrhs, uint32_t seed, double* d_B, cudaStream_t s);
+// Load the two generators' kernels now.  With lazy module loading the first
+// launch of a kernel waits for the device to be idle, which never happens
+// while a persistent executor waits for work: load them before one starts.
+ttg_status ttg_gen_preload();
 
 // Block-GEMM inputs in tile layout (ttg_gen.cu).
 ttg_status ttg_gen_gemm_tiles(ttg_ctx* c, int32_t N, int32_t b, int32_t inputs, uint32_t seed, double* d_A, double* d_B,

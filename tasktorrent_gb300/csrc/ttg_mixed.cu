@@ -303,8 +303,32 @@ __device__ inline void convert_input_chunk(const double* __restrict__ src, float
     __syncthreads();
 }
 
+// A task's tables, read through L2: in an open graph they are written while
+// the launch runs, and an earlier system at the same address may sit in L1.
+__device__ inline MixedTables load_tables(const void* aux) {
+    static_assert(sizeof(MixedTables) % 8 == 0, "MixedTables words");
+    MixedTables t;
+    const unsigned long long* s = (const unsigned long long*)aux;
+    unsigned long long* d = (unsigned long long*)&t;
+#pragma unroll
+    for (int i = 0; i < (int)(sizeof(MixedTables) / 8); ++i) d[i] = __ldcg(s + i);
+    return t;
+}
+
+// open: the launch serves an open graph, whose systems' tensor maps are
+// written in device memory while it runs (possibly where an earlier map was).
 __device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem, int* team, int* fin, tc::TcShared* tsh,
-                             uint8_t* ring, const CUtensorMap* tmap, int* err, long long limit_ns) {
+                             uint8_t* ring, const CUtensorMap* tmap, int* err, long long limit_ns, bool open) {
+    if (op.kind == kOpSignal) {
+        // A request of an open graph is complete: tell the host (op.c is a
+        // word of host-mapped memory).
+        if (threadIdx.x == 0) {
+            __threadfence_system();
+            *(volatile int*)op.c = op.m;
+            __threadfence_system();
+        }
+        return 0;
+    }
     if (op.prec == TTG_PREC_F64) {
         if (op.kind == TTG_OP_POTRF_L) {
             if (team)
@@ -346,8 +370,9 @@ __device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem,
                     if (r1 > r0) trsm_rltn_f32_resident(op.n, (float)op.alpha, (const float*)op.a, op.lda, (float*)op.c, op.ldc, r0,
                                                         r1 - r0, fsm);
                     if (op.flags >= kMixedBF16) {
-                        const MixedTables* tb = (const MixedTables*)op.aux;
-                        const float s = tb->rowscale[op.k];
+                        const MixedTables tbv = load_tables(op.aux);
+                        const MixedTables* tb = &tbv;
+                        const float s = __ldcg(tb->rowscale + op.k);
                         const size_t slice = (size_t)tb->n_slots * tb->b * tb->b;
                         if (r1 > r0)
                             publish_bf16_resident(fsm, op.n, r0, r1 - r0, tb->b16 + (size_t)op.ldb * tb->b * tb->b, slice, tb->b,
@@ -364,10 +389,11 @@ __device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem,
                                   parts);
             {
                 // Publish this row slice as the tile's BF16 panel copy.
-                const MixedTables* tb = (const MixedTables*)op.aux;
+                const MixedTables tbv = load_tables(op.aux);
+                const MixedTables* tb = &tbv;
                 const int per = ((op.m + parts - 1) / parts + 15) / 16 * 16;
                 const int r0 = min(op.m, part * per), r1 = min(op.m, r0 + per);
-                const float s = tb->rowscale[op.k];
+                const float s = __ldcg(tb->rowscale + op.k);
                 __syncthreads();
                 const size_t slice = (size_t)tb->n_slots * tb->b * tb->b;
                 if (op.flags == kMixedBF16x3)
@@ -386,7 +412,8 @@ __device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem,
         case TTG_OP_SYRK_LN:
         case TTG_OP_GEMM_NT:
             if (op.flags >= kMixedBF16) {
-                const MixedTables* tb = (const MixedTables*)op.aux;
+                const MixedTables tbv = load_tables(op.aux);
+                const MixedTables* tb = &tbv;
                 const bool lower = op.kind == TTG_OP_SYRK_LN;
                 // The part's share of the 128×256 output blocks, in turn.
                 const int nblk = tc::tc_num_blocks(op.m, op.n, lower);
@@ -394,6 +421,10 @@ __device__ int run_op_mixed(const ttg_op& op, int part, int parts, double* smem,
                 const float f = (float)op.alpha * __ldcg(tb->slot_scale + op.lda) * __ldcg(tb->slot_scale + op.ldb);
                 const int b0 = min(nblk, part * per), b1 = min(nblk, (part + 1) * per);
                 const CUtensorMap* mp = tb->map ? tb->map : tmap;
+                // The map was written by a copy after this launch began: drop
+                // any stale copy of that address from the descriptor cache.
+                if (open && tb->map)
+                    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(tb->map) : "memory");
                 if (b1 > b0 && !tc::tc_gemm_blocks(tsh, ring, mp, op.lda, op.ldb, b0, b1 - b0, op.k, f, (float*)op.c, op.ldc, op.m,
                                                    op.n, lower, limit_ns, mixed_split(op.flags), tb->n_slots) &&
                     threadIdx.x == 0)
@@ -450,7 +481,7 @@ __global__ void __launch_bounds__(kThreads, 1) exec_kernel_mixed(ExecParams p, c
     if (g.has_tc) tc::tc_setup(&tsh);
     const CUtensorMap* tmap = &g.tmap;
     executor_loop(p, smem_mx, [&](const ttg_op& op, int part, int parts, double* smem, int* team, int* fin) {
-        return run_op_mixed(op, part, parts, smem, team, fin, &tsh, ring, tmap, p.err, p.timeout_ns);
+        return run_op_mixed(op, part, parts, smem, team, fin, &tsh, ring, tmap, p.err, p.timeout_ns, p.pub != nullptr);
     });
     if (g.has_tc) tc::tc_teardown(&tsh, p.timeout_ns);
 }
@@ -646,6 +677,12 @@ ttg_status ttg_mixed_row_scales(const TcRowScaleItem* d_items, int n, void* stre
     ttg_note_launch();
     row_scales_list<<<std::min(n, 4096), 128, 0, (cudaStream_t)stream>>>(d_items, n);
     TTG_CUDA_CHECK(cudaGetLastError());
+    return TTG_OK;
+}
+
+ttg_status ttg_mixed_row_scales_preload() {
+    cudaFuncAttributes fa;
+    TTG_CUDA_CHECK(cudaFuncGetAttributes(&fa, row_scales_list));
     return TTG_OK;
 }
 

@@ -81,5 +81,8 @@ struct TcRowScaleItem {
     float* out;
 };
 ttg_status ttg_mixed_row_scales(const TcRowScaleItem* d_items, int n, void* stream);
+// Load the row-scale kernel now (before a persistent executor starts: with
+// lazy module loading a first launch waits for the device to be idle).
+ttg_status ttg_mixed_row_scales_preload();
 // Whether the mixed executor of ctx sets up the tensor cores (TMEM, barriers).
 void ttg_mixed_set_tc(ttg_ctx* ctx, bool on);

@@ -359,6 +359,9 @@ extern "C" ttg_status ttg_run_graph_noalloc(int device, const ttg_graph_desc* gd
             p.err_info = &dst->err_info;
             p.trace = nullptr;
             p.timeout_ns = (long long)((timeout_s > 0 ? timeout_s : 10.0) * 1e9);
+            p.pub = nullptr;  // a closed graph
+            p.roots = nullptr;
+            p.admit = nullptr;
             p.team_ctr = nullptr;  // POTRF tasks run on one block here
             p.team_slot = nullptr;
             void* args[] = {(void*)&p, (void*)&dst};

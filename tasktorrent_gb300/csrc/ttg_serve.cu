@@ -11,8 +11,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <list>
@@ -24,6 +27,8 @@
 #include "../../include/ttg_philox.h"
 #include "../../include/ttg_serve.h"
 #include "batch_graph.h"
+#include "exec.cuh"
+#include "tile_f64.cuh"
 #include "ttg_mixed_api.h"
 #include "ttg_internal.h"
 
@@ -121,6 +126,9 @@ struct ServeRequest {
     double* D64 = nullptr;  // mixed factorisation scratch
     uint8_t* tc = nullptr;  // mixed, tensor-core updates: header, scales, panel slots
     size_t work_bytes = 0;
+    // Open lanes: the lane and in-flight slot of the attempt, its phase (1
+    // published, 2 backward error under way) and its attempt number.
+    int lane = -1, slot = -1, phase = 0, attempt = 0;
     int key = -1;  // resident factor it factors or uses
     std::vector<double> result;
 };
@@ -159,8 +167,63 @@ struct Lane {
     int rs_cap = 0, n_hdr = 0;
 };
 
+// An open lane: one executor launch that keeps taking work (an epoch).  Its
+// arena holds the tasks of the epoch's requests back to back — ops, counters,
+// successor lists, team counters, one first-in-first-out queue — and the
+// host appends a request's tasks on the lane's copy stream, then publishes
+// them (task and root counts) with stream-ordered 32-bit writes that the idle
+// workers poll (exec.cuh, admit_roots).  An epoch whose arena is full is
+// closed: its launch ends once every published task has run, and the next
+// epoch starts from an empty arena.
+// Left to the side stream (on the SMs the lanes leave free): the input
+// generators (an O(N³) int8 product per synthetic request), block-row scales
+// and backward errors.
+// Where the open loop's host thread is (TTG_SERVE_VERBOSE reports it from a
+// watchdog thread, so that a blocking call shows by name).
+std::atomic<const char*> g_open_at{"start"};
+constexpr int kOpenTasks = 1 << 20;         // tasks per epoch
+constexpr int64_t kOpenEdges = 8ll << 20;   // successor entries per epoch
+constexpr int kOpenParts = 4 << 20;         // queue slots per epoch
+constexpr int kOpenTeams = 16384;           // team POTRFs per epoch
+constexpr int kOpenInflight = 64;           // requests in flight per lane
+struct OpenLane {
+    ttg_ctx* ctx = nullptr;
+    cudaStream_t ks = nullptr, cs = nullptr;  // the executor; copies and publication
+    cudaEvent_t kdone = nullptr;
+    bool running = false, closing = false;
+    int cap_tasks = kOpenTasks;  // tasks per epoch (TTG_SERVE_EPOCH_TASKS lowers it)
+    ttg_op* ops = nullptr;
+    int *count = nullptr, *runs = nullptr, *parts = nullptr, *part_next = nullptr, *part_done = nullptr;
+    uint8_t* level = nullptr;
+    int32_t* bind = nullptr;
+    int64_t* succ_ptr = nullptr;
+    int32_t* succ_idx = nullptr;
+    int *team_slot = nullptr, *team_ctr = nullptr, *roots = nullptr;
+    int *qbuf = nullptr, *q_off = nullptr, *q_head = nullptr, *q_tail = nullptr;
+    int *bq = nullptr;  // unused bound queues (offsets, heads, tails: zeros)
+    int *status = nullptr, *pub = nullptr, *admit = nullptr;
+    int n_tasks = 0, n_roots = 0, n_teams = 0, n_parts = 0;
+    int64_t n_edges = 0;
+    int n_inflight = 0;
+    std::vector<int> slot_req;  // request in each in-flight slot, or -1
+    BwdItem* h_items = nullptr;  // pinned, per slot
+    BwdItem* d_items = nullptr;
+    unsigned long long* d_acc = nullptr;
+    double* h_err = nullptr;  // pinned, per slot
+    double* d_err = nullptr;
+    std::vector<cudaEvent_t> ev;  // per slot: backward error read
+    std::vector<TcRowScaleItem> rs;
+    TcRowScaleItem* d_rs = nullptr;
+    int rs_cap = 0;
+};
+
 struct ttg_serve {
     int device = 0, sms = 0;
+    // Open lanes (admission 1).
+    std::vector<OpenLane> open;
+    cudaStream_t side = nullptr;  // input generation, block-row scales, backward errors
+    int* h_flag = nullptr;        // host-mapped, per request: the attempt whose tasks all ran
+    int* d_flag = nullptr;
     ttg_serve_args a{};
     std::vector<ServeRequest> req;
     std::unordered_map<int, Resident> res;  // keyed by the request that first factored the matrix
@@ -243,7 +306,21 @@ void use_factor(ttg_serve* s, int k) {
 }
 
 // Try to add request i to lane L's launch; false when it must wait.
-bool admit(ttg_serve* s, Lane& L, int i, ttg_status* err) {
+// Where an admitted request goes: the stream that allocates and generates
+// its operands (stream-ordered), the graph its tasks are added to, the
+// diagonal tiles whose block-row scales must be computed before it runs, and
+// the pinned staging of its tensor-core header (null: a pageable copy).
+struct AdmitTarget {
+    ttg_ctx* ctx;  // the generators' device context
+    cudaStream_t st;
+    Graph* g;
+    std::vector<TcRowScaleItem>* rs;
+    uint8_t* h_hdr;
+    int* n_hdr;
+    int max_hdr;
+};
+
+bool admit_to(ttg_serve* s, AdmitTarget& T, int i, ttg_status* err) {
     ServeRequest& q = s->req[i];
     const bool mixed = s->a.precision == TTG_PREC_MIXED;
     int key = q.followup_of >= 0 ? q.followup_of : i;
@@ -262,10 +339,10 @@ bool admit(ttg_serve* s, Lane& L, int i, ttg_status* err) {
     const size_t wb = work_bytes(s, q.N, q.tile, need_factor);
     if (!need_factor) use_factor(s, key);  // pin it before making room
     if (!make_room(s, fb + wb)) {
-        if (!need_factor) release_factor(s, key, L.s);
+        if (!need_factor) release_factor(s, key, T.st);
         return false;
     }
-    cudaStream_t st = L.s;
+    cudaStream_t st = T.st;
     System S;
     S.set_size(q.N, q.tile);
     S.mixed = mixed;
@@ -283,7 +360,7 @@ bool admit(ttg_serve* s, Lane& L, int i, ttg_status* err) {
         const size_t el = (size_t)S.elems();
         if ((e = pool_alloc(&r.A64, el, st)) == TTG_OK)
             e = mixed ? pool_alloc(&r.W32, el, st) : pool_alloc(&r.W64, el, st);
-        if (e == TTG_OK) e = ttg_gen_gram_async(L.ctx, q.N, q.tile, s->a.alpha, q.seed_a, r.A64, st);
+        if (e == TTG_OK) e = ttg_gen_gram_async(T.ctx, q.N, q.tile, s->a.alpha, q.seed_a, r.A64, st);
         if (e == TTG_OK && !mixed)
             e = cudaMemcpyAsync(r.W64, r.A64, sizeof(double) * el, cudaMemcpyDeviceToDevice, st) == cudaSuccess ? TTG_OK : TTG_ECUDA;
         r.users = 1;
@@ -299,19 +376,21 @@ bool admit(ttg_serve* s, Lane& L, int i, ttg_status* err) {
         if ((e = pool_alloc(&q.R, v, st)) == TTG_OK) e = pool_alloc(&q.D32, v, st);
         if (e == TTG_OK && need_factor) e = pool_alloc(&q.D64, (size_t)S.nb * S.tile * S.tile, st);
         // Split-BF16 updates on the tensor cores when the tiles allow it.
-        if (e == TTG_OK && need_factor && System::tc_fits(S.N, S.tile) && L.n_hdr < s->a.max_batch) {
+        if (e == TTG_OK && need_factor && System::tc_fits(S.N, S.tile) && (!T.h_hdr || *T.n_hdr < T.max_hdr)) {
             e = pool_alloc(&q.tc, tc_bytes(S), st);
             if (e == TTG_OK) {
                 float* slot_scale = (float*)(q.tc + kTcHeaderBytes);
                 float* rowscale = slot_scale + S.nb * (S.nb + 1) / 2;
                 __nv_bfloat16* slots = (__nv_bfloat16*)(q.tc + kTcHeaderBytes + tc_scale_bytes(S));
-                uint8_t* h = L.h_hdr + kTcHeaderBytes * (size_t)L.n_hdr;
+                std::vector<uint8_t> local(T.h_hdr ? 0 : kTcHeaderBytes);
+                uint8_t* h = T.h_hdr ? T.h_hdr + kTcHeaderBytes * (size_t)*T.n_hdr : local.data();
                 e = ttg_mixed_tc_header(h, q.tc, slots, slot_scale, rowscale, S.tile, S.nb, &S.tc_tables);
+                // (A pageable source is staged before the call returns.)
                 if (e == TTG_OK)
                     e = cudaMemcpyAsync(q.tc, h, kTcHeaderBytes, cudaMemcpyHostToDevice, st) == cudaSuccess ? TTG_OK : TTG_ECUDA;
                 if (e == TTG_OK) {
-                    ++L.n_hdr;
-                    for (int i = 0; i < S.nb; ++i) L.rs.push_back(TcRowScaleItem{r.A64 + S.off(i, i), S.bs(i), S.bs(i), rowscale + i});
+                    ++*T.n_hdr;
+                    for (int i = 0; i < S.nb; ++i) T.rs->push_back(TcRowScaleItem{r.A64 + S.off(i, i), S.bs(i), S.bs(i), rowscale + i});
                 }
             }
         }
@@ -335,7 +414,13 @@ bool admit(ttg_serve* s, Lane& L, int i, ttg_status* err) {
     S.X = q.X;
     S.R = q.R;
     S.D32 = q.D32;
-    add_system(L.g, S);
+    add_system(*T.g, S);
+    return true;
+}
+
+bool admit(ttg_serve* s, Lane& L, int i, ttg_status* err) {
+    AdmitTarget T{L.ctx, L.s, &L.g, &L.rs, L.h_hdr, &L.n_hdr, s->a.max_batch};
+    if (!admit_to(s, T, i, err)) return false;
     L.reqs.push_back(i);
     return true;
 }
@@ -450,6 +535,511 @@ ttg_status complete(ttg_serve* s, Lane& L, std::deque<int>& queue, double t) {
 
 }  // namespace
 
+namespace {
+
+// ------------------------------------------------------------ open lanes
+
+using ttg::kMaxLevels;
+using ttg::kTeamStride;
+using ttg::team_fits;
+
+template <class T>
+cudaError_t dev_zero(T** p, size_t count) {
+    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * std::max<size_t>(1, count));
+    if (e == cudaSuccess) e = cudaMemset(*p, 0, sizeof(T) * std::max<size_t>(1, count));
+    return e;
+}
+
+ttg_status open_lane_setup(ttg_serve* s, OpenLane& L, int workers) {
+    ttg_opts o{};
+    o.device = s->device;
+    o.workers = workers;
+    o.timeout_s = 60.0;
+    ttg_status st = ttg_create(&L.ctx, &o);
+    if (st != TTG_OK) return st;
+    L.ctx->coop = false;  // lanes share the GPU
+    if (const char* v = getenv("TTG_SERVE_EPOCH_TASKS")) L.cap_tasks = std::max(256, std::min(kOpenTasks, atoi(v)));
+    cudaError_t e = cudaStreamCreateWithFlags(&L.ks, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&L.cs, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&L.kdone, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = dev_zero(&L.ops, kOpenTasks);
+    if (e == cudaSuccess) e = dev_zero(&L.count, kOpenTasks);
+    if (e == cudaSuccess) e = dev_zero(&L.runs, kOpenTasks);
+    if (e == cudaSuccess) e = dev_zero(&L.parts, kOpenTasks);
+    if (e == cudaSuccess) e = dev_zero(&L.part_next, kOpenTasks);
+    if (e == cudaSuccess) e = dev_zero(&L.part_done, kOpenTasks);
+    if (e == cudaSuccess) e = dev_zero(&L.level, kOpenTasks);
+    if (e == cudaSuccess) e = dev_zero(&L.bind, kOpenTasks);
+    if (e == cudaSuccess) e = dev_zero(&L.succ_ptr, (size_t)kOpenTasks + 1);
+    if (e == cudaSuccess) e = dev_zero(&L.succ_idx, (size_t)kOpenEdges);
+    if (e == cudaSuccess) e = dev_zero(&L.team_slot, kOpenTasks);
+    if (e == cudaSuccess) e = dev_zero(&L.team_ctr, (size_t)kOpenTeams * kTeamStride);
+    if (e == cudaSuccess) e = dev_zero(&L.roots, kOpenTasks);
+    if (e == cudaSuccess) e = dev_zero(&L.qbuf, kOpenParts);
+    if (e == cudaSuccess) e = dev_zero(&L.q_off, 2);
+    if (e == cudaSuccess) e = dev_zero(&L.q_head, (size_t)kMaxLevels * 32);
+    if (e == cudaSuccess) e = dev_zero(&L.q_tail, (size_t)kMaxLevels * 32);
+    if (e == cudaSuccess) e = dev_zero(&L.bq, (size_t)3 * (workers + 1));
+    if (e == cudaSuccess) e = dev_zero(&L.status, 8);
+    if (e == cudaSuccess) e = dev_zero(&L.pub, 4);
+    if (e == cudaSuccess) e = dev_zero(&L.admit, 2);
+    if (e == cudaSuccess) {
+        const int off[2] = {0, kOpenParts};
+        e = cudaMemcpy(L.q_off, off, sizeof(off), cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&L.h_items, sizeof(BwdItem) * kOpenInflight);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&L.d_items, sizeof(BwdItem) * kOpenInflight);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&L.d_acc, sizeof(unsigned long long) * 33 * kOpenInflight);
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&L.h_err, sizeof(double) * kOpenInflight);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&L.d_err, sizeof(double) * kOpenInflight);
+    L.rs_cap = s->a.n_max / 128 + 2;  // the diagonal tiles of one request
+    if (e == cudaSuccess) e = cudaMalloc((void**)&L.d_rs, sizeof(TcRowScaleItem) * (size_t)L.rs_cap);
+    L.slot_req.assign(kOpenInflight, -1);
+    L.ev.assign(kOpenInflight, nullptr);
+    for (int k = 0; k < kOpenInflight && e == cudaSuccess; ++k) e = cudaEventCreateWithFlags(&L.ev[k], cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        ttg_set_last_cuda_error(e, "open lane set-up", __FILE__, __LINE__);
+        return e == cudaErrorMemoryAllocation ? TTG_ENOMEM : TTG_ECUDA;
+    }
+    return TTG_OK;
+}
+
+void open_lane_free(OpenLane& L) {
+    if (L.ks) cudaStreamSynchronize(L.ks);
+    if (L.cs) cudaStreamSynchronize(L.cs);
+    for (void* p : {(void*)L.ops, (void*)L.count, (void*)L.runs, (void*)L.parts, (void*)L.part_next, (void*)L.part_done,
+                    (void*)L.level, (void*)L.bind, (void*)L.succ_ptr, (void*)L.succ_idx, (void*)L.team_slot, (void*)L.team_ctr,
+                    (void*)L.roots, (void*)L.qbuf, (void*)L.q_off, (void*)L.q_head, (void*)L.q_tail, (void*)L.bq, (void*)L.status,
+                    (void*)L.pub, (void*)L.admit, (void*)L.d_items, (void*)L.d_acc, (void*)L.d_err, (void*)L.d_rs})
+        if (p) cudaFree(p);
+    if (L.h_items) cudaFreeHost(L.h_items);
+    if (L.h_err) cudaFreeHost(L.h_err);
+    for (cudaEvent_t e : L.ev)
+        if (e) cudaEventDestroy(e);
+    if (L.kdone) cudaEventDestroy(L.kdone);
+    if (L.ks) cudaStreamDestroy(L.ks);
+    if (L.cs) cudaStreamDestroy(L.cs);
+    if (L.ctx) ttg_destroy(L.ctx);
+}
+
+// Start an epoch: an empty arena and the executor launch that serves it.
+ttg_status open_epoch_start(ttg_serve* s, OpenLane& L) {
+    g_open_at = "epoch start";
+    TTG_CUDA_CHECK(cudaMemsetAsync(L.qbuf, 0xff, sizeof(int) * (size_t)kOpenParts, L.ks));  // every slot unwritten (-1)
+    TTG_CUDA_CHECK(cudaMemsetAsync(L.q_head, 0, sizeof(int) * kMaxLevels * 32, L.ks));
+    TTG_CUDA_CHECK(cudaMemsetAsync(L.q_tail, 0, sizeof(int) * kMaxLevels * 32, L.ks));
+    TTG_CUDA_CHECK(cudaMemsetAsync(L.status, 0, sizeof(int) * 8, L.ks));
+    TTG_CUDA_CHECK(cudaMemsetAsync(L.pub, 0, sizeof(int) * 4, L.ks));
+    TTG_CUDA_CHECK(cudaMemsetAsync(L.admit, 0, sizeof(int) * 2, L.ks));
+    // The copy stream publishes only after the reset.
+    TTG_CUDA_CHECK(cudaEventRecord(L.kdone, L.ks));
+    TTG_CUDA_CHECK(cudaStreamWaitEvent(L.cs, L.kdone, 0));
+    L.n_tasks = L.n_roots = L.n_teams = L.n_parts = 0;
+    L.n_edges = 0;
+    ttg::ExecParams p{};
+    p.ops = L.ops;
+    p.n_tasks = kOpenTasks;
+    p.n_runnable = 0;
+    p.count = L.count;
+    p.runs = L.runs;
+    p.parts = L.parts;
+    p.part_next = L.part_next;
+    p.part_done = L.part_done;
+    p.succ_ptr = L.succ_ptr;
+    p.succ_idx = L.succ_idx;
+    p.level = L.level;
+    p.bind = L.bind;
+    p.n_levels = 1;
+    p.n_workers = L.ctx->workers;
+    p.qbuf = L.qbuf;
+    p.q_off = L.q_off;
+    p.q_head = L.q_head;
+    p.q_tail = L.q_tail;
+    p.bq_buf = L.bq;
+    p.bq_off = L.bq;
+    p.bq_head = L.bq + (L.ctx->workers + 1);
+    p.bq_tail = L.bq + 2 * (L.ctx->workers + 1);
+    p.has_bound = 0;
+    p.done = L.status + 0;
+    p.err = L.status + 1;
+    p.err_task = L.status + 2;
+    p.err_info = L.status + 3;
+    p.trace = nullptr;
+    p.timeout_ns = (long long)(L.ctx->timeout_s * 1e9);
+    p.team_ctr = L.team_ctr;
+    p.team_slot = L.team_slot;
+    p.pub = L.pub;
+    p.roots = L.roots;
+    p.admit = L.admit;
+    ttg_mixed_set_tc(L.ctx, true);
+    ttg_status st = ttg_launch_mixed(L.ctx, p, L.ks);
+    if (st != TTG_OK) return st;
+    TTG_CUDA_CHECK(cudaEventRecord(L.kdone, L.ks));
+    ++s->launches;
+    L.running = true;
+    L.closing = false;
+    return TTG_OK;
+}
+
+// Close the epoch: the launch ends once every published task has run.
+ttg_status open_close(OpenLane& L) {
+    if (!L.running || L.closing) return TTG_OK;
+    L.closing = true;
+    return ttg_stream_write_u32(L.cs, (uint32_t*)(L.pub + 2), 1u);
+}
+
+// Admit request i into lane L: operands on the side stream, its tasks (and a
+// last task that raises its host flag) appended to the arena and published.
+// false: it must wait — no room in this epoch (*full), no request slot free
+// in this lane (*busy), or memory / its factor not ready (neither).
+bool open_admit(ttg_serve* s, OpenLane& L, int i, bool* full, bool* busy, ttg_status* err) {
+    *full = *busy = false;
+    if (L.n_inflight >= kOpenInflight) {
+        *busy = true;  // no request slot free: another lane, or later
+        return false;
+    }
+    ServeRequest& q = s->req[i];
+    Graph g;
+    L.rs.clear();
+    int n_hdr = 0;
+    AdmitTarget T{L.ctx, s->side, &g, &L.rs, nullptr, &n_hdr, 0};
+    // Room first, from upper bounds of the request's graph (batch_graph.h):
+    // factor nb + nb(nb-1)/2 + (nb³-nb)/6 + nb(nb+1)/2 tasks, each solve
+    // nb² + nb, each refinement round 2 + nb(nb+2) + nb more, and the
+    // conversions around them; at most 8 successors and 32 parts a task.
+    {
+        System S;
+        S.set_size(q.N, q.tile);
+        const long nb = S.nb;
+        const long fac = nb + nb * (nb - 1) / 2 + (nb * nb * nb - nb) / 6 + nb * (nb + 1) / 2;
+        const long per_solve = nb * nb + nb;
+        const long est = fac + 2 * nb + per_solve + (long)(q.ir_steps + 1) * (2 + nb * (nb + 2) + per_solve + nb) + 1;
+        const bool fits_empty = est <= L.cap_tasks && 8 * est <= kOpenEdges && 32 * est <= kOpenParts && nb <= kOpenTeams &&
+                                nb <= L.rs_cap;
+        if (!fits_empty) {
+            ttg_set_last_cuda_error(cudaErrorInvalidValue, "open lane: a request exceeds an empty epoch", __FILE__, __LINE__);
+            *err = TTG_EINVAL;
+            return true;
+        }
+        if (L.n_tasks + est > L.cap_tasks || L.n_edges + 8 * est > kOpenEdges || L.n_parts + 32 * est > kOpenParts ||
+            L.n_teams + nb > kOpenTeams) {
+            *full = true;
+            return false;
+        }
+    }
+    g_open_at = "admit: operands";
+    if (!admit_to(s, T, i, err)) return false;
+    if (*err != TTG_OK) return true;
+    g_open_at = "admit: row scales";
+    // Block-row scales of its tensor-core factorisation (after its input).
+    if (!L.rs.empty()) {
+        cudaError_t e = cudaMemcpyAsync(L.d_rs, L.rs.data(), sizeof(TcRowScaleItem) * L.rs.size(), cudaMemcpyHostToDevice, s->side);
+        if (e != cudaSuccess) {
+            *err = TTG_ECUDA;
+            return true;
+        }
+        if ((*err = ttg_mixed_row_scales(L.d_rs, (int)L.rs.size(), s->side)) != TTG_OK) return true;
+    }
+    // The request's last task: after every sink of its graph.
+    {
+        std::vector<char> has_succ(g.ops.size(), 0);
+        for (auto& e : g.edges) has_succ[e.first] = 1;
+        ttg_op sig{};
+        sig.kind = ttg::kOpSignal;
+        sig.prec = TTG_PREC_MIXED;
+        sig.m = ++q.attempt;
+        sig.c = s->d_flag + i;
+        const int t = g.add(sig);
+        for (int u = 0; u < t; ++u)
+            if (!has_succ[u]) g.edge(u, t);
+    }
+    if ((*err = g.finish(false)) != TTG_OK) return true;
+    const int n = (int)g.ops.size();
+    const int base = L.n_tasks;
+    const int64_t ebase = L.n_edges;
+    std::vector<int> parts(n), team(n, -1), roots;
+    std::vector<int64_t> ptr(n + 1);
+    std::vector<int32_t> idx(g.idx.size()), bind(n, -1);
+    std::vector<uint8_t> level(n, 0);
+    int nparts = 0, nteam = 0;
+    for (int t = 0; t < n; ++t) {
+        parts[t] = ttg_task_parts(g.ops[t], true);
+        nparts += parts[t];
+        if (g.ops[t].kind == TTG_OP_POTRF_L && team_fits(g.ops[t].n)) team[t] = L.n_teams + nteam++;
+        if (g.init[t] == 0) roots.push_back(base + t);
+        ptr[t] = ebase + g.ptr[t];
+    }
+    ptr[n] = ebase + g.ptr[n];
+    for (size_t e = 0; e < g.idx.size(); ++e) idx[e] = base + g.idx[e];
+    if (base + n > L.cap_tasks || ebase + (int64_t)idx.size() > kOpenEdges || L.n_parts + nparts > kOpenParts ||
+        L.n_teams + nteam > kOpenTeams) {
+        ttg_set_last_cuda_error(cudaErrorInvalidValue, "open lane: a request's graph exceeds its bounds", __FILE__, __LINE__);
+        *err = TTG_EINVAL;  // the bounds above are wrong
+        return true;
+    }
+    // Into the arena after its operands, then published.
+    int slot = -1;
+    for (int k = 0; k < kOpenInflight && slot < 0; ++k)
+        if (L.slot_req[k] < 0) slot = k;
+    if (slot < 0) {
+        *err = TTG_EINVAL;  // n_inflight said there was one
+        return true;
+    }
+    g_open_at = "admit: publish copies";
+    cudaEvent_t ready = L.ev[slot];
+    auto ok = [&](cudaError_t e) { return e == cudaSuccess; };
+    bool good = ok(cudaEventRecord(ready, s->side)) && ok(cudaStreamWaitEvent(L.cs, ready, 0)) &&
+                ok(cudaMemcpyAsync(L.ops + base, g.ops.data(), sizeof(ttg_op) * n, cudaMemcpyHostToDevice, L.cs)) &&
+                ok(cudaMemcpyAsync(L.count + base, g.init.data(), sizeof(int) * n, cudaMemcpyHostToDevice, L.cs)) &&
+                ok(cudaMemcpyAsync(L.parts + base, parts.data(), sizeof(int) * n, cudaMemcpyHostToDevice, L.cs)) &&
+                ok(cudaMemcpyAsync(L.level + base, level.data(), n, cudaMemcpyHostToDevice, L.cs)) &&
+                ok(cudaMemcpyAsync(L.bind + base, bind.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, L.cs)) &&
+                ok(cudaMemcpyAsync(L.succ_ptr + base, ptr.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, L.cs)) &&
+                (idx.empty() || ok(cudaMemcpyAsync(L.succ_idx + ebase, idx.data(), sizeof(int32_t) * idx.size(), cudaMemcpyHostToDevice, L.cs))) &&
+                ok(cudaMemcpyAsync(L.team_slot + base, team.data(), sizeof(int) * n, cudaMemcpyHostToDevice, L.cs)) &&
+                ok(cudaMemcpyAsync(L.roots + L.n_roots, roots.data(), sizeof(int) * roots.size(), cudaMemcpyHostToDevice, L.cs)) &&
+                ok(cudaMemsetAsync(L.runs + base, 0, sizeof(int) * n, L.cs)) &&
+                ok(cudaMemsetAsync(L.part_next + base, 0, sizeof(int) * n, L.cs)) &&
+                ok(cudaMemsetAsync(L.part_done + base, 0, sizeof(int) * n, L.cs)) &&
+                (nteam == 0 || ok(cudaMemsetAsync(L.team_ctr + (size_t)L.n_teams * kTeamStride, 0,
+                                                  sizeof(int) * (size_t)nteam * kTeamStride, L.cs)));
+    if (!good) {
+        ttg_set_last_cuda_error(cudaGetLastError(), "open lane publish", __FILE__, __LINE__);
+        *err = TTG_ECUDA;
+        return true;
+    }
+    L.n_tasks += n;
+    L.n_edges += (int64_t)idx.size();
+    L.n_parts += nparts;
+    L.n_teams += nteam;
+    L.n_roots += (int)roots.size();
+    g_open_at = "admit: publish words";
+    if ((*err = ttg_stream_write_u32(L.cs, (uint32_t*)L.pub, (uint32_t)L.n_tasks)) != TTG_OK) return true;
+    if ((*err = ttg_stream_write_u32(L.cs, (uint32_t*)(L.pub + 1), (uint32_t)L.n_roots)) != TTG_OK) return true;
+    L.slot_req[slot] = i;
+    ++L.n_inflight;
+    q.lane = (int)(&L - s->open.data());
+    q.slot = slot;
+    q.phase = 1;
+    return true;
+}
+
+// The lane's executor failed (timeout, overcount, not positive definite):
+// its status words, read after the launch ended.
+ttg_status open_lane_error(OpenLane& L) {
+    int h[4] = {0, 0, 0, 0};
+    TTG_CUDA_CHECK(cudaMemcpy(h, L.status, sizeof(h), cudaMemcpyDeviceToHost));
+    return (ttg_status)h[1];
+}
+
+// Completions of lane L: a raised flag starts the request's backward error on
+// the side stream; a finished backward error ends the request (or retries it
+// with twice the refinement rounds).  Returns the requests completed.
+int open_poll(ttg_serve* s, OpenLane& L, std::deque<int>& queue, double t, ttg_status* err) {
+    int done = 0;
+    const bool mixed = s->a.precision == TTG_PREC_MIXED;
+    const volatile int* flag = s->h_flag;
+    for (int k = 0; k < kOpenInflight; ++k) {
+        const int i = L.slot_req[k];
+        if (i < 0) continue;
+        ServeRequest& q = s->req[i];
+        if (q.phase == 1 && flag[i] == q.attempt) {
+            g_open_at = "poll: backward error";
+            int slices = (q.N + kRowsPerBlock - 1) / kRowsPerBlock;
+            L.h_items[k] = BwdItem{q.N, q.tile, s->a.nrhs, s->res[q.key].A64, q.B, q.X, L.d_acc + (size_t)k * 33};
+            cudaError_t e = cudaMemcpyAsync(L.d_items + k, L.h_items + k, sizeof(BwdItem), cudaMemcpyHostToDevice, s->side);
+            if (e == cudaSuccess) e = cudaMemsetAsync(L.d_acc + (size_t)k * 33, 0, sizeof(unsigned long long) * 33, s->side);
+            if (e == cudaSuccess) {
+                ttg_note_launch();
+                serve_bwd_partial<<<dim3(1, slices), kRowsPerBlock, 0, s->side>>>(L.d_items + k);
+                ttg_note_launch();
+                serve_bwd_final<<<1, 128, 0, s->side>>>(L.d_items + k, 1, L.d_err + k);
+                e = cudaGetLastError();
+            }
+            if (e == cudaSuccess) e = cudaMemcpyAsync(L.h_err + k, L.d_err + k, sizeof(double), cudaMemcpyDeviceToHost, s->side);
+            if (e == cudaSuccess) e = cudaEventRecord(L.ev[k], s->side);
+            if (e != cudaSuccess) {
+                ttg_set_last_cuda_error(e, "open lane backward error", __FILE__, __LINE__);
+                *err = TTG_ECUDA;
+                return done;
+            }
+            q.phase = 2;
+        } else if (q.phase == 2 && cudaEventQuery(L.ev[k]) == cudaSuccess) {
+            g_open_at = "poll: completion";
+            q.bwd = L.h_err[k];
+            if (s->a.keep_results) {
+                std::vector<double> v((size_t)q.N * s->a.nrhs);
+                if (cudaMemcpy(v.data(), q.X, sizeof(double) * v.size(), cudaMemcpyDeviceToHost) != cudaSuccess) {
+                    *err = TTG_ECUDA;
+                    return done;
+                }
+                q.result.assign((size_t)q.N * s->a.nrhs, 0.0);
+                for (int c = 0; c < s->a.nrhs; ++c)
+                    for (int r = 0; r < q.N; ++r) q.result[r + (size_t)c * q.N] = v[c + (size_t)r * s->a.nrhs];
+            }
+            pool_free(q.B, s->side);
+            pool_free(q.X, s->side);
+            pool_free(q.R, s->side);
+            pool_free(q.D32, s->side);
+            pool_free(q.D64, s->side);
+            pool_free(q.tc, s->side);
+            s->used -= q.work_bytes;
+            q.work_bytes = 0;
+            Resident& r = s->res[q.key];
+            r.complete = true;
+            release_factor(s, q.key, s->side);
+            L.slot_req[k] = -1;
+            --L.n_inflight;
+            q.phase = 0;
+            q.lane = q.slot = -1;
+            if (mixed && !(q.bwd <= s->a.tol) && q.retries < 2) {
+                ++q.retries;
+                ++s->retries;
+                q.ir_steps *= 2;
+                queue.push_front(i);
+                continue;
+            }
+            q.done = true;
+            q.finish = t;
+            ++done;
+        }
+    }
+    return done;
+}
+
+// The request loop with open lanes.
+ttg_status serve_loop_open(ttg_serve* s, double t0, int* completed_out) {
+    const int n = (int)s->req.size();
+    const bool verbose = getenv("TTG_SERVE_VERBOSE") != nullptr;
+    double next_report = 2.0;
+    std::deque<int> queue;
+    int next = 0, completed = 0;
+    ttg_status st = TTG_OK;
+    std::atomic<bool> stop{false};
+    std::atomic<int> done_count{0};
+    std::thread watch;
+    if (verbose)
+        watch = std::thread([&] {
+            while (!stop) {
+                std::this_thread::sleep_for(std::chrono::seconds(2));
+                if (!stop)
+                    fprintf(stderr, "[ttg serve] watchdog t %.1f s: completed %d, host thread at: %s\n", now_s() - t0,
+                            done_count.load(), g_open_at.load());
+            }
+        });
+    struct Join {
+        std::atomic<bool>& stop;
+        std::thread& w;
+        ~Join() {
+            stop = true;
+            if (w.joinable()) w.join();
+        }
+    } join{stop, watch};
+    while (completed < n) {
+        done_count = completed;
+        g_open_at = "loop";
+        const double t = now_s() - t0;
+        bool progress = false;
+        while (next < n && s->req[next].arrival <= t) {
+            queue.push_back(next++);
+            progress = true;
+        }
+        for (OpenLane& L : s->open) {
+            const int d = open_poll(s, L, queue, now_s() - t0, &st);
+            if (st != TTG_OK) return st;
+            completed += d;
+            progress = progress || d > 0;
+            if (L.running && cudaEventQuery(L.kdone) == cudaSuccess) {
+                // The launch ended: after its close once its requests are
+                // through, or early by an error (a request still in flight
+                // would never be done).
+                if ((st = open_lane_error(L)) != TTG_OK) return st;
+                if (L.n_inflight > 0) {
+                    // Every request of a closed epoch raises its flag before
+                    // the launch ends; poll once more before calling it lost.
+                    const int d2 = open_poll(s, L, queue, now_s() - t0, &st);
+                    if (st != TTG_OK) return st;
+                    completed += d2;
+                    bool lost = false;
+                    for (int k = 0; k < kOpenInflight; ++k)
+                        if (L.slot_req[k] >= 0 && s->req[L.slot_req[k]].phase == 1) lost = true;
+                    if (lost) {
+                        ttg_set_last_cuda_error(cudaErrorLaunchFailure, "open lane: the launch ended before a request was done",
+                                                __FILE__, __LINE__);
+                        return TTG_ETIMEOUT;
+                    }
+                    continue;  // backward errors still running
+                }
+                L.running = false;
+                L.closing = false;  // free for the next epoch
+                progress = true;
+            }
+        }
+        // Admission: each waiting request, in arrival order, into the open
+        // lane with the fewest requests in flight; a lane whose epoch is full
+        // closes (a new epoch starts once its launch has ended).
+        for (auto it = queue.begin(); it != queue.end();) {
+            const int i = *it;
+            bool admitted = false, blocked = false;
+            std::vector<OpenLane*> order;
+            for (OpenLane& L : s->open)
+                if (!L.closing) order.push_back(&L);
+            std::sort(order.begin(), order.end(), [](const OpenLane* a, const OpenLane* b) { return a->n_inflight < b->n_inflight; });
+            for (OpenLane* L : order) {
+                if (!L->running && (st = open_epoch_start(s, *L)) != TTG_OK) return st;
+                bool full = false, busy = false;
+                admitted = open_admit(s, *L, i, &full, &busy, &st);
+                if (st != TTG_OK) return st;
+                if (admitted) break;
+                if (busy) continue;
+                if (full) {
+                    if ((st = open_close(*L)) != TTG_OK) return st;
+                    continue;
+                }
+                blocked = true;  // memory, or its factor is not ready: it waits
+                break;
+            }
+            if (admitted) {
+                it = queue.erase(it);
+                progress = true;
+            } else {
+                ++it;
+                (void)blocked;
+            }
+        }
+        bool any = false;
+        for (OpenLane& L : s->open) any = any || L.n_inflight > 0 || L.closing;
+        if (!any && !queue.empty() && !progress) return TTG_ENOMEM;  // nothing in flight and nothing admitted
+        if (verbose && now_s() - t0 > next_report) {
+            next_report += 2.0;
+            fprintf(stderr, "[ttg serve] t %.1f s: completed %d of %d, waiting %zu, arrived %d\n", now_s() - t0, completed, n,
+                    queue.size(), next);
+            for (const OpenLane& L : s->open)
+                fprintf(stderr,
+                        "[ttg serve]   lane: running %d closing %d in flight %d, tasks %d roots %d parts %d edges %lld; "
+                        "copies idle %d, launch ended %d, side idle %d\n",
+                        (int)L.running, (int)L.closing, L.n_inflight, L.n_tasks, L.n_roots, L.n_parts, (long long)L.n_edges,
+                        (int)(cudaStreamQuery(L.cs) == cudaSuccess), (int)(cudaEventQuery(L.kdone) == cudaSuccess),
+                        (int)(cudaStreamQuery(s->side) == cudaSuccess));
+        }
+        if (!progress) std::this_thread::sleep_for(std::chrono::microseconds(20));
+    }
+    g_open_at = "drain";
+    for (OpenLane& L : s->open)
+        if ((st = open_close(L)) != TTG_OK) return st;
+    for (OpenLane& L : s->open) {
+        cudaStreamSynchronize(L.cs);
+        cudaStreamSynchronize(L.ks);
+        if (L.running && (st = open_lane_error(L)) != TTG_OK) return st;
+        L.running = false;
+    }
+    cudaStreamSynchronize(s->side);
+    *completed_out = completed;
+    return TTG_OK;
+}
+
+}  // namespace
+
 extern "C" ttg_status ttg_serve_create(int device, const ttg_serve_args* a, ttg_serve** out) {
     if (!a || !out || a->n_requests < 1 || !(a->rate > 0) || a->n_min < 1 || a->n_max < a->n_min || a->n_max > 131072 ||
         a->nrhs < 1 || a->nrhs > 16 || a->lanes < 1 || a->max_batch < 1 || !(a->hbm_budget_gb > 0) || a->ir_steps < 0 ||
@@ -486,6 +1076,58 @@ extern "C" ttg_status ttg_serve_create(int device, const ttg_serve_args* a, ttg_
             factors.push_back(i);
         }
         q.tile = ttg_serve_tile(q.N);
+    }
+    if (a->admission == 1 && a->precision == TTG_PREC_MIXED) {
+        // Open lanes, with half the SMs (TTG_SERVE_SPARE_SMS sets the count)
+        // left to the side stream's kernels: at 1000 requests/s on two lanes
+        // 16, 48 and 76 spare SMs gave 36, 91 and 127 solves/s — the input
+        // generators are the side stream's largest share.
+        int spare = s->sms / 2;
+        if (const char* v = getenv("TTG_SERVE_SPARE_SMS")) spare = std::max(1, std::min(s->sms - a->lanes, atoi(v)));
+        const int workers = std::max(1, (s->sms - spare) / a->lanes);
+        cudaError_t e = cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaHostAlloc((void**)&s->h_flag, sizeof(int) * (size_t)a->n_requests, cudaHostAllocMapped);
+        if (e == cudaSuccess) {
+            memset(s->h_flag, 0, sizeof(int) * (size_t)a->n_requests);
+            e = cudaHostGetDevicePointer((void**)&s->d_flag, s->h_flag, 0);
+        }
+        if (e != cudaSuccess) {
+            ttg_set_last_cuda_error(e, "serve open set-up", __FILE__, __LINE__);
+            ttg_serve_destroy(s);
+            return TTG_ECUDA;
+        }
+        // Every kernel the side stream launches is loaded before the first
+        // lane starts: with lazy module loading a first launch waits for the
+        // device to be idle, and a lane's executor is never idle until closed.
+        cudaFuncAttributes fa;
+        ttg_status pst = ttg_gen_preload();
+        if (pst == TTG_OK) pst = ttg_mixed_row_scales_preload();
+        if (pst == TTG_OK && (cudaFuncGetAttributes(&fa, serve_bwd_partial) != cudaSuccess ||
+                              cudaFuncGetAttributes(&fa, serve_bwd_final) != cudaSuccess))
+            pst = TTG_ECUDA;
+        if (pst != TTG_OK) {
+            ttg_serve_destroy(s);
+            return pst;
+        }
+        s->open.resize(a->lanes);
+        for (OpenLane& L : s->open) {
+            ttg_status st = open_lane_setup(s, L, workers);
+            if (st != TTG_OK) {
+                ttg_serve_destroy(s);
+                return st;
+            }
+        }
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+            uint64_t thr = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        }
+        *out = s;
+        return TTG_OK;
+    }
+    if (a->admission != 0 && a->admission != 1) {
+        ttg_serve_destroy(s);
+        return TTG_EINVAL;
     }
     // Lanes: one executor context and stream each.
     const int workers = std::max(1, s->sms / a->lanes);
@@ -532,6 +1174,15 @@ extern "C" ttg_status ttg_serve_create(int device, const ttg_serve_args* a, ttg_
 extern "C" void ttg_serve_destroy(ttg_serve* s) {
     if (!s) return;
     cudaSetDevice(s->device);
+    for (OpenLane& L : s->open) {
+        open_close(L);  // a running epoch ends once its published tasks have run
+        open_lane_free(L);
+    }
+    if (s->side) {
+        cudaStreamSynchronize(s->side);
+        cudaStreamDestroy(s->side);
+    }
+    if (s->h_flag) cudaFreeHost(s->h_flag);
     for (Lane& L : s->lanes)
         if (L.s) cudaStreamSynchronize(L.s);
     for (auto& kv : s->res) {
@@ -566,6 +1217,17 @@ extern "C" ttg_status ttg_serve_run(ttg_serve* s, ttg_serve_report* rep, double*
     int next = 0, completed = 0;
     const double t0 = now_s();
     ttg_status st = TTG_OK;
+    if (!s->open.empty()) {
+        st = serve_loop_open(s, t0, &completed);
+        if (st != TTG_OK) {
+            for (OpenLane& L : s->open) {
+                open_close(L);
+                cudaStreamSynchronize(L.cs);
+                cudaStreamSynchronize(L.ks);
+            }
+            return st;
+        }
+    }
     while (completed < n && st == TTG_OK) {
         const double t = now_s() - t0;
         bool progress = false;
