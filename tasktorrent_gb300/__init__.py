@@ -554,7 +554,10 @@ def batch_autotune(ctx, sizes, tiles, workers, precision=PREC_F64, nrhs=1, ir_st
 
 class Serve:
     """The request loop of include/ttg_serve.h (a Poisson stream of
-    factor-and-solve and follow-up requests over `lanes` executors)."""
+    factor-and-solve and follow-up requests over `lanes` executors).
+    admission 0: each lane takes the waiting requests as its next launch;
+    1 (mixed precision): open lanes — a persistent executor per lane takes a
+    request's tasks while it runs."""
 
     def __init__(self, n_requests, rate, n_min=64, n_max=8192, alpha=1e-4, seed=2, followup_frac=0.3,
                  precision=PREC_MIXED, ir_steps=4, nrhs=1, lanes=2, max_batch=16, hbm_budget_gb=180.0, tol=1e-14,
