@@ -72,6 +72,9 @@ struct SweepArgs {
     int fold;
     const int64_t* woff;       // [nb] offset of W_i in Wd (ld bs[i])
     int* zready;               // [nb]
+    // The TMA sweep's claim order (folded form): claim k takes item
+    // order[k] (an index in step order); null in the other sweeps.
+    const int* order;
 };
 
 __device__ __forceinline__ long long sweep_clock() {

@@ -1,10 +1,12 @@
 // sweep_tma.cuh — the FP32 block sweeps (the preconditioner M⁻¹ = L̃⁻ᵀL̃⁻¹
 // of the refinement) with every item's factor strip staged by TMA.
 //
-// Same work items, order, waits and flags as sweep_kernel<float, float>
+// Same work items, waits and flags as sweep_kernel<float, float>
 // (solve_kernels.cuh): an item is out[strip] (=, or -=) M[strip, 0:kc] ·
-// V[0:kc, 0:nrhs] for a 64-row strip.  The difference is how M reaches the
-// SM.  The generic kernel streams it through registers and keeps ~16 KB of
+// V[0:kc, 0:nrhs] for a 64-row strip.  Items are claimed in the order the
+// host builds (SweepArgs::order: each step's chain items ahead of the
+// previous step's bulk; N = 32768, tile 512: 1.67 -> 1.51 ms per sweep).
+// The other difference is how M reaches the SM.  The generic kernel streams it through registers and keeps ~16 KB of
 // loads in flight per block, which left each item at ~15 µs (a 128 KB strip
 // at ~10 GB/s per block).  Here one thread issues the whole strip as TMA
 // boxes of 64 rows × 128 columns as soon as the item is claimed — the factor
@@ -73,7 +75,10 @@ __global__ void __launch_bounds__(256, 1) sweep_kernel_f32_tma(SweepArgs a, cons
     uint32_t phase = 0;
     for (;;) {
         __syncthreads();
-        if (threadIdx.x == 0) s_item = atomicAdd(a.claim, 1);
+        if (threadIdx.x == 0) {
+            const int k = atomicAdd(a.claim, 1);
+            s_item = k < total ? __ldg(a.order + k) : total;
+        }
         __syncthreads();
         const int it = s_item;
         if (it >= total) break;
