@@ -248,6 +248,14 @@ __device__ inline int potrf_l_f64(int n, double* A, int lda, double* smem) {
     return 0;
 }
 
+// The TRSM's column update for slices of at most 64 rows, in 64-row blocks;
+// out of line, so that the executor's register budget stays with its tile
+// kernels.
+static __device__ __noinline__ void trsm_update_f64_small(int m, int n, int k, const double* A, int lda, const double* B, int ldb,
+                                                          double* C, int ldc, double* smem) {
+    gemm_tile<double, false, false, 64>(m, n, k, -1.0, A, lda, B, ldb, 1.0, C, ldc, smem);
+}
+
 // B[m×n] <- alpha·B·L⁻ᵀ, L n×n lower non-unit (right-looking, 32-column panels).
 // Rows are independent: part `part` of `parts` solves one slice of rows.
 template <class T>
@@ -276,7 +284,18 @@ __device__ inline void trsm_rltn_tile(int m, int n, T alpha, const T* L, int ldl
         trsm_rows_panel<T>(B + (size_t)p * ldb, ldb, 0, m, nb, Ls, p == 0 ? alpha : T(1));
         __syncthreads();
         const int rest = n - p - nb;
-        if (rest > 0)
+        // The update of the columns right of the panel: FP64 slices of at
+        // most 64 rows in 64-row blocks (a part of 32 rows in a 128-row block
+        // ran four times the DFMAs it needs: 381 of a 527 µs TRSM at tile
+        // 128).  The block edge does not change any output's summation order.
+        if constexpr (sizeof(T) == 8) {
+            if (rest > 0 && m <= 64)
+                trsm_update_f64_small(m, rest, nb, B + (size_t)p * ldb, ldb, L + (p + nb) + (size_t)p * ldl, ldl,
+                                      B + (size_t)(p + nb) * ldb, ldb, smem);
+            else if (rest > 0)
+                gemm_tile<T, false, false>(m, rest, nb, T(-1), B + (size_t)p * ldb, ldb, L + (p + nb) + (size_t)p * ldl, ldl, T(1),
+                                           B + (size_t)(p + nb) * ldb, ldb, smem);
+        } else if (rest > 0)
             gemm_tile<T, false, false>(m, rest, nb, T(-1), B + (size_t)p * ldb, ldb, L + (p + nb) + (size_t)p * ldl, ldl, T(1),
                                        B + (size_t)(p + nb) * ldb, ldb, smem);
         __syncthreads();
