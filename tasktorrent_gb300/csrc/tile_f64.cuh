@@ -40,7 +40,7 @@ __device__ __forceinline__ float ldcg(const float* p) { return __ldcg(p); }
 template <class T, bool B_NN, bool LOWER, int BS = 128>
 __device__ void gemm_tile(int m, int n, int k, T alpha, const T* __restrict__ A, int lda, const T* __restrict__ B, int ldb,
                           T beta, T* C, int ldc, T* smem, int part = 0, int parts = 1) {
-    static_assert(BS == 128 || BS == 64, "output block edge");
+    static_assert(BS == 128 || BS == 64 || BS == 32, "output block edge");
     constexpr int R = BS / 16;  // outputs per thread and dimension
     T(*As)[BS] = reinterpret_cast<T(*)[BS]>(smem);
     T(*Bs)[BS + 1] = reinterpret_cast<T(*)[BS + 1]>(smem + kBK * BS);
@@ -129,17 +129,32 @@ __device__ void gemm_tile(int m, int n, int k, T alpha, const T* __restrict__ A,
     }
 }
 
-// Output block edge of an FP64 tile update: 64 for tiles up to 256 (more
-// parts, so that small tiles spread over more SMs: at this GPU's FP64 rate a
-// 128×128×128 update takes ~0.5 ms on one block), else 128.  FP32 updates
+// Output block edge of an FP64 tile update: 32 for tiles up to 128, 64 up
+// to 256 (more parts, so that small tiles spread over more SMs: at this
+// GPU's FP64 rate a 128×128×128 update takes ~0.5 ms on one block), else
+// 128.  The edge never changes an output's summation order.  FP32 updates
 // keep 128 (their 8×8 register blocks use the FMA pipe better).
 __host__ __device__ constexpr int gemm_block_edge(int m, int n, bool f64 = true) {
-    return (f64 && m <= 256 && n <= 256) ? 64 : 128;
+    return (f64 && m <= 128 && n <= 128) ? 32 : (f64 && m <= 256 && n <= 256) ? 64 : 128;
+}
+
+// FP64 updates in 32-row blocks, out of line (the executor's register
+// budget stays with the larger blocks).
+template <bool B_NN, bool LOWER>
+static __device__ __noinline__ void gemm_tile_f64_e32(int m, int n, int k, double alpha, const double* A, int lda, const double* B,
+                                                      int ldb, double beta, double* C, int ldc, double* smem, int part, int parts) {
+    gemm_tile<double, B_NN, LOWER, 32>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, smem, part, parts);
 }
 
 template <class T, bool B_NN, bool LOWER>
 __device__ __forceinline__ void gemm_tile_auto(int m, int n, int k, T alpha, const T* A, int lda, const T* B, int ldb, T beta, T* C,
                                                int ldc, T* smem, int part = 0, int parts = 1) {
+    if constexpr (sizeof(T) == 8) {
+        if (gemm_block_edge(m, n, true) == 32) {
+            gemm_tile_f64_e32<B_NN, LOWER>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, smem, part, parts);
+            return;
+        }
+    }
     if (gemm_block_edge(m, n, sizeof(T) == 8) == 64)
         gemm_tile<T, B_NN, LOWER, 64>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, smem, part, parts);
     else
@@ -285,11 +300,15 @@ __device__ inline void trsm_rltn_tile(int m, int n, T alpha, const T* L, int ldl
         __syncthreads();
         const int rest = n - p - nb;
         // The update of the columns right of the panel: FP64 slices of at
-        // most 64 rows in 64-row blocks (a part of 32 rows in a 128-row block
-        // ran four times the DFMAs it needs: 381 of a 527 µs TRSM at tile
-        // 128).  The block edge does not change any output's summation order.
+        // most 32 (64) rows in 32-row (64-row) blocks (a part of 32 rows in a
+        // 128-row block ran four times the DFMAs it needs: 381 of a 527 µs
+        // TRSM at tile 128).  The block edge does not change any output's
+        // summation order.
         if constexpr (sizeof(T) == 8) {
-            if (rest > 0 && m <= 64)
+            if (rest > 0 && m <= 32)
+                gemm_tile_f64_e32<false, false>(m, rest, nb, -1.0, B + (size_t)p * ldb, ldb, L + (p + nb) + (size_t)p * ldl, ldl,
+                                                1.0, B + (size_t)(p + nb) * ldb, ldb, smem, 0, 1);
+            else if (rest > 0 && m <= 64)
                 trsm_update_f64_small(m, rest, nb, B + (size_t)p * ldb, ldb, L + (p + nb) + (size_t)p * ldl, ldl,
                                       B + (size_t)(p + nb) * ldb, ldb, smem);
             else if (rest > 0)
