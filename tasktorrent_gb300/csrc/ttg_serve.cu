@@ -980,7 +980,7 @@ ttg_status serve_loop_open(ttg_serve* s, double t0, int* completed_out) {
         // closes (a new epoch starts once its launch has ended).
         for (auto it = queue.begin(); it != queue.end();) {
             const int i = *it;
-            bool admitted = false, blocked = false;
+            bool admitted = false;
             std::vector<OpenLane*> order;
             for (OpenLane& L : s->open)
                 if (!L.closing) order.push_back(&L);
@@ -996,15 +996,13 @@ ttg_status serve_loop_open(ttg_serve* s, double t0, int* completed_out) {
                     if ((st = open_close(*L)) != TTG_OK) return st;
                     continue;
                 }
-                blocked = true;  // memory, or its factor is not ready: it waits
-                break;
+                break;  // memory, or its factor is not ready: it waits
             }
             if (admitted) {
                 it = queue.erase(it);
                 progress = true;
             } else {
                 ++it;
-                (void)blocked;
             }
         }
         bool any = false;
