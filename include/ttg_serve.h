@@ -52,7 +52,8 @@ typedef struct ttg_serve_args {
     double tol;             /* backward-error target                                        */
     int32_t keep_results;   /* keep every solution for ttg_serve_get_x                      */
     int32_t admission;      /* 0: a lane takes waiting requests when its launch ends (one
-                               launch per batch of requests); 1 (mixed): open lanes — each
+                               launch per batch of requests); 1 (mixed only, else
+                               TTG_EINVAL): open lanes — each
                                lane's executor keeps running and takes a request's tasks as
                                soon as they are published, between other tasks; the lanes
                                leave half the SMs to the input generators and backward

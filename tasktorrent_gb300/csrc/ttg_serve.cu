@@ -1041,7 +1041,8 @@ ttg_status serve_loop_open(ttg_serve* s, double t0, int* completed_out) {
 extern "C" ttg_status ttg_serve_create(int device, const ttg_serve_args* a, ttg_serve** out) {
     if (!a || !out || a->n_requests < 1 || !(a->rate > 0) || a->n_min < 1 || a->n_max < a->n_min || a->n_max > 131072 ||
         a->nrhs < 1 || a->nrhs > 16 || a->lanes < 1 || a->max_batch < 1 || !(a->hbm_budget_gb > 0) || a->ir_steps < 0 ||
-        (a->precision != TTG_PREC_F64 && a->precision != TTG_PREC_MIXED))
+        (a->precision != TTG_PREC_F64 && a->precision != TTG_PREC_MIXED) || a->admission < 0 || a->admission > 1 ||
+        (a->admission == 1 && a->precision != TTG_PREC_MIXED))
         return TTG_EINVAL;
     *out = nullptr;
     TTG_CUDA_CHECK(cudaSetDevice(device));
@@ -1122,10 +1123,6 @@ extern "C" ttg_status ttg_serve_create(int device, const ttg_serve_args* a, ttg_
         }
         *out = s;
         return TTG_OK;
-    }
-    if (a->admission != 0 && a->admission != 1) {
-        ttg_serve_destroy(s);
-        return TTG_EINVAL;
     }
     // Lanes: one executor context and stream each.
     const int workers = std::max(1, s->sms / a->lanes);

@@ -47,6 +47,22 @@ def test_strerror_without_gpu():
     assert "positive definite" in t.strerror(t.TTG_ENOTPD)
 
 
+def test_serve_rejects_bad_arguments_before_any_device_call():
+    """ttg_serve_create checks its arguments first: each bad field gives
+    TTG_EINVAL with no GPU present (a device call would give TTG_ECUDA)."""
+    import ctypes
+    good = dict(n_requests=10, rate=100.0, n_min=64, n_max=512, alpha=1e-4, seed=2, followup_frac=0.3,
+                precision=t.PREC_MIXED, ir_steps=3, nrhs=1, lanes=2, max_batch=4, hbm_budget_gb=1.0, tol=1e-14,
+                keep_results=0, admission=0)
+    bad = [dict(admission=2), dict(admission=-1), dict(admission=1, precision=t.PREC_F64), dict(lanes=0),
+           dict(nrhs=17), dict(n_max=32), dict(rate=0.0), dict(precision=7)]
+    for b in bad:
+        args = t.ServeArgs(**dict(good, **b))
+        h = ctypes.c_void_p()
+        assert t.lib().ttg_serve_create(0, ctypes.byref(args), ctypes.byref(h)) == t.TTG_EINVAL, b
+        assert not h.value
+
+
 @pytest.mark.parametrize("kind,acc", [(0, 0), (0, 1), (2, 0), (2, 1)])
 def test_captured_cholesky_dag_equals_reference(tmp_path, kind, acc):
     pre = str(tmp_path / "c")
