@@ -151,3 +151,35 @@ def test_cli_help_and_bad_args():
         assert r.returncode == 2
         r = subprocess.run([exe, "--no_such_flag=1"], capture_output=True, text=True)
         assert r.returncode == 2
+
+
+def _noalloc_desc(ops, indeg, ptr, idx):
+    import ctypes
+    import numpy as np
+    n = len(ops)
+    keep = [(t.Op * n)(*ops), np.ascontiguousarray(indeg, np.int32), np.ascontiguousarray(ptr, np.int64),
+            np.ascontiguousarray(idx if len(idx) else [0], np.int32)]
+    g = t.GraphDesc(n, keep[0], keep[1].ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), None, None,
+                    keep[2].ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                    keep[3].ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
+    return g, keep
+
+
+def test_noalloc_rejects_bad_graphs_before_any_device_call():
+    """ttg_run_graph_noalloc validates the whole graph on the host first:
+    every malformed case returns TTG_EINVAL with no GPU present."""
+    import ctypes
+    import numpy as np
+    nop = t.Op(kind=t.OP_NOP)
+    cases = [
+        ([nop] * 16385, np.zeros(16385), np.zeros(16386), []),                     # beyond the task limit
+        ([t.Op(kind=t.OP_POTRF_L, prec=t.PREC_MIXED, m=64, n=64, ldc=64)], [0], [0, 0], []),  # not FP64
+        ([nop, nop], [0, 1], [0, 1, 1], [2]),                                       # successor out of range
+        ([nop, nop], [0, -1], [0, 0, 0], []),                                       # negative counter
+        ([nop, nop], [0, 1], [1, 1, 1], [1]),                                       # offsets not from 0
+        ([t.Op(kind=99)], [0], [0, 0], []),                                         # unknown kind
+    ]
+    for ops, indeg, ptr, idx in cases:
+        g, keep = _noalloc_desc(ops, indeg, ptr, idx)
+        rep = t.Report()
+        assert t.lib().ttg_run_graph_noalloc(0, ctypes.byref(g), 0, 5.0, None, ctypes.byref(rep)) == t.TTG_EINVAL
