@@ -177,53 +177,22 @@ static ttg_status solver_init(ttg_solver* S) {
 
 // Host tables of the sweeps (strips, item counts per step) and of the tile
 // transposes.
-static ttg_status solver_tables(ttg_solver* S, const int* bs, const int64_t* off) {
-    const int nb = S->nb;
-    std::vector<int64_t> doff(nb, 0);
-    int64_t d = 0;
-    for (int i = 0; i < nb; ++i) {
-        doff[i] = d;
-        d += (int64_t)bs[i] * bs[i];
-    }
-    S->dsize = d;
-    std::vector<int> sp(nb + 1, 0);
-    for (int i = 0; i < nb; ++i) sp[i + 1] = sp[i] + (bs[i] + kStrip - 1) / kStrip;
-    S->n_strips = sp[nb];
-    std::vector<int> fwd(nb + 1, 0), bwd(nb + 1, 0);
-    for (int st = 0; st < nb; ++st) {
-        const int i = st, ib = nb - 1 - st;
-        const int64_t nf = (int64_t)(sp[i + 1] - sp[i]) + (sp[nb] - sp[i + 1]);
-        const int64_t nbk = (int64_t)(sp[ib + 1] - sp[ib]) + sp[ib];
-        if ((int64_t)fwd[st] + nf > INT32_MAX || (int64_t)bwd[st] + nbk > INT32_MAX) return TTG_EINVAL;
-        fwd[st + 1] = fwd[st] + (int)nf;
-        bwd[st + 1] = bwd[st] + (int)nbk;
-    }
-    std::vector<TransposeDesc> to, td;
-    std::vector<int64_t> so(1, 0), sd(1, 0);
-    for (int j = 0; j < nb; ++j) {
-        for (int i = j + 1; i < nb; ++i) {
-            const int64_t o = off[i + (size_t)j * nb];
-            to.push_back({o, o, bs[i], bs[j]});
-            so.push_back(so.back() + (int64_t)((bs[i] + kTrEdge - 1) / kTrEdge) * ((bs[j] + kTrEdge - 1) / kTrEdge));
-        }
-        td.push_back({doff[j], doff[j], bs[j], bs[j]});
-        sd.push_back(sd.back() + (int64_t)((bs[j] + kTrEdge - 1) / kTrEdge) * ((bs[j] + kTrEdge - 1) / kTrEdge));
-    }
-    S->items_fwd = fwd[nb];
-    S->items_bwd = bwd[nb];
-    // The TMA sweep's claim order (folded form).  Step s holds D(s), the
-    // diagonal strips of its row; Z(s), the Z strips of the next row; and
-    // its bulk B(s), the updates of the rows after that, nearest row first.
-    // The order D(0) Z(0), then for s >= 1: B(s-1)'s first row, D(s), Z(s),
-    // the rest of B(s-1), claims each step's chain items before the bulk of
-    // the step before it (step order claims them after it: at N = 32768 the
-    // next diagonal waited ~37 µs behind ~500 bulk items).  Every item still
-    // follows all the items it reads — D(s): D(s-1), Z(s-1); Z(s): the
-    // updates of its row, the last in B(s-1)'s first row; B(s-1): D(s-1) and
-    // the same strips in B(s-2) — so blocks claiming in this order never
-    // wait on an unclaimed item.
-    std::vector<int> order;
-    order.reserve((size_t)S->items_fwd + S->items_bwd);
+// The TMA sweep's claim order (folded form), forward items then backward,
+// each an item index in step order.  sp: strips before each block row;
+// fwd / bwd: items before each step of the two directions.  Step s holds
+// D(s), the diagonal strips of its row; Z(s), the Z strips of the next row;
+// and its bulk B(s), the updates of the rows after that, nearest row first.
+// The order D(0) Z(0), then for s >= 1: B(s-1)'s first row, D(s), Z(s), the
+// rest of B(s-1), claims each step's chain items before the bulk of the step
+// before it (step order claims them after it: at N = 32768 the next diagonal
+// waited ~37 µs behind ~500 bulk items).  Every item still follows all the
+// items it reads — D(s): D(s-1), Z(s-1); Z(s): the updates of its row, the
+// last in B(s-1)'s first row; B(s-1): D(s-1) and the same strips in B(s-2) —
+// so blocks claiming in this order never wait on an unclaimed item.
+static void sweep_claim_order(int nb, const std::vector<int>& sp, const std::vector<int>& fwd, const std::vector<int>& bwd,
+                              std::vector<int>& order) {
+    order.clear();
+    order.reserve((size_t)fwd[nb] + bwd[nb]);
     for (int dir = 0; dir < 2; ++dir) {
         const std::vector<int>& steps = dir ? bwd : fwd;
         auto row = [&](int st) { return dir ? nb - 1 - st : st; };
@@ -242,6 +211,53 @@ static ttg_status solver_tables(ttg_solver* S, const int* bs, const int64_t* off
             push(bulk0(p) + first_row(p), steps[p + 1] - bulk0(p) - first_row(p));
         }
     }
+}
+
+// Strips before each block row and items before each sweep step (forward,
+// backward) for block rows of bs[i] rows; false if a count overflows.
+static bool sweep_step_tables(int nb, const int* bs, std::vector<int>& sp, std::vector<int>& fwd, std::vector<int>& bwd) {
+    sp.assign(nb + 1, 0);
+    for (int i = 0; i < nb; ++i) sp[i + 1] = sp[i] + (bs[i] + kStrip - 1) / kStrip;
+    fwd.assign(nb + 1, 0);
+    bwd.assign(nb + 1, 0);
+    for (int st = 0; st < nb; ++st) {
+        const int i = st, ib = nb - 1 - st;
+        const int64_t nf = (int64_t)(sp[i + 1] - sp[i]) + (sp[nb] - sp[i + 1]);
+        const int64_t nbk = (int64_t)(sp[ib + 1] - sp[ib]) + sp[ib];
+        if ((int64_t)fwd[st] + nf > INT32_MAX || (int64_t)bwd[st] + nbk > INT32_MAX) return false;
+        fwd[st + 1] = fwd[st] + (int)nf;
+        bwd[st + 1] = bwd[st] + (int)nbk;
+    }
+    return true;
+}
+
+static ttg_status solver_tables(ttg_solver* S, const int* bs, const int64_t* off) {
+    const int nb = S->nb;
+    std::vector<int64_t> doff(nb, 0);
+    int64_t d = 0;
+    for (int i = 0; i < nb; ++i) {
+        doff[i] = d;
+        d += (int64_t)bs[i] * bs[i];
+    }
+    S->dsize = d;
+    std::vector<int> sp, fwd, bwd;
+    if (!sweep_step_tables(nb, bs, sp, fwd, bwd)) return TTG_EINVAL;
+    S->n_strips = sp[nb];
+    std::vector<TransposeDesc> to, td;
+    std::vector<int64_t> so(1, 0), sd(1, 0);
+    for (int j = 0; j < nb; ++j) {
+        for (int i = j + 1; i < nb; ++i) {
+            const int64_t o = off[i + (size_t)j * nb];
+            to.push_back({o, o, bs[i], bs[j]});
+            so.push_back(so.back() + (int64_t)((bs[i] + kTrEdge - 1) / kTrEdge) * ((bs[j] + kTrEdge - 1) / kTrEdge));
+        }
+        td.push_back({doff[j], doff[j], bs[j], bs[j]});
+        sd.push_back(sd.back() + (int64_t)((bs[j] + kTrEdge - 1) / kTrEdge) * ((bs[j] + kTrEdge - 1) / kTrEdge));
+    }
+    S->items_fwd = fwd[nb];
+    S->items_bwd = bwd[nb];
+    std::vector<int> order;
+    sweep_claim_order(nb, sp, fwd, bwd, order);
     if (order.size() != (size_t)S->items_fwd + S->items_bwd) return TTG_EINVAL;
     {
         bool uni = bs[0] % 128 == 0 && bs[0] <= kTmaMaxK;
@@ -979,4 +995,19 @@ ttg_status ttg_solver_solve(ttg_solver* S, const double* pristine, const double*
     if (h_err[0] || h_err[1]) r.status = TTG_ETIMEOUT;  // a sweep or a product gave up waiting: X is not valid
     if (rep) *rep = r;
     return r.status;
+}
+
+// Test hook (no device work): the claim order of the TMA sweeps over nb
+// block rows of bs[i] rows — forward items, then backward, each an item
+// index in step order — as the solver builds it.  Returns the number of
+// items (written when it is at most cap), or -1 for bad sizes.
+extern "C" int64_t ttg_internal_sweep_order(int32_t nb, const int32_t* bs, int32_t* out, int64_t cap) {
+    if (nb < 1 || !bs) return -1;
+    for (int i = 0; i < nb; ++i)
+        if (bs[i] < 1) return -1;
+    std::vector<int> sp, fwd, bwd, order;
+    if (!sweep_step_tables(nb, bs, sp, fwd, bwd)) return -1;
+    sweep_claim_order(nb, sp, fwd, bwd, order);
+    if (out && (int64_t)order.size() <= cap) std::copy(order.begin(), order.end(), out);
+    return (int64_t)order.size();
 }

@@ -183,3 +183,70 @@ def test_noalloc_rejects_bad_graphs_before_any_device_call():
         g, keep = _noalloc_desc(ops, indeg, ptr, idx)
         rep = t.Report()
         assert t.lib().ttg_run_graph_noalloc(0, ctypes.byref(g), 0, 5.0, None, ctypes.byref(rep)) == t.TTG_EINVAL
+
+
+def _sweep_items(nb, bs, backward):
+    """Decode every item of one sweep direction as the TMA sweep kernel does:
+    (kind, step, strip) with kind 0 = diagonal strip D, 1 = Z strip of the
+    next row, 2 = bulk update of strip g; and each item's inputs, from the
+    kernel's wait conditions (folded form)."""
+    sp = [0]
+    for b in bs:
+        sp.append(sp[-1] + (b + 63) // 64)
+    row = (lambda s: nb - 1 - s) if backward else (lambda s: s)
+    strips = lambda r: sp[r + 1] - sp[r]
+    items = []
+    for s in range(nb):
+        i = row(s)
+        items += [(0, s, sp[i] + u) for u in range(strips(i))]
+        if s + 1 < nb:
+            nx = row(s + 1)
+            items += [(1, s, sp[nx] + u) for u in range(strips(nx))]
+        if backward:  # rows i-2 … 0, last strip first
+            bulk = range(sp[i - 1] - 1, -1, -1) if i >= 1 else range(0)
+        else:  # rows i+2 … nb-1
+            bulk = range(sp[min(i + 2, nb)], sp[nb])
+        items += [(2, s, g) for g in bulk]
+    index = {it: n for n, it in enumerate(items)}
+
+    def inputs(it):
+        kind, s, g = it
+        if kind == 0:
+            if s == 0:
+                return []
+            i, p = row(s), row(s - 1)
+            return [index[(1, s - 1, h)] for h in range(sp[i], sp[i + 1])] + \
+                   [index[(0, s - 1, h)] for h in range(sp[p], sp[p + 1])]
+        if kind == 1:
+            return [index[(2, s - 1, g)]] if s > 0 else []
+        i = row(s)
+        return [index[(0, s, h)] for h in range(sp[i], sp[i + 1])] + ([index[(2, s - 1, g)]] if s > 0 else [])
+    return items, inputs
+
+
+@pytest.mark.parametrize("bs", [[512], [512] * 2, [512] * 3, [512] * 7, [128] * 16, [64, 512, 200, 128, 1, 300]])
+def test_sweep_claim_order_is_a_topological_order(bs):
+    """The TMA sweeps' claim order (ttg_solve.cu) is a permutation of each
+    direction's items in which every item follows all the items it waits
+    for, so blocks claiming in that order never wait on an unclaimed item."""
+    import ctypes
+    import numpy as np
+    f = t.lib().ttg_internal_sweep_order
+    f.restype = ctypes.c_int64
+    f.argtypes = [ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]
+    nb = len(bs)
+    b = np.asarray(bs, np.int32)
+    n = f(nb, b.ctypes.data, None, 0)
+    out = np.zeros(n, np.int32)
+    assert f(nb, b.ctypes.data, out.ctypes.data, n) == n
+    off = 0
+    for backward in (0, 1):
+        items, inputs = _sweep_items(nb, bs, backward)
+        order = out[off: off + len(items)]
+        off += len(items)
+        assert sorted(order.tolist()) == list(range(len(items)))
+        pos = np.empty(len(items), np.int64)
+        pos[order] = np.arange(len(items))
+        for k, it in enumerate(items):
+            assert all(pos[d] < pos[k] for d in inputs(it)), (backward, it)
+    assert off == n
