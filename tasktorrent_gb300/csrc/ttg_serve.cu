@@ -688,6 +688,34 @@ ttg_status open_close(OpenLane& L) {
     return ttg_stream_write_u32(L.cs, (uint32_t*)(L.pub + 2), 1u);
 }
 
+// Upper bound of the tasks of one request's graph (batch_graph.h, plus its
+// last task): factor nb + nb(nb-1)/2 + (nb³-nb)/6 + nb(nb+1)/2 tasks, each
+// solve nb² + nb, each refinement round 2 + nb(nb+2) + nb more, and the
+// conversions around them.  Its edges stay within 8 and its parts within 32
+// per task of the bound (tests/test_abi.py checks all three).
+long open_task_bound(int N, int tile, int ir_steps) {
+    System S;
+    S.set_size(N, tile);
+    const long nb = S.nb;
+    const long fac = nb + nb * (nb - 1) / 2 + (nb * nb * nb - nb) / 6 + nb * (nb + 1) / 2;
+    const long per_solve = nb * nb + nb;
+    return fac + 2 * nb + per_solve + (long)(ir_steps + 1) * (2 + nb * (nb + 2) + per_solve + nb) + 1;
+}
+
+// The request's last task: after every sink of its graph.
+void add_signal_task(Graph& g, int attempt, int* flag) {
+    std::vector<char> has_succ(g.ops.size(), 0);
+    for (auto& e : g.edges) has_succ[e.first] = 1;
+    ttg_op sig{};
+    sig.kind = ttg::kOpSignal;
+    sig.prec = TTG_PREC_MIXED;
+    sig.m = attempt;
+    sig.c = flag;
+    const int t = g.add(sig);
+    for (int u = 0; u < t; ++u)
+        if (!has_succ[u]) g.edge(u, t);
+}
+
 // Admit request i into lane L: operands on the side stream, its tasks (and a
 // last task that raises its host flag) appended to the arena and published.
 // false: it must wait — no room in this epoch (*full), no request slot free
@@ -703,17 +731,12 @@ bool open_admit(ttg_serve* s, OpenLane& L, int i, bool* full, bool* busy, ttg_st
     L.rs.clear();
     int n_hdr = 0;
     AdmitTarget T{L.ctx, s->side, &g, &L.rs, nullptr, &n_hdr, 0};
-    // Room first, from upper bounds of the request's graph (batch_graph.h):
-    // factor nb + nb(nb-1)/2 + (nb³-nb)/6 + nb(nb+1)/2 tasks, each solve
-    // nb² + nb, each refinement round 2 + nb(nb+2) + nb more, and the
-    // conversions around them; at most 8 successors and 32 parts a task.
+    // Room first, from upper bounds of the request's graph.
     {
         System S;
         S.set_size(q.N, q.tile);
         const long nb = S.nb;
-        const long fac = nb + nb * (nb - 1) / 2 + (nb * nb * nb - nb) / 6 + nb * (nb + 1) / 2;
-        const long per_solve = nb * nb + nb;
-        const long est = fac + 2 * nb + per_solve + (long)(q.ir_steps + 1) * (2 + nb * (nb + 2) + per_solve + nb) + 1;
+        const long est = open_task_bound(q.N, q.tile, q.ir_steps);
         const bool fits_empty = est <= L.cap_tasks && 8 * est <= kOpenEdges && 32 * est <= kOpenParts && nb <= kOpenTeams &&
                                 nb <= L.rs_cap;
         if (!fits_empty) {
@@ -740,19 +763,7 @@ bool open_admit(ttg_serve* s, OpenLane& L, int i, bool* full, bool* busy, ttg_st
         }
         if ((*err = ttg_mixed_row_scales(L.d_rs, (int)L.rs.size(), s->side)) != TTG_OK) return true;
     }
-    // The request's last task: after every sink of its graph.
-    {
-        std::vector<char> has_succ(g.ops.size(), 0);
-        for (auto& e : g.edges) has_succ[e.first] = 1;
-        ttg_op sig{};
-        sig.kind = ttg::kOpSignal;
-        sig.prec = TTG_PREC_MIXED;
-        sig.m = ++q.attempt;
-        sig.c = s->d_flag + i;
-        const int t = g.add(sig);
-        for (int u = 0; u < t; ++u)
-            if (!has_succ[u]) g.edge(u, t);
-    }
+    add_signal_task(g, ++q.attempt, s->d_flag + i);
     if ((*err = g.finish(false)) != TTG_OK) return true;
     const int n = (int)g.ops.size();
     const int base = L.n_tasks;
@@ -1324,5 +1335,40 @@ extern "C" ttg_status ttg_serve_get_x(const ttg_serve* s, int32_t i, double* h_X
     const ServeRequest& q = s->req[i];
     if (!q.done || q.result.empty()) return TTG_ESTATE;
     std::copy(q.result.begin(), q.result.end(), h_X);
+    return TTG_OK;
+}
+
+// Test hook (no device work): the open-lane bound of one request and the
+// graph it admits — a system of N (tile, nrhs, ir_steps; mixed or FP64;
+// factored = a follow-up's solve only; tc = tensor-core updates where the
+// tiles allow) plus its last task.  out[5]: the bound, tasks, edges, parts
+// (as the executor counts them), tile rows.  Never dereferences the fake
+// device addresses it builds the ops with.
+extern "C" ttg_status ttg_internal_open_request_graph(int32_t N, int32_t tile, int32_t nrhs, int32_t ir_steps, int32_t mixed,
+                                                      int32_t factored, int32_t tc, int64_t* out) {
+    if (N < 1 || tile < 1 || nrhs < 1 || ir_steps < 0 || !out) return TTG_EINVAL;
+    using namespace ttg::batch;
+    System S;
+    S.set_size(N, tile);
+    S.mixed = mixed != 0;
+    S.nrhs = nrhs;
+    S.ir_steps = ir_steps;
+    S.factored = factored != 0;
+    static char fake[64];  // stands in for every device array (never read)
+    S.A64 = S.W64 = S.D64 = S.B = S.X = S.R = (double*)fake;
+    S.W32 = S.D32 = (float*)fake;
+    if (S.mixed && tc && System::tc_fits(S.N, S.tile)) S.tc_tables = fake;
+    Graph g;
+    add_system(g, S);
+    add_signal_task(g, 1, (int*)fake);
+    const ttg_status st = g.finish(false);
+    if (st != TTG_OK) return st;
+    int64_t parts = 0;
+    for (const ttg_op& op : g.ops) parts += ttg_task_parts(op, true);
+    out[0] = open_task_bound(N, S.tile, ir_steps);
+    out[1] = (int64_t)g.ops.size();
+    out[2] = (int64_t)g.idx.size();
+    out[3] = parts;
+    out[4] = S.nb;
     return TTG_OK;
 }

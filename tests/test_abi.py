@@ -250,3 +250,29 @@ def test_sweep_claim_order_is_a_topological_order(bs):
         for k, it in enumerate(items):
             assert all(pos[d] < pos[k] for d in inputs(it)), (backward, it)
     assert off == n
+
+
+@pytest.mark.parametrize("factored", [0, 1])
+@pytest.mark.parametrize("tc", [0, 1])
+def test_open_lane_bounds_cover_every_request_graph(factored, tc):
+    """An open serving lane reserves room for a request from a closed-form
+    bound before it builds the request's graph (ttg_serve.cu); the graph it
+    then appends (the system's tasks and its last task) stays within the
+    bound's tasks, 8 edges and 32 executor parts per bounded task, for every
+    request size the serving tile rule produces and up to 12 refinement
+    rounds (3, doubled twice on retries)."""
+    import ctypes
+    import numpy as np
+    f = t.lib().ttg_internal_open_request_graph
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int32] * 7 + [ctypes.c_void_p]
+    out = np.zeros(5, np.int64)
+    sizes = sorted(set([64, 65, 100, 127, 128, 129, 255, 256, 257, 300, 511, 512, 700, 1000, 1023, 1024, 1500, 2047, 2048,
+                        2049, 2304, 3000, 4096, 5000, 8191, 8192]))
+    for N in sizes:
+        tile = t.lib().ttg_serve_tile(N)
+        for ir in (0, 3, 6, 12):
+            for nrhs in (1, 16):
+                assert f(N, tile, nrhs, ir, 1, factored, tc, out.ctypes.data) == t.TTG_OK
+                bound, tasks, edges, parts, nb = out.tolist()
+                assert tasks <= bound and edges <= 8 * bound and parts <= 32 * bound, (N, tile, ir, nrhs, out.tolist())
